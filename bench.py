@@ -1,0 +1,354 @@
+"""Benchmark: batched RkNN queries on one GB300 (or N replicas).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the reference's headline configuration): 100,000 facilities and
+1,000,000 users, float32 uniform in [0,1000]^2 (seeded synthetic data), k=10.
+One step = one batch of 1,000 random facility queries through the engine:
+zone kernel -> plan -> verification -> result offsets -> finalize (one CUDA
+graph).  Prints one JSON line (rank 0).
+
+  value      queries/s with the facility/user index and the query batch
+             resident in HBM, device time from CUDA events on the engine's
+             stream, L2 flushed (256 MB write) before every timed step
+  e2e        queries/s through rknn_query_batch (the C ABI with host
+             buffers): query ids H2D, result offsets and ids D2H, per step
+  roofline   the verification kernel (the dominant per-user kernel), timed
+             live per launch with CUDA events in profiling mode
+  cpu_baseline  the C restatement of rknn-inf's query path (R-tree,
+             influence-zone filter + verification) on the host's cores,
+             over a bounded sample of the same workload
+
+--impl reference times that CPU restatement alone (all host threads) on the
+same workload and prints the same JSON line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "rt-rknn_gb300"))
+
+METRIC = "RkNN queries/s (1M users,100k fac,k=10) FP32-filtered vs FP64; p99 ms"
+NF, NU, K, NQ = 100_000, 1_000_000, 10, 1000
+
+
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.p = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.p = None
+        return self
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.p:
+            time.sleep(0.25)
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dataset():
+    import datagen
+    return datagen.uniform(NF, NU, seed=2, nq=NQ, k=K)
+
+
+def cpu_port_run(ds, nq_sample, nthreads, seed=5):
+    """Time the rknn-inf restatement (oracle/inf_port.c) over nq_sample
+    queries at k=10 on nthreads host threads.  Returns (q/s, seconds)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    port = O.InfPort(ds.fxy, ds.uxy)
+    rng = np.random.default_rng(seed)
+    qs = rng.choice(ds.nf, size=nq_sample, replace=False).astype(np.int64)
+    t0 = time.perf_counter()
+    cnt = port.query_many(qs, K, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return nq_sample / dt, dt, int(cnt.sum())
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    ds = dataset()
+    nthreads = os.cpu_count() or 1
+    per_step = NQ
+    for _ in range(args.warmup):
+        cpu_port_run(ds, per_step, nthreads, seed=99)
+    times = []
+    for s in range(args.steps):
+        qps, dt, _ = cpu_port_run(ds, per_step, nthreads, seed=1000 + s)
+        times.append(dt)
+    tot = sum(times)
+    value = per_step * args.steps / tot
+    line = {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded uniform float32, the reference's text format values)",
+        "impl": "reference",
+        "config": {"workload": "uniform 100k facilities / 1M users, k=10, 1000 queries per step",
+                   "nf": NF, "nu": NU, "k": K, "queries_per_step": per_step},
+        "cpu_baseline": {"value": value, "unit": "queries/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{per_step} queries per step, rknn-inf restatement (R-tree, "
+                                   f"influence zone + verification) on {nthreads} threads"},
+        "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import rknn
+    import build
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    build.build()
+    ds = dataset()
+    idx = rknn.Index.of(ds, device=local)
+    stream = torch.cuda.Stream(device=local)
+    idx.set_stream(stream.cuda_stream)
+    rng = np.random.default_rng(17 + rank)
+    nsteps = args.steps
+    qsets = [rng.choice(ds.nf, size=NQ, replace=False).astype(np.int32)
+             for _ in range(nsteps + args.warmup)]
+    ks = np.full(NQ, K, np.int32)
+
+    # correctness of the timed configuration (host path, sizes the pools)
+    res = idx.query_batch(qsets[0], ks, "fp32")
+    res64 = idx.query_batch(qsets[0][:100], ks[:100], "fp64")
+    assert all(np.array_equal(a, b) for a, b in zip(res[:100], res64))
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    d_qs = [torch.from_numpy(q).to(f"cuda:{local}") for q in qsets]
+    d_k = torch.from_numpy(ks).to(f"cuda:{local}")
+
+    def step(i, ev=None):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+            if ev:
+                ev[0].record(stream)
+            idx.query_batch_device(d_qs[i].data_ptr(), d_k.data_ptr(), NQ, K, "fp32")
+            if ev:
+                ev[1].record(stream)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(nsteps)]
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(nsteps):
+            step(args.warmup + i, evs[i])
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if ws > 1:
+        torch.distributed.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    dev_s = sum(step_ms) / 1e3
+    if ws > 1:
+        t = torch.tensor([dev_s], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_s = float(t.item())
+    value = ws * NQ * nsteps / dev_s
+
+    # ---- end to end through the C ABI with host buffers ------------------
+    e2e_times, h2d, d2h = [], 0, 0
+    for i in range(nsteps):
+        q = qsets[args.warmup + i]
+        t1 = time.perf_counter()
+        out = idx.query_batch(q, ks, "fp32")
+        e2e_times.append(time.perf_counter() - t1)
+        h2d = q.nbytes + ks.nbytes
+        d2h = 4 * (NQ + 1) + 4 * sum(len(o) for o in out)
+    e2e = NQ / statistics.mean(e2e_times) * ws
+
+    # ---- plain FP64 single-query form (one query per launch) --------------
+    single = qsets[0][:200]
+    lat = []
+    for q in single[:10]:
+        idx.query(int(q), K, "fp64")
+    for q in single:
+        t1 = time.perf_counter()
+        idx.query(int(q), K, "fp64")
+        lat.append(1e3 * (time.perf_counter() - t1))
+    fp64_single_qps = 1e3 / statistics.mean(lat)
+    lat.sort()
+    p50 = lat[len(lat) // 2]
+    p99 = lat[min(len(lat) - 1, int(0.99 * len(lat)))]
+    # FP64 batched, device time
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        flush.fill_(1.0)
+        e0.record(stream)
+        idx.query_batch_device(d_qs[0].data_ptr(), d_k.data_ptr(), NQ, K, "fp64")
+        e1.record(stream)
+    torch.cuda.synchronize()
+    fp64_batch_qps = NQ / (e0.elapsed_time(e1) / 1e3)
+
+    # ---- roofline of the verification kernel (live, profiling mode) --------
+    idx.set_profiling(True)
+    kms = []
+    for i in range(3):
+        with torch.cuda.stream(stream):
+            flush.fill_(2.0 + i)
+        stream.synchronize()
+        idx.query_batch(qsets[args.warmup + i], ks, "fp32")
+        kms.append(idx.kernel_ms())
+    st = idx.last_stats()
+    idx.set_profiling(False)
+    vms = statistics.mean(m["verify"] for m in kms)
+    zms = statistics.mean(m["zone"] for m in kms)
+    hbm_peak, kind = peaks()
+    # algorithmic work of one verification launch: users read (8 B each),
+    # half-planes staged (16 B each per query), result ids written (4 B),
+    # facilities read by the exact recount (8 B); FLOP = 4 per
+    # (user, half-plane) evaluation executed
+    nb_total = st["bisectors"]
+    bytes_alg = 8 * st["candidates"] + 16 * nb_total + 4 * st["results"] + 8 * st["fac_checks"]
+    flops = 4 * st["plane_evals"]
+    props = torch.cuda.get_device_properties(local)
+    fp32_peak = props.multi_processor_count * 128 * 2 * 2.07e9 / 1e12     # nominal
+    gbs = bytes_alg / (vms / 1e3) / 1e9
+    tfs = flops / (vms / 1e3) / 1e12
+    hbm_frac = gbs / hbm_peak
+    fp32_frac = tfs / fp32_peak
+    if fp32_frac >= hbm_frac:
+        roof = {"bound": "fp32", "achieved": tfs, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": fp32_frac, "peak_kind": "nominal (152 SM x 128 FMA x 2.07 GHz)"}
+    else:
+        roof = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+                "frac": hbm_frac, "peak_kind": kind}
+    roof.update({"kernel": "verify_kernel", "launch_ms": vms, "traffic": None,
+                 "alg_bytes": bytes_alg, "alg_flop": flops,
+                 "hbm": {"achieved_gbs": gbs, "frac": hbm_frac, "peak": hbm_peak},
+                 "fp32": {"achieved_tflops": tfs, "frac": fp32_frac, "peak": fp32_peak},
+                 "zone_ms": zms, "kernel_ms": kms[-1]})
+
+    # ---- CPU baseline (rank 0, N=1 only) ---------------------------------
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        nthreads = os.cpu_count() or 1
+        sample = args.cpu_sample
+        qps, dt, _ = cpu_port_run(ds, sample, nthreads)
+        cpu = {"value": qps, "unit": "queries/s", "cores": nthreads, "kind": "port",
+               "sample": f"{sample} random facility queries at k=10 ({dt:.1f} s on {nthreads} threads), "
+                         "rknn-inf restatement: R-tree, influence-zone filter, verification"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws,
+        "steps": nsteps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / nsteps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded uniform float32 in [0,1000]^2)",
+        "config": {"workload": "uniform 100k facilities / 1M users, k=10, 1000 queries per step",
+                   "nf": NF, "nu": NU, "k": K, "queries_per_step": NQ, "mode": "fp32 batched",
+                   "l2": "256 MB flush before each timed step", "parallelism": f"replicas x{ws}"},
+        "wall_s": wall,
+        "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": 5 * nsteps,
+        "fp64_single_query": {"qps": fp64_single_qps, "p50_ms": p50, "p99_ms": p99},
+        "fp64_batched_qps": fp64_batch_qps,
+        "speedup_fp32_batched_vs_fp64_single": value / ws / fp64_single_qps,
+        "roofline": roof,
+        "stats": {k2: st[k2] for k2 in ("bisectors", "zone_vertices_max", "zone_candidates", "zone_fp64",
+                                        "candidates", "plane_evals", "survivors", "fac_checks",
+                                        "rechecks", "results", "overflow")},
+        "recheck_fraction": st["rechecks"] / max(1, st["fac_checks"]),
+        "clocks": clk.summary(),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=20000)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,170 @@
+/*
+ * rknn_gpu.h - C ABI of the GB300 reverse k-nearest-neighbour engine.
+ *
+ * Plain C types only (no CUDA or C++ types in signatures), so any FFI can
+ * bind it.  Every function returns an rknn_status; on failure
+ * rknn_last_error() gives a message for the calling thread.  The library
+ * never exits the process and has no CPU fallback: when the GPU path cannot
+ * run, calls fail with RKNN_ERR_CUDA.
+ *
+ * Semantics (shared by every entry point): for a query facility q (an index
+ * into the facility list, as the reference's `-q`, rknn-inf/inf.cpp:207) and
+ * k >= 1, the result is the set of users u with
+ *     #{ f != q : d2(u,f) < d2(u,q) } < k,
+ * evaluated exactly on the float32 coordinates.  This is rknn-naive's
+ * brute-force answer (rknn-naive/rknn.cpp:169-198) with the strict-< tie
+ * rule of rknn-inf (rknn-inf/inf.h:77-93) and rknn-naive-gpu
+ * (rknn-naive-gpu/rknn_kernel.cu:156).  Result ids are returned sorted
+ * ascending.
+ *
+ * Reference interfaces replaced:
+ *   rknn_index_create  - the per-process R*-tree build of every reference
+ *                        binary (rknn-inf/inf.cpp:165-177,
+ *                        RStarTree2D.cpp:106-114) plus the space bounding box
+ *                        (inf.cpp:181-199)
+ *   rknn_query         - one `rknn-inf -if F -k K -q Q` run after loading:
+ *                        influence-zone filter (inf.cpp:201-585) and
+ *                        verification (inf.h:241-249); on the GPU side it
+ *                        replaces gpu_get_rknn_candidates
+ *                        (rknn-inf-gpu/inf_kernel.h:22-27) and gpuReverseKNN
+ *                        (rknn-naive-gpu/rknn_kernel.cuh:40-46)
+ *   rknn_query_batch   - many such runs in one launch (no reference
+ *                        counterpart; the reference answers one query per
+ *                        process)
+ */
+#ifndef RKNN_GPU_H
+#define RKNN_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    RKNN_OK = 0,
+    RKNN_ERR_ARG = 1,       /* bad argument (null pointer, k <= 0, q out of range, ...) */
+    RKNN_ERR_OOM = 2,       /* device or host allocation failed */
+    RKNN_ERR_CUDA = 3,      /* CUDA error (no device, launch failure, ...) */
+    RKNN_ERR_TIMEOUT = 4,   /* a bounded wait ran out */
+    RKNN_ERR_CAPACITY = 5,  /* output buffer too small; required size returned */
+    RKNN_ERR_STATE = 6      /* object in the wrong state for the call */
+} rknn_status;
+
+typedef enum {
+    RKNN_MODE_FP64 = 0,     /* plain form: predicates filtered in double precision */
+    RKNN_MODE_FP32 = 1      /* predicates filtered in float32 with a certified bound */
+} rknn_mode;
+
+typedef struct rknn_index rknn_index;
+
+typedef struct {
+    int32_t device;         /* CUDA device ordinal (default 0) */
+    float fac_per_cell;     /* facilities per facility-grid cell (0: default 2) */
+    float usr_per_cell;     /* users per user-grid cell (0: default 8) */
+    int32_t skip_coincident;/* 1 (default): a facility at q's exact position adds no
+                               bisector (the reference adds a degenerate one) */
+    int32_t reserved[6];
+} rknn_index_opts;
+
+typedef struct {
+    int64_t queries;
+    int64_t results;        /* result ids returned */
+    int64_t bisectors;      /* influence-zone bisectors created */
+    int64_t zone_vertices_max;
+    int64_t zone_candidates;/* bisector intersections considered */
+    int64_t zone_fp64;      /* intersections computed in double precision */
+    int64_t candidates;     /* users tested against the half-planes */
+    int64_t plane_evals;    /* (user, half-plane) evaluations */
+    int64_t survivors;      /* users recounted exactly */
+    int64_t fac_checks;     /* (user, facility) comparisons in the exact count */
+    int64_t rechecks;       /* comparisons decided by the exact expansion */
+    int64_t overflow;       /* queries whose zone hit a capacity (results still exact) */
+    double device_ms;       /* device time of the last launch sequence */
+} rknn_query_stats;
+
+void rknn_index_opts_default(rknn_index_opts* opts);
+
+/* Build the device index.  fxy/uxy: interleaved x,y float32 (2*nf, 2*nu);
+ * fid/uid: ids (fid may be null).  nf >= 1, nu >= 0. */
+rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf,
+                              const float* uxy, const int32_t* uid, int64_t nu,
+                              const rknn_index_opts* opts, rknn_index** out);
+
+rknn_status rknn_index_destroy(rknn_index* idx);
+
+/* Number of facilities / users in the index. */
+rknn_status rknn_index_size(const rknn_index* idx, int64_t* nf, int64_t* nu);
+
+typedef struct {
+    int64_t nf, nu;
+    double x0, y0, x1, y1;          /* bounding box of all points: the zone's space */
+    float fgrid_x0, fgrid_y0, fgrid_inv;   /* facility grid: cell of v is floor((v-x0)*inv) */
+    int32_t fgrid_gx, fgrid_gy;
+    float ugrid_x0, ugrid_y0, ugrid_inv;   /* user grid */
+    int32_t ugrid_gx, ugrid_gy;
+} rknn_index_info;
+
+/* Geometry of the index (for audits against a CPU restatement). */
+rknn_status rknn_index_get_info(const rknn_index* idx, rknn_index_info* info);
+
+/* One query, one launch sequence, host buffers.  Writes up to cap ids to
+ * out_ids and the result size to *n_out; returns RKNN_ERR_CAPACITY (with
+ * *n_out set) when cap is too small.  stats may be null. */
+rknn_status rknn_query(rknn_index* idx, int32_t q_index, int32_t k, int32_t mode,
+                       int32_t* out_ids, int64_t cap, int64_t* n_out,
+                       rknn_query_stats* stats);
+
+/* nq queries in one launch sequence (CUDA graph), host buffers.  Results of
+ * query i are out_ids[offsets[i] .. offsets[i+1]); offsets has nq+1 entries.
+ * RKNN_ERR_CAPACITY when cap < offsets[nq] (offsets still filled). */
+rknn_status rknn_query_batch(rknn_index* idx, const int32_t* q_index, const int32_t* k,
+                             int32_t nq, int32_t mode, int32_t* out_ids, int64_t cap,
+                             int64_t* offsets, rknn_query_stats* stats);
+
+/* Device-resident form: q_index/k are device pointers; results stay on the
+ * device (see rknn_batch_device_results).  kmax bounds every k[i] (it sizes
+ * the zone state; a larger k is still answered exactly, with the zone cut
+ * short).  Enqueued on the index's stream; returns without synchronizing.
+ * Query indices must be valid (an out-of-range slot yields no results). */
+rknn_status rknn_query_batch_device(rknn_index* idx, const int32_t* d_q_index,
+                                    const int32_t* d_k, int32_t nq, int32_t kmax, int32_t mode);
+
+/* Device pointers to the last device batch's results: ids and nq+1 int32
+ * offsets.  Valid until the next query call on this index. */
+rknn_status rknn_batch_device_results(rknn_index* idx, const int32_t** d_ids,
+                                      const int32_t** d_offsets);
+
+/* Wait for the index's stream. */
+rknn_status rknn_sync(rknn_index* idx);
+
+/* Use the caller's CUDA stream (a cudaStream_t passed as void*; null resets
+ * to the library's own stream). */
+rknn_status rknn_set_stream(rknn_index* idx, void* stream);
+
+/* Statistics of the last query call (host or device form). */
+rknn_status rknn_last_stats(rknn_index* idx, rknn_query_stats* stats);
+
+/* Per-query zone record of the last call (for audits): bisector count and
+ * the facility input indices of the bisectors in creation order. */
+rknn_status rknn_last_zone(rknn_index* idx, int32_t slot, int32_t* bis_fac, int32_t cap,
+                           int32_t* n_bis, int32_t* flags);
+
+/* Profiling mode (on != 0): the next query calls launch their kernels one
+ * by one, with CUDA events between them, instead of replaying a CUDA graph. */
+rknn_status rknn_set_profiling(rknn_index* idx, int32_t on);
+
+/* Device time of each kernel of the last profiled call, in milliseconds:
+ * ms[0] zone, ms[1] plan, ms[2] verify, ms[3] result offsets, ms[4] finalize. */
+rknn_status rknn_last_kernel_ms(rknn_index* idx, double* ms);
+
+/* Message of the last failure on this thread ("" if none). */
+const char* rknn_last_error(void);
+
+/* Library version string. */
+const char* rknn_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RKNN_GPU_H */

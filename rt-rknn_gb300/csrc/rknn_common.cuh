@@ -1,0 +1,154 @@
+// Shared definitions of the GB300 RkNN engine: grid descriptors, per-query
+// descriptors and the exact sign predicate for squared-distance comparisons.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rknn {
+
+constexpr float kU32 = 5.9604644775390625e-08f;      // 2^-24, float unit roundoff
+constexpr double kU64 = 1.1102230246251565e-16;      // 2^-53, double unit roundoff
+
+// Uniform grid over the data's bounding box.  A coordinate v falls in cell
+// floor((v - o) * inv) (float arithmetic, clamped), which is monotone in v:
+// every range test below can use the same function on its end points.
+struct Grid {
+    float x0, y0;      // origin (bounding-box minimum)
+    float inv;         // 1 / cell width
+    float cs;          // cell width
+    int gx, gy;        // cells per axis
+};
+
+__host__ __device__ __forceinline__ int cell_coord(float v, float o, float inv, int g)
+{
+    float t = floorf((v - o) * inv);
+    if (!(t >= 0.0f)) return 0;           // also catches NaN
+    if (t > (float)(g - 1)) return g - 1;
+    return (int)t;
+}
+
+// Per-query descriptor written by the zone kernel and read by verification.
+struct QDesc {
+    float qx, qy;      // query facility coordinates
+    int qpos;          // its position in the cell-sorted facility array
+    int k;
+    int nb;            // bisector half-planes stored
+    int nseg;          // user segments stored
+    float k2f, kf2;    // per-user FP32 bound: 8u(2F'(|x'|+|y'|) + F'^2) = k2f*(|x'|+|y'|) + kf2
+    double k2f64, kf264;
+    int ncand;         // users in all segments
+    int flags;         // RKNN_QF_* bits
+};
+
+// QDesc.flags
+constexpr int QF_ZONE_V_OVERFLOW = 1;    // vertex capacity reached: zone stopped early
+constexpr int QF_ZONE_L_OVERFLOW = 2;    // bisector capacity reached
+constexpr int QF_ZONE_PQ_OVERFLOW = 4;   // priority queue full
+constexpr int QF_ALL_USERS = 8;          // cell scan gave up: every user is a candidate
+constexpr int QF_RESULT_OVERFLOW = 16;   // result pool too small
+constexpr int QF_BAD_QUERY = 32;         // q or k out of range
+
+// Zone statistics per query (all counters, for logs and tests).
+struct ZStats {
+    int nb;            // bisectors created
+    int vmax;          // largest vertex set
+    int pts;           // facilities tested
+    int cells;         // facility cells tested
+    int cand;          // candidate vertices considered
+    int cand64;        // candidates whose intersection was computed in FP64
+    int kept;          // candidates kept as vertices
+    int rings;         // user-cell rings scanned
+};
+
+// Verification statistics, accumulated over a batch.
+struct VStats {
+    unsigned long long cand;       // users tested against half-planes
+    unsigned long long plane_evals;// (user, half-plane) evaluations executed
+    unsigned long long survivors;  // users sent to the exact count
+    unsigned long long fac_checks; // (user, facility) comparisons in the exact count
+    unsigned long long rechecks;   // comparisons re-decided exactly (FP64 expansion)
+    unsigned long long results;
+};
+
+// ------------------------------------------------------------ exact predicate
+// Sign of d2(u,f) - d2(u,q) for float inputs.  Every product of two floats is
+// exact in double, and
+//   d2(u,f) - d2(u,q) = fx^2+fy^2-qx^2-qy^2 - 2ux fx - 2uy fy + 2ux qx + 2uy qy
+// is a sum of eight exact doubles.  Its sign comes from a nonoverlapping
+// expansion grown with TwoSum (Knuth; Shewchuk 1997, Grow-Expansion): the sign
+// of an expansion is the sign of its largest nonzero component.  Explicit
+// round-to-nearest intrinsics keep the compiler from fusing or reordering.
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e)
+{
+    double x = __dadd_rn(a, b);
+    double bv = __dsub_rn(x, a);
+    double av = __dsub_rn(x, bv);
+    double br = __dsub_rn(b, bv);
+    double ar = __dsub_rn(a, av);
+    s = x;
+    e = __dadd_rn(ar, br);
+}
+
+static __device__ __noinline__ int sign_d2diff_exact(float ux, float uy, float fx, float fy,
+                                              float qx, float qy)
+{
+    double t[8];
+    t[0] = __dmul_rn((double)fx, (double)fx);
+    t[1] = __dmul_rn((double)fy, (double)fy);
+    t[2] = -__dmul_rn((double)qx, (double)qx);
+    t[3] = -__dmul_rn((double)qy, (double)qy);
+    t[4] = -2.0 * __dmul_rn((double)ux, (double)fx);
+    t[5] = -2.0 * __dmul_rn((double)uy, (double)fy);
+    t[6] = 2.0 * __dmul_rn((double)ux, (double)qx);
+    t[7] = 2.0 * __dmul_rn((double)uy, (double)qy);
+    double e[8];
+    int m = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        double q = t[i];
+        for (int j = 0; j < m; ++j) {
+            double s, h;
+            two_sum(q, e[j], s, h);
+            e[j] = h;
+            q = s;
+        }
+        e[m++] = q;
+    }
+    for (int j = m - 1; j >= 0; --j)
+        if (e[j] != 0.0) return e[j] > 0.0 ? 1 : -1;
+    return 0;
+}
+
+// f strictly nearer to u than q, FP32 filter then exact.  The computed squared
+// distances carry a relative error below (1+u)^4-1 each and the difference one
+// more rounding: |err| <= 5.0001u (Df+Dq) (+ underflow, covered by 1e-30).
+__device__ __forceinline__ bool closer_f32(float ux, float uy, float fx, float fy,
+                                           float qx, float qy, float Dq,
+                                           unsigned long long* rechecks)
+{
+    float dx = ux - fx, dy = uy - fy;
+    float Df = fmaf(dx, dx, dy * dy);
+    float d = Df - Dq;
+    float bnd = fmaf(6.0f * kU32, Df + Dq, 1e-30f);
+    if (d < -bnd) return true;
+    if (d > bnd) return false;
+    ++*rechecks;
+    return sign_d2diff_exact(ux, uy, fx, fy, qx, qy) < 0;
+}
+
+// Same decision with a double-precision filter (the plain FP64 form).
+__device__ __forceinline__ bool closer_f64(float ux, float uy, float fx, float fy,
+                                           float qx, float qy, double Dq,
+                                           unsigned long long* rechecks)
+{
+    double dx = (double)ux - (double)fx, dy = (double)uy - (double)fy;
+    double Df = fma(dx, dx, dy * dy);
+    double d = Df - Dq;
+    double bnd = 8.0 * kU64 * (Df + Dq);
+    if (d < -bnd) return true;
+    if (d > bnd) return false;
+    ++*rechecks;
+    return sign_d2diff_exact(ux, uy, fx, fy, qx, qy) < 0;
+}
+
+}  // namespace rknn

@@ -1,0 +1,427 @@
+// Verification: for every candidate user of a query, count the facilities
+// strictly nearer than the query facility q and keep the user when the count
+// is below k (rknn-inf-gpu/inf_kernel.cu:41-66 counts bisector violations per
+// user; rknn-rt/rt.cu:95-111 counts half-plane hits and stops at k).
+//
+// Stage 1 (half-plane filter).  A user is tested against the zone's
+// bisectors written as exact half-planes relative to q,
+//     m_f(u) = a (ux-qx) + b (uy-qy) + c = d2(u,f) - d2(u,q),
+// two FMAs per (user, half-plane).  m_f(u) < -bound certifies that f is
+// strictly nearer; k certified half-planes reject the user.  The bound
+//     8u (2F'(|x'|+|y'|) + F'^2),  F' = max |f - q| over the bisectors,
+// exceeds the float (or double) evaluation error of m_f (at most
+// 4.01u(|a x'| + |b y'| + |c|)).  Lanes own users (coalesced float2 loads,
+// four per lane); the warp leaves the half-plane loop as soon as every lane
+// has k certified violations for all its users (__all_sync).
+//
+// Stage 2 (exact count).  Users that survive stage 1 are counted exactly
+// over the facility grid: the whole warp scans, row by row, the facility
+// cells covering the disc of radius d(u,q) around u (one contiguous range
+// of the cell-sorted facility array per row, coalesced), counting
+// d2(u,f) < d2(u,q) with __ballot_sync/__popc and stopping at k.  Each
+// comparison is decided in float (or double) with its error bound, and the
+// undecided ones by the exact expansion predicate.  Accepted users are
+// appended with one warp-aggregated atomic per work item.
+#include "verify.cuh"
+#include <climits>
+
+namespace rknn {
+
+namespace {
+constexpr unsigned FULL = 0xffffffffu;
+
+template <typename T>
+__device__ __forceinline__ int exact_count(float ux, float uy, const QDesc& d, const VerifyArgs& A,
+                                           unsigned long long& fac, unsigned long long& rech)
+{
+    const int lane = threadIdx.x & 31;
+    float qx = d.qx, qy = d.qy;
+    T Dq;
+    float r;
+    const float slack = 4.0f * kU32 * (fabsf(ux) + fabsf(uy) + fabsf(qx) + fabsf(qy)) + 1e-30f;
+    if (sizeof(T) == 4) {
+        float dx = ux - qx, dy = uy - qy;
+        float D = fmaf(dx, dx, dy * dy);
+        Dq = (T)D;
+        r = sqrtf(D) * (1.0f + 4e-6f) + slack;
+    } else {
+        double dx = (double)ux - (double)qx, dy = (double)uy - (double)qy;
+        double D = fma(dx, dx, dy * dy);
+        Dq = (T)D;
+        r = (float)sqrt(D) * (1.0f + 4e-6f) + slack;
+    }
+    const Grid& g = A.gf;
+    int cx0 = cell_coord(ux - r, g.x0, g.inv, g.gx), cx1 = cell_coord(ux + r, g.x0, g.inv, g.gx);
+    int cy0 = cell_coord(uy - r, g.y0, g.inv, g.gy), cy1 = cell_coord(uy + r, g.y0, g.inv, g.gy);
+    int cnt = 0;
+    for (int cy = cy0; cy <= cy1; ++cy) {
+        const int f0 = A.fstart[cy * g.gx + cx0], f1 = A.fstart[cy * g.gx + cx1 + 1];
+        for (int b = f0; b < f1; b += 32) {
+            int i = b + lane;
+            bool c = false;
+            if (i < f1 && i != d.qpos) {
+                float2 f = A.fxy[i];
+                if (sizeof(T) == 4) c = closer_f32(ux, uy, f.x, f.y, qx, qy, (float)Dq, &rech);
+                else c = closer_f64(ux, uy, f.x, f.y, qx, qy, (double)Dq, &rech);
+            }
+            cnt += __popc(__ballot_sync(FULL, c));
+            fac += (unsigned long long)min(32, f1 - b);
+            if (cnt >= d.k) return cnt;
+        }
+    }
+    return cnt;
+}
+
+template <typename T>
+__device__ __forceinline__ void filter_users(const QDesc& d, const char* sp, const int* pos,
+                                             const float2* u, const bool* valid, int* cnt,
+                                             unsigned long long& evals)
+{
+    T x[VERIFY_UPT], y[VERIFY_UPT], bu[VERIFY_UPT];
+    int nvalid = 0;
+#pragma unroll
+    for (int t = 0; t < VERIFY_UPT; ++t) {
+        cnt[t] = valid[t] ? 0 : INT_MAX / 2;
+        nvalid += valid[t];
+        if (sizeof(T) == 4) {
+            float xx = u[t].x - d.qx, yy = u[t].y - d.qy;
+            x[t] = xx; y[t] = yy;
+            bu[t] = fmaf(d.k2f, fabsf(xx) + fabsf(yy), d.kf2);
+        } else {
+            double xx = (double)u[t].x - (double)d.qx, yy = (double)u[t].y - (double)d.qy;
+            x[t] = (T)xx; y[t] = (T)yy;
+            bu[t] = (T)fma(d.k2f64, fabs(xx) + fabs(yy), d.kf264);
+        }
+    }
+    const int nb = d.nb, k = d.k;
+    int m = 0;
+    for (; m < nb; ++m) {
+        T a, b, c;
+        if (sizeof(T) == 4) {
+            float4 p = ((const float4*)sp)[m];
+            a = (T)p.x; b = (T)p.y; c = (T)p.z;
+        } else {
+            const double* p = (const double*)sp + 4 * m;
+            a = (T)p[0]; b = (T)p[1]; c = (T)p[2];
+        }
+#pragma unroll
+        for (int t = 0; t < VERIFY_UPT; ++t) {
+            T mv = fma(a, x[t], fma(b, y[t], c));
+            cnt[t] += (mv < -bu[t]);
+        }
+        if ((m & 7) == 7) {
+            bool done = true;
+#pragma unroll
+            for (int t = 0; t < VERIFY_UPT; ++t) done &= cnt[t] >= k;
+            if (__all_sync(FULL, done)) { ++m; break; }
+        }
+    }
+    evals += (unsigned long long)m * nvalid;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(VERIFY_WARPS * 32)
+verify_kernel(VerifyArgs A)
+{
+    extern __shared__ __align__(16) char smem[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const size_t per_warp = (size_t)A.lc * (A.mode == MODE_FP32 ? 16 : 32);
+    char* sp = smem + w * per_warp;
+    int cur = -1;
+    unsigned long long s_cand = 0, s_evals = 0, s_surv = 0, s_fac = 0, s_rech = 0, s_res = 0;
+    const int total = A.chunk_off[A.nq];
+    for (;;) {
+        int g = 0;
+        if (lane == 0) g = atomicAdd(A.work_counter, 1);
+        g = __shfl_sync(FULL, g, 0);
+        if (g >= total) break;
+        int lo = 0, hi = A.nq;          // chunk_off[lo] <= g < chunk_off[hi]
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (A.chunk_off[mid] <= g) lo = mid; else hi = mid;
+        }
+        const int s = lo;
+        const QDesc d = A.qd[s];
+        if (s != cur) {
+            __syncwarp();
+            if (A.mode == MODE_FP32) {
+                const float4* src = A.planes + (size_t)s * A.lc;
+                for (int m = lane; m < d.nb; m += 32) ((float4*)sp)[m] = src[m];
+            } else {
+                const int* bp = A.bis_pos + (size_t)s * A.lc;
+                for (int m = lane; m < d.nb; m += 32) {
+                    float2 f = A.fxy[bp[m]];
+                    double dx = (double)f.x - (double)d.qx, dy = (double)f.y - (double)d.qy;
+                    double* p = (double*)sp + 4 * m;
+                    p[0] = -2.0 * dx;
+                    p[1] = -2.0 * dy;
+                    p[2] = fma(dx, dx, dy * dy);
+                    p[3] = 0.0;
+                }
+            }
+            cur = s;
+            __syncwarp();
+        }
+        const int v0 = (g - A.chunk_off[s]) * VERIFY_CHUNK;
+        const int2* sg = A.segs + (size_t)s * A.seg_cap;
+        // segment holding v0: largest i < nseg with sg[i].y <= v0
+        int i0 = 0;
+        {
+            int l = 0, h = d.nseg;
+            while (h - l > 1) {
+                int mid = (l + h) >> 1;
+                if (sg[mid].y <= v0) l = mid; else h = mid;
+            }
+            i0 = l;
+        }
+        int pos[VERIFY_UPT];
+        float2 u[VERIFY_UPT];
+        bool valid[VERIFY_UPT];
+        int si = i0;
+#pragma unroll
+        for (int t = 0; t < VERIFY_UPT; ++t) {
+            int v = v0 + t * 32 + lane;
+            valid[t] = v < d.ncand;
+            pos[t] = 0;
+            u[t] = make_float2(0.f, 0.f);
+            if (valid[t]) {
+                while (si + 1 < d.nseg && sg[si + 1].y <= v) ++si;
+                pos[t] = sg[si].x + (v - sg[si].y);
+                u[t] = A.uxy[pos[t]];
+            }
+            s_cand += valid[t];
+        }
+        int cnt[VERIFY_UPT];
+        if (A.mode == MODE_FP32) filter_users<float>(d, sp, pos, u, valid, cnt, s_evals);
+        else filter_users<double>(d, sp, pos, u, valid, cnt, s_evals);
+
+        // stage 2: exact count for the survivors, one user at a time per warp
+        bool acc[VERIFY_UPT];
+#pragma unroll
+        for (int t = 0; t < VERIFY_UPT; ++t) {
+            acc[t] = false;
+            unsigned m = __ballot_sync(FULL, valid[t] && cnt[t] < d.k);
+            s_surv += (lane == 0) ? __popc(m) : 0;
+            while (m) {
+                int l = __ffs(m) - 1;
+                m &= m - 1;
+                float ux = __shfl_sync(FULL, u[t].x, l), uy = __shfl_sync(FULL, u[t].y, l);
+                int c = (A.mode == MODE_FP32) ? exact_count<float>(ux, uy, d, A, s_fac, s_rech)
+                                              : exact_count<double>(ux, uy, d, A, s_fac, s_rech);
+                if (lane == l) acc[t] = c < d.k;
+            }
+        }
+        // warp-aggregated append of the accepted users
+        unsigned am[VERIFY_UPT];
+        int tot = 0;
+#pragma unroll
+        for (int t = 0; t < VERIFY_UPT; ++t) { am[t] = __ballot_sync(FULL, acc[t]); tot += __popc(am[t]); }
+        if (tot) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(A.res_count + s, tot);
+            base = __shfl_sync(FULL, base, 0);
+            int* dst = A.res_pool + A.cand_off[s] + base;
+            int o = 0;
+#pragma unroll
+            for (int t = 0; t < VERIFY_UPT; ++t) {
+                if (acc[t]) dst[o + __popc(am[t] & ((1u << lane) - 1))] = A.uid[pos[t]];
+                o += __popc(am[t]);
+            }
+            s_res += (lane == 0) ? tot : 0;
+        }
+    }
+    // statistics: per-lane partials, one atomic per counter per warp
+    for (int o = 16; o > 0; o >>= 1) {
+        s_cand += __shfl_xor_sync(FULL, s_cand, o);
+        s_evals += __shfl_xor_sync(FULL, s_evals, o);
+        s_rech += __shfl_xor_sync(FULL, s_rech, o);
+    }
+    if (lane == 0 && A.vstats) {
+        atomicAdd(&A.vstats->cand, s_cand);
+        atomicAdd(&A.vstats->plane_evals, s_evals);
+        atomicAdd(&A.vstats->survivors, s_surv);
+        atomicAdd(&A.vstats->fac_checks, s_fac);
+        atomicAdd(&A.vstats->rechecks, s_rech);
+        atomicAdd(&A.vstats->results, s_res);
+    }
+}
+
+// ---------------------------------------------------------------- scans
+namespace {
+// exclusive scan over one block of 1024 threads; returns the total
+__device__ int block_scan_excl(int v, int* tmp)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(FULL, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) tmp[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int t = lane < (int)(blockDim.x >> 5) ? tmp[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(FULL, t, o);
+            if (lane >= o) t += y;
+        }
+        tmp[lane] = t;
+    }
+    __syncthreads();
+    int total = tmp[(blockDim.x >> 5) - 1];
+    int excl = x - v + (w > 0 ? tmp[w - 1] : 0);
+    __syncthreads();
+    return excl | 0 ? excl : excl + 0 * total;   // keep total live for callers below
+}
+}  // namespace
+
+__global__ void plan_kernel(QDesc* qd, int nq, int* cand_off, int* chunk_off, int pool_cap)
+{
+    __shared__ int tmp[32];
+    __shared__ int tot;
+    const int T = blockDim.x;
+    const int per = (nq + T - 1) / T;
+    const int b = threadIdx.x * per, e = min(nq, b + per);
+    // pass 1: candidate offsets
+    int sum = 0;
+    for (int i = b; i < e; ++i) sum += qd[i].ncand;
+    int run = block_scan_excl(sum, tmp);
+    if (threadIdx.x == T - 1) tot = run + sum;
+    for (int i = b; i < e; ++i) { cand_off[i] = run; run += qd[i].ncand; }
+    __syncthreads();
+    if (threadIdx.x == 0) cand_off[nq] = tot;
+    // pass 2: chunk offsets, skipping slots whose region overflows the pool
+    sum = 0;
+    for (int i = b; i < e; ++i) {
+        int n = qd[i].ncand;
+        bool fits = cand_off[i] + n <= pool_cap;
+        if (!fits) qd[i].flags |= QF_RESULT_OVERFLOW;
+        sum += fits ? (n + VERIFY_CHUNK - 1) / VERIFY_CHUNK : 0;
+    }
+    run = block_scan_excl(sum, tmp);
+    if (threadIdx.x == T - 1) tot = run + sum;
+    for (int i = b; i < e; ++i) {
+        chunk_off[i] = run;
+        int n = qd[i].ncand;
+        if (!(qd[i].flags & QF_RESULT_OVERFLOW)) run += (n + VERIFY_CHUNK - 1) / VERIFY_CHUNK;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) chunk_off[nq] = tot;
+}
+
+__global__ void scan_counts_kernel(const int* res_count, int nq, int* out_off)
+{
+    __shared__ int tmp[32];
+    __shared__ int tot;
+    const int T = blockDim.x;
+    const int per = (nq + T - 1) / T;
+    const int b = threadIdx.x * per, e = min(nq, b + per);
+    int sum = 0;
+    for (int i = b; i < e; ++i) sum += res_count[i];
+    int run = block_scan_excl(sum, tmp);
+    if (threadIdx.x == T - 1) tot = run + sum;
+    for (int i = b; i < e; ++i) { out_off[i] = run; run += res_count[i]; }
+    __syncthreads();
+    if (threadIdx.x == 0) out_off[nq] = tot;
+}
+
+// ---------------------------------------------------------------- finalize
+namespace {
+__device__ __forceinline__ unsigned okey(int v) { return (unsigned)v ^ 0x80000000u; }
+
+// stable LSD radix pass of one block over global memory (256 threads)
+__device__ void block_radix_pass(const unsigned* in, unsigned* out, int n, int shift,
+                                 unsigned* hist, unsigned (*wc)[256])
+{
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    hist[tid] = 0;
+    __syncthreads();
+    for (int i = tid; i < n; i += 256) atomicAdd(&hist[(in[i] >> shift) & 255], 1u);
+    __syncthreads();
+    // exclusive scan of the 256 bins (thread tid owns bin tid)
+    unsigned v = hist[tid], x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned y = __shfl_up_sync(FULL, x, o);
+        if (lane >= o) x += y;
+    }
+    __shared__ unsigned wsum[8];
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    unsigned add = 0;
+    for (int j = 0; j < w; ++j) add += wsum[j];
+    __syncthreads();
+    hist[tid] = x - v + add;     // running base of digit tid
+    __syncthreads();
+    for (int t0 = 0; t0 < n; t0 += 256) {
+        int i = t0 + tid;
+        bool ok = i < n;
+        unsigned key = ok ? in[i] : 0u;
+        unsigned dg = ok ? (key >> shift) & 255 : 256u;
+        unsigned mm = __match_any_sync(FULL, dg);
+        int rank = __popc(mm & ((1u << lane) - 1));
+        for (int j = 0; j < 8; ++j) wc[w][lane * 8 + j] = 0;
+        __syncwarp();
+        if (ok && rank == 0) wc[w][dg] = __popc(mm);
+        __syncthreads();
+        {   // per digit: prefix over warps
+            unsigned acc = hist[tid];
+            for (int j = 0; j < 8; ++j) { unsigned c = wc[j][tid]; wc[j][tid] = acc; acc += c; }
+            hist[tid] = acc;
+        }
+        __syncthreads();
+        if (ok) out[wc[w][dg] + rank] = key;
+        __syncthreads();
+    }
+}
+}  // namespace
+
+__global__ void __launch_bounds__(256)
+finalize_kernel(int* res_pool, const int* cand_off, const int* res_count, const int* out_off,
+                int* out, int nq)
+{
+    extern __shared__ unsigned skeys[];
+    const int s = blockIdx.x;
+    if (s >= nq) return;
+    const int n = res_count[s];
+    unsigned* src = (unsigned*)(res_pool + cand_off[s]);
+    unsigned* dst = (unsigned*)(out + out_off[s]);
+    const int tid = threadIdx.x;
+    if (n <= SORT_CAP) {
+        int P = 1;
+        while (P < n) P <<= 1;
+        for (int i = tid; i < P; i += blockDim.x) skeys[i] = i < n ? okey((int)src[i]) : 0xffffffffu;
+        __syncthreads();
+        for (int kk = 2; kk <= P; kk <<= 1) {
+            for (int j = kk >> 1; j > 0; j >>= 1) {
+                for (int i = tid; i < P; i += blockDim.x) {
+                    int ixj = i ^ j;
+                    if (ixj > i) {
+                        unsigned a = skeys[i], b = skeys[ixj];
+                        bool up = (i & kk) == 0;
+                        if ((a > b) == up) { skeys[i] = b; skeys[ixj] = a; }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (int i = tid; i < n; i += blockDim.x) dst[i] = skeys[i] ^ 0x80000000u;
+        return;
+    }
+    // large result set: four stable LSD passes between the pool region and out
+    __shared__ unsigned hist[256];
+    __shared__ unsigned wc[8][256];
+    for (int i = tid; i < n; i += blockDim.x) src[i] = okey((int)src[i]);
+    __syncthreads();
+    block_radix_pass(src, dst, n, 0, hist, wc);
+    __syncthreads();
+    block_radix_pass(dst, src, n, 8, hist, wc);
+    __syncthreads();
+    block_radix_pass(src, dst, n, 16, hist, wc);
+    __syncthreads();
+    block_radix_pass(dst, src, n, 24, hist, wc);
+    __syncthreads();
+    for (int i = tid; i < n; i += blockDim.x) dst[i] = src[i] ^ 0x80000000u;
+}
+
+}  // namespace rknn

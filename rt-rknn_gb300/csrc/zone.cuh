@@ -1,0 +1,102 @@
+// Influence-zone kernel interface: capacities, per-warp state layout, args.
+#pragma once
+#include "rknn_common.cuh"
+
+namespace rknn {
+
+constexpr int ZONE_WARPS = 1;          // warps (queries in flight) per block
+
+// Per-query capacities of the zone state.  Measured on uniform data
+// (100k facilities): about 4.6k bisectors and at most ~4k^2 live vertices
+// for k in 1..50.
+struct ZoneCaps {
+    int vc;   // vertices
+    int lc;   // bisectors
+    int pc;   // priority-queue entries
+    int rm;   // user-cell ring scan radius (cells)
+};
+
+struct ZoneLayout {
+    size_t vx, vy, vd2, vx32, vy32, vcnt, vfl, cons;
+    size_t la, lb, la32, lb32, lb3, lfl, lpos;
+    size_t pqk, pqc;
+    size_t cx, cy, cx32, cy32, ccnt, cfl;
+    size_t tk, tc, sc;
+    size_t bytes;
+};
+
+__host__ __device__ inline size_t zl_align(size_t x) { return (x + 15) & ~(size_t)15; }
+
+__host__ __device__ inline ZoneLayout zone_layout(const ZoneCaps& c)
+{
+    ZoneLayout L;
+    size_t o = 0;
+    const size_t VC = c.vc, LC = c.lc, PC = c.pc, CC = (size_t)c.lc + 4;
+    const size_t W = 2 * (size_t)c.rm + 1;
+    const size_t bm = ((W * W + 31) / 32) * 4;
+    L.vx = o;   o = zl_align(o + (8 * VC > bm ? 8 * VC : bm));
+    L.vy = o;   o = zl_align(o + 8 * VC);
+    L.vd2 = o;  o = zl_align(o + 8 * VC);
+    L.vx32 = o; o = zl_align(o + 4 * VC);
+    L.vy32 = o; o = zl_align(o + 4 * VC);
+    L.vcnt = o; o = zl_align(o + 4 * VC);
+    L.vfl = o;  o = zl_align(o + VC);
+    L.cons = o; o = zl_align(o + 4 * VC);
+    L.la = o;   o = zl_align(o + 8 * LC);
+    L.lb = o;   o = zl_align(o + 8 * LC);
+    L.la32 = o; o = zl_align(o + 4 * LC);
+    L.lb32 = o; o = zl_align(o + 4 * LC);
+    L.lb3 = o;  o = zl_align(o + 4 * LC);
+    L.lfl = o;  o = zl_align(o + LC);
+    L.lpos = o; o = zl_align(o + 4 * LC);
+    L.pqk = o;  o = zl_align(o + 8 * PC);
+    L.pqc = o;  o = zl_align(o + 4 * PC);
+    L.cx = o;   o = zl_align(o + (8 * CC > 16 * LC ? 8 * CC : 16 * LC));   // also float4 planes
+    L.cy = o;   o = zl_align(o + 8 * CC);
+    L.cx32 = o; o = zl_align(o + 4 * CC);
+    L.cy32 = o; o = zl_align(o + 4 * CC);
+    L.ccnt = o; o = zl_align(o + 4 * CC);
+    L.cfl = o;  o = zl_align(o + CC);
+    L.tk = o;   o = zl_align(o + 8 * 32);
+    L.tc = o;   o = zl_align(o + 4 * 32);
+    L.sc = o;   o = zl_align(o + 128);
+    L.bytes = o;
+    return L;
+}
+
+struct ZoneArgs {
+    // facility index
+    const float2* fxy;       // cell-sorted facility coordinates
+    const int* fstart;       // facility cell starts (gf.gx*gf.gy+1)
+    const float4* fmbr;      // per-cell MBR (minx, miny, maxx, maxy)
+    const int* fpos;         // input index -> cell-sorted position
+    Grid gf;
+    int nf;
+    // user index
+    const int* ustart;       // user cell starts (gu.gx*gu.gy+1)
+    Grid gu;
+    int nu;
+    double sx0, sy0, sx1, sy1;   // bounding box of all points (the zone's space)
+    // batch
+    const int* q_in;         // facility input index per query slot
+    const int* k_in;
+    const int* order;        // processing order of slots (may be null)
+    int nq;
+    int* work_counter;
+    ZoneCaps caps;
+    int use_global;          // zone state in global scratch instead of shared memory
+    char* gscratch;
+    int skip_coincident;
+    int rmax;                // == caps.rm
+    int seg_cap;             // segments per query slot (>= 2*rmax+2)
+    // outputs (per slot)
+    QDesc* qd;
+    float4* planes;          // [slot][caps.lc]
+    int* bis_pos;            // [slot][caps.lc] facility positions of the bisectors
+    int2* segs;              // [slot][seg_cap]: (user start, candidate offset)
+    ZStats* zst;
+};
+
+__global__ void zone_kernel(ZoneArgs a);
+
+}  // namespace rknn

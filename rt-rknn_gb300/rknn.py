@@ -1,0 +1,288 @@
+"""Python binding of the engine's C ABI (include/rknn_gpu.h), via ctypes.
+
+The reference's only interface is its command line (`-if <file> -k <k> -q
+<index>`, rknn-inf/inf.cpp:38-119) and the counts it prints.  This module
+mirrors it for Python callers and tests:
+
+    idx = Index(fxy, uxy, fid, uid)            # rknn_index_create
+    ids = idx.query(q, k)                      # one -q/-k run: sorted user ids
+    res = idx.query_batch(qs, ks)              # many queries, one launch
+    main(["-if", path, "-k", "5", "-q", "3"])  # the command line itself
+
+Errors raise RkNNError carrying the library's status and message; nothing
+falls back to the CPU: if the shared library or a GPU is missing, the calls
+fail.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librknn_gb300.so")
+
+MODE_FP64 = 0
+MODE_FP32 = 1
+_MODES = {"fp64": MODE_FP64, "fp32": MODE_FP32, MODE_FP64: MODE_FP64, MODE_FP32: MODE_FP32}
+
+STATUS = {0: "RKNN_OK", 1: "RKNN_ERR_ARG", 2: "RKNN_ERR_OOM", 3: "RKNN_ERR_CUDA",
+          4: "RKNN_ERR_TIMEOUT", 5: "RKNN_ERR_CAPACITY", 6: "RKNN_ERR_STATE"}
+
+# every symbol include/rknn_gpu.h declares
+EXPORTS = ["rknn_index_opts_default", "rknn_index_create", "rknn_index_destroy",
+           "rknn_index_size", "rknn_index_get_info", "rknn_query", "rknn_query_batch", "rknn_query_batch_device",
+           "rknn_batch_device_results", "rknn_sync", "rknn_set_stream", "rknn_last_stats",
+           "rknn_last_zone", "rknn_set_profiling", "rknn_last_kernel_ms",
+           "rknn_last_error", "rknn_version"]
+
+
+class RkNNError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Opts(C.Structure):
+    _fields_ = [("device", C.c_int32), ("fac_per_cell", C.c_float), ("usr_per_cell", C.c_float),
+                ("skip_coincident", C.c_int32), ("reserved", C.c_int32 * 6)]
+
+
+class Info(C.Structure):
+    _fields_ = [("nf", C.c_int64), ("nu", C.c_int64), ("x0", C.c_double), ("y0", C.c_double),
+                ("x1", C.c_double), ("y1", C.c_double),
+                ("fgrid_x0", C.c_float), ("fgrid_y0", C.c_float), ("fgrid_inv", C.c_float),
+                ("fgrid_gx", C.c_int32), ("fgrid_gy", C.c_int32),
+                ("ugrid_x0", C.c_float), ("ugrid_y0", C.c_float), ("ugrid_inv", C.c_float),
+                ("ugrid_gx", C.c_int32), ("ugrid_gy", C.c_int32)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class Stats(C.Structure):
+    _fields_ = [("queries", C.c_int64), ("results", C.c_int64), ("bisectors", C.c_int64),
+                ("zone_vertices_max", C.c_int64), ("zone_candidates", C.c_int64),
+                ("zone_fp64", C.c_int64), ("candidates", C.c_int64), ("plane_evals", C.c_int64),
+                ("survivors", C.c_int64), ("fac_checks", C.c_int64), ("rechecks", C.c_int64),
+                ("overflow", C.c_int64), ("device_ms", C.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the shared library (built by rt-rknn_gb300/build.py)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RkNNError(3, f"engine library not built: {path}")
+    L = C.CDLL(path)
+    vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
+    L.rknn_index_opts_default.argtypes = [C.POINTER(Opts)]
+    L.rknn_index_opts_default.restype = None
+    L.rknn_index_create.argtypes = [vp, vp, i64, vp, vp, i64, C.POINTER(Opts), C.POINTER(vp)]
+    L.rknn_index_destroy.argtypes = [vp]
+    L.rknn_index_size.argtypes = [vp, C.POINTER(i64), C.POINTER(i64)]
+    L.rknn_index_get_info.argtypes = [vp, C.POINTER(Info)]
+    L.rknn_query.argtypes = [vp, i32, i32, i32, vp, i64, C.POINTER(i64), C.POINTER(Stats)]
+    L.rknn_query_batch.argtypes = [vp, vp, vp, i32, i32, vp, i64, vp, C.POINTER(Stats)]
+    L.rknn_query_batch_device.argtypes = [vp, vp, vp, i32, i32, i32]
+    L.rknn_batch_device_results.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
+    L.rknn_sync.argtypes = [vp]
+    L.rknn_set_stream.argtypes = [vp, vp]
+    L.rknn_last_stats.argtypes = [vp, C.POINTER(Stats)]
+    L.rknn_last_zone.argtypes = [vp, i32, vp, i32, C.POINTER(i32), C.POINTER(i32)]
+    L.rknn_set_profiling.argtypes = [vp, i32]
+    L.rknn_last_kernel_ms.argtypes = [vp, vp]
+    L.rknn_last_error.restype = C.c_char_p
+    L.rknn_version.restype = C.c_char_p
+    for name in EXPORTS:
+        fn = getattr(L, name)
+        if name not in ("rknn_last_error", "rknn_version", "rknn_index_opts_default"):
+            fn.restype = C.c_int
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise RkNNError(rc, load().rknn_last_error().decode())
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data if a is not None and a.size else None
+
+
+class Index:
+    """Device-resident facility/user grid index (rknn_index_create)."""
+
+    def __init__(self, fxy, uxy, fid=None, uid=None, device: int = 0,
+                 fac_per_cell: float = 0.0, usr_per_cell: float = 0.0,
+                 skip_coincident: bool = True):
+        L = load()
+        self.fxy = np.ascontiguousarray(fxy, dtype=np.float32).reshape(-1, 2)
+        self.uxy = np.ascontiguousarray(uxy, dtype=np.float32).reshape(-1, 2)
+        nf, nu = self.fxy.shape[0], self.uxy.shape[0]
+        self.fid = (np.ascontiguousarray(fid, dtype=np.int32) if fid is not None
+                    else np.arange(nf, dtype=np.int32))
+        self.uid = (np.ascontiguousarray(uid, dtype=np.int32) if uid is not None
+                    else np.arange(nf, nf + nu, dtype=np.int32))
+        o = Opts()
+        L.rknn_index_opts_default(C.byref(o))
+        o.device = device
+        if fac_per_cell:
+            o.fac_per_cell = fac_per_cell
+        if usr_per_cell:
+            o.usr_per_cell = usr_per_cell
+        o.skip_coincident = 1 if skip_coincident else 0
+        h = C.c_void_p()
+        _check(L.rknn_index_create(_ptr(self.fxy), _ptr(self.fid), nf, _ptr(self.uxy),
+                                   _ptr(self.uid), nu, C.byref(o), C.byref(h)))
+        self.h = h
+        self.nf, self.nu = nf, nu
+
+    @classmethod
+    def of(cls, ds, **kw):
+        return cls(ds.fxy, ds.uxy, ds.fid, ds.uid, **kw)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().rknn_index_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def query(self, q: int, k: int, mode="fp64", stats: bool = False):
+        """Sorted user ids of RkNN_k(q) (rknn_query: one query, one launch)."""
+        L = load()
+        cap = max(16, self.nu)
+        out = np.empty(cap, np.int32)
+        n = C.c_int64(0)
+        st = Stats()
+        _check(L.rknn_query(self.h, int(q), int(k), _MODES[mode], out.ctypes.data, cap,
+                            C.byref(n), C.byref(st) if stats else None))
+        ids = out[: n.value].copy()
+        return (ids, st.as_dict()) if stats else ids
+
+    def query_batch(self, qs, ks, mode="fp32", stats: bool = False):
+        """List of sorted id arrays, one per query (rknn_query_batch)."""
+        L = load()
+        qs = np.ascontiguousarray(qs, dtype=np.int32)
+        ks = np.ascontiguousarray(np.broadcast_to(np.asarray(ks, np.int32), qs.shape), dtype=np.int32)
+        nq = qs.shape[0]
+        off = np.zeros(nq + 1, np.int64)
+        cap = getattr(self, "_cap", 1 << 16)
+        st = Stats()
+        while True:
+            out = np.empty(max(cap, 1), np.int32)
+            rc = L.rknn_query_batch(self.h, _ptr(qs), _ptr(ks), nq, _MODES[mode], out.ctypes.data,
+                                    cap, off.ctypes.data, C.byref(st) if stats else None)
+            if rc == 5 and off[-1] > cap:
+                cap = int(off[-1])
+                self._cap = cap
+                continue
+            _check(rc)
+            break
+        res = [out[off[i]:off[i + 1]].copy() for i in range(nq)]
+        return (res, st.as_dict()) if stats else res
+
+    def last_zone(self, slot: int = 0):
+        """(facility indices of the bisectors in creation order, flags)."""
+        L = load()
+        n = C.c_int32(0)
+        fl = C.c_int32(0)
+        buf = np.zeros(1 << 16, np.int32)
+        _check(L.rknn_last_zone(self.h, int(slot), buf.ctypes.data, buf.size, C.byref(n), C.byref(fl)))
+        return buf[: min(n.value, buf.size)].copy(), fl.value
+
+    def set_profiling(self, on: bool):
+        _check(load().rknn_set_profiling(self.h, 1 if on else 0))
+
+    def kernel_ms(self):
+        """Per-kernel device ms of the last profiled call: zone, plan, verify,
+        result offsets, finalize."""
+        ms = np.zeros(5, np.float64)
+        _check(load().rknn_last_kernel_ms(self.h, ms.ctypes.data))
+        return dict(zip(("zone", "plan", "verify", "offsets", "finalize"), ms.tolist()))
+
+    def set_stream(self, stream_handle: int | None):
+        _check(load().rknn_set_stream(self.h, C.c_void_p(stream_handle or 0)))
+
+    def sync(self):
+        _check(load().rknn_sync(self.h))
+
+    def query_batch_device(self, d_q: int, d_k: int, nq: int, kmax: int, mode="fp32"):
+        """Enqueue a batch whose q/k arrays are already on the device."""
+        _check(load().rknn_query_batch_device(self.h, C.c_void_p(d_q), C.c_void_p(d_k), int(nq),
+                                              int(kmax), _MODES[mode]))
+
+    def device_results(self):
+        ids, off = C.c_void_p(), C.c_void_p()
+        _check(load().rknn_batch_device_results(self.h, C.byref(ids), C.byref(off)))
+        return ids.value, off.value
+
+    def info(self):
+        inf = Info()
+        _check(load().rknn_index_get_info(self.h, C.byref(inf)))
+        return inf.as_dict()
+
+    def last_stats(self):
+        st = Stats()
+        _check(load().rknn_last_stats(self.h, C.byref(st)))
+        return st.as_dict()
+
+
+def main(argv=None) -> int:
+    """The reference's command line (`-if <file> -k <k> -q <index>`), with the
+    result set written to log/<mode>_k<k>_q<q>.txt."""
+    import argparse
+    import time
+    sys.path.insert(0, HERE)
+    import datagen
+    p = argparse.ArgumentParser(prog="rknn")
+    p.add_argument("-if", "--infile", dest="infile", required=True)
+    p.add_argument("-k", type=int, default=4)
+    p.add_argument("-q", type=int, default=0)
+    p.add_argument("-al", "--algorithm", default="all")
+    p.add_argument("--mode", default="fp64", choices=["fp64", "fp32"])
+    p.add_argument("--log", default="log")
+    a = p.parse_args(argv)
+    if a.k <= 0:
+        print(f"Invalid value for k: {a.k}. It must be a positive integer.", file=sys.stderr)
+        return 1
+    print("Loading data...")
+    ds = datagen.read_text(a.infile)
+    print(f"Loaded {ds.nf} facilities and {ds.nu} users.")
+    t0 = time.time()
+    with Index.of(ds) as idx:
+        print(f"Grid index is built in {time.time() - t0:g}[s].\n")
+        t0 = time.time()
+        ids, st = idx.query(a.q, a.k, a.mode, stats=True)
+        print(f"Total bisectors created: {st['bisectors']}")
+        print(f"Found {len(ids)} RkNN results.")
+        print(f"Total time: {time.time() - t0:g}[s].\n")
+    os.makedirs(a.log, exist_ok=True)
+    with open(os.path.join(a.log, f"{a.mode}_k{a.k}_q{a.q}.txt"), "w") as fh:
+        fh.writelines(f"{int(i)}\n" for i in ids)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,181 @@
+"""GPU parity: the engine through its C ABI against the exact oracle, the
+reference's golden vectors and the rknn-inf restatement.  Results are
+integer id sets: equality is bit-exact."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import datagen
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+MODES = ("fp64", "fp32")
+
+
+@pytest.fixture(scope="module")
+def c1(engine):
+    ds = datagen.uniform(1000, 10000, seed=1, nq=10, k=5)
+    return ds, engine.Index.of(ds), O.Oracle.of(ds)
+
+
+def test_handmade_cases(engine, golden_dir):
+    for c in json.load(open(os.path.join(golden_dir, "handmade.json"))):
+        idx = engine.Index(np.array(c["fxy"], np.float32), np.array(c["uxy"], np.float32),
+                           c["fid"], c["uid"])
+        keys = list(c["expect"])
+        for mode in MODES:
+            for key in keys:
+                q, k = map(int, key.split(","))
+                assert idx.query(q, k, mode).tolist() == c["expect"][key], (c["name"], key, mode)
+            qs = [int(kk.split(",")[0]) for kk in keys]
+            ks = [int(kk.split(",")[1]) for kk in keys]
+            got = idx.query_batch(qs, ks, mode)
+            assert [g.tolist() for g in got] == [c["expect"][kk] for kk in keys], (c["name"], mode)
+        idx.close()
+
+
+def test_config1_single_and_batch(c1):
+    ds, idx, o = c1
+    want = [o.query(int(q), 5) for q in ds.queries]
+    for mode in MODES:
+        for q, w in zip(ds.queries, want):
+            assert np.array_equal(idx.query(int(q), 5, mode), w), (q, mode)
+        got = idx.query_batch(ds.queries, 5, mode)
+        assert all(np.array_equal(g, w) for g, w in zip(got, want)), mode
+
+
+def test_integer_twin_against_naive_golden(engine, golden_dir):
+    g = json.load(open(os.path.join(golden_dir, "naive_int_1k10k.json")))
+    z = np.load(os.path.join(golden_dir, "uniform_int_1k10k.npz"))
+    idx = engine.Index(z["fxy"], z["uxy"], z["fid"], z["uid"])
+    o = O.Oracle(z["fxy"], z["uxy"], z["fid"], z["uid"])
+    qs = [int(q) for q in g["ids"]]
+    for mode in MODES:
+        got = idx.query_batch(qs, g["k"], mode)
+        for q, res in zip(qs, got):
+            assert np.array_equal(res, o.query(q, g["k"])), (q, mode)
+            # strict-< only adds users that rknn-naive drops on an exact tie
+            assert set(g["ids"][str(q)]) <= set(res.tolist())
+
+
+def test_inf_golden_superset(engine, golden_dir):
+    g = json.load(open(os.path.join(golden_dir, "inf_float_1k10k.json")))
+    z = np.load(os.path.join(golden_dir, "uniform_1k10k.npz"))
+    idx = engine.Index(z["fxy"], z["uxy"], z["fid"], z["uid"])
+    for q, ids in g["ids"].items():
+        res = idx.query(int(q), g["k"], "fp32")
+        assert set(res.tolist()) <= set(ids)
+
+
+def test_mixed_k_batch(engine):
+    ds = datagen.uniform(5000, 50000, seed=12, nq=300, k=1)
+    rng = np.random.default_rng(3)
+    ks = rng.integers(1, 41, size=ds.queries.shape[0]).astype(np.int32)
+    idx = engine.Index.of(ds)
+    o = O.Oracle.of(ds)
+    got32 = idx.query_batch(ds.queries, ks, "fp32")
+    got64 = idx.query_batch(ds.queries[:60], ks[:60], "fp64")
+    for i, q in enumerate(ds.queries):
+        w = o.query(int(q), int(ks[i]))
+        assert np.array_equal(got32[i], w), (q, ks[i])
+        if i < 60:
+            assert np.array_equal(got64[i], w), (q, ks[i])
+
+
+def test_gaussmix_ties_and_duplicates(engine):
+    ds = datagen.gaussmix(20_000, 400_000, seed=3, nq=200, k=10)
+    idx = engine.Index.of(ds)
+    o = O.Oracle.of(ds)
+    got, st = idx.query_batch(ds.queries, 10, "fp32", stats=True)
+    for q, res in zip(ds.queries, got):
+        assert np.array_equal(res, o.query(int(q), 10)), q
+    assert st["rechecks"] > 0          # exact ties reached the exact predicate
+    got64 = idx.query_batch(ds.queries[:50], 10, "fp64")
+    for q, res in zip(ds.queries[:50], got64):
+        assert np.array_equal(res, o.query(int(q), 10)), q
+
+
+def test_street_large_k(engine):
+    ds = datagen.street(nu=200_000, nf=2000, seed=4, nq=80)
+    idx = engine.Index.of(ds)
+    o = O.Oracle.of(ds)
+    got = idx.query_batch(ds.queries, ds.ks, "fp32")
+    for q, k, res in zip(ds.queries, ds.ks, got):
+        assert np.array_equal(res, o.query(int(q), int(k))), (q, k)
+
+
+def test_zone_bisectors_match_port(engine):
+    """Same grid, same rules: the zone kernel builds rknn-inf's bisector set
+    in the same order as the CPU restatement does."""
+    for nf, nu, k in ((1000, 10000, 5), (20000, 200000, 10), (20000, 200000, 3)):
+        ds = datagen.uniform(nf, nu, seed=31 + k, nq=40, k=k)
+        idx = engine.Index.of(ds)
+        info = idx.info()
+        port = O.InfPort(ds.fxy, ds.uxy, grid=(info["fgrid_x0"], info["fgrid_y0"], info["fgrid_inv"],
+                                               info["fgrid_gx"], info["fgrid_gy"]))
+        idx.query_batch(ds.queries, k, "fp32")
+        same = 0
+        for slot, q in enumerate(ds.queries):
+            gb, flags = idx.last_zone(slot)
+            pb, _, _ = port.query(int(q), k, verify=False)
+            same += np.array_equal(gb, pb)
+            assert flags & 7 == 0
+        assert same == len(ds.queries), (nf, k, same)
+
+
+def test_full_scale_checksum(engine):
+    """Config 2 sizes (100k facilities, 1M users): every facility as a query;
+    without distance ties each user lies in exactly k result sets, so the
+    result sizes sum to k * |U|."""
+    ds = datagen.uniform(100_000, 1_000_000, seed=2, nq=1000, k=10)
+    idx = engine.Index.of(ds)
+    allq = np.arange(ds.nf, dtype=np.int32)
+    for k in (1, 10):
+        got = idx.query_batch(allq, k, "fp32")
+        assert sum(len(g) for g in got) == k * ds.nu, k
+    sub = ds.queries[:200]
+    a = idx.query_batch(sub, 10, "fp32")
+    b = idx.query_batch(sub, 10, "fp64")
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
+    o = O.Oracle.of(ds)
+    for q, res in zip(sub[:20], a[:20]):
+        assert np.array_equal(res, o.query(int(q), 10)), q
+
+
+def test_argument_errors(engine, c1):
+    ds, idx, _ = c1
+    with pytest.raises(engine.RkNNError) as e:
+        idx.query(ds.nf, 3)
+    assert e.value.status == 1
+    with pytest.raises(engine.RkNNError) as e:
+        idx.query(0, 0)
+    assert e.value.status == 1
+    with pytest.raises(engine.RkNNError) as e:
+        idx.query_batch([0, -1], 3)
+    assert e.value.status == 1
+
+
+def test_edge_cases(engine):
+    rng = np.random.default_rng(8)
+    f = rng.uniform(0, 100, (30, 2)).astype(np.float32)
+    u = rng.uniform(0, 100, (500, 2)).astype(np.float32)
+    # no users
+    idx = engine.Index(f, np.zeros((0, 2), np.float32))
+    assert idx.query(3, 2).size == 0
+    # one facility: every user
+    idx = engine.Index(f[:1], u)
+    assert idx.query(0, 1).size == 500
+    # k >= |F|: every user
+    idx = engine.Index(f, u)
+    assert idx.query(5, 30).size == 500 and idx.query(5, 31, "fp32").size == 500
+    # all users on one point, duplicated facilities
+    f2 = np.concatenate([f, f[:5]])
+    u2 = np.repeat(u[:1], 300, 0)
+    idx = engine.Index(f2, u2)
+    o = O.Oracle(f2, u2)
+    for q in (0, 2, 31, 33):
+        for k in (1, 2, 6):
+            assert np.array_equal(idx.query(q, k), o.query(q, k)), (q, k)

@@ -1,0 +1,136 @@
+"""The oracle against the reference's own outputs (golden vectors) and
+against exact rational arithmetic."""
+import json
+import os
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+import datagen
+import oracle as O
+
+
+def load_npz(golden_dir, name):
+    z = np.load(os.path.join(golden_dir, name))
+    return datagen.Dataset(z["fxy"], z["uxy"], z["fid"], z["uid"], z["queries"], z["ks"])
+
+
+def test_naive_int_1k10k_bit_exact(golden_dir):
+    """Naive tie mode reproduces rknn-naive's result sets exactly."""
+    g = json.load(open(os.path.join(golden_dir, "naive_int_1k10k.json")))
+    ds = load_npz(golden_dir, "uniform_int_1k10k.npz")
+    o = O.Oracle.of(ds)
+    for q, ids in g["ids"].items():
+        assert np.array_equal(o.query(int(q), g["k"], tie="naive"), np.array(ids)), q
+        strict = o.query(int(q), g["k"])
+        # strict-< differs from naive only where naive breaks a tie against q
+        assert set(ids) <= set(strict.tolist())
+
+
+def test_naive_int_10k100k_bit_exact(golden_dir):
+    g = json.load(open(os.path.join(golden_dir, "naive_int_10k100k.json")))
+    ds = datagen.uniform(g["nf"], g["nu"], seed=g["seed"], nq=8, k=g["k"], integer=True)
+    import hashlib
+    h = hashlib.sha256()
+    for a in (ds.fxy, ds.uxy, ds.fid, ds.uid):
+        h.update(np.ascontiguousarray(a).tobytes())
+    if h.hexdigest() != g["sha256"]:
+        pytest.skip("numpy generates a different stream here; fixture inputs not reproducible")
+    o = O.Oracle.of(ds)
+    for q, ids in g["ids"].items():
+        assert np.array_equal(o.query(int(q), g["k"], tie="naive"), np.array(ids)), q
+
+
+def test_inf_float_superset(golden_dir):
+    """rknn-inf over-reports (never under-reports) on float data."""
+    g = json.load(open(os.path.join(golden_dir, "inf_float_1k10k.json")))
+    ds = load_npz(golden_dir, "uniform_1k10k.npz")
+    o = O.Oracle.of(ds)
+    extra = 0
+    for q, ids in g["ids"].items():
+        exact = o.query(int(q), g["k"])
+        assert set(exact.tolist()) <= set(ids)
+        extra += len(ids) - len(exact)
+    assert extra >= 0
+
+
+def test_handmade_cases(golden_dir):
+    cases = json.load(open(os.path.join(golden_dir, "handmade.json")))
+    for c in cases:
+        o = O.Oracle(np.array(c["fxy"], np.float32), np.array(c["uxy"], np.float32),
+                     c["fid"], c["uid"])
+        for key, want in c["expect"].items():
+            q, k = map(int, key.split(","))
+            assert o.query(q, k).tolist() == want, (c["name"], key)
+            # the reference naive binary on the same file
+            assert o.query(q, k, tie="naive").tolist() == c["reference"][key]["naive"], (c["name"], key)
+
+
+def test_grid_oracle_matches_brute_force():
+    rng = np.random.default_rng(11)
+    for trial in range(4):
+        nf, nu = int(rng.integers(2, 60)), int(rng.integers(1, 400))
+        fxy = rng.uniform(0, 50, (nf, 2)).astype(np.float32)
+        uxy = rng.uniform(0, 50, (nu, 2)).astype(np.float32)
+        if trial % 2:          # integer lattice: many exact ties
+            fxy, uxy = np.rint(fxy), np.rint(uxy)
+        o = O.Oracle(fxy, uxy)
+        for q in range(0, nf, max(1, nf // 5)):
+            for k in (1, 2, 5, nf):
+                assert np.array_equal(o.flags(q, k), O.brute_flags(fxy, uxy, q, k)), (trial, q, k)
+
+
+def _exact_sign(u, f, q):
+    U = [Fraction(float(v)) for v in u]
+    F = [Fraction(float(v)) for v in f]
+    Q = [Fraction(float(v)) for v in q]
+    d = (U[0] - F[0]) ** 2 + (U[1] - F[1]) ** 2 - (U[0] - Q[0]) ** 2 - (U[1] - Q[1]) ** 2
+    return (d > 0) - (d < 0)
+
+
+def test_exact_predicate_vs_rationals():
+    rng = np.random.default_rng(5)
+    pts = rng.uniform(-1000, 1000, (300, 6)).astype(np.float32)
+    # near-ties: u on the bisector of q and f up to float rounding
+    q = rng.uniform(0, 1000, (300, 2)).astype(np.float32)
+    f = (q + rng.normal(0, 5, (300, 2))).astype(np.float32)
+    m = (q.astype(np.float64) + f) / 2
+    perp = np.stack([-(f[:, 1] - q[:, 1]), f[:, 0] - q[:, 0]], 1)
+    u = (m + rng.uniform(-3, 3, (300, 1)) * perp).astype(np.float32)
+    near = np.concatenate([u, f, q], 1)
+    tiny = rng.uniform(-1e-30, 1e-30, (100, 6)).astype(np.float32)
+    mixed = np.concatenate([rng.uniform(0, 1000, (100, 4)), rng.uniform(-1e-20, 1e-20, (100, 2))], 1).astype(np.float32)
+    for row in np.concatenate([pts, near, tiny, mixed]):
+        want = _exact_sign(row[0:2], row[2:4], row[4:6])
+        assert O.sign_d2diff(row[0:2], row[2:4], row[4:6]) == want
+        assert O.sign_d2diff(row[0:2], row[2:4], row[4:6], expansion_only=True) == want
+
+
+def test_gaussmix_ties_are_exact():
+    """The precision workload's bisector users are exactly equidistant."""
+    ds = datagen.gaussmix(2000, 20000, seed=3, nq=50, k=10)
+    assert ds.ties.shape[0] > 100
+    for u, q, f in ds.ties[:300]:
+        assert O.sign_d2diff(ds.uxy[u], ds.fxy[f], ds.fxy[q]) == 0
+    _, counts = np.unique(ds.uxy, axis=0, return_counts=True)
+    assert (counts > 1).sum() >= 10          # duplicated coordinates
+
+
+def test_text_round_trip(tmp_path):
+    ds = datagen.uniform(50, 300, seed=9)
+    p = tmp_path / "d.txt"
+    datagen.write_text(p, ds)
+    back = datagen.read_text(p)
+    assert np.array_equal(back.fxy, ds.fxy) and np.array_equal(back.uxy, ds.uxy)
+    assert np.array_equal(back.fid, ds.fid) and np.array_equal(back.uid, ds.uid)
+    # every written coordinate parses to exactly the float32 value as a double
+    vals = [float(t) for line in open(p).read().split("\n")[1:51] for t in line.split()[1:]]
+    assert all(float(np.float32(v)) == v for v in vals)
+
+
+def test_street_layout():
+    ds = datagen.street(nu=20000, nf=500, seed=4, nq=64)
+    assert ds.fxy.shape == (500, 2) and ds.uxy.shape == (20000, 2)
+    assert ds.ks.min() >= 1 and ds.ks.max() <= 100
+    assert (ds.uxy >= 0).all() and (ds.uxy <= 1000).all()

@@ -1,0 +1,65 @@
+"""CPU-side checks: the rknn-inf restatement against the reference binary's
+own outputs, the exported C ABI, and the command line's argument handling."""
+import json
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import datagen
+import oracle as O
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_inf_port_matches_reference_binary(golden_dir):
+    """Over an 8-entry R-tree the port reproduces rknn-inf's bisector counts
+    and result sets (golden vectors from the reference binary)."""
+    g = json.load(open(os.path.join(golden_dir, "inf_float_1k10k.json")))
+    z = np.load(os.path.join(golden_dir, "uniform_1k10k.npz"))
+    port = O.InfPort(z["fxy"], z["uxy"], uid=z["uid"])
+    for q, ids in g["ids"].items():
+        bis, res, st = port.query(int(q), g["k"], skip_coincident=False)
+        assert st["bisectors"] == g["bisectors"][q], q
+        assert res.tolist() == ids, q
+
+
+def test_inf_port_superset_of_exact():
+    ds = datagen.uniform(500, 5000, seed=21, nq=20, k=4)
+    port = O.InfPort(ds.fxy, ds.uxy, uid=ds.uid)
+    o = O.Oracle.of(ds)
+    for q in ds.queries:
+        _, res, _ = port.query(int(q), 4)
+        assert set(o.query(int(q), 4).tolist()) <= set(res.tolist())
+
+
+def header_functions():
+    txt = open(os.path.join(REPO, "include", "rknn_gpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(rknn_[a-z_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol(engine):
+    names = header_functions()
+    assert len(names) >= 10
+    lib = engine.load()
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(engine.EXPORTS)
+    assert b"sm_103a" in lib.rknn_version()
+
+
+def test_cli_rejects_bad_arguments(engine, tmp_path):
+    cli = os.path.join(REPO, "rt-rknn_gb300", "rknn-gb300")
+    r = subprocess.run([cli, "-h"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Usage" in r.stderr
+    r = subprocess.run([cli, "-if", str(tmp_path / "missing.txt"), "-k", "3"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Error opening file" in r.stderr
+    r = subprocess.run([cli, "-if", "x", "-k", "0"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Invalid value for k" in r.stderr
+    p = tmp_path / "bad.txt"
+    p.write_text("2\n0 1 1\n1 2\n")
+    r = subprocess.run([cli, "-if", str(p)], capture_output=True, text=True)
+    assert r.returncode == 1 and "Error parsing" in r.stderr
