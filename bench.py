@@ -263,7 +263,7 @@ def run_ours(args):
         with torch.cuda.stream(stream):
             flush.fill_(2.0 + i)
         stream.synchronize()
-        idx.query_batch(qsets[args.warmup + i], ks, "fp32")
+        idx.query_batch(qsets[(args.warmup + i) % len(qsets)], ks, "fp32")
         kms.append(idx.kernel_ms())
     st = idx.last_stats()
     idx.set_profiling(False)

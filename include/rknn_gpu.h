@@ -81,6 +81,9 @@ typedef struct {
     int64_t rechecks;       /* comparisons decided by the exact expansion */
     int64_t overflow;       /* queries whose zone hit a capacity (results still exact) */
     double device_ms;       /* device time of the last launch sequence */
+    int64_t zone_cycles[8]; /* zone kernel SM cycles by phase, summed over queries: ring
+                               expansion, pop + rules, vertex test, vertex count pass,
+                               candidate intersections, dedup, counts/erase/append, epilogue */
 } rknn_query_stats;
 
 void rknn_index_opts_default(rknn_index_opts* opts);

@@ -24,6 +24,8 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librknn_gb300.so")
 CLI = os.path.join(HERE, "rknn-gb300")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# RKNN_CHECKED=1: bounds-checked zone state (records the first bad index)
+CHECKED = os.environ.get("RKNN_CHECKED", "0") == "1"
 NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")
 
 UNITS = {
@@ -41,6 +43,7 @@ def _digest(paths) -> str:
         with open(p, "rb") as fh:
             h.update(fh.read())
     h.update(" ".join(ARCH).encode())
+    h.update(b"checked" if CHECKED else b"plain")
     return h.hexdigest()
 
 
@@ -62,6 +65,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     common = [NVCC, *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fno-strict-aliasing", f"-I{os.path.join(REPO, 'include')}"]
+    if CHECKED:
+        common.append("-DRKNN_CHECKED")
 
     def cc(unit):
         src = os.path.join(CSRC, unit)

@@ -57,7 +57,7 @@ ZoneCaps caps_for(int kmax)
 {
     ZoneCaps c;
     long long k = std::max(1, kmax);
-    c.vc = (int)std::min<long long>(5 * k * k + 96, 1 << 22);
+    c.vc = (int)std::min<long long>(4 * k * k + 96, 1 << 22);
     c.lc = (int)std::min<long long>(6 * k + 40, 1 << 16);
     c.pc = (int)std::min<long long>(256 + 24 * k, 1 << 20);
     c.rm = 64;
@@ -83,7 +83,7 @@ struct Workspace {
     int2* d_segs = nullptr;
     ZStats* d_zst = nullptr;
     int *d_cand_off = nullptr, *d_chunk_off = nullptr, *d_res_count = nullptr, *d_out_off = nullptr;
-    int* d_counters = nullptr;     // [0] zone work, [1] verify work
+    int* d_counters = nullptr;     // [0] zone work, [1] verify work, [4..8] zone fault record
     VStats* d_vstats = nullptr;
     int *d_pool = nullptr, *d_out = nullptr;
     long long pool_cap = 0;
@@ -143,9 +143,10 @@ void drop_graphs(Workspace& w)
     w.graphs.clear();
 }
 
-// Launch geometry of the zone kernel for given caps.
+// Launch geometry of the zone kernel for given caps.  The zone state always
+// lives in shared memory (one warp per block); caps_fit() has already sized
+// it to fit the per-block limit.
 struct ZoneLaunch {
-    int use_global;
     size_t slice, smem;
     int grid;
 };
@@ -154,16 +155,27 @@ ZoneLaunch zone_launch(rknn_index* ix, const ZoneCaps& c, int nq)
 {
     ZoneLaunch L;
     L.slice = zone_layout(c).bytes;
-    L.use_global = L.slice * ZONE_WARPS > std::min<size_t>(ix->smem_optin, 112 * 1024);
-    L.smem = L.use_global ? 0 : L.slice * ZONE_WARPS;
+    L.smem = L.slice * ZONE_WARPS;
     int per_sm = 1;
-    if (L.smem > 48 * 1024) cudaFuncSetAttribute(zone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zone_kernel, 32 * ZONE_WARPS, L.smem);
+    if (L.smem > 48 * 1024)
+        cudaFuncSetAttribute(zone_kernel_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zone_kernel_smem, 32 * ZONE_WARPS, L.smem);
     if (per_sm < 1) per_sm = 1;
-    if (L.use_global) per_sm = std::min(per_sm, 16);
     long long want = (nq + ZONE_WARPS - 1) / ZONE_WARPS;
     L.grid = (int)std::max(1LL, std::min<long long>(want, (long long)per_sm * ix->num_sms));
     return L;
+}
+
+// Shrink the vertex and queue capacities until the per-warp state fits the
+// shared memory a block may use.  A zone that outgrows them stops early
+// (fewer bisectors, a weaker filter); results stay exact.
+ZoneCaps caps_fit(rknn_index* ix, ZoneCaps c)
+{
+    const size_t budget = std::min<size_t>(ix->smem_optin, 200 * 1024) - 1024;
+    while (zone_layout(c).bytes * ZONE_WARPS > budget && c.vc > 256) c.vc = c.vc * 7 / 8;
+    while (zone_layout(c).bytes * ZONE_WARPS > budget && c.pc > 512) c.pc = c.pc * 7 / 8;
+    while (zone_layout(c).bytes * ZONE_WARPS > budget && c.lc > 64) c.lc = c.lc * 7 / 8;
+    return c;
 }
 
 rknn_status ensure_ws(rknn_index* ix, int nq, const ZoneCaps& caps, long long pool_need)
@@ -186,7 +198,8 @@ rknn_status ensure_ws(rknn_index* ix, int nq, const ZoneCaps& caps, long long po
         CK(dalloc(w.d_zst, nqc));
         CK(dalloc(w.d_cand_off, nqc + 1)); CK(dalloc(w.d_chunk_off, nqc + 1));
         CK(dalloc(w.d_res_count, nqc)); CK(dalloc(w.d_out_off, nqc + 1));
-        CK(dalloc(w.d_counters, 4));
+        CK(dalloc(w.d_counters, 16));
+        CK(cudaMemset(w.d_counters, 0, sizeof(int) * 16));
         CK(dalloc(w.d_vstats, 1));
         CK(cudaMallocHost(&w.h_q, sizeof(int) * nqc));
         CK(cudaMallocHost(&w.h_k, sizeof(int) * nqc));
@@ -203,17 +216,6 @@ rknn_status ensure_ws(rknn_index* ix, int nq, const ZoneCaps& caps, long long po
         CK(dalloc(w.d_pool, (size_t)cap));
         CK(dalloc(w.d_out, (size_t)cap));
         w.pool_cap = cap;
-    }
-    ZoneLaunch zl = zone_launch(ix, caps, nq);
-    if (zl.use_global) {
-        size_t need = zl.slice * (size_t)zl.grid * ZONE_WARPS;
-        if (need > w.zscratch_bytes) {
-            drop_graphs(w);
-            cudaFree(w.d_zscratch);
-            w.d_zscratch = nullptr;
-            CK(dalloc(w.d_zscratch, need));
-            w.zscratch_bytes = need;
-        }
     }
     return RKNN_OK;
 }
@@ -263,16 +265,17 @@ rknn_status enqueue(rknn_index* ix, int nq, int mode, const ZoneCaps& caps, bool
     za.q_in = w.d_q; za.k_in = w.d_k; za.order = use_order ? w.d_order : nullptr; za.nq = nq;
     za.work_counter = w.d_counters + 0;
     za.caps = caps;
-    za.use_global = zl.use_global;
-    za.gscratch = w.d_zscratch;
+    za.use_global = 0;
+    za.gscratch = nullptr;
     za.skip_coincident = ix->skip_coincident;
     za.rmax = caps.rm;
     za.seg_cap = w.seg_cap;
     za.qd = w.d_qd; za.planes = w.d_planes; za.bis_pos = w.d_bispos; za.segs = w.d_segs; za.zst = w.d_zst;
+    za.fault = w.d_counters + 4;
     // planes/bis_pos are strided by the workspace lc
     za.caps.lc = caps.lc;
     mark(0);
-    zone_kernel<<<zl.grid, 32 * ZONE_WARPS, zl.smem, st>>>(za);
+    zone_kernel_smem<<<zl.grid, 32 * ZONE_WARPS, zl.smem, st>>>(za);
     CK(cudaGetLastError());
     mark(1);
 
@@ -287,6 +290,8 @@ rknn_status enqueue(rknn_index* ix, int nq, int mode, const ZoneCaps& caps, bool
     va.uxy = ix->d_uxy; va.uid = ix->d_uid; va.fxy = ix->d_fxy; va.fstart = ix->d_fstart; va.gf = ix->gf;
     va.res_count = w.d_res_count; va.res_pool = w.d_pool; va.work_counter = w.d_counters + 1;
     va.vstats = w.d_vstats; va.mode = mode;
+    va.nu = (int)ix->nu; va.nf = (int)ix->nf; va.ncf = ix->gf.gx * ix->gf.gy;
+    va.pool_cap = w.pool_cap; va.fault = w.d_counters + 10;
     verify_kernel<<<bl.vgrid, VERIFY_WARPS * 32, bl.vsmem, st>>>(va);
     CK(cudaGetLastError());
     mark(3);
@@ -308,7 +313,7 @@ rknn_status launch(rknn_index* ix, int nq, int mode, const ZoneCaps& caps, bool 
     const BatchLaunch bl = batch_launch(ix, nq, mode, caps);
     if (ix->profiling) return enqueue(ix, nq, mode, caps, use_order, bl, true);
     const ZoneLaunch& zl = bl.zl;
-    GraphKey key{nq, mode, caps.vc, caps.lc, caps.pc, caps.rm, zl.use_global, w.pool_cap};
+    GraphKey key{nq, mode, caps.vc, caps.lc, caps.pc, caps.rm, 0, w.pool_cap};
     key.nq = use_order ? nq : -nq;
     auto it = w.graphs.find(key);
     if (it == w.graphs.end()) {
@@ -346,6 +351,7 @@ rknn_status collect_stats(rknn_index* ix, int nq, rknn_query_stats* out)
         s.zone_candidates += z[i].cand;
         s.zone_fp64 += z[i].cand64;
         if (qd[i].flags & (QF_ZONE_V_OVERFLOW | QF_ZONE_L_OVERFLOW | QF_ZONE_PQ_OVERFLOW)) s.overflow++;
+        for (int j = 0; j < 8; ++j) s.zone_cycles[j] += z[i].cyc[j];
     }
     s.results = (int64_t)v.results;
     s.candidates = (int64_t)v.cand;
@@ -363,7 +369,7 @@ rknn_status collect_stats(rknn_index* ix, int nq, rknn_query_stats* out)
 rknn_status run_sync(rknn_index* ix, int nq, int mode, int kmax, bool use_order)
 {
     Workspace& w = ix->ws;
-    ZoneCaps caps = caps_for(kmax);
+    ZoneCaps caps = caps_fit(ix, caps_for(kmax));
     long long need = std::max<long long>(w.pool_cap, (long long)nq * 4096);
     rknn_status s = ensure_ws(ix, nq, caps, need);
     if (s != RKNN_OK) return s;
@@ -574,6 +580,17 @@ rknn_status rknn_last_kernel_ms(rknn_index* ix, double* ms)
     return RKNN_OK;
 }
 
+// Zone-kernel fault record of a build with RKNN_CHECKED (all zero otherwise):
+// {flag, array id, index, capacity, source line}.  Not part of the public
+// header; used by bounds-check runs.
+rknn_status rknn_debug_zone_fault(rknn_index* ix, int32_t* out5)
+{
+    if (!ix || !out5 || !ix->ws.d_counters) return fail(RKNN_ERR_ARG, "no workspace");
+    CK(cudaMemcpy(out5, ix->ws.d_counters + 4, sizeof(int) * 5, cudaMemcpyDeviceToHost));
+    if (!out5[0]) CK(cudaMemcpy(out5, ix->ws.d_counters + 10, sizeof(int) * 5, cudaMemcpyDeviceToHost));
+    return RKNN_OK;
+}
+
 rknn_status rknn_set_stream(rknn_index* ix, void* stream)
 {
     if (!ix) return fail(RKNN_ERR_ARG, "index is null");
@@ -606,7 +623,7 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
     if (s != RKNN_OK) return s;
     std::lock_guard<std::mutex> lk(ix->mu);
     CK(cudaSetDevice(ix->device));
-    s = ensure_ws(ix, nq, caps_for(kmax), ix->ws.pool_cap);
+    s = ensure_ws(ix, nq, caps_fit(ix, caps_for(kmax)), ix->ws.pool_cap);
     if (s != RKNN_OK) return s;
     Workspace& w = ix->ws;
     // descending k: the longest zones start first
@@ -623,7 +640,7 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
     CK(cudaMemcpyAsync(w.d_k, w.h_k, sizeof(int) * nq, cudaMemcpyHostToDevice, ix->stream));
     s = run_sync(ix, nq, mode, kmax, !uniform);
     if (s != RKNN_OK) return s;
-    ix->last_lc = caps_for(kmax).lc;
+    ix->last_lc = caps_fit(ix, caps_for(kmax)).lc;
     const long long total = w.h_off[nq];
     for (int i = 0; i <= nq; ++i) offsets[i] = w.h_off[i];
     ix->last_nq = nq;
@@ -660,7 +677,7 @@ rknn_status rknn_query_batch_device(rknn_index* ix, const int32_t* d_q, const in
     if (mode != RKNN_MODE_FP32 && mode != RKNN_MODE_FP64) return fail(RKNN_ERR_ARG, "bad mode");
     std::lock_guard<std::mutex> lk(ix->mu);
     Workspace& w = ix->ws;
-    ZoneCaps caps = caps_for(kmax);
+    ZoneCaps caps = caps_fit(ix, caps_for(kmax));
     ix->last_lc = caps.lc;
     rknn_status s = ensure_ws(ix, nq, caps, std::max<long long>(w.pool_cap, (long long)nq * 4096));
     if (s != RKNN_OK) return s;

@@ -58,6 +58,9 @@ struct ZStats {
     int cand64;        // candidates whose intersection was computed in FP64
     int kept;          // candidates kept as vertices
     int rings;         // user-cell rings scanned
+    long long cyc[8];  // SM cycles per phase: 0 ring expansion, 1 pop + rules,
+                       // 2 vertex test, 3 count pass, 4 candidates, 5 dedup,
+                       // 6 counts/erase/append, 7 epilogue
 };
 
 // Verification statistics, accumulated over a batch.

@@ -30,6 +30,22 @@ namespace rknn {
 namespace {
 constexpr unsigned FULL = 0xffffffffu;
 
+#ifdef RKNN_CHECKED
+__device__ __forceinline__ long long vck(const VerifyArgs& A, long long i, long long n, int id, int line)
+{
+    if (i < 0 || i >= n) {
+        if (A.fault && atomicCAS(A.fault, 0, 1) == 0) {
+            A.fault[1] = id; A.fault[2] = (int)i; A.fault[3] = (int)n; A.fault[4] = line;
+        }
+        return 0;
+    }
+    return i;
+}
+#define VX(i, n, id) vck(A, (i), (n), (id), __LINE__)
+#else
+#define VX(i, n, id) (i)
+#endif
+
 template <typename T>
 __device__ __forceinline__ int exact_count(float ux, float uy, const QDesc& d, const VerifyArgs& A,
                                            unsigned long long& fac, unsigned long long& rech)
@@ -55,12 +71,12 @@ __device__ __forceinline__ int exact_count(float ux, float uy, const QDesc& d, c
     int cy0 = cell_coord(uy - r, g.y0, g.inv, g.gy), cy1 = cell_coord(uy + r, g.y0, g.inv, g.gy);
     int cnt = 0;
     for (int cy = cy0; cy <= cy1; ++cy) {
-        const int f0 = A.fstart[cy * g.gx + cx0], f1 = A.fstart[cy * g.gx + cx1 + 1];
+        const int f0 = A.fstart[VX(cy * g.gx + cx0, A.ncf + 1, 201)], f1 = A.fstart[VX(cy * g.gx + cx1 + 1, A.ncf + 1, 202)];
         for (int b = f0; b < f1; b += 32) {
             int i = b + lane;
             bool c = false;
             if (i < f1 && i != d.qpos) {
-                float2 f = A.fxy[i];
+                float2 f = A.fxy[VX(i, A.nf, 203)];
                 if (sizeof(T) == 4) c = closer_f32(ux, uy, f.x, f.y, qx, qy, (float)Dq, &rech);
                 else c = closer_f64(ux, uy, f.x, f.y, qx, qy, (double)Dq, &rech);
             }
@@ -151,7 +167,7 @@ verify_kernel(VerifyArgs A)
             } else {
                 const int* bp = A.bis_pos + (size_t)s * A.lc;
                 for (int m = lane; m < d.nb; m += 32) {
-                    float2 f = A.fxy[bp[m]];
+                    float2 f = A.fxy[VX(bp[m], A.nf, 204)];
                     double dx = (double)f.x - (double)d.qx, dy = (double)f.y - (double)d.qy;
                     double* p = (double*)sp + 4 * m;
                     p[0] = -2.0 * dx;
@@ -188,7 +204,7 @@ verify_kernel(VerifyArgs A)
             if (valid[t]) {
                 while (si + 1 < d.nseg && sg[si + 1].y <= v) ++si;
                 pos[t] = sg[si].x + (v - sg[si].y);
-                u[t] = A.uxy[pos[t]];
+                u[t] = A.uxy[VX(pos[t], A.nu, 205)];
             }
             s_cand += valid[t];
         }
@@ -225,7 +241,7 @@ verify_kernel(VerifyArgs A)
             int o = 0;
 #pragma unroll
             for (int t = 0; t < VERIFY_UPT; ++t) {
-                if (acc[t]) dst[o + __popc(am[t] & ((1u << lane) - 1))] = A.uid[pos[t]];
+                if (acc[t]) A.res_pool[VX((long long)A.cand_off[s] + base + o + __popc(am[t] & ((1u << lane) - 1)), A.pool_cap, 206)] = A.uid[VX(pos[t], A.nu, 207)];
                 o += __popc(am[t]);
             }
             s_res += (lane == 0) ? tot : 0;

@@ -31,6 +31,9 @@ struct VerifyArgs {
     int* work_counter;
     VStats* vstats;
     int mode;
+    int nu, nf, ncf;         // array sizes (bounds-checked builds)
+    long long pool_cap;
+    int* fault;              // checked builds: {flag, array id, index, size, line}
 };
 
 __global__ void verify_kernel(VerifyArgs a);

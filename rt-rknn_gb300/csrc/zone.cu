@@ -51,6 +51,7 @@ struct Line64 {
 };
 
 struct WarpScalars {
+    double dummy[4];    // checked builds: target of rejected accesses
     int nV, nL, nP, nC;
     int nCons;
     int flags;
@@ -79,6 +80,14 @@ __device__ __forceinline__ double rect_d2_64(double px, double py, float4 r)
     if (py < (double)r.y) dy = __dsub_rn((double)r.y, py);
     else if (py > (double)r.w) dy = __dsub_rn(py, (double)r.w);
     return __dadd_rn(dsq(dx), dsq(dy));
+}
+
+// Integer key with the numeric order of a finite double (-0 counts as +0).
+__device__ __forceinline__ long long order_key(double d)
+{
+    long long b = __double_as_longlong(d);
+    if (b == (long long)0x8000000000000000ull) b = 0;
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
 }
 
 __device__ __forceinline__ float rect_dx32(float v, float lo, float hi)
@@ -140,25 +149,70 @@ __device__ double line_dist64(double px, double py, double a, double b, int vert
     return __ddiv_rn(num, den);
 }
 
+// Per-warp state array.  With RKNN_CHECKED every index is checked against
+// the capacity; the first violation is recorded (array id, index, capacity,
+// source line) and the access goes to a spare element instead.
+#ifdef RKNN_CHECKED
+__device__ int* g_fault;
+template <typename T>
+struct Arr {
+    T* p;
+    int cap, id;
+    T* dummy;
+    __device__ T& at(long long i, int line) const
+    {
+        if (i < 0 || i >= cap) {
+            if (g_fault && atomicCAS(g_fault, 0, 1) == 0) {
+                g_fault[1] = id; g_fault[2] = (int)i; g_fault[3] = cap; g_fault[4] = line;
+            }
+            return *dummy;
+        }
+        return p[i];
+    }
+};
+#define IX(a, i) (a).at((i), __LINE__)
+// index i into a global array of n elements: checked, clamped to 0 if bad
+__device__ __forceinline__ long long gck(long long i, long long n, int id, int line)
+{
+    if (i < 0 || i >= n) {
+        if (g_fault && atomicCAS(g_fault, 0, 1) == 0) {
+            g_fault[1] = id; g_fault[2] = (int)i; g_fault[3] = (int)n; g_fault[4] = line;
+        }
+        return 0;
+    }
+    return i;
+}
+#define GX(i, n, id) gck((i), (n), (id), __LINE__)
+#else
+#define GX(i, n, id) (i)
+template <typename T>
+struct Arr {
+    T* p;
+    __device__ __forceinline__ T& at(long long i, int) const { return p[i]; }
+};
+#define IX(a, i) (a).p[(i)]
+#endif
+
 struct Slice {
-    double *vx, *vy, *vd2;
-    float *vx32, *vy32;
-    int *vcnt;
-    uint8_t *vfl;
-    int *cons;
-    double *la, *lb;
-    float *la32, *lb32, *lb3;
-    uint8_t *lfl;
-    int *lpos;
-    uint64_t *pqk;
-    uint32_t *pqc;
-    double *cx, *cy;
-    float *cx32, *cy32;
-    int *ccnt;
-    uint8_t *cfl;
-    uint64_t *tk;
-    uint32_t *tc;
-    uint32_t *bitmap;
+    Arr<double> vx, vy, vd2;
+    Arr<float> vx32, vy32, vd2f;
+    Arr<int> vcnt;
+    Arr<uint8_t> vfl;
+    Arr<int> cons;
+    Arr<double> la, lb;
+    Arr<float> la32, lb32, lb3;
+    Arr<uint8_t> lfl;
+    Arr<int> lpos;
+    Arr<uint64_t> pqk;
+    Arr<uint32_t> pqc;
+    Arr<double> cx, cy;
+    Arr<float> cx32, cy32;
+    Arr<int> ccnt;
+    Arr<uint8_t> cfl;
+    Arr<uint64_t> tk;
+    Arr<uint32_t> tc;
+    Arr<uint32_t> bitmap;
+    Arr<float4> splanes;
     WarpScalars *sc;
 };
 
@@ -166,32 +220,25 @@ __device__ Slice carve(char* base, const ZoneCaps& c)
 {
     ZoneLayout L = zone_layout(c);
     Slice s;
-    s.vx = (double*)(base + L.vx);
-    s.vy = (double*)(base + L.vy);
-    s.vd2 = (double*)(base + L.vd2);
-    s.vx32 = (float*)(base + L.vx32);
-    s.vy32 = (float*)(base + L.vy32);
-    s.vcnt = (int*)(base + L.vcnt);
-    s.vfl = (uint8_t*)(base + L.vfl);
-    s.cons = (int*)(base + L.cons);
-    s.la = (double*)(base + L.la);
-    s.lb = (double*)(base + L.lb);
-    s.la32 = (float*)(base + L.la32);
-    s.lb32 = (float*)(base + L.lb32);
-    s.lb3 = (float*)(base + L.lb3);
-    s.lfl = (uint8_t*)(base + L.lfl);
-    s.lpos = (int*)(base + L.lpos);
-    s.pqk = (uint64_t*)(base + L.pqk);
-    s.pqc = (uint32_t*)(base + L.pqc);
-    s.cx = (double*)(base + L.cx);
-    s.cy = (double*)(base + L.cy);
-    s.cx32 = (float*)(base + L.cx32);
-    s.cy32 = (float*)(base + L.cy32);
-    s.ccnt = (int*)(base + L.ccnt);
-    s.cfl = (uint8_t*)(base + L.cfl);
-    s.tk = (uint64_t*)(base + L.tk);
-    s.tc = (uint32_t*)(base + L.tc);
-    s.bitmap = (uint32_t*)(base + L.vx);   // reused after the zone is built
+    const int VC = c.vc, LC = c.lc, PC = c.pc, CC = c.lc + 4;
+    const int W = 2 * c.rm + 1;
+#ifdef RKNN_CHECKED
+#define CARVE(f, T, off, n, i) s.f = Arr<T>{(T*)(base + L.off), (int)(n), i, (T*)(base + L.sc)}
+#else
+#define CARVE(f, T, off, n, i) s.f = Arr<T>{(T*)(base + L.off)}
+#endif
+    CARVE(vx, double, vx, VC, 1); CARVE(vy, double, vy, VC, 2); CARVE(vd2, double, vd2, VC, 3);
+    CARVE(vx32, float, vx32, VC, 4); CARVE(vy32, float, vy32, VC, 5); CARVE(vd2f, float, vd2f, VC, 6);
+    CARVE(vcnt, int, vcnt, VC, 7); CARVE(vfl, uint8_t, vfl, VC, 8); CARVE(cons, int, cons, VC, 9);
+    CARVE(la, double, la, LC, 10); CARVE(lb, double, lb, LC, 11); CARVE(la32, float, la32, LC, 12);
+    CARVE(lb32, float, lb32, LC, 13); CARVE(lb3, float, lb3, LC, 14); CARVE(lfl, uint8_t, lfl, LC, 15);
+    CARVE(lpos, int, lpos, LC, 16); CARVE(pqk, uint64_t, pqk, PC, 17); CARVE(pqc, uint32_t, pqc, PC, 18);
+    CARVE(cx, double, cx, CC, 19); CARVE(cy, double, cy, CC, 20); CARVE(cx32, float, cx32, CC, 21);
+    CARVE(cy32, float, cy32, CC, 22); CARVE(ccnt, int, ccnt, CC, 23); CARVE(cfl, uint8_t, cfl, CC, 24);
+    CARVE(tk, uint64_t, tk, 32, 25); CARVE(tc, uint32_t, tc, 32, 26);
+    CARVE(bitmap, uint32_t, vx, (W * W + 31) / 32, 27);    // reused after the zone is built
+    CARVE(splanes, float4, cx, LC, 28);                     // reused for the epilogue
+#undef CARVE
     s.sc = (WarpScalars*)(base + L.sc);
     return s;
 }
@@ -205,7 +252,7 @@ __device__ __forceinline__ bool pq_less(uint64_t k1, uint32_t c1, uint64_t k2, u
     return k1 < k2 || (k1 == k2 && c1 < c2);
 }
 
-__device__ bool pq_push(uint64_t* K, uint32_t* C, int& n, int cap, uint64_t key, uint32_t code)
+__device__ __forceinline__ bool pq_push(uint64_t* K, uint32_t* C, int& n, int cap, uint64_t key, uint32_t code)
 {
     if (n >= cap) return false;
     int i = n++;
@@ -221,7 +268,7 @@ __device__ bool pq_push(uint64_t* K, uint32_t* C, int& n, int cap, uint64_t key,
     return true;
 }
 
-__device__ void pq_pop(uint64_t* K, uint32_t* C, int& n)
+__device__ __forceinline__ void pq_pop(uint64_t* K, uint32_t* C, int& n)
 {
     uint64_t lk = K[n - 1];
     uint32_t lc = C[n - 1];
@@ -259,13 +306,12 @@ __device__ __forceinline__ int warp_sum(int v)
 // dist64(p, v) < dist64(q, v) as the reference computes it.
 //   D  = squared distance from the facility (or rectangle) to the vertex
 //   d2v = vertex's squared distance to q (FP64, the reference's dq squared)
-__device__ __forceinline__ bool closer_than_q(float dxp, float dyp, float E, double d2v,
+__device__ __forceinline__ bool closer_than_q(float dxp, float dyp, float E, float V, double d2v,
                                               double dx64, double dy64)
 {
     float D = fmaf(dxp, dxp, dyp * dyp);
     float ep = E + kU32 * (fabsf(dxp) + fabsf(dyp));
     float err = fmaf(2.0f * (fabsf(dxp) + fabsf(dyp)) + 2.0f * ep, ep, 4.0f * kU32 * D) + 1e-30f;
-    float V = (float)d2v;
     float vlo = V * (1.0f - 4.0f * kU32), vhi = V * (1.0f + 4.0f * kU32);
     if (D + err < vlo) return true;
     if (D - err > vhi) return false;
@@ -276,18 +322,31 @@ __device__ __forceinline__ bool closer_than_q(float dxp, float dyp, float E, dou
 }  // namespace
 
 // ============================================================================
-__global__ void __launch_bounds__(ZONE_WARPS * 32)
-zone_kernel(ZoneArgs A)
+// Lanes hand zone state to each other through memory between warp
+// barriers.  With the state in global memory the handoff is made explicit: a
+// block-scope fence orders each lane's stores and loads around the barrier.
+#define WSYNC() do { if (GMEM) __threadfence_block(); __syncwarp(); } while (0)
+
+template <bool GMEM>
+__device__ __forceinline__ void zone_body(const ZoneArgs& A)
 {
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
+#ifdef RKNN_CHECKED
+    if (threadIdx.x == 0 && blockIdx.x == 0) g_fault = A.fault;
+    __syncthreads();
+    if (!g_fault) g_fault = A.fault;
+#endif
     const ZoneLayout LY = zone_layout(A.caps);
-    char* base = A.use_global
-        ? A.gscratch + (size_t)(blockIdx.x * ZONE_WARPS + wib) * LY.bytes
-        : smem + (size_t)wib * LY.bytes;
+    // the shared-memory instantiation derives every state pointer from the
+    // __shared__ array itself (no generic pointer that could be global)
+    char* base;
+    if (GMEM) base = A.gscratch + (size_t)(blockIdx.x * ZONE_WARPS + wib) * LY.bytes;
+    else base = smem + (size_t)wib * LY.bytes;
     Slice S = carve(base, A.caps);
     const int VC = A.caps.vc, LC = A.caps.lc, PC = A.caps.pc;
+    const long long NCF = (long long)A.gf.gx * A.gf.gy, NCU = (long long)A.gu.gx * A.gu.gy;
     const double sx0 = A.sx0, sy0 = A.sy0, sx1 = A.sx1, sy1 = A.sy1;
     // largest rounding error of a vertex coordinate stored as float
     const float E = kU32 * (float)fmax(fmax(fabs(sx0), fabs(sx1)), fmax(fabs(sy0), fabs(sy1))) * 1.01f + 1e-37f;
@@ -318,36 +377,36 @@ zone_kernel(ZoneArgs A)
             }
             continue;
         }
-        const int qpos = A.fpos[qin];
-        const float2 qf = A.fxy[qpos];
+        const int qpos = A.fpos[GX(qin, A.nf, 105)];
+        const float2 qf = A.fxy[GX(qpos, A.nf, 101)];
         const double qx = qf.x, qy = qf.y;
-        WarpScalars* sc = S.sc;
+        // Warp-uniform scalars live in registers (identical in every lane);
+        // lane 0 alone touches the heap and broadcasts what it changes.
+        int nV = 4, nL = 0, nP = 0, nCons = -1, flags = 0;
+        double far_ = 0.0, nearb = DBL_MAX;
 
         // ---- init: four space corners (inf.cpp:211-226) -------------------
         if (lane < 4) {
             double x = (lane & 1) ? sx1 : sx0;
             double y = (lane & 2) ? sy1 : sy0;
-            S.vx[lane] = x;
-            S.vy[lane] = y;
-            S.vx32[lane] = (float)x;
-            S.vy32[lane] = (float)y;
-            S.vd2[lane] = d2_64(x, y, qx, qy);
-            S.vcnt[lane] = 0;
-            S.vfl[lane] = VB_BND;
+            IX(S.vx, lane) = x;
+            IX(S.vy, lane) = y;
+            IX(S.vx32, lane) = (float)x;
+            IX(S.vy32, lane) = (float)y;
+            IX(S.vd2, lane) = d2_64(x, y, qx, qy);
+            IX(S.vd2f, lane) = (float)IX(S.vd2, lane);
+            IX(S.vcnt, lane) = 0;
+            IX(S.vfl, lane) = VB_BND;
         }
-        if (lane == 0) {
-            sc->nV = 4; sc->nL = 0; sc->nP = 0; sc->flags = 0; sc->stop = 0;
-            sc->nCons = -1;
-            sc->nearb = DBL_MAX;
-        }
-        __syncwarp();
+        WSYNC();
         {
-            double m = lane < 4 ? S.vd2[lane] : 0.0;
+            double m = lane < 4 ? IX(S.vd2, lane) : 0.0;
             m = warp_max(m);
-            if (lane == 0) sc->far_ = __dsqrt_rn(m);
+            far_ = __dsqrt_rn(m);
         }
-        __syncwarp();
 
+        long long tph = clock64();
+#define PHASE(i) do { long long t_ = clock64(); zs.cyc[i] += t_ - tph; tph = t_; } while (0)
         const int qcx = cell_coord(qf.x, A.gf.x0, A.gf.inv, A.gf.gx);
         const int qcy = cell_coord(qf.y, A.gf.y0, A.gf.inv, A.gf.gy);
         const int rmaxf = max(max(qcx, A.gf.gx - 1 - qcx), max(qcy, A.gf.gy - 1 - qcy));
@@ -357,14 +416,18 @@ zone_kernel(ZoneArgs A)
         for (;;) {
             // make the top poppable: expand rings whose cells could precede it
             for (;;) {
-                int nP = sc->nP;
-                double far2 = 2.0 * sc->far_;
+                const double far2 = 2.0 * far_;
                 bool can_expand = ring <= rmaxf;
                 double Lr = ring == 0 ? 0.0 : (double)(ring - 1) * (double)A.gf.cs - slack;
                 if (Lr < 0) Lr = 0;
                 if (can_expand && Lr > far2 * (1.0 + 1e-9) + slack) can_expand = false;
                 if (!can_expand) break;
-                if (nP > 0 && __longlong_as_double((long long)S.pqk[0]) < Lr * Lr) break;
+                if (nP > 0) {
+                    uint64_t top = 0;
+                    if (lane == 0) top = IX(S.pqk, 0);
+                    top = __shfl_sync(FULL, top, 0);
+                    if (__longlong_as_double((long long)top) < Lr * Lr) break;
+                }
                 // expand ring `ring`: 8*ring cells (1 for ring 0)
                 int ncell = ring == 0 ? 1 : 8 * ring;
                 for (int t0 = 0; t0 < ncell; t0 += 32) {
@@ -385,38 +448,37 @@ zone_kernel(ZoneArgs A)
                     int cid = 0;
                     if (ok) {
                         cid = cyy * A.gf.gx + cxx;
-                        ok = A.fstart[cid + 1] > A.fstart[cid];
+                        ok = A.fstart[GX(cid + 1, NCF + 1, 102)] > A.fstart[GX(cid, NCF + 1, 102)];
                     }
-                    double key = ok ? rect_d2_64(qx, qy, A.fmbr[cid]) : 0.0;
+                    double key = ok ? rect_d2_64(qx, qy, A.fmbr[GX(cid, NCF, 103)]) : 0.0;
                     unsigned m = __ballot_sync(FULL, ok);
                     int rank = __popc(m & ((1u << lane) - 1));
-                    if (ok) { S.tk[rank] = (uint64_t)__double_as_longlong(key); S.tc[rank] = (uint32_t)cid; }
-                    __syncwarp();
+                    if (ok) { IX(S.tk, rank) = (uint64_t)__double_as_longlong(key); IX(S.tc, rank) = (uint32_t)cid; }
+                    WSYNC();
                     if (lane == 0) {
-                        int n = sc->nP;
                         for (int i = 0; i < __popc(m); ++i)
-                            if (!pq_push(S.pqk, S.pqc, n, PC, S.tk[i], S.tc[i])) { sc->flags |= QF_ZONE_PQ_OVERFLOW; break; }
-                        sc->nP = n;
+                            if (!pq_push(S.pqk.p, S.pqc.p, nP, PC, IX(S.tk, i), IX(S.tc, i))) { flags |= QF_ZONE_PQ_OVERFLOW; break; }
                     }
-                    __syncwarp();
+                    nP = __shfl_sync(FULL, nP, 0);
+                    flags = __shfl_sync(FULL, flags, 0);
+                    WSYNC();
                 }
                 ring++;
-                if (sc->flags) break;
+                if (flags) break;
             }
-            if (sc->flags || sc->nP == 0) break;
+            PHASE(0);
+            if (flags || nP == 0) break;
             uint64_t keybits = 0;
             uint32_t code = 0;
             if (lane == 0) {
-                keybits = S.pqk[0];
-                code = S.pqc[0];
-                int n = sc->nP;
-                pq_pop(S.pqk, S.pqc, n);
-                sc->nP = n;
+                keybits = IX(S.pqk, 0);
+                code = IX(S.pqc, 0);
+                pq_pop(S.pqk.p, S.pqc.p, nP);
             }
             keybits = __shfl_sync(FULL, keybits, 0);
             code = __shfl_sync(FULL, code, 0);
+            nP = __shfl_sync(FULL, nP, 0);
             const double key = __longlong_as_double((long long)keybits);
-            __syncwarp();
 
             const bool is_point = (code & KIND_POINT) != 0;
             const int id = (int)(code & ~KIND_POINT);
@@ -424,145 +486,134 @@ zone_kernel(ZoneArgs A)
             float4 mbr = make_float4(0, 0, 0, 0);
             if (is_point) {
                 if (id == qpos) continue;
-                float2 pf = A.fxy[id];
+                float2 pf = A.fxy[GX(id, A.nf, 101)];
                 px = pf.x; py = pf.y;
                 if (A.skip_coincident && pf.x == qf.x && pf.y == qf.y) continue;
                 zs.pts++;
             } else {
-                mbr = A.fmbr[id];
+                mbr = A.fmbr[GX(id, NCF, 103)];
                 zs.cells++;
             }
             // rules 1 and 2 (inf.cpp:262-267, 460-465): key is the squared distance
             const double dq = __dsqrt_rn(key);
             bool prune;
-            if (dq > 2.0 * sc->far_) prune = true;
-            else if (dq < 2.0 * sc->nearb) prune = false;
+            PHASE(1);
+            if (dq > 2.0 * far_) prune = true;
+            else if (dq < 2.0 * nearb) prune = false;
             else {
                 // ---- vertex test (inf.cpp:268-353, 466-551) -------------
-                if (sc->nCons < 0) {
-                    // extreme boundary vertices with count < k
-                    // e[0..7]: left min/max y, right min/max y, bottom min/max x, top min/max x
-                    int nV = sc->nV;
-                    int best[8];
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) best[j] = -1;
-                    for (int i = lane; i < nV; i += 32) {
-                        if (!((S.vfl[i] & VB_BND) && S.vcnt[i] < k)) continue;
-                        double x = S.vx[i], y = S.vy[i];
-                        bool onL = fabs(__dsub_rn(x, sx0)) < EPS, onR = fabs(__dsub_rn(x, sx1)) < EPS;
-                        bool onB = fabs(__dsub_rn(y, sy0)) < EPS, onT = fabs(__dsub_rn(y, sy1)) < EPS;
-                        if (onL) {
-                            if (best[0] < 0 || y < S.vy[best[0]]) best[0] = i;
-                            if (best[1] < 0 || y > S.vy[best[1]]) best[1] = i;
-                        }
-                        if (onR) {
-                            if (best[2] < 0 || y < S.vy[best[2]]) best[2] = i;
-                            if (best[3] < 0 || y > S.vy[best[3]]) best[3] = i;
-                        }
-                        if (onB) {
-                            if (best[4] < 0 || x < S.vx[best[4]]) best[4] = i;
-                            if (best[5] < 0 || x > S.vx[best[5]]) best[5] = i;
-                        }
-                        if (onT) {
-                            if (best[6] < 0 || x < S.vx[best[6]]) best[6] = i;
-                            if (best[7] < 0 || x > S.vx[best[7]]) best[7] = i;
+                if (nCons < 0) {
+                    // boundary vertices with count < k, in vertex order
+                    int nB = 0;
+                    for (int i0 = 0; i0 < nV; i0 += 32) {
+                        int i = i0 + lane;
+                        bool b = i < nV && (IX(S.vfl, i) & VB_BND) && IX(S.vcnt, i) < k;
+                        unsigned m = __ballot_sync(FULL, b);
+                        if (b) IX(S.cons, nB + __popc(m & ((1u << lane) - 1))) = i;
+                        nB += __popc(m);
+                    }
+                    WSYNC();
+                    // lane j < 8 scans them in order for extreme j (first strict
+                    // min / max wins, as the reference's pointer updates):
+                    // left min/max y, right min/max y, bottom min/max x, top min/max x
+                    int best = -1;
+                    if (lane < 8) {
+                        const bool byY = lane < 4;
+                        const bool wantMin = (lane & 1) == 0;
+                        const double edge = lane < 2 ? sx0 : lane < 4 ? sx1 : lane < 6 ? sy0 : sy1;
+                        long long bk = 0;
+                        for (int t = 0; t < nB; ++t) {
+                            const int i = IX(S.cons, t);
+                            const double x = IX(S.vx, i), y = IX(S.vy, i);
+                            if (!(fabs(__dsub_rn(byY ? x : y, edge)) < EPS)) continue;
+                            const long long key = order_key(byY ? y : x);
+                            if (best < 0 || (wantMin ? key < bk : key > bk)) { best = i; bk = key; }
                         }
                     }
-                    // reduce: strict improvement, earliest index on ties
+                    int ext[8];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        int b = best[j];
-                        for (int o = 16; o > 0; o >>= 1) {
-                            int ob = __shfl_xor_sync(FULL, b, o);
-                            if (ob < 0) continue;
-                            if (b < 0) { b = ob; continue; }
-                            double vb = (j < 4) ? S.vy[b] : S.vx[b];
-                            double vo = (j < 4) ? S.vy[ob] : S.vx[ob];
-                            bool wantMin = (j & 1) == 0;
-                            bool better = wantMin ? (vo < vb) : (vo > vb);
-                            if (better || (vo == vb && ob < b)) b = ob;
-                        }
-                        best[j] = b;
-                    }
-                    // considered list
+                    for (int j = 0; j < 8; ++j) ext[j] = __shfl_sync(FULL, best, j);
+                    WSYNC();
+                    // considered: count == k-1, or a boundary vertex (count < k)
+                    // within EPS of one of the extreme points (inf.cpp:326-346)
                     int nC = 0;
                     for (int i0 = 0; i0 < nV; i0 += 32) {
                         int i = i0 + lane;
                         bool c = false;
                         if (i < nV) {
-                            int cnt = S.vcnt[i];
+                            int cnt = IX(S.vcnt, i);
                             if (cnt == k - 1) c = true;
-                            else if ((S.vfl[i] & VB_BND) && cnt < k) {
-                                double x = S.vx[i], y = S.vy[i];
+                            else if ((IX(S.vfl, i) & VB_BND) && cnt < k) {
+                                double x = IX(S.vx, i), y = IX(S.vy, i);
 #pragma unroll
                                 for (int j = 0; j < 8; ++j) {
-                                    int b = best[j];
-                                    if (b >= 0 && fabs(__dsub_rn(x, S.vx[b])) < EPS &&
-                                        fabs(__dsub_rn(y, S.vy[b])) < EPS) c = true;
+                                    int b = ext[j];
+                                    if (b >= 0 && fabs(__dsub_rn(x, IX(S.vx, b))) < EPS &&
+                                        fabs(__dsub_rn(y, IX(S.vy, b))) < EPS) c = true;
                                 }
                             }
                         }
                         unsigned m = __ballot_sync(FULL, c);
-                        if (c) S.cons[nC + __popc(m & ((1u << lane) - 1))] = i;
+                        if (c) IX(S.cons, nC + __popc(m & ((1u << lane) - 1))) = i;
                         nC += __popc(m);
                     }
-                    if (lane == 0) sc->nCons = nC;
-                    __syncwarp();
+                    nCons = nC;
+                    WSYNC();
                 }
-                const int nC = sc->nCons;
+                const int nC = nCons;
                 bool hit = false;
                 const float px32 = (float)px, py32 = (float)py;
                 for (int t = lane; t < nC && !hit; t += 32) {
-                    int i = S.cons[t];
-                    double d2v = S.vd2[i];
+                    int i = IX(S.cons, t);
+                    const float d2f = IX(S.vd2f, i);
                     if (is_point) {
-                        float dxp = px32 - S.vx32[i], dyp = py32 - S.vy32[i];
-                        hit = closer_than_q(dxp, dyp, E, d2v, __dsub_rn(px, S.vx[i]), __dsub_rn(py, S.vy[i]));
+                        float dxp = px32 - IX(S.vx32, i), dyp = py32 - IX(S.vy32, i);
+                        hit = closer_than_q(dxp, dyp, E, d2f, IX(S.vd2, i), __dsub_rn(px, IX(S.vx, i)), __dsub_rn(py, IX(S.vy, i)));
                     } else {
-                        float dxp = rect_dx32(S.vx32[i], mbr.x, mbr.z);
-                        float dyp = rect_dx32(S.vy32[i], mbr.y, mbr.w);
-                        double vx = S.vx[i], vy = S.vy[i];
+                        float dxp = rect_dx32(IX(S.vx32, i), mbr.x, mbr.z);
+                        float dyp = rect_dx32(IX(S.vy32, i), mbr.y, mbr.w);
+                        double vx = IX(S.vx, i), vy = IX(S.vy, i);
                         double dx64 = 0, dy64 = 0;
                         if (vx < (double)mbr.x) dx64 = __dsub_rn((double)mbr.x, vx);
                         else if (vx > (double)mbr.z) dx64 = __dsub_rn(vx, (double)mbr.z);
                         if (vy < (double)mbr.y) dy64 = __dsub_rn((double)mbr.y, vy);
                         else if (vy > (double)mbr.w) dy64 = __dsub_rn(vy, (double)mbr.w);
-                        hit = closer_than_q(dxp, dyp, E, d2v, dx64, dy64);
+                        hit = closer_than_q(dxp, dyp, E, d2f, IX(S.vd2, i), dx64, dy64);
                     }
                 }
                 prune = !__any_sync(FULL, hit);
+                PHASE(2);
             }
             if (prune) continue;
 
             if (!is_point) {
                 // push the cell's facilities (inf.cpp:556-565)
-                const int p0 = A.fstart[id], p1 = A.fstart[id + 1];
+                const int p0 = A.fstart[GX(id, NCF + 1, 102)], p1 = A.fstart[GX(id + 1, NCF + 1, 102)];
                 for (int t0 = p0; t0 < p1; t0 += 32) {
                     int t = t0 + lane;
                     bool ok = t < p1;
                     if (ok) {
-                        float2 pf = A.fxy[t];
-                        S.tk[lane] = (uint64_t)__double_as_longlong(d2_64(qx, qy, (double)pf.x, (double)pf.y));
-                        S.tc[lane] = KIND_POINT | (uint32_t)t;
+                        float2 pf = A.fxy[GX(t, A.nf, 101)];
+                        IX(S.tk, lane) = (uint64_t)__double_as_longlong(d2_64(qx, qy, (double)pf.x, (double)pf.y));
+                        IX(S.tc, lane) = KIND_POINT | (uint32_t)t;
                     }
-                    __syncwarp();
+                    WSYNC();
                     if (lane == 0) {
-                        int n = sc->nP;
                         int cnt = min(32, p1 - t0);
                         for (int i = 0; i < cnt; ++i)
-                            if (!pq_push(S.pqk, S.pqc, n, PC, S.tk[i], S.tc[i])) { sc->flags |= QF_ZONE_PQ_OVERFLOW; break; }
-                        sc->nP = n;
+                            if (!pq_push(S.pqk.p, S.pqc.p, nP, PC, IX(S.tk, i), IX(S.tc, i))) { flags |= QF_ZONE_PQ_OVERFLOW; break; }
                     }
-                    __syncwarp();
+                    nP = __shfl_sync(FULL, nP, 0);
+                    flags = __shfl_sync(FULL, flags, 0);
+                    WSYNC();
                 }
-                if (sc->flags) break;
+                if (flags) break;
                 continue;
             }
 
             // ================= accept facility `id`: add its bisector ======
-            const int nL = sc->nL;
-            if (nL >= LC) { if (lane == 0) sc->flags |= QF_ZONE_L_OVERFLOW; __syncwarp(); break; }
-            Line64 nb;
+            if (nL >= LC) { flags |= QF_ZONE_L_OVERFLOW; break; }
+            Line64 nb = {0.0, 0.0, 0, 0};
             if (lane == 0) nb = make_bisector(qx, qy, px, py);
             nb.a = __shfl_sync(FULL, nb.a, 0);
             nb.b = __shfl_sync(FULL, nb.b, 0);
@@ -573,9 +624,9 @@ zone_kernel(ZoneArgs A)
             zs.nb++;
 
             // (1) count pass over the existing vertices (inf.cpp:359-364)
-            const int nV0 = sc->nV;
+            const int nV0 = nV;
             for (int i = lane; i < nV0; i += 32) {
-                float x32 = S.vx32[i], y32 = S.vy32[i];
+                float x32 = IX(S.vx32, i), y32 = IX(S.vy32, i);
                 float r32, err;
                 if (nb.vert) {
                     r32 = x32 - nb32;
@@ -588,16 +639,17 @@ zone_kernel(ZoneArgs A)
                 bool valid;
                 if (r32 > err) valid = nb.valid == 1;
                 else if (r32 < -err) valid = nb.valid == 0;
-                else valid = valid64(nb.a, nb.b, nb.vert, nb.valid, S.vx[i], S.vy[i]);
+                else valid = valid64(nb.a, nb.b, nb.vert, nb.valid, IX(S.vx, i), IX(S.vy, i));
                 // near the new line: may coincide (within 1e-9) with one of its intersections
                 float tol = (1.0f + nab) * 1.2e-9f + err;
-                uint8_t fl = S.vfl[i] & ~VB_ON;
+                uint8_t fl = IX(S.vfl, i) & ~VB_ON;
                 if (fabsf(r32) <= tol || !(fabsf(r32) < FLT_MAX)) fl |= VB_ON;
-                S.vfl[i] = fl;
-                if (!valid) S.vcnt[i] += 1;
+                IX(S.vfl, i) = fl;
+                if (!valid) IX(S.vcnt, i) += 1;
             }
-            __syncwarp();
+            WSYNC();
 
+            PHASE(3);
             // (2) candidate intersections: boundary edges (bottom, top, left,
             //     right; inf.h:340-374) then every earlier bisector in order
             const int C = 4 + nL;
@@ -615,8 +667,8 @@ zone_kernel(ZoneArgs A)
                     zs.cand += ok;
                 } else {
                     const int j = c - 4;
-                    const double ea = S.la[j], eb = S.lb[j];
-                    const int ev = S.lfl[j] & LB_VERT;
+                    const double ea = IX(S.la, j), eb = IX(S.lb, j);
+                    const int ev = IX(S.lfl, j) & LB_VERT;
                     bool need64 = true;
                     if (!nb.vert && !ev) {
                         // float interval of the intersection (directed rounding)
@@ -628,10 +680,16 @@ zone_kernel(ZoneArgs A)
                         float nl = __fsub_rd(b2l, b1h), nh = __fsub_ru(b2h, b1l);
                         if ((dl > 4e-9f || dh < -4e-9f) && fabsf(nl) < FLT_MAX && fabsf(nh) < FLT_MAX &&
                             fabsf(dl) < FLT_MAX && fabsf(dh) < FLT_MAX) {
-                            float q1 = __fdiv_rd(nl, dl), q2 = __fdiv_rd(nl, dh), q3 = __fdiv_rd(nh, dl), q4 = __fdiv_rd(nh, dh);
-                            float r1 = __fdiv_ru(nl, dl), r2 = __fdiv_ru(nl, dh), r3 = __fdiv_ru(nh, dl), r4 = __fdiv_ru(nh, dh);
-                            float xl = fminf(fminf(q1, q2), fminf(q3, q4));
-                            float xh = fmaxf(fmaxf(r1, r2), fmaxf(r3, r4));
+                            // x = N / D, N in [nl, nh], D in [dl, dh] not containing 0
+                            float xl, xh;
+                            if (dl > 0.0f) {
+                                xl = __fdiv_rd(nl, nl >= 0.0f ? dh : dl);
+                                xh = __fdiv_ru(nh, nh >= 0.0f ? dl : dh);
+                            } else {
+                                const float pl = -dh, ph = -dl;      // |D| in [pl, ph]
+                                xl = -__fdiv_ru(nh, nh >= 0.0f ? pl : ph);
+                                xh = -__fdiv_rd(nl, nl >= 0.0f ? ph : pl);
+                            }
                             // y = a1 x + b1 over the box
                             float m1 = __fmul_rd(a1l, xl), m2 = __fmul_rd(a1l, xh), m3 = __fmul_rd(a1h, xl), m4 = __fmul_rd(a1h, xh);
                             float n1 = __fmul_ru(a1l, xl), n2 = __fmul_ru(a1l, xh), n3 = __fmul_ru(a1h, xl), n4 = __fmul_ru(a1h, xh);
@@ -654,15 +712,15 @@ zone_kernel(ZoneArgs A)
                                     float K0 = ry + 3.01f * kU32 * fabsf(yc) + 1e-37f;
                                     int cert = 0;
                                     for (int m = 0; m < nL && cert < k; ++m) {
-                                        uint8_t lf = S.lfl[m];
-                                        float a = S.la32[m], b = S.lb32[m];
+                                        uint8_t lf = IX(S.lfl, m);
+                                        float a = IX(S.la32, m), b = IX(S.lb32, m);
                                         float sgn, err;
                                         if (lf & LB_VERT) {
                                             sgn = xc - b;
                                             err = K1 + 3.01f * kU32 * fabsf(b);
                                         } else {
                                             sgn = yc - fmaf(a, xc, b);
-                                            err = fmaf(fabsf(a), K1, K0 + S.lb3[m]);
+                                            err = fmaf(fabsf(a), K1, K0 + IX(S.lb3, m));
                                         }
                                         bool inval = (lf & LB_VALID) ? (sgn < -err) : (sgn > err);
                                         cert += inval;
@@ -679,14 +737,15 @@ zone_kernel(ZoneArgs A)
                     }
                     zs.cand++;
                 }
-                S.cx[c] = x;
-                S.cy[c] = y;
-                S.cx32[c] = (float)x;
-                S.cy32[c] = (float)y;
-                S.cfl[c] = ok ? (uint8_t)(cf | 0x80) : (uint8_t)0;
+                IX(S.cx, c) = x;
+                IX(S.cy, c) = y;
+                IX(S.cx32, c) = (float)x;
+                IX(S.cy32, c) = (float)y;
+                IX(S.cfl, c) = ok ? (uint8_t)(cf | 0x80) : (uint8_t)0;
             }
-            __syncwarp();
+            WSYNC();
 
+            PHASE(4);
             // (3) deduplicate (|dx| < 1e-9 and |dy| < 1e-9) against existing
             //     vertices near the new line and against earlier candidates
             {
@@ -694,154 +753,179 @@ zone_kernel(ZoneArgs A)
                 int nOn = 0;
                 for (int i0 = 0; i0 < nV0; i0 += 32) {
                     int i = i0 + lane;
-                    bool on = i < nV0 && (S.vfl[i] & VB_ON);
+                    bool on = i < nV0 && (IX(S.vfl, i) & VB_ON);
                     unsigned m = __ballot_sync(FULL, on);
-                    if (on) S.cons[nOn + __popc(m & ((1u << lane) - 1))] = i;   // cons reused as scratch
+                    if (on) IX(S.cons, nOn + __popc(m & ((1u << lane) - 1))) = i;   // cons reused as scratch
                     nOn += __popc(m);
                 }
-                __syncwarp();
-                if (lane == 0) sc->nCons = -1;   // considered list must be rebuilt
-                bool anyclose = false;
-                for (int c = lane; c < C; c += 32) {
-                    if (!(S.cfl[c] & 0x80)) continue;
-                    double x = S.cx[c], y = S.cy[c];
-                    bool dup = false;
-                    for (int t = 0; t < nOn && !dup; ++t) {
-                        int i = S.cons[t];
-                        if (fabs(__dsub_rn(S.vx[i], x)) < EPS && fabs(__dsub_rn(S.vy[i], y)) < EPS) dup = true;
-                    }
-                    if (dup) S.cfl[c] &= 0x7f;
-                    else {
-                        // any earlier valid candidate within float reach?
-                        // doubles within 1e-9 give floats within 1e-9 + u(|x1|+|x2|)
-                        float x32 = S.cx32[c], y32 = S.cy32[c];
-                        float tx = 3.0f * kU32 * fabsf(x32) + 2e-9f, ty = 3.0f * kU32 * fabsf(y32) + 2e-9f;
-                        for (int c2 = 0; c2 < c; ++c2) {
-                            if (!(S.cfl[c2] & 0x80)) continue;
-                            if (fabsf(S.cx32[c2] - x32) <= tx && fabsf(S.cy32[c2] - y32) <= ty) { anyclose = true; break; }
+                WSYNC();
+                nCons = -1;   // considered list must be rebuilt
+                if (nOn > 0) {
+                    for (int c = lane; c < C; c += 32) {
+                        if (!(IX(S.cfl, c) & 0x80)) continue;
+                        double x = IX(S.cx, c), y = IX(S.cy, c);
+                        bool dup = false;
+                        for (int t = 0; t < nOn && !dup; ++t) {
+                            int i = IX(S.cons, t);
+                            if (fabs(__dsub_rn(IX(S.vx, i), x)) < EPS && fabs(__dsub_rn(IX(S.vy, i), y)) < EPS) dup = true;
                         }
+                        if (dup) IX(S.cfl, c) &= 0x7f;
                     }
                 }
-                __syncwarp();
-                if (__any_sync(FULL, anyclose) && lane == 0) {
-                    // exact sequential resolution, in candidate order
-                    for (int c = 0; c < C; ++c) {
-                        if (!(S.cfl[c] & 0x80)) continue;
-                        for (int c2 = 0; c2 < c; ++c2) {
-                            if (!(S.cfl[c2] & 0x80)) continue;
-                            if (fabs(__dsub_rn(S.cx[c2], S.cx[c])) < EPS &&
-                                fabs(__dsub_rn(S.cy[c2], S.cy[c])) < EPS) { S.cfl[c] &= 0x7f; break; }
-                        }
-                    }
-                }
-                __syncwarp();
+                WSYNC();
             }
 
+            PHASE(5);
             // (4) counts of the surviving candidates over earlier bisectors
             for (int c = lane; c < C; c += 32) {
                 int cnt = k;
-                if (S.cfl[c] & 0x80) {
-                    double x = S.cx[c], y = S.cy[c];
-                    float xc = S.cx32[c], yc = S.cy32[c];
+                if (IX(S.cfl, c) & 0x80) {
+                    double x = IX(S.cx, c), y = IX(S.cy, c);
+                    float xc = IX(S.cx32, c), yc = IX(S.cy32, c);
                     float K1 = kU32 * fabsf(xc) * (1.0f + kU32) + 3.01f * kU32 * fabsf(xc);
                     float K0 = kU32 * fabsf(yc) + 3.01f * kU32 * fabsf(yc) + 1e-37f;
                     cnt = 0;
+                    // the bisector that generated this candidate passes through
+                    // it: its side is a rounding question, decided in FP64
+                    const int gen = c - 4;
+                    if (gen >= 0) {
+                        uint8_t lf = IX(S.lfl, gen);
+                        cnt += !valid64(IX(S.la, gen), IX(S.lb, gen), lf & LB_VERT, (lf & LB_VALID) ? 1 : 0, x, y);
+                    }
                     for (int m = 0; m < nL; ++m) {
-                        uint8_t lf = S.lfl[m];
-                        float a = S.la32[m], b = S.lb32[m];
+                        if (m == gen) continue;
+                        uint8_t lf = IX(S.lfl, m);
+                        float a = IX(S.la32, m), b = IX(S.lb32, m);
                         float sgn, err;
                         if (lf & LB_VERT) {
                             sgn = xc - b;
                             err = K1 + 3.01f * kU32 * fabsf(b);
                         } else {
                             sgn = yc - fmaf(a, xc, b);
-                            err = fmaf(fabsf(a), K1, K0 + S.lb3[m]);
+                            err = fmaf(fabsf(a), K1, K0 + IX(S.lb3, m));
                         }
                         bool inval;
                         if (sgn > err) inval = !(lf & LB_VALID);
                         else if (sgn < -err) inval = (lf & LB_VALID) != 0;
-                        else inval = !valid64(S.la[m], S.lb[m], lf & LB_VERT, (lf & LB_VALID) ? 1 : 0, x, y);
+                        else inval = !valid64(IX(S.la, m), IX(S.lb, m), lf & LB_VERT, (lf & LB_VALID) ? 1 : 0, x, y);
                         cnt += inval;
                     }
                 }
-                S.ccnt[c] = cnt;
+                IX(S.ccnt, c) = cnt;
             }
-            __syncwarp();
+            WSYNC();
+            // (4b) a candidate closer than 1e-9 to an earlier one is not added
+            // (the reference keeps the first).  Only a kept candidate can change
+            // the vertex set, so the float prefilter runs for those; any hit
+            // triggers the exact sequential resolution over all candidates.
+            {
+                bool anyclose = false;
+                for (int c = lane; c < C; c += 32) {
+                    if (!(IX(S.cfl, c) & 0x80) || IX(S.ccnt, c) >= k) continue;
+                    // doubles within 1e-9 give floats within 1e-9 + u(|x1|+|x2|)
+                    float x32 = IX(S.cx32, c), y32 = IX(S.cy32, c);
+                    float tx = 3.0f * kU32 * fabsf(x32) + 2e-9f, ty = 3.0f * kU32 * fabsf(y32) + 2e-9f;
+                    for (int c2 = 0; c2 < c; ++c2) {
+                        if (!(IX(S.cfl, c2) & 0x80)) continue;
+                        if (fabsf(IX(S.cx32, c2) - x32) <= tx && fabsf(IX(S.cy32, c2) - y32) <= ty) { anyclose = true; break; }
+                    }
+                }
+                if (__any_sync(FULL, anyclose)) {
+                    if (lane == 0) {
+                        for (int c = 0; c < C; ++c) {
+                            if (!(IX(S.cfl, c) & 0x80)) continue;
+                            for (int c2 = 0; c2 < c; ++c2) {
+                                if (!(IX(S.cfl, c2) & 0x80)) continue;
+                                if (fabs(__dsub_rn(IX(S.cx, c2), IX(S.cx, c))) < EPS &&
+                                    fabs(__dsub_rn(IX(S.cy, c2), IX(S.cy, c))) < EPS) { IX(S.cfl, c) &= 0x7f; break; }
+                            }
+                        }
+                    }
+                    WSYNC();
+                }
+            }
 
             // (5) erase old vertices with count >= k (order kept), then append
             //     the new vertices with count < k in candidate order
             int w = 0;
             for (int i0 = 0; i0 < nV0; i0 += 32) {
                 int i = i0 + lane;
-                bool keep = i < nV0 && S.vcnt[i] < k;
+                bool keep = i < nV0 && IX(S.vcnt, i) < k;
                 double x = 0, y = 0, d2 = 0;
-                float x32 = 0, y32 = 0;
+                float x32 = 0, y32 = 0, d2f = 0;
                 int cnt = 0;
                 uint8_t fl = 0;
                 if (keep) {
-                    x = S.vx[i]; y = S.vy[i]; d2 = S.vd2[i];
-                    x32 = S.vx32[i]; y32 = S.vy32[i]; cnt = S.vcnt[i]; fl = S.vfl[i] & ~VB_ON;
+                    x = IX(S.vx, i); y = IX(S.vy, i); d2 = IX(S.vd2, i); d2f = IX(S.vd2f, i);
+                    x32 = IX(S.vx32, i); y32 = IX(S.vy32, i); cnt = IX(S.vcnt, i); fl = IX(S.vfl, i) & ~VB_ON;
                 }
                 unsigned m = __ballot_sync(FULL, keep);
-                __syncwarp();
+                WSYNC();
                 if (keep) {
                     int o = w + __popc(m & ((1u << lane) - 1));
-                    S.vx[o] = x; S.vy[o] = y; S.vd2[o] = d2;
-                    S.vx32[o] = x32; S.vy32[o] = y32; S.vcnt[o] = cnt; S.vfl[o] = fl;
+                    IX(S.vx, o) = x; IX(S.vy, o) = y; IX(S.vd2, o) = d2; IX(S.vd2f, o) = d2f;
+                    IX(S.vx32, o) = x32; IX(S.vy32, o) = y32; IX(S.vcnt, o) = cnt; IX(S.vfl, o) = fl;
                 }
                 w += __popc(m);
-                __syncwarp();
+                WSYNC();
             }
             int nnew = 0;
             for (int c0 = 0; c0 < C; c0 += 32) {
                 int c = c0 + lane;
-                bool keep = c < C && (S.cfl[c] & 0x80) && S.ccnt[c] < k;
+                bool keep = c < C && (IX(S.cfl, c) & 0x80) && IX(S.ccnt, c) < k;
                 unsigned m = __ballot_sync(FULL, keep);
                 int o = w + nnew + __popc(m & ((1u << lane) - 1));
                 if (keep && o < VC) {
-                    double x = S.cx[c], y = S.cy[c];
-                    S.vx[o] = x; S.vy[o] = y;
-                    S.vx32[o] = S.cx32[c]; S.vy32[o] = S.cy32[c];
-                    S.vd2[o] = d2_64(x, y, qx, qy);
-                    S.vcnt[o] = S.ccnt[c];
-                    S.vfl[o] = S.cfl[c] & VB_BND;
+                    double x = IX(S.cx, c), y = IX(S.cy, c);
+                    IX(S.vx, o) = x; IX(S.vy, o) = y;
+                    IX(S.vx32, o) = IX(S.cx32, c); IX(S.vy32, o) = IX(S.cy32, c);
+                    const double d2n = d2_64(x, y, qx, qy);
+                    IX(S.vd2, o) = d2n;
+                    IX(S.vd2f, o) = (float)d2n;
+                    IX(S.vcnt, o) = IX(S.ccnt, c);
+                    IX(S.vfl, o) = IX(S.cfl, c) & VB_BND;
                 }
                 nnew += __popc(m);
             }
             zs.kept += nnew;
-            int nV = w + nnew;
-            bool vover = nV > VC;
+            nV = w + nnew;
+            const bool vover = nV > VC;
             if (vover) nV = VC;
 
             // (6) nearest bisector distance, store the line (inf.cpp:430-434)
-            if (lane == 0) {
-                double dl = line_dist64(qx, qy, nb.a, nb.b, nb.vert);
-                if (dl < sc->nearb) sc->nearb = dl;
-                S.la[nL] = nb.a;
-                S.lb[nL] = nb.b;
-                S.lfl[nL] = (uint8_t)((nb.vert ? LB_VERT : 0) | (nb.valid ? LB_VALID : 0));
-                S.la32[nL] = na32;
-                S.lb32[nL] = nb32;
-                S.lb3[nL] = 3.01f * kU32 * fabsf(nb32) + 1e-37f;
-                S.lpos[nL] = id;
-                sc->nL = nL + 1;
-                sc->nV = nV;
-                if (vover) sc->flags |= QF_ZONE_V_OVERFLOW;
+            {
+                double dl = 0.0;
+                if (lane == 0) dl = line_dist64(qx, qy, nb.a, nb.b, nb.vert);
+                dl = __shfl_sync(FULL, dl, 0);
+                if (dl < nearb) nearb = dl;
             }
+            if (lane == 0) {
+                IX(S.la, nL) = nb.a;
+                IX(S.lb, nL) = nb.b;
+                IX(S.lfl, nL) = (uint8_t)((nb.vert ? LB_VERT : 0) | (nb.valid ? LB_VALID : 0));
+                IX(S.la32, nL) = na32;
+                IX(S.lb32, nL) = nb32;
+                IX(S.lb3, nL) = 3.01f * kU32 * fabsf(nb32) + 1e-37f;
+                IX(S.lpos, nL) = id;
+            }
+            nL += 1;
+            if (vover) flags |= QF_ZONE_V_OVERFLOW;
             if (nV > zs.vmax) zs.vmax = nV;
-            __syncwarp();
+            WSYNC();
             // (7) furthest remaining vertex (inf.cpp:445-451)
             {
-                double m = 0.0;
-                for (int i = lane; i < nV; i += 32) m = fmax(m, S.vd2[i]);
-                m = warp_max(m);
-                if (lane == 0) sc->far_ = __dsqrt_rn(m);
+                long long m = 0;
+                for (int i = lane; i < nV; i += 32) m = max(m, __double_as_longlong(IX(S.vd2, i)));
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(FULL, m, o));
+                far_ = __dsqrt_rn(__longlong_as_double(m));
             }
-            __syncwarp();
-            if (sc->flags) break;
+            WSYNC();
+            PHASE(6);
+            if (flags) break;
         }
-        qflags |= sc->flags;
-        const int nL = sc->nL;
+        WSYNC();
+        qflags |= flags;
         zs.nb = nL;
         zs.cand = warp_sum(zs.cand);
         zs.cand64 = warp_sum(zs.cand64);
@@ -851,16 +935,15 @@ zone_kernel(ZoneArgs A)
         // nearer than q  <=>  m < 0.
         float4* planes = A.planes + (size_t)s * LC;
         double cmax = 0.0;
-        float4* splanes = (float4*)S.cx;      // staging copy for the cell scan
         for (int m = lane; m < nL; m += 32) {
-            int pos = S.lpos[m];
-            float2 f = A.fxy[pos];
+            int pos = IX(S.lpos, m);
+            float2 f = A.fxy[GX(pos, A.nf, 101)];
             double dx = (double)f.x - qx, dy = (double)f.y - qy;
             double c = dx * dx + dy * dy;
             float4 p = make_float4((float)(-2.0 * dx), (float)(-2.0 * dy), (float)c, 0.0f);
-            planes[m] = p;
-            splanes[m] = p;
-            A.bis_pos[(size_t)s * LC + m] = pos;
+            planes[GX(m, LC, 106)] = p;
+            IX(S.splanes, m) = p;
+            A.bis_pos[(size_t)s * LC + GX(m, LC, 107)] = pos;
             cmax = fmax(cmax, c);
         }
         cmax = warp_max(cmax);
@@ -870,7 +953,7 @@ zone_kernel(ZoneArgs A)
         const float kf2 = (float)(8.0 * (double)kU32 * Fp * Fp * (1.0 + 1e-6)) + 1e-30f;
         const double k2f64 = 8.0 * kU64 * 2.0 * Fp * (1.0 + 1e-6);
         const double kf264 = 8.0 * kU64 * Fp * Fp * (1.0 + 1e-6) + 1e-300;
-        __syncwarp();
+        WSYNC();
 
         // ---- epilogue 2: ring scan over user cells ------------------------
         const Grid gu = A.gu;
@@ -879,8 +962,8 @@ zone_kernel(ZoneArgs A)
         const int RM = A.rmax;
         const int W = 2 * RM + 1;
         const int nwords = (W * W + 31) / 32;
-        for (int i = lane; i < nwords; i += 32) S.bitmap[i] = 0u;
-        __syncwarp();
+        for (int i = lane; i < nwords; i += 32) IX(S.bitmap, i) = 0u;
+        WSYNC();
         const float delta = 8.0f * kU32 * (fabsf(gu.x0) + fabsf(gu.y0) + gu.cs * (float)max(gu.gx, gu.gy) + fabsf(qf.x) + fabsf(qf.y) + gu.cs) + 1e-30f;
         const int rmaxu = max(max(ucx, gu.gx - 1 - ucx), max(ucy, gu.gy - 1 - ucy));
         bool all_users = nL == 0 && A.nu > 0;
@@ -912,7 +995,7 @@ zone_kernel(ZoneArgs A)
                         float Y1 = (gu.y0 + (float)(cyy + 1) * gu.cs) - qf.y + delta;
                         int viol = 0;
                         for (int m = 0; m < nL && viol < k; ++m) {
-                            float4 p = splanes[m];
+                            float4 p = IX(S.splanes, m);
                             float X = p.x > 0.0f ? X1 : X0;
                             float Y = p.y > 0.0f ? Y1 : Y0;
                             float mx = fmaf(p.x, X, fmaf(p.y, Y, p.z));
@@ -923,7 +1006,7 @@ zone_kernel(ZoneArgs A)
                     }
                     if (keep) {
                         int bit = (dy + RM) * W + (dx + RM);
-                        atomicOr(&S.bitmap[bit >> 5], 1u << (bit & 31));
+                        atomicOr(&IX(S.bitmap, bit >> 5), 1u << (bit & 31));
                     }
                     anykeep |= keep;
                 }
@@ -933,7 +1016,7 @@ zone_kernel(ZoneArgs A)
             }
             zs.rings = rend + 1;
         }
-        __syncwarp();
+        WSYNC();
 
         // ---- segments: one user range per row ------------------------------
         int2* seg = A.segs + (size_t)s * A.seg_cap;
@@ -955,14 +1038,14 @@ zone_kernel(ZoneArgs A)
                     int xmin = INT_MAX, xmax = -1;
                     for (int cxx = xl0; cxx <= xl1; ++cxx) {
                         int bit = (dy + RM) * W + (cxx - ucx + RM);
-                        if (S.bitmap[bit >> 5] & (1u << (bit & 31))) {
+                        if (IX(S.bitmap, bit >> 5) & (1u << (bit & 31))) {
                             xmin = min(xmin, cxx);
                             xmax = cxx;
                         }
                     }
                     if (xmax >= 0) {
-                        st = A.ustart[row * gu.gx + xmin];
-                        len = A.ustart[row * gu.gx + xmax + 1] - st;
+                        st = A.ustart[GX(row * gu.gx + xmin, NCU + 1, 104)];
+                        len = A.ustart[GX(row * gu.gx + xmax + 1, NCU + 1, 104)] - st;
                     }
                 }
                 bool has = len > 0;
@@ -975,13 +1058,15 @@ zone_kernel(ZoneArgs A)
                     if (lane >= o) incl += v;
                 }
                 int excl = incl - (has ? len : 0);
-                if (has) seg[nseg + pre] = make_int2(st, ncand + excl);
+                if (has) seg[GX(nseg + pre, A.seg_cap, 108)] = make_int2(st, ncand + excl);
                 nseg += __popc(m);
                 ncand += __shfl_sync(FULL, incl, 31);
             }
-            if (lane == 0) seg[nseg] = make_int2(0, ncand);
+            if (lane == 0) seg[GX(nseg, A.seg_cap, 109)] = make_int2(0, ncand);
         }
 
+        PHASE(7);
+#undef PHASE
         if (lane == 0) {
             QDesc d;
             d.qx = qf.x;
@@ -999,8 +1084,11 @@ zone_kernel(ZoneArgs A)
             *qd = d;
             A.zst[s] = zs;
         }
-        __syncwarp();
+        WSYNC();
     }
 }
+#undef WSYNC
+
+__global__ void __launch_bounds__(ZONE_WARPS * 32) zone_kernel_smem(ZoneArgs a) { zone_body<false>(a); }
 
 }  // namespace rknn

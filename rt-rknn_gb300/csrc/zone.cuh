@@ -17,7 +17,7 @@ struct ZoneCaps {
 };
 
 struct ZoneLayout {
-    size_t vx, vy, vd2, vx32, vy32, vcnt, vfl, cons;
+    size_t vx, vy, vd2, vx32, vy32, vd2f, vcnt, vfl, cons;
     size_t la, lb, la32, lb32, lb3, lfl, lpos;
     size_t pqk, pqc;
     size_t cx, cy, cx32, cy32, ccnt, cfl;
@@ -27,18 +27,26 @@ struct ZoneLayout {
 
 __host__ __device__ inline size_t zl_align(size_t x) { return (x + 15) & ~(size_t)15; }
 
+#if defined(RKNN_CHECKED) && defined(RKNN_CHECKED_SPARE)
+constexpr size_t ZL_SPARE = 1;     // one spare element per array takes rejected accesses
+#else
+constexpr size_t ZL_SPARE = 0;
+#endif
+
 __host__ __device__ inline ZoneLayout zone_layout(const ZoneCaps& c)
 {
     ZoneLayout L;
     size_t o = 0;
-    const size_t VC = c.vc, LC = c.lc, PC = c.pc, CC = (size_t)c.lc + 4;
+    const size_t VC = c.vc + ZL_SPARE, LC = c.lc + ZL_SPARE, PC = c.pc + ZL_SPARE;
+    const size_t CC = (size_t)c.lc + 4 + ZL_SPARE;
     const size_t W = 2 * (size_t)c.rm + 1;
-    const size_t bm = ((W * W + 31) / 32) * 4;
+    const size_t bm = ((W * W + 31) / 32 + ZL_SPARE) * 4;
     L.vx = o;   o = zl_align(o + (8 * VC > bm ? 8 * VC : bm));
     L.vy = o;   o = zl_align(o + 8 * VC);
     L.vd2 = o;  o = zl_align(o + 8 * VC);
     L.vx32 = o; o = zl_align(o + 4 * VC);
     L.vy32 = o; o = zl_align(o + 4 * VC);
+    L.vd2f = o; o = zl_align(o + 4 * VC);
     L.vcnt = o; o = zl_align(o + 4 * VC);
     L.vfl = o;  o = zl_align(o + VC);
     L.cons = o; o = zl_align(o + 4 * VC);
@@ -57,8 +65,8 @@ __host__ __device__ inline ZoneLayout zone_layout(const ZoneCaps& c)
     L.cy32 = o; o = zl_align(o + 4 * CC);
     L.ccnt = o; o = zl_align(o + 4 * CC);
     L.cfl = o;  o = zl_align(o + CC);
-    L.tk = o;   o = zl_align(o + 8 * 32);
-    L.tc = o;   o = zl_align(o + 4 * 32);
+    L.tk = o;   o = zl_align(o + 8 * (32 + ZL_SPARE));
+    L.tc = o;   o = zl_align(o + 4 * (32 + ZL_SPARE));
     L.sc = o;   o = zl_align(o + 128);
     L.bytes = o;
     return L;
@@ -95,8 +103,10 @@ struct ZoneArgs {
     int* bis_pos;            // [slot][caps.lc] facility positions of the bisectors
     int2* segs;              // [slot][seg_cap]: (user start, candidate offset)
     ZStats* zst;
+    int* fault;              // checked builds: {flag, array id, index, capacity, line}
 };
 
-__global__ void zone_kernel(ZoneArgs a);
+// zone state in shared memory, one warp (one query at a time) per block
+__global__ void zone_kernel_smem(ZoneArgs a);
 
 }  // namespace rknn

@@ -67,10 +67,13 @@ class Stats(C.Structure):
                 ("zone_vertices_max", C.c_int64), ("zone_candidates", C.c_int64),
                 ("zone_fp64", C.c_int64), ("candidates", C.c_int64), ("plane_evals", C.c_int64),
                 ("survivors", C.c_int64), ("fac_checks", C.c_int64), ("rechecks", C.c_int64),
-                ("overflow", C.c_int64), ("device_ms", C.c_double)]
+                ("overflow", C.c_int64), ("device_ms", C.c_double),
+                ("zone_cycles", C.c_int64 * 8)]
 
     def as_dict(self):
-        return {n: getattr(self, n) for n, _ in self._fields_}
+        d = {n: getattr(self, n) for n, _ in self._fields_}
+        d["zone_cycles"] = list(self.zone_cycles)
+        return d
 
 
 _lib = None
