@@ -118,6 +118,22 @@ rknn_status rknn_query(rknn_index* idx, int32_t q_index, int32_t k, int32_t mode
                        int32_t* out_ids, int64_t cap, int64_t* n_out,
                        rknn_query_stats* stats);
 
+/* One query that allocates nothing.  No counterpart in the reference.
+ * For callers that cannot allocate device memory at query time (plugins in a
+ * host process whose device memory all belongs to that host's own allocator,
+ * serving loops that must not stall on cudaMalloc): the per-query scratch lives in a
+ * fixed 16 MiB device array that the library holds on every device that
+ * loads it, until exit.  Same semantics and outputs as rknn_query, host
+ * buffers, synchronous.  Limits: k <= 128 (larger k: RKNN_ERR_CAPACITY) and
+ * at most about 2 million candidate users for the query (otherwise
+ * RKNN_ERR_CAPACITY; use rknn_query).  The first call on a device looks up
+ * the array's device address; make that first call before any stream
+ * capture.  All calls share the array: they are serialized by a process-wide
+ * lock and finish before returning (calls that overlapped on the GPU would
+ * race on it).  The index is built beforehand by rknn_index_create. */
+rknn_status rknn_query_noalloc(rknn_index* idx, int32_t q_index, int32_t k, int32_t mode,
+                               int32_t* out_ids, int64_t cap, int64_t* n_out);
+
 /* nq queries in one launch sequence (CUDA graph), host buffers.  Results of
  * query i are out_ids[offsets[i] .. offsets[i+1]); offsets has nq+1 entries.
  * RKNN_ERR_CAPACITY when cap < offsets[nq] (offsets still filled). */

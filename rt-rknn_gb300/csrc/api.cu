@@ -726,3 +726,163 @@ rknn_status rknn_last_zone(rknn_index* ix, int32_t slot, int32_t* bis_fac, int32
 }
 
 }  // extern "C"
+
+// ====================================================================
+// Allocation-free single query.
+//
+// Some callers may not allocate device memory at query time: plugins loaded
+// into a host process whose device memory all belongs to that host's own
+// allocator, or latency-critical serving loops that must not stall on
+// cudaMalloc.  For them rknn_query_noalloc answers one query with all of
+// its per-query scratch (query descriptor, half-planes, user segments,
+// offsets, counters and the result pool) in one file-scope device array of
+// fixed size; the kernels are the same ones rknn_query launches.  The index
+// itself is built beforehand by rknn_index_create.
+namespace {
+
+constexpr size_t NOALLOC_BYTES = 16u << 20;      // 16 MiB per device, held until exit
+constexpr int NOALLOC_KMAX = 128;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+// scratch shared by every call on this device; calls are serialized below
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+struct NoallocLayout {
+    int *counters, *q, *k, *cand_off, *chunk_off, *res_count, *out_off, *bispos, *pool, *out;
+    QDesc* qd;
+    ZStats* zst;
+    float4* planes;
+    int2* segs;
+    VStats* vstats;
+    long long pool_cap;
+};
+
+inline size_t na_align(size_t x) { return (x + 255) & ~(size_t)255; }
+
+NoallocLayout noalloc_layout(unsigned char* base, int lc, int seg_cap)
+{
+    NoallocLayout L;
+    size_t o = 0;
+    auto take = [&](size_t bytes) { unsigned char* p = base + o; o = na_align(o + bytes); return p; };
+    L.counters = (int*)take(sizeof(int) * 16);
+    L.q = (int*)take(sizeof(int));
+    L.k = (int*)take(sizeof(int));
+    L.cand_off = (int*)take(sizeof(int) * 2);
+    L.chunk_off = (int*)take(sizeof(int) * 2);
+    L.res_count = (int*)take(sizeof(int));
+    L.out_off = (int*)take(sizeof(int) * 2);
+    L.qd = (QDesc*)take(sizeof(QDesc));
+    L.zst = (ZStats*)take(sizeof(ZStats));
+    L.vstats = (VStats*)take(sizeof(VStats));
+    L.planes = (float4*)take(sizeof(float4) * lc);
+    L.bispos = (int*)take(sizeof(int) * lc);
+    L.segs = (int2*)take(sizeof(int2) * seg_cap);
+    const size_t rest = NOALLOC_BYTES > o ? NOALLOC_BYTES - o : 0;
+    L.pool_cap = (long long)(rest / 2 / sizeof(int)) - 64;
+    L.pool = (int*)take(sizeof(int) * (size_t)L.pool_cap);
+    L.out = (int*)take(sizeof(int) * (size_t)L.pool_cap);
+    return L;
+}
+
+}  // namespace
+
+extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, int32_t mode,
+                                          int32_t* out_ids, int64_t cap, int64_t* n_out)
+{
+    g_err.clear();
+    if (!ix || !n_out || (cap > 0 && !out_ids)) return fail(RKNN_ERR_ARG, "null argument");
+    *n_out = 0;
+    if (mode != RKNN_MODE_FP32 && mode != RKNN_MODE_FP64) return fail(RKNN_ERR_ARG, "bad mode");
+    if (q < 0 || q >= ix->nf) return fail(RKNN_ERR_ARG, "query index out of range");
+    if (k <= 0) return fail(RKNN_ERR_ARG, "k must be a positive integer");
+    if (k > NOALLOC_KMAX)
+        return fail(RKNN_ERR_CAPACITY, "rknn_query_noalloc supports k <= 128 (fixed scratch); use rknn_query");
+    if (ix->device < 0 || ix->device >= NOALLOC_MAX_DEVICES) return fail(RKNN_ERR_ARG, "device ordinal too large");
+
+    std::lock_guard<std::mutex> glk(g_noalloc_mu);
+    std::lock_guard<std::mutex> lk(ix->mu);
+    CK(cudaSetDevice(ix->device));
+    // once per device, with that device current: the array's device address
+    if (!g_noalloc_ptr[ix->device]) {
+        void* p = nullptr;
+        CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[ix->device] = (unsigned char*)p;
+    }
+    const ZoneCaps caps = caps_fit(ix, caps_for(k));
+    const int seg_cap = 2 * caps.rm + 2;
+    NoallocLayout L = noalloc_layout(g_noalloc_ptr[ix->device], caps_for(NOALLOC_KMAX).lc, seg_cap);
+    cudaStream_t st = ix->stream;
+
+    // inputs and zeroed counters (the array keeps the previous call's contents)
+    int qk[2] = {q, k};
+    CK(cudaMemcpyAsync(L.q, &qk[0], sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(L.k, &qk[1], sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(L.counters, 0, sizeof(int) * 16, st));
+    CK(cudaMemsetAsync(L.res_count, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(L.vstats, 0, sizeof(VStats), st));
+
+    ZoneArgs za;
+    za.fxy = ix->d_fxy; za.fstart = ix->d_fstart; za.fmbr = ix->d_fmbr; za.fpos = ix->d_fpos;
+    za.gf = ix->gf; za.nf = (int)ix->nf;
+    za.ustart = ix->d_ustart; za.gu = ix->gu; za.nu = (int)ix->nu;
+    za.sx0 = ix->sx0; za.sy0 = ix->sy0; za.sx1 = ix->sx1; za.sy1 = ix->sy1;
+    za.q_in = L.q; za.k_in = L.k; za.order = nullptr; za.nq = 1;
+    za.work_counter = L.counters + 0;
+    za.caps = caps;
+    za.use_global = 0;
+    za.gscratch = nullptr;
+    za.skip_coincident = ix->skip_coincident;
+    za.rmax = caps.rm;
+    za.seg_cap = seg_cap;
+    za.qd = L.qd; za.planes = L.planes; za.bis_pos = L.bispos; za.segs = L.segs; za.zst = L.zst;
+    za.fault = L.counters + 4;
+    const size_t zsmem = zone_layout(caps).bytes * ZONE_WARPS;
+    if (zsmem > 48 * 1024)
+        CK(cudaFuncSetAttribute(zone_kernel_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsmem));
+    zone_kernel_smem<<<1, 32 * ZONE_WARPS, zsmem, st>>>(za);
+    CK(cudaGetLastError());
+    plan_kernel<<<1, 1024, 0, st>>>(L.qd, 1, L.cand_off, L.chunk_off, (int)std::min<long long>(L.pool_cap, INT32_MAX));
+    CK(cudaGetLastError());
+
+    VerifyArgs va;
+    va.qd = L.qd; va.planes = L.planes; va.bis_pos = L.bispos; va.lc = caps.lc;
+    va.segs = L.segs; va.seg_cap = seg_cap;
+    va.chunk_off = L.chunk_off; va.cand_off = L.cand_off; va.nq = 1;
+    va.uxy = ix->d_uxy; va.uid = ix->d_uid; va.fxy = ix->d_fxy; va.fstart = ix->d_fstart; va.gf = ix->gf;
+    va.res_count = L.res_count; va.res_pool = L.pool; va.work_counter = L.counters + 1;
+    va.vstats = L.vstats; va.mode = mode;
+    va.nu = (int)ix->nu; va.nf = (int)ix->nf; va.ncf = ix->gf.gx * ix->gf.gy;
+    va.pool_cap = L.pool_cap; va.fault = L.counters + 10;
+    const size_t vsmem = (size_t)VERIFY_WARPS * caps.lc * (mode == MODE_FP32 ? 16 : 32);
+    if (vsmem > 48 * 1024)
+        CK(cudaFuncSetAttribute(verify_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem));
+    verify_kernel<<<2 * ix->num_sms, VERIFY_WARPS * 32, vsmem, st>>>(va);
+    CK(cudaGetLastError());
+    scan_counts_kernel<<<1, 1024, 0, st>>>(L.res_count, 1, L.out_off);
+    CK(cudaGetLastError());
+    CK(cudaFuncSetAttribute(finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)(SORT_CAP * sizeof(unsigned))));
+    finalize_kernel<<<1, 256, SORT_CAP * sizeof(unsigned), st>>>(L.pool, L.cand_off, L.res_count, L.out_off,
+                                                                  L.out, 1);
+    CK(cudaGetLastError());
+
+    QDesc d;
+    int off[2] = {0, 0};
+    CK(cudaMemcpyAsync(&d, L.qd, sizeof(QDesc), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(off, L.out_off, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (d.flags & QF_RESULT_OVERFLOW)
+        return fail(RKNN_ERR_CAPACITY, "rknn_query_noalloc: the query's candidate users exceed the fixed "
+                                       "scratch (about 2M); use rknn_query");
+    const int64_t n = off[1];
+    *n_out = n;
+    if (n > cap) return fail(RKNN_ERR_CAPACITY, "output buffer too small");
+    if (n > 0) {
+        CK(cudaMemcpyAsync(out_ids, L.out, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    return RKNN_OK;
+}

@@ -33,7 +33,7 @@ STATUS = {0: "RKNN_OK", 1: "RKNN_ERR_ARG", 2: "RKNN_ERR_OOM", 3: "RKNN_ERR_CUDA"
 
 # every symbol include/rknn_gpu.h declares
 EXPORTS = ["rknn_index_opts_default", "rknn_index_create", "rknn_index_destroy",
-           "rknn_index_size", "rknn_index_get_info", "rknn_query", "rknn_query_batch", "rknn_query_batch_device",
+           "rknn_index_size", "rknn_index_get_info", "rknn_query", "rknn_query_noalloc", "rknn_query_batch", "rknn_query_batch_device",
            "rknn_batch_device_results", "rknn_sync", "rknn_set_stream", "rknn_last_stats",
            "rknn_last_zone", "rknn_set_profiling", "rknn_last_kernel_ms",
            "rknn_last_error", "rknn_version"]
@@ -96,6 +96,7 @@ def load(path: str = LIB_PATH):
     L.rknn_index_get_info.argtypes = [vp, C.POINTER(Info)]
     L.rknn_query.argtypes = [vp, i32, i32, i32, vp, i64, C.POINTER(i64), C.POINTER(Stats)]
     L.rknn_query_batch.argtypes = [vp, vp, vp, i32, i32, vp, i64, vp, C.POINTER(Stats)]
+    L.rknn_query_noalloc.argtypes = [vp, i32, i32, i32, vp, i64, C.POINTER(i64)]
     L.rknn_query_batch_device.argtypes = [vp, vp, vp, i32, i32, i32]
     L.rknn_batch_device_results.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
     L.rknn_sync.argtypes = [vp]
@@ -183,6 +184,17 @@ class Index:
                             C.byref(n), C.byref(st) if stats else None))
         ids = out[: n.value].copy()
         return (ids, st.as_dict()) if stats else ids
+
+    def query_noalloc(self, q: int, k: int, mode="fp64"):
+        """Sorted user ids of RkNN_k(q) through rknn_query_noalloc: no device
+        allocation at query time (the scratch is a fixed device array)."""
+        L = load()
+        cap = max(16, self.nu)
+        out = np.empty(cap, np.int32)
+        n = C.c_int64(0)
+        _check(L.rknn_query_noalloc(self.h, int(q), int(k), _MODES[mode], out.ctypes.data, cap,
+                                    C.byref(n)))
+        return out[: n.value].copy()
 
     def query_batch(self, qs, ks, mode="fp32", stats: bool = False):
         """List of sorted id arrays, one per query (rknn_query_batch)."""
