@@ -175,6 +175,9 @@ ZoneCaps caps_fit(rknn_index* ix, ZoneCaps c)
     while (zone_layout(c).bytes * ZONE_WARPS > budget && c.vc > 256) c.vc = c.vc * 7 / 8;
     while (zone_layout(c).bytes * ZONE_WARPS > budget && c.pc > 512) c.pc = c.pc * 7 / 8;
     while (zone_layout(c).bytes * ZONE_WARPS > budget && c.lc > 64) c.lc = c.lc * 7 / 8;
+    // vertex counts and indices are stored in 16 bits
+    c.vc = std::min(c.vc, 65535);
+    c.lc = std::min(c.lc, 65535);
     return c;
 }
 

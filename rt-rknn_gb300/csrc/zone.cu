@@ -40,8 +40,10 @@ namespace {
 constexpr unsigned FULL = 0xffffffffu;
 constexpr double EPS = 1e-9;           // inf.cpp:270,375,408; inf.h:324
 
-// flags of a vertex
-constexpr uint8_t VB_BND = 1, VB_ON = 2;
+// flags of a vertex: created on the space boundary, near the newest line,
+// and within EPS of the left / right / bottom / top edge (decided once in
+// FP64 when the vertex is created; inf.cpp:283-321 tests the same per lookup)
+constexpr uint8_t VB_BND = 1, VB_ON = 2, VB_EL = 4, VB_ER = 8, VB_EB = 16, VB_ET = 32;
 // flags of a line
 constexpr uint8_t LB_VERT = 1, LB_VALID = 2;
 
@@ -194,11 +196,11 @@ struct Arr {
 #endif
 
 struct Slice {
-    Arr<double> vx, vy, vd2;
+    Arr<double> vx, vy;
     Arr<float> vx32, vy32, vd2f;
-    Arr<int> vcnt;
+    Arr<uint16_t> vcnt;
     Arr<uint8_t> vfl;
-    Arr<int> cons;
+    Arr<uint16_t> cons;
     Arr<double> la, lb;
     Arr<float> la32, lb32, lb3;
     Arr<uint8_t> lfl;
@@ -227,9 +229,9 @@ __device__ Slice carve(char* base, const ZoneCaps& c)
 #else
 #define CARVE(f, T, off, n, i) s.f = Arr<T>{(T*)(base + L.off)}
 #endif
-    CARVE(vx, double, vx, VC, 1); CARVE(vy, double, vy, VC, 2); CARVE(vd2, double, vd2, VC, 3);
+    CARVE(vx, double, vx, VC, 1); CARVE(vy, double, vy, VC, 2);
     CARVE(vx32, float, vx32, VC, 4); CARVE(vy32, float, vy32, VC, 5); CARVE(vd2f, float, vd2f, VC, 6);
-    CARVE(vcnt, int, vcnt, VC, 7); CARVE(vfl, uint8_t, vfl, VC, 8); CARVE(cons, int, cons, VC, 9);
+    CARVE(vcnt, uint16_t, vcnt, VC, 7); CARVE(vfl, uint8_t, vfl, VC, 8); CARVE(cons, uint16_t, cons, VC, 9);
     CARVE(la, double, la, LC, 10); CARVE(lb, double, lb, LC, 11); CARVE(la32, float, la32, LC, 12);
     CARVE(lb32, float, lb32, LC, 13); CARVE(lb3, float, lb3, LC, 14); CARVE(lfl, uint8_t, lfl, LC, 15);
     CARVE(lpos, int, lpos, LC, 16); CARVE(pqk, uint64_t, pqk, PC, 17); CARVE(pqc, uint32_t, pqc, PC, 18);
@@ -302,22 +304,90 @@ __device__ __forceinline__ int warp_sum(int v)
     return v;
 }
 
-// Decision of the vertex test for one vertex, float32 first.  Returns 1 if
-// dist64(p, v) < dist64(q, v) as the reference computes it.
-//   D  = squared distance from the facility (or rectangle) to the vertex
-//   d2v = vertex's squared distance to q (FP64, the reference's dq squared)
-__device__ __forceinline__ bool closer_than_q(float dxp, float dyp, float E, float V, double d2v,
-                                              double dx64, double dy64)
+// Vertex test for one vertex in float32: 1 if the facility (or rectangle)
+// is certainly nearer to the vertex than q is, 0 if certainly not, -1 if the
+// float evaluation cannot decide (the caller then decides in FP64).
+//   dxp, dyp = float offsets from the facility (rectangle) to the vertex
+//   E = bound on a vertex coordinate's float rounding error
+//   V = the vertex's squared distance to q, rounded to float
+__device__ __forceinline__ int closer32(float dxp, float dyp, float E, float V)
 {
     float D = fmaf(dxp, dxp, dyp * dyp);
     float ep = E + kU32 * (fabsf(dxp) + fabsf(dyp));
     float err = fmaf(2.0f * (fabsf(dxp) + fabsf(dyp)) + 2.0f * ep, ep, 4.0f * kU32 * D) + 1e-30f;
     float vlo = V * (1.0f - 4.0f * kU32), vhi = V * (1.0f + 4.0f * kU32);
-    if (D + err < vlo) return true;
-    if (D - err > vhi) return false;
-    double dp = __dsqrt_rn(__dadd_rn(dsq(dx64), dsq(dy64)));
-    return dp < __dsqrt_rn(d2v);
+    if (D + err < vlo) return 1;
+    if (D - err > vhi) return 0;
+    return -1;
 }
+
+// The reference's comparison dist(p, v) < dist(q, v) in FP64, with (dx, dy)
+// the offset from p (or the rectangle) to v.
+__device__ __forceinline__ bool closer64(double dx, double dy, double vx, double vy, double qx, double qy)
+{
+    return __dsqrt_rn(__dadd_rn(dsq(dx), dsq(dy))) < __dsqrt_rn(d2_64(vx, vy, qx, qy));
+}
+
+// Edge flags of a vertex (within EPS of each side of the space, in FP64).
+__device__ __forceinline__ uint8_t edge_bits(double x, double y, double sx0, double sy0,
+                                             double sx1, double sy1)
+{
+    uint8_t f = 0;
+    if (fabs(__dsub_rn(x, sx0)) < EPS) f |= VB_EL;
+    if (fabs(__dsub_rn(x, sx1)) < EPS) f |= VB_ER;
+    if (fabs(__dsub_rn(y, sy0)) < EPS) f |= VB_EB;
+    if (fabs(__dsub_rn(y, sy1)) < EPS) f |= VB_ET;
+    return f;
+}
+
+constexpr uint64_t INF_BITS = 0x7ff0000000000000ull;
+
+// Rules 1 and 2 compare sqrt(key) with a threshold T (2 x furthest vertex,
+// 2 x nearest bisector).  sqrt_rn is monotone, so there is a smallest key
+// whose root passes the test, and the test on a key becomes an integer
+// comparison of its bits (keys are non-negative doubles).  Returns the bits
+// of the smallest non-negative double x with sqrt_rn(x) > T (strict) or
+// sqrt_rn(x) >= T; ok is cleared if the search did not settle (the caller
+// then evaluates the square root per key).
+__device__ uint64_t sqrt_cut(double T, bool strict, bool& ok)
+{
+    ok = true;
+    if (!(T <= DBL_MAX)) return INF_BITS;           // T = +inf: no finite key passes
+    if (T <= 0.0) {
+        if (!strict) return 0;
+        T = 0.0;
+    }
+    uint64_t b = (uint64_t)__double_as_longlong(__dmul_rn(T, T));
+    if (b > INF_BITS) b = INF_BITS;
+    int it = 0;
+    auto pass = [&](uint64_t x) {
+        double r = __dsqrt_rn(__longlong_as_double((long long)x));
+        return strict ? (r > T) : (r >= T);
+    };
+    if (pass(b)) {
+        while (b > 0 && it < 64 && pass(b - 1)) { --b; ++it; }
+    } else {
+        while (b < INF_BITS && it < 64 && !pass(b)) { ++b; ++it; }
+    }
+    ok = it < 64;
+    return b;
+}
+
+// Whether facility ring `ring` (cells at Chebyshev distance `ring` from q's
+// cell) may still hold entries that rule 1 keeps, and the squared lower
+// bound of its cells' distances to q, as key bits.
+__device__ __forceinline__ void ring_gate(int ring, int rmaxf, double cs, double slack, double far_,
+                                          bool& open, uint64_t& key)
+{
+    double Lr = ring == 0 ? 0.0 : (double)(ring - 1) * cs - slack;
+    if (!(Lr > 0.0)) Lr = 0.0;
+    open = ring <= rmaxf && !(Lr > 2.0 * far_ * (1.0 + 1e-9) + slack);
+    key = (uint64_t)__double_as_longlong(Lr * Lr);
+}
+
+// Float bounds of the double that rounded (to nearest) to v.
+__device__ __forceinline__ float lo32(float v) { return __fsub_rd(v, __fmaf_ru(fabsf(v), 0x1p-23f, 0x1p-126f)); }
+__device__ __forceinline__ float hi32(float v) { return __fadd_ru(v, __fmaf_ru(fabsf(v), 0x1p-23f, 0x1p-126f)); }
 
 }  // namespace
 
@@ -386,6 +456,7 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
         double far_ = 0.0, nearb = DBL_MAX;
 
         // ---- init: four space corners (inf.cpp:211-226) -------------------
+        double d2c = 0.0;
         if (lane < 4) {
             double x = (lane & 1) ? sx1 : sx0;
             double y = (lane & 2) ? sy1 : sy0;
@@ -393,17 +464,17 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             IX(S.vy, lane) = y;
             IX(S.vx32, lane) = (float)x;
             IX(S.vy32, lane) = (float)y;
-            IX(S.vd2, lane) = d2_64(x, y, qx, qy);
-            IX(S.vd2f, lane) = (float)IX(S.vd2, lane);
+            d2c = d2_64(x, y, qx, qy);
+            IX(S.vd2f, lane) = (float)d2c;
             IX(S.vcnt, lane) = 0;
-            IX(S.vfl, lane) = VB_BND;
+            IX(S.vfl, lane) = VB_BND | edge_bits(x, y, sx0, sy0, sx1, sy1);
         }
         WSYNC();
-        {
-            double m = lane < 4 ? IX(S.vd2, lane) : 0.0;
-            m = warp_max(m);
-            far_ = __dsqrt_rn(m);
-        }
+        far_ = __dsqrt_rn(warp_max(d2c));
+        // integer thresholds of rules 1 and 2 on the queue keys
+        bool ok1 = true, ok2 = true;
+        uint64_t K1 = sqrt_cut(2.0 * far_, true, ok1);
+        uint64_t K2 = INF_BITS;                  // nearest bisector: none yet (2 x DBL_MAX = inf)
 
         long long tph = clock64();
 #define PHASE(i) do { long long t_ = clock64(); zs.cyc[i] += t_ - tph; tph = t_; } while (0)
@@ -411,22 +482,20 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
         const int qcy = cell_coord(qf.y, A.gf.y0, A.gf.inv, A.gf.gy);
         const int rmaxf = max(max(qcx, A.gf.gx - 1 - qcx), max(qcy, A.gf.gy - 1 - qcy));
         int ring = 0;        // next facility ring to expand
+        bool ring_open;
+        uint64_t ring_key;
+        ring_gate(ring, rmaxf, (double)A.gf.cs, slack, far_, ring_open, ring_key);
 
         // ---- best-first search --------------------------------------------
         for (;;) {
             // make the top poppable: expand rings whose cells could precede it
             for (;;) {
-                const double far2 = 2.0 * far_;
-                bool can_expand = ring <= rmaxf;
-                double Lr = ring == 0 ? 0.0 : (double)(ring - 1) * (double)A.gf.cs - slack;
-                if (Lr < 0) Lr = 0;
-                if (can_expand && Lr > far2 * (1.0 + 1e-9) + slack) can_expand = false;
-                if (!can_expand) break;
+                if (!ring_open) break;
                 if (nP > 0) {
                     uint64_t top = 0;
                     if (lane == 0) top = IX(S.pqk, 0);
                     top = __shfl_sync(FULL, top, 0);
-                    if (__longlong_as_double((long long)top) < Lr * Lr) break;
+                    if (top < ring_key) break;
                 }
                 // expand ring `ring`: 8*ring cells (1 for ring 0)
                 int ncell = ring == 0 ? 1 : 8 * ring;
@@ -464,6 +533,7 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                     WSYNC();
                 }
                 ring++;
+                ring_gate(ring, rmaxf, (double)A.gf.cs, slack, far_, ring_open, ring_key);
                 if (flags) break;
             }
             PHASE(0);
@@ -495,11 +565,15 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                 zs.cells++;
             }
             // rules 1 and 2 (inf.cpp:262-267, 460-465): key is the squared distance
-            const double dq = __dsqrt_rn(key);
             bool prune;
             PHASE(1);
-            if (dq > 2.0 * far_) prune = true;
-            else if (dq < 2.0 * nearb) prune = false;
+            // Rule 1 prunes this entry.  Every entry still queued has a key
+            // >= this one, and every cell not yet expanded lies beyond the
+            // heap's top (the expansion loop above guarantees it), so rule 1
+            // prunes all of them as well and the zone is final: stop here
+            // instead of draining the queue.
+            if (ok1 ? keybits >= K1 : __dsqrt_rn(key) > 2.0 * far_) break;
+            if (ok2 ? keybits < K2 : __dsqrt_rn(key) < 2.0 * nearb) prune = false;
             else {
                 // ---- vertex test (inf.cpp:268-353, 466-551) -------------
                 if (nCons < 0) {
@@ -520,13 +594,12 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                     if (lane < 8) {
                         const bool byY = lane < 4;
                         const bool wantMin = (lane & 1) == 0;
-                        const double edge = lane < 2 ? sx0 : lane < 4 ? sx1 : lane < 6 ? sy0 : sy1;
+                        const uint8_t ebit = lane < 2 ? VB_EL : lane < 4 ? VB_ER : lane < 6 ? VB_EB : VB_ET;
                         long long bk = 0;
                         for (int t = 0; t < nB; ++t) {
                             const int i = IX(S.cons, t);
-                            const double x = IX(S.vx, i), y = IX(S.vy, i);
-                            if (!(fabs(__dsub_rn(byY ? x : y, edge)) < EPS)) continue;
-                            const long long key = order_key(byY ? y : x);
+                            if (!(IX(S.vfl, i) & ebit)) continue;
+                            const long long key = order_key(byY ? IX(S.vy, i) : IX(S.vx, i));
                             if (best < 0 || (wantMin ? key < bk : key > bk)) { best = i; bk = key; }
                         }
                     }
@@ -544,12 +617,16 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                             int cnt = IX(S.vcnt, i);
                             if (cnt == k - 1) c = true;
                             else if ((IX(S.vfl, i) & VB_BND) && cnt < k) {
-                                double x = IX(S.vx, i), y = IX(S.vy, i);
-#pragma unroll
-                                for (int j = 0; j < 8; ++j) {
-                                    int b = ext[j];
-                                    if (b >= 0 && fabs(__dsub_rn(x, IX(S.vx, b))) < EPS &&
-                                        fabs(__dsub_rn(y, IX(S.vy, b))) < EPS) c = true;
+                                // within EPS of an extreme point; coordinates within
+                                // EPS in double are within EPS + 2E as floats
+                                const float x32 = IX(S.vx32, i), y32 = IX(S.vy32, i);
+                                const float tol = (1e-9f + 2.0f * E) * (1.0f + 0x1p-20f);
+                                for (int j = 0; j < 8 && !c; ++j) {
+                                    const int b = ext[j];
+                                    if (b < 0 || fabsf(x32 - IX(S.vx32, b)) > tol || fabsf(y32 - IX(S.vy32, b)) > tol)
+                                        continue;
+                                    if (fabs(__dsub_rn(IX(S.vx, i), IX(S.vx, b))) < EPS &&
+                                        fabs(__dsub_rn(IX(S.vy, i), IX(S.vy, b))) < EPS) c = true;
                                 }
                             }
                         }
@@ -564,22 +641,26 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                 bool hit = false;
                 const float px32 = (float)px, py32 = (float)py;
                 for (int t = lane; t < nC && !hit; t += 32) {
-                    int i = IX(S.cons, t);
-                    const float d2f = IX(S.vd2f, i);
-                    if (is_point) {
-                        float dxp = px32 - IX(S.vx32, i), dyp = py32 - IX(S.vy32, i);
-                        hit = closer_than_q(dxp, dyp, E, d2f, IX(S.vd2, i), __dsub_rn(px, IX(S.vx, i)), __dsub_rn(py, IX(S.vy, i)));
-                    } else {
-                        float dxp = rect_dx32(IX(S.vx32, i), mbr.x, mbr.z);
-                        float dyp = rect_dx32(IX(S.vy32, i), mbr.y, mbr.w);
-                        double vx = IX(S.vx, i), vy = IX(S.vy, i);
+                    const int i = IX(S.cons, t);
+                    const float vx32 = IX(S.vx32, i), vy32 = IX(S.vy32, i);
+                    int r;
+                    if (is_point) r = closer32(px32 - vx32, py32 - vy32, E, IX(S.vd2f, i));
+                    else r = closer32(rect_dx32(vx32, mbr.x, mbr.z), rect_dx32(vy32, mbr.y, mbr.w), E, IX(S.vd2f, i));
+                    if (r < 0) {
+                        const double vx = IX(S.vx, i), vy = IX(S.vy, i);
                         double dx64 = 0, dy64 = 0;
-                        if (vx < (double)mbr.x) dx64 = __dsub_rn((double)mbr.x, vx);
-                        else if (vx > (double)mbr.z) dx64 = __dsub_rn(vx, (double)mbr.z);
-                        if (vy < (double)mbr.y) dy64 = __dsub_rn((double)mbr.y, vy);
-                        else if (vy > (double)mbr.w) dy64 = __dsub_rn(vy, (double)mbr.w);
-                        hit = closer_than_q(dxp, dyp, E, d2f, IX(S.vd2, i), dx64, dy64);
+                        if (is_point) {
+                            dx64 = __dsub_rn(px, vx);
+                            dy64 = __dsub_rn(py, vy);
+                        } else {
+                            if (vx < (double)mbr.x) dx64 = __dsub_rn((double)mbr.x, vx);
+                            else if (vx > (double)mbr.z) dx64 = __dsub_rn(vx, (double)mbr.z);
+                            if (vy < (double)mbr.y) dy64 = __dsub_rn((double)mbr.y, vy);
+                            else if (vy > (double)mbr.w) dy64 = __dsub_rn(vy, (double)mbr.w);
+                        }
+                        r = closer64(dx64, dy64, vx, vy, qx, qy);
                     }
+                    hit = r != 0;
                 }
                 prune = !__any_sync(FULL, hit);
                 PHASE(2);
@@ -653,6 +734,9 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             // (2) candidate intersections: boundary edges (bottom, top, left,
             //     right; inf.h:340-374) then every earlier bisector in order
             const int C = 4 + nL;
+            // float interval of the new line's coefficients (directed rounding)
+            const float a1l = __double2float_rd(nb.a), a1h = __double2float_ru(nb.a);
+            const float b1l = __double2float_rd(nb.b), b1h = __double2float_ru(nb.b);
             for (int c = lane; c < C; c += 32) {
                 double x = 0, y = 0;
                 bool ok = false;
@@ -672,10 +756,9 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                     bool need64 = true;
                     if (!nb.vert && !ev) {
                         // float interval of the intersection (directed rounding)
-                        float a1l = __double2float_rd(nb.a), a1h = __double2float_ru(nb.a);
-                        float b1l = __double2float_rd(nb.b), b1h = __double2float_ru(nb.b);
-                        float a2l = __double2float_rd(ea), a2h = __double2float_ru(ea);
-                        float b2l = __double2float_rd(eb), b2h = __double2float_ru(eb);
+                        const float ea32 = IX(S.la32, j), eb32 = IX(S.lb32, j);
+                        const float a2l = lo32(ea32), a2h = hi32(ea32);
+                        const float b2l = lo32(eb32), b2h = hi32(eb32);
                         float dl = __fsub_rd(a1l, a2h), dh = __fsub_ru(a1h, a2l);
                         float nl = __fsub_rd(b2l, b1h), nh = __fsub_ru(b2h, b1l);
                         if ((dl > 4e-9f || dh < -4e-9f) && fabsf(nl) < FLT_MAX && fabsf(nh) < FLT_MAX &&
@@ -792,7 +875,8 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                         uint8_t lf = IX(S.lfl, gen);
                         cnt += !valid64(IX(S.la, gen), IX(S.lb, gen), lf & LB_VERT, (lf & LB_VALID) ? 1 : 0, x, y);
                     }
-                    for (int m = 0; m < nL; ++m) {
+                    // a count that reaches k erases the candidate: stop there
+                    for (int m = 0; m < nL && cnt < k; ++m) {
                         if (m == gen) continue;
                         uint8_t lf = IX(S.lfl, m);
                         float a = IX(S.la32, m), b = IX(S.lb32, m);
@@ -851,20 +935,20 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             for (int i0 = 0; i0 < nV0; i0 += 32) {
                 int i = i0 + lane;
                 bool keep = i < nV0 && IX(S.vcnt, i) < k;
-                double x = 0, y = 0, d2 = 0;
+                double x = 0, y = 0;
                 float x32 = 0, y32 = 0, d2f = 0;
                 int cnt = 0;
                 uint8_t fl = 0;
                 if (keep) {
-                    x = IX(S.vx, i); y = IX(S.vy, i); d2 = IX(S.vd2, i); d2f = IX(S.vd2f, i);
+                    x = IX(S.vx, i); y = IX(S.vy, i); d2f = IX(S.vd2f, i);
                     x32 = IX(S.vx32, i); y32 = IX(S.vy32, i); cnt = IX(S.vcnt, i); fl = IX(S.vfl, i) & ~VB_ON;
                 }
                 unsigned m = __ballot_sync(FULL, keep);
                 WSYNC();
                 if (keep) {
                     int o = w + __popc(m & ((1u << lane) - 1));
-                    IX(S.vx, o) = x; IX(S.vy, o) = y; IX(S.vd2, o) = d2; IX(S.vd2f, o) = d2f;
-                    IX(S.vx32, o) = x32; IX(S.vy32, o) = y32; IX(S.vcnt, o) = cnt; IX(S.vfl, o) = fl;
+                    IX(S.vx, o) = x; IX(S.vy, o) = y; IX(S.vd2f, o) = d2f;
+                    IX(S.vx32, o) = x32; IX(S.vy32, o) = y32; IX(S.vcnt, o) = (uint16_t)cnt; IX(S.vfl, o) = fl;
                 }
                 w += __popc(m);
                 WSYNC();
@@ -879,11 +963,9 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                     double x = IX(S.cx, c), y = IX(S.cy, c);
                     IX(S.vx, o) = x; IX(S.vy, o) = y;
                     IX(S.vx32, o) = IX(S.cx32, c); IX(S.vy32, o) = IX(S.cy32, c);
-                    const double d2n = d2_64(x, y, qx, qy);
-                    IX(S.vd2, o) = d2n;
-                    IX(S.vd2f, o) = (float)d2n;
-                    IX(S.vcnt, o) = IX(S.ccnt, c);
-                    IX(S.vfl, o) = IX(S.cfl, c) & VB_BND;
+                    IX(S.vd2f, o) = (float)d2_64(x, y, qx, qy);
+                    IX(S.vcnt, o) = (uint16_t)IX(S.ccnt, c);
+                    IX(S.vfl, o) = (IX(S.cfl, c) & VB_BND) | edge_bits(x, y, sx0, sy0, sx1, sy1);
                 }
                 nnew += __popc(m);
             }
@@ -892,12 +974,35 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             const bool vover = nV > VC;
             if (vover) nV = VC;
 
-            // (6) nearest bisector distance, store the line (inf.cpp:430-434)
+            // (6) nearest bisector distance, store the line (inf.cpp:430-434).
+            //     A float estimate with an error bound skips the FP64
+            //     evaluation when the new line is certainly not nearer.
             {
-                double dl = 0.0;
-                if (lane == 0) dl = line_dist64(qx, qy, nb.a, nb.b, nb.vert);
+                double dl = nearb;
+                if (lane == 0) {
+                    bool need = true;
+                    if (nearb < DBL_MAX) {
+                        float est, err;
+                        if (nb.vert) {
+                            est = fabsf(qf.x - nb32);
+                            err = 4.0f * kU32 * (fabsf(qf.x) + fabsf(nb32)) + 1e-30f;
+                        } else {
+                            const float den = sqrtf(fmaf(na32, na32, 1.0f));
+                            est = fabsf(fmaf(na32, qf.x, nb32 - qf.y)) / den;
+                            err = 8.0f * kU32 * ((fabsf(na32 * qf.x) + fabsf(qf.y) + fabsf(nb32)) / den + est) + 1e-30f;
+                        }
+                        if ((double)__fsub_rd(est, err) > nearb) need = false;   // NaN keeps need
+                    }
+                    if (need) {
+                        const double d = line_dist64(qx, qy, nb.a, nb.b, nb.vert);
+                        if (d < nearb) dl = d;
+                    }
+                }
                 dl = __shfl_sync(FULL, dl, 0);
-                if (dl < nearb) nearb = dl;
+                if (dl != nearb) {
+                    nearb = dl;
+                    K2 = sqrt_cut(2.0 * nearb, false, ok2);
+                }
             }
             if (lane == 0) {
                 IX(S.la, nL) = nb.a;
@@ -912,13 +1017,27 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             if (vover) flags |= QF_ZONE_V_OVERFLOW;
             if (nV > zs.vmax) zs.vmax = nV;
             WSYNC();
-            // (7) furthest remaining vertex (inf.cpp:445-451)
+            // (7) furthest remaining vertex (inf.cpp:445-451).  The float
+            //     squared distances are the FP64 ones rounded to nearest, a
+            //     monotone map: the FP64 maximum is among the vertices whose
+            //     float value is the float maximum.
             {
+                float m32 = 0.0f;
+                for (int i = lane; i < nV; i += 32) m32 = fmaxf(m32, IX(S.vd2f, i));
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) m32 = fmaxf(m32, __shfl_xor_sync(FULL, m32, o));
                 long long m = 0;
-                for (int i = lane; i < nV; i += 32) m = max(m, __double_as_longlong(IX(S.vd2, i)));
+                for (int i = lane; i < nV; i += 32)
+                    if (IX(S.vd2f, i) == m32)
+                        m = max(m, __double_as_longlong(d2_64(IX(S.vx, i), IX(S.vy, i), qx, qy)));
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(FULL, m, o));
-                far_ = __dsqrt_rn(__longlong_as_double(m));
+                const double f = __dsqrt_rn(__longlong_as_double(m));
+                if (f != far_) {
+                    far_ = f;
+                    K1 = sqrt_cut(2.0 * far_, true, ok1);
+                    ring_gate(ring, rmaxf, (double)A.gf.cs, slack, far_, ring_open, ring_key);
+                }
             }
             WSYNC();
             PHASE(6);

@@ -17,7 +17,7 @@ struct ZoneCaps {
 };
 
 struct ZoneLayout {
-    size_t vx, vy, vd2, vx32, vy32, vd2f, vcnt, vfl, cons;
+    size_t vx, vy, vx32, vy32, vd2f, vcnt, vfl, cons;
     size_t la, lb, la32, lb32, lb3, lfl, lpos;
     size_t pqk, pqc;
     size_t cx, cy, cx32, cy32, ccnt, cfl;
@@ -43,13 +43,12 @@ __host__ __device__ inline ZoneLayout zone_layout(const ZoneCaps& c)
     const size_t bm = ((W * W + 31) / 32 + ZL_SPARE) * 4;
     L.vx = o;   o = zl_align(o + (8 * VC > bm ? 8 * VC : bm));
     L.vy = o;   o = zl_align(o + 8 * VC);
-    L.vd2 = o;  o = zl_align(o + 8 * VC);
     L.vx32 = o; o = zl_align(o + 4 * VC);
     L.vy32 = o; o = zl_align(o + 4 * VC);
     L.vd2f = o; o = zl_align(o + 4 * VC);
-    L.vcnt = o; o = zl_align(o + 4 * VC);
+    L.vcnt = o; o = zl_align(o + 2 * VC);      // counts <= bisectors < 65536
     L.vfl = o;  o = zl_align(o + VC);
-    L.cons = o; o = zl_align(o + 4 * VC);
+    L.cons = o; o = zl_align(o + 2 * VC);      // vertex indices < 65536
     L.la = o;   o = zl_align(o + 8 * LC);
     L.lb = o;   o = zl_align(o + 8 * LC);
     L.la32 = o; o = zl_align(o + 4 * LC);
