@@ -13,8 +13,9 @@ graph).  Prints one JSON line (rank 0).
              stream, L2 flushed (256 MB write) before every timed step
   e2e        queries/s through rknn_query_batch (the C ABI with host
              buffers): query ids H2D, result offsets and ids D2H, per step
-  roofline   the verification kernel (the dominant per-user kernel), timed
-             live per launch with CUDA events in profiling mode
+  roofline   the zone kernel (the dominant one), timed live per launch with
+             CUDA events in profiling mode; roofline_verify: the same for the
+             verification kernel
   cpu_baseline  the C restatement of rknn-inf's query path (R-tree,
              influence-zone filter + verification) on the host's cores,
              over a bounded sample of the same workload
@@ -40,6 +41,10 @@ sys.path.insert(0, os.path.join(REPO, "rt-rknn_gb300"))
 
 METRIC = "RkNN queries/s (1M users,100k fac,k=10) FP32-filtered vs FP64; p99 ms"
 NF, NU, K, NQ = 100_000, 1_000_000, 10, 1000
+
+# DRAM bytes (read + write) per launch of each kernel on this workload, from
+# one ncu capture of the same 1000-query batch (profiles/zone_verify_config2_k10.md)
+TRAFFIC = {"zone_kernel_smem": 2189312, "verify_kernel": 4915200}
 
 
 def peaks():
@@ -113,7 +118,7 @@ def cpu_port_run(ds, nq_sample, nthreads, seed=5):
     import oracle as O
     port = O.InfPort(ds.fxy, ds.uxy)
     rng = np.random.default_rng(seed)
-    qs = rng.choice(ds.nf, size=nq_sample, replace=False).astype(np.int64)
+    qs = rng.choice(ds.nf, size=nq_sample, replace=nq_sample > ds.nf).astype(np.int64)
     t0 = time.perf_counter()
     cnt = port.query_many(qs, K, nthreads=nthreads)
     dt = time.perf_counter() - t0
@@ -256,7 +261,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     fp64_batch_qps = NQ / (e0.elapsed_time(e1) / 1e3)
 
-    # ---- roofline of the verification kernel (live, profiling mode) --------
+    # ---- rooflines (live, profiling mode: per-kernel CUDA events) ----------
     idx.set_profiling(True)
     kms = []
     for i in range(3):
@@ -267,33 +272,38 @@ def run_ours(args):
         kms.append(idx.kernel_ms())
     st = idx.last_stats()
     idx.set_profiling(False)
-    vms = statistics.mean(m["verify"] for m in kms)
-    zms = statistics.mean(m["zone"] for m in kms)
+    kavg = {n: statistics.mean(m[n] for m in kms) for n in kms[0]}
     hbm_peak, kind = peaks()
-    # algorithmic work of one verification launch: users read (8 B each),
-    # half-planes staged (16 B each per query), result ids written (4 B),
-    # facilities read by the exact recount (8 B); FLOP = 4 per
-    # (user, half-plane) evaluation executed
-    nb_total = st["bisectors"]
-    bytes_alg = 8 * st["candidates"] + 16 * nb_total + 4 * st["results"] + 8 * st["fac_checks"]
-    flops = 4 * st["plane_evals"]
     props = torch.cuda.get_device_properties(local)
     fp32_peak = props.multi_processor_count * 128 * 2 * 2.07e9 / 1e12     # nominal
-    gbs = bytes_alg / (vms / 1e3) / 1e9
-    tfs = flops / (vms / 1e3) / 1e12
-    hbm_frac = gbs / hbm_peak
-    fp32_frac = tfs / fp32_peak
-    if fp32_frac >= hbm_frac:
-        roof = {"bound": "fp32", "achieved": tfs, "peak": fp32_peak, "unit": "TFLOP/s",
-                "frac": fp32_frac, "peak_kind": "nominal (152 SM x 128 FMA x 2.07 GHz)"}
-    else:
-        roof = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
-                "frac": hbm_frac, "peak_kind": kind}
-    roof.update({"kernel": "verify_kernel", "launch_ms": vms, "traffic": None,
-                 "alg_bytes": bytes_alg, "alg_flop": flops,
-                 "hbm": {"achieved_gbs": gbs, "frac": hbm_frac, "peak": hbm_peak},
-                 "fp32": {"achieved_tflops": tfs, "frac": fp32_frac, "peak": fp32_peak},
-                 "zone_ms": zms, "kernel_ms": kms[-1]})
+    # zone kernel, the dominant one: bytes it must move per launch = facility
+    # cells taken from the queue (16 B box + 8 B start pair), facilities taken
+    # (8 B), half-planes and bisector positions written (20 B), one 64 B query
+    # descriptor per query
+    zms = kavg["zone"]
+    zbytes = 24 * st["zone_cells"] + 8 * st["zone_points"] + 20 * st["bisectors"] + 64 * NQ
+    zgbs = zbytes / (zms / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": zgbs, "peak": hbm_peak, "unit": "GB/s",
+            "frac": zgbs / hbm_peak, "peak_kind": kind, "kernel": "zone_kernel_smem",
+            "launch_ms": zms, "alg_bytes": zbytes,
+            "traffic": TRAFFIC.get("zone_kernel_smem"),
+            "note": "latency-bound: one warp per query runs the sequential best-first search; "
+                    "neither HBM nor FP32 issue bounds it",
+            "kernel_ms": kavg, "share": {n: v / sum(kavg.values()) for n, v in kavg.items()}}
+    # verification kernel: users read (8 B), half-planes staged (16 B each
+    # per query), result ids written (4 B), facilities read by the exact
+    # recount (8 B); FLOP = 4 per (user, half-plane) evaluation executed
+    vms = kavg["verify"]
+    vbytes = 8 * st["candidates"] + 16 * st["bisectors"] + 4 * st["results"] + 8 * st["fac_checks"]
+    vflops = 4 * st["plane_evals"]
+    vgbs = vbytes / (vms / 1e3) / 1e9
+    vtfs = vflops / (vms / 1e3) / 1e12
+    vroof = {"bound": "hbm" if vgbs / hbm_peak >= vtfs / fp32_peak else "fp32",
+             "achieved": vgbs, "peak": hbm_peak, "unit": "GB/s", "frac": vgbs / hbm_peak,
+             "peak_kind": kind, "kernel": "verify_kernel", "launch_ms": vms,
+             "alg_bytes": vbytes, "alg_flop": vflops, "traffic": TRAFFIC.get("verify_kernel"),
+             "fp32": {"achieved_tflops": vtfs, "frac": vtfs / fp32_peak, "peak": fp32_peak,
+                      "peak_kind": "nominal (SMs x 128 FMA x 2.07 GHz)"}}
 
     # ---- CPU baseline (rank 0, N=1 only) ---------------------------------
     cpu = None
@@ -320,7 +330,9 @@ def run_ours(args):
         "fp64_batched_qps": fp64_batch_qps,
         "speedup_fp32_batched_vs_fp64_single": value / ws / fp64_single_qps,
         "roofline": roof,
+        "roofline_verify": vroof,
         "stats": {k2: st[k2] for k2 in ("bisectors", "zone_vertices_max", "zone_candidates", "zone_fp64",
+                                        "zone_points", "zone_cells",
                                         "candidates", "plane_evals", "survivors", "fac_checks",
                                         "rechecks", "results", "overflow")},
         "recheck_fraction": st["rechecks"] / max(1, st["fac_checks"]),
@@ -341,7 +353,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-sample", type=int, default=20000)
+    ap.add_argument("--cpu-sample", type=int, default=400000)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

@@ -84,6 +84,8 @@ typedef struct {
     int64_t zone_cycles[8]; /* zone kernel SM cycles by phase, summed over queries: ring
                                expansion, pop + rules, vertex test, vertex count pass,
                                candidate intersections, dedup, counts/erase/append, epilogue */
+    int64_t zone_points;    /* facilities taken from the zone search's queue */
+    int64_t zone_cells;     /* facility grid cells taken from the queue */
 } rknn_query_stats;
 
 void rknn_index_opts_default(rknn_index_opts* opts);

@@ -355,6 +355,8 @@ rknn_status collect_stats(rknn_index* ix, int nq, rknn_query_stats* out)
         s.zone_fp64 += z[i].cand64;
         if (qd[i].flags & (QF_ZONE_V_OVERFLOW | QF_ZONE_L_OVERFLOW | QF_ZONE_PQ_OVERFLOW)) s.overflow++;
         for (int j = 0; j < 8; ++j) s.zone_cycles[j] += z[i].cyc[j];
+        s.zone_points += z[i].pts;
+        s.zone_cells += z[i].cells;
     }
     s.results = (int64_t)v.results;
     s.candidates = (int64_t)v.cand;

@@ -342,35 +342,32 @@ __device__ __forceinline__ uint8_t edge_bits(double x, double y, double sx0, dou
 
 constexpr uint64_t INF_BITS = 0x7ff0000000000000ull;
 
-// Rules 1 and 2 compare sqrt(key) with a threshold T (2 x furthest vertex,
-// 2 x nearest bisector).  sqrt_rn is monotone, so there is a smallest key
-// whose root passes the test, and the test on a key becomes an integer
-// comparison of its bits (keys are non-negative doubles).  Returns the bits
-// of the smallest non-negative double x with sqrt_rn(x) > T (strict) or
-// sqrt_rn(x) >= T; ok is cleared if the search did not settle (the caller
-// then evaluates the square root per key).
-__device__ uint64_t sqrt_cut(double T, bool strict, bool& ok)
+// Rules 1 and 2 compare sqrt_rn(key) with a threshold T (2 x furthest
+// vertex, 2 x nearest bisector).  Keys are non-negative doubles, so their bit
+// patterns order like their values, and two integer bounds settle almost
+// every key:
+//   key >= hi  =>  sqrt(key) >= T (1 + 2^-51) > next(T)  =>  sqrt_rn(key) > T
+//   key <= lo  =>  sqrt(key) <= T (1 - 2^-50) < prev(T)  =>  sqrt_rn(key) < T
+// with lo, hi = T*T (1 -/+ 2^-48), each product rounded.  Keys in between
+// (within about 2^-48 of T*T) take the square root.
+struct Cut {
+    uint64_t lo, hi;
+};
+constexpr uint64_t NEVER = INF_BITS + 1;       // no finite key reaches it
+
+// Callers test hi first, then lo.  For T = 0 the two rules need different
+// bounds: rule 1 (sqrt_rn(key) > 0) holds for every key but 0; rule 2
+// (sqrt_rn(key) < 0) never holds.
+__device__ __forceinline__ Cut sqrt_cut(double T, bool rule2)
 {
-    ok = true;
-    if (!(T <= DBL_MAX)) return INF_BITS;           // T = +inf: no finite key passes
-    if (T <= 0.0) {
-        if (!strict) return 0;
-        T = 0.0;
-    }
-    uint64_t b = (uint64_t)__double_as_longlong(__dmul_rn(T, T));
-    if (b > INF_BITS) b = INF_BITS;
-    int it = 0;
-    auto pass = [&](uint64_t x) {
-        double r = __dsqrt_rn(__longlong_as_double((long long)x));
-        return strict ? (r > T) : (r >= T);
-    };
-    if (pass(b)) {
-        while (b > 0 && it < 64 && pass(b - 1)) { --b; ++it; }
-    } else {
-        while (b < INF_BITS && it < 64 && !pass(b)) { ++b; ++it; }
-    }
-    ok = it < 64;
-    return b;
+    Cut c;
+    if (!(T <= DBL_MAX)) { c.lo = INF_BITS; c.hi = NEVER; return c; }   // T = +inf
+    if (T == 0.0) { c.lo = 0; c.hi = rule2 ? 0 : 1; return c; }
+    if (T < 0x1p-900) { c.lo = 0; c.hi = NEVER; return c; }             // no margins near subnormals
+    const double t2 = __dmul_rn(T, T);
+    c.lo = (uint64_t)__double_as_longlong(__dmul_rn(t2, 1.0 - 0x1p-48));
+    c.hi = (uint64_t)__double_as_longlong(__dmul_rn(t2, 1.0 + 0x1p-48));
+    return c;
 }
 
 // Whether facility ring `ring` (cells at Chebyshev distance `ring` from q's
@@ -472,9 +469,8 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
         WSYNC();
         far_ = __dsqrt_rn(warp_max(d2c));
         // integer thresholds of rules 1 and 2 on the queue keys
-        bool ok1 = true, ok2 = true;
-        uint64_t K1 = sqrt_cut(2.0 * far_, true, ok1);
-        uint64_t K2 = INF_BITS;                  // nearest bisector: none yet (2 x DBL_MAX = inf)
+        Cut K1 = sqrt_cut(2.0 * far_, false);
+        Cut K2 = sqrt_cut(2.0 * DBL_MAX, true);  // nearest bisector: none yet (threshold +inf)
 
         long long tph = clock64();
 #define PHASE(i) do { long long t_ = clock64(); zs.cyc[i] += t_ - tph; tph = t_; } while (0)
@@ -572,8 +568,17 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             // heap's top (the expansion loop above guarantees it), so rule 1
             // prunes all of them as well and the zone is final: stop here
             // instead of draining the queue.
-            if (ok1 ? keybits >= K1 : __dsqrt_rn(key) > 2.0 * far_) break;
-            if (ok2 ? keybits < K2 : __dsqrt_rn(key) < 2.0 * nearb) prune = false;
+            bool r1;
+            if (keybits >= K1.hi) r1 = true;
+            else if (keybits <= K1.lo) r1 = false;
+            else r1 = __dsqrt_rn(key) > 2.0 * far_;
+            if (r1) break;
+            // rule 2: keep when nearer than twice the nearest bisector
+            bool r2;
+            if (keybits >= K2.hi) r2 = false;
+            else if (keybits <= K2.lo) r2 = true;
+            else r2 = __dsqrt_rn(key) < 2.0 * nearb;
+            if (r2) prune = false;
             else {
                 // ---- vertex test (inf.cpp:268-353, 466-551) -------------
                 if (nCons < 0) {
@@ -1001,7 +1006,7 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                 dl = __shfl_sync(FULL, dl, 0);
                 if (dl != nearb) {
                     nearb = dl;
-                    K2 = sqrt_cut(2.0 * nearb, false, ok2);
+                    K2 = sqrt_cut(2.0 * nearb, true);
                 }
             }
             if (lane == 0) {
@@ -1035,7 +1040,7 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                 const double f = __dsqrt_rn(__longlong_as_double(m));
                 if (f != far_) {
                     far_ = f;
-                    K1 = sqrt_cut(2.0 * far_, true, ok1);
+                    K1 = sqrt_cut(2.0 * far_, false);
                     ring_gate(ring, rmaxf, (double)A.gf.cs, slack, far_, ring_open, ring_key);
                 }
             }
