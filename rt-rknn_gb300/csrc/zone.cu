@@ -43,25 +43,13 @@ constexpr double EPS = 1e-9;           // inf.cpp:270,375,408; inf.h:324
 // flags of a vertex: created on the space boundary, near the newest line,
 // and within EPS of the left / right / bottom / top edge (decided once in
 // FP64 when the vertex is created; inf.cpp:283-321 tests the same per lookup)
-constexpr uint8_t VB_BND = 1, VB_ON = 2, VB_EL = 4, VB_ER = 8, VB_EB = 16, VB_ET = 32;
+constexpr uint32_t VB_BND = 1, VB_ON = 2, VB_EL = 4, VB_ER = 8, VB_EB = 16, VB_ET = 32;
 // flags of a line
-constexpr uint8_t LB_VERT = 1, LB_VALID = 2;
+constexpr uint32_t LB_VERT = 1, LB_VALID = 2;
 
 struct Line64 {
     double a, b;        // y = a x + b, or x = b when vertical
     int vert, valid;
-};
-
-struct WarpScalars {
-    double dummy[4];    // checked builds: target of rejected accesses
-    int nV, nL, nP, nC;
-    int nCons;
-    int flags;
-    int stop;
-    int pad;
-    double far_;        // furthest vertex distance (FP64, as the reference)
-    double nearb;       // nearest bisector distance
-    double maxd2;
 };
 
 __device__ __forceinline__ double dsq(double a) { return __dmul_rn(a, a); }
@@ -194,56 +182,6 @@ struct Arr {
 };
 #define IX(a, i) (a).p[(i)]
 #endif
-
-struct Slice {
-    Arr<double> vx, vy;
-    Arr<float> vx32, vy32, vd2f;
-    Arr<uint16_t> vcnt;
-    Arr<uint8_t> vfl;
-    Arr<uint16_t> cons;
-    Arr<double> la, lb;
-    Arr<float> la32, lb32, lb3;
-    Arr<uint8_t> lfl;
-    Arr<int> lpos;
-    Arr<uint64_t> pqk;
-    Arr<uint32_t> pqc;
-    Arr<double> cx, cy;
-    Arr<float> cx32, cy32;
-    Arr<int> ccnt;
-    Arr<uint8_t> cfl;
-    Arr<uint64_t> tk;
-    Arr<uint32_t> tc;
-    Arr<uint32_t> bitmap;
-    Arr<float4> splanes;
-    WarpScalars *sc;
-};
-
-__device__ Slice carve(char* base, const ZoneCaps& c)
-{
-    ZoneLayout L = zone_layout(c);
-    Slice s;
-    const int VC = c.vc, LC = c.lc, PC = c.pc, CC = c.lc + 4;
-    const int W = 2 * c.rm + 1;
-#ifdef RKNN_CHECKED
-#define CARVE(f, T, off, n, i) s.f = Arr<T>{(T*)(base + L.off), (int)(n), i, (T*)(base + L.sc)}
-#else
-#define CARVE(f, T, off, n, i) s.f = Arr<T>{(T*)(base + L.off)}
-#endif
-    CARVE(vx, double, vx, VC, 1); CARVE(vy, double, vy, VC, 2);
-    CARVE(vx32, float, vx32, VC, 4); CARVE(vy32, float, vy32, VC, 5); CARVE(vd2f, float, vd2f, VC, 6);
-    CARVE(vcnt, uint16_t, vcnt, VC, 7); CARVE(vfl, uint8_t, vfl, VC, 8); CARVE(cons, uint16_t, cons, VC, 9);
-    CARVE(la, double, la, LC, 10); CARVE(lb, double, lb, LC, 11); CARVE(la32, float, la32, LC, 12);
-    CARVE(lb32, float, lb32, LC, 13); CARVE(lb3, float, lb3, LC, 14); CARVE(lfl, uint8_t, lfl, LC, 15);
-    CARVE(lpos, int, lpos, LC, 16); CARVE(pqk, uint64_t, pqk, PC, 17); CARVE(pqc, uint32_t, pqc, PC, 18);
-    CARVE(cx, double, cx, CC, 19); CARVE(cy, double, cy, CC, 20); CARVE(cx32, float, cx32, CC, 21);
-    CARVE(cy32, float, cy32, CC, 22); CARVE(ccnt, int, ccnt, CC, 23); CARVE(cfl, uint8_t, cfl, CC, 24);
-    CARVE(tk, uint64_t, tk, 32, 25); CARVE(tc, uint32_t, tc, 32, 26);
-    CARVE(bitmap, uint32_t, vx, (W * W + 31) / 32, 27);    // reused after the zone is built
-    CARVE(splanes, float4, cx, LC, 28);                     // reused for the epilogue
-#undef CARVE
-    s.sc = (WarpScalars*)(base + L.sc);
-    return s;
-}
 
 // ---- priority queue (lane 0 only) ------------------------------------------
 // Keys are squared distances (non-negative doubles), stored as their bit
@@ -386,15 +324,90 @@ __device__ __forceinline__ void ring_gate(int ring, int rmaxf, double cs, double
 __device__ __forceinline__ float lo32(float v) { return __fsub_rd(v, __fmaf_ru(fabsf(v), 0x1p-23f, 0x1p-126f)); }
 __device__ __forceinline__ float hi32(float v) { return __fadd_ru(v, __fmaf_ru(fabsf(v), 0x1p-23f, 0x1p-126f)); }
 
+struct Slice {
+    Arr<double2> vd;         // vertex coordinates
+    Arr<float4> v4;          // x, y, d2 to q (float), count | flags << 16
+    Arr<uint16_t> cons;      // considered vertices of the vertex test
+    Arr<uint16_t> blist;     // boundary vertices with count < k (aliases cd)
+    Arr<double2> ld;         // bisectors (FP64)
+    Arr<float4> l4;          // bisectors (float): a, b, 3.01u|b| + tiny, flags
+    Arr<int> lpos;           // facility position of each bisector
+    Arr<uint64_t> pqk;
+    Arr<uint32_t> pqc;
+    Arr<double2> cd;         // candidate intersections (FP64)
+    Arr<float2> c2;          // the same rounded to float
+    Arr<int> ccnt;
+    Arr<uint8_t> cfl;
+    Arr<uint64_t> tk;
+    Arr<uint32_t> tc;
+    Arr<uint32_t> bitmap;    // user-cell ring bitmap (aliases vd once the zone is built)
+    Arr<float4> splanes;     // half-planes for the ring scan (aliases cd)
+};
+
+__device__ Slice carve(char* base, const ZoneCaps& c)
+{
+    ZoneLayout L = zone_layout(c);
+    Slice s;
+    const int VC = c.vc, LC = c.lc, PC = c.pc, CC = c.lc + 4;
+    const int W = 2 * c.rm + 1;
+#ifdef RKNN_CHECKED
+#define CARVE(f, T, off, n, i) s.f = Arr<T>{(T*)(base + L.off), (int)(n), i, (T*)(base + L.sc)}
+#else
+#define CARVE(f, T, off, n, i) s.f = Arr<T>{(T*)(base + L.off)}
+#endif
+    CARVE(vd, double2, vd, VC, 1); CARVE(v4, float4, v4, VC, 2); CARVE(cons, uint16_t, cons, VC, 3);
+    CARVE(blist, uint16_t, cd, 8 * CC, 4);
+    CARVE(ld, double2, ld, LC, 5); CARVE(l4, float4, l4, LC, 6); CARVE(lpos, int, lpos, LC, 7);
+    CARVE(pqk, uint64_t, pqk, PC, 8); CARVE(pqc, uint32_t, pqc, PC, 9);
+    CARVE(cd, double2, cd, CC, 10); CARVE(c2, float2, c2, CC, 11); CARVE(ccnt, int, ccnt, CC, 12);
+    CARVE(cfl, uint8_t, cfl, CC, 13);
+    CARVE(tk, uint64_t, tk, 32, 14); CARVE(tc, uint32_t, tc, 32, 15);
+    CARVE(bitmap, uint32_t, vd, (W * W + 31) / 32, 16);
+    CARVE(splanes, float4, cd, LC, 17);
+#undef CARVE
+    (void)VC; (void)LC; (void)PC; (void)CC; (void)W;
+    return s;
+}
+
+// v4.w holds a vertex's count (bits 0-15) and flags (bits 16-23)
+__device__ __forceinline__ float vpack(uint32_t cnt, uint32_t fl) { return __uint_as_float(cnt | (fl << 16)); }
+__device__ __forceinline__ uint32_t vcnt_of(float w) { return __float_as_uint(w) & 0xffffu; }
+__device__ __forceinline__ uint32_t vfl_of(float w) { return __float_as_uint(w) >> 16; }
+
+// Float side test of a point (x, y) against a bisector record L: 1 if it
+// lies certainly on the invalid side, -1 if certainly on the valid side, 0
+// if the float evaluation cannot decide.  K1, K0 bound the error that the
+// point's float coordinates (or interval) contribute; vertical bisectors
+// have a = 0 and compare x with b.
+__device__ __forceinline__ int side32(const float4& L, float x, float y, float K1, float K0)
+{
+    const uint32_t lf = __float_as_uint(L.w);
+    const bool vert = (lf & LB_VERT) != 0;
+    const float sgn = (vert ? x : y) - fmaf(L.x, x, L.y);
+    const float err = fmaf(fabsf(L.x), K1, (vert ? K1 : K0) + L.z);
+    const bool valid_above = (lf & LB_VALID) != 0;
+    if (sgn > err) return valid_above ? -1 : 1;
+    if (sgn < -err) return valid_above ? 1 : -1;
+    return 0;
+}
+
+// Certainly-invalid test only (for the certified pre-discard).
+__device__ __forceinline__ int inval32(const float4& L, float x, float y, float K1, float K0)
+{
+    const uint32_t lf = __float_as_uint(L.w);
+    const bool vert = (lf & LB_VERT) != 0;
+    const float sgn = (vert ? x : y) - fmaf(L.x, x, L.y);
+    const float err = fmaf(fabsf(L.x), K1, (vert ? K1 : K0) + L.z);
+    return (lf & LB_VALID) ? (sgn < -err) : (sgn > err);
+}
+
 }  // namespace
 
 // ============================================================================
-// Lanes hand zone state to each other through memory between warp
-// barriers.  With the state in global memory the handoff is made explicit: a
-// block-scope fence orders each lane's stores and loads around the barrier.
-#define WSYNC() do { if (GMEM) __threadfence_block(); __syncwarp(); } while (0)
+// Lanes hand zone state to each other through shared memory between warp
+// barriers.
+#define WSYNC() __syncwarp()
 
-template <bool GMEM>
 __device__ __forceinline__ void zone_body(const ZoneArgs& A)
 {
     extern __shared__ __align__(16) char smem[];
@@ -406,20 +419,19 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
     if (!g_fault) g_fault = A.fault;
 #endif
     const ZoneLayout LY = zone_layout(A.caps);
-    // the shared-memory instantiation derives every state pointer from the
-    // __shared__ array itself (no generic pointer that could be global)
-    char* base;
-    if (GMEM) base = A.gscratch + (size_t)(blockIdx.x * ZONE_WARPS + wib) * LY.bytes;
-    else base = smem + (size_t)wib * LY.bytes;
-    Slice S = carve(base, A.caps);
+    // every state pointer derives from the __shared__ array itself
+    Slice S = carve(smem + (size_t)wib * LY.bytes, A.caps);
     const int VC = A.caps.vc, LC = A.caps.lc, PC = A.caps.pc;
     const long long NCF = (long long)A.gf.gx * A.gf.gy, NCU = (long long)A.gu.gx * A.gu.gy;
+    (void)NCF; (void)NCU;     // bounds of the checked build's index checks
     const double sx0 = A.sx0, sy0 = A.sy0, sx1 = A.sx1, sy1 = A.sy1;
     // largest rounding error of a vertex coordinate stored as float
     const float E = kU32 * (float)fmax(fmax(fabs(sx0), fabs(sx1)), fmax(fabs(sy0), fabs(sy1))) * 1.01f + 1e-37f;
     const float fsx0 = __double2float_rd(sx0), fsy0 = __double2float_rd(sy0);
     const float fsx1 = __double2float_ru(sx1), fsy1 = __double2float_ru(sy1);
     const double slack = 1e-5 * ((double)A.gf.cs + fmax(fmax(fabs(sx0), fabs(sx1)), fmax(fabs(sy0), fabs(sy1))));
+    // coordinates within EPS in double are within EPS + 2E as floats
+    const float tolE = (1e-9f + 2.0f * E) * (1.0f + 0x1p-20f);
 
     for (;;) {
         int slot = 0;
@@ -447,6 +459,7 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
         const int qpos = A.fpos[GX(qin, A.nf, 105)];
         const float2 qf = A.fxy[GX(qpos, A.nf, 101)];
         const double qx = qf.x, qy = qf.y;
+        const uint32_t ku = (uint32_t)k;
         // Warp-uniform scalars live in registers (identical in every lane);
         // lane 0 alone touches the heap and broadcasts what it changes.
         int nV = 4, nL = 0, nP = 0, nCons = -1, flags = 0;
@@ -455,16 +468,12 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
         // ---- init: four space corners (inf.cpp:211-226) -------------------
         double d2c = 0.0;
         if (lane < 4) {
-            double x = (lane & 1) ? sx1 : sx0;
-            double y = (lane & 2) ? sy1 : sy0;
-            IX(S.vx, lane) = x;
-            IX(S.vy, lane) = y;
-            IX(S.vx32, lane) = (float)x;
-            IX(S.vy32, lane) = (float)y;
+            const double x = (lane & 1) ? sx1 : sx0;
+            const double y = (lane & 2) ? sy1 : sy0;
             d2c = d2_64(x, y, qx, qy);
-            IX(S.vd2f, lane) = (float)d2c;
-            IX(S.vcnt, lane) = 0;
-            IX(S.vfl, lane) = VB_BND | edge_bits(x, y, sx0, sy0, sx1, sy1);
+            IX(S.vd, lane) = make_double2(x, y);
+            IX(S.v4, lane) = make_float4((float)x, (float)y, (float)d2c,
+                                         vpack(0, VB_BND | edge_bits(x, y, sx0, sy0, sx1, sy1)));
         }
         WSYNC();
         far_ = __dsqrt_rn(warp_max(d2c));
@@ -494,15 +503,15 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                     if (top < ring_key) break;
                 }
                 // expand ring `ring`: 8*ring cells (1 for ring 0)
-                int ncell = ring == 0 ? 1 : 8 * ring;
+                const int ncell = ring == 0 ? 1 : 8 * ring;
                 for (int t0 = 0; t0 < ncell; t0 += 32) {
-                    int t = t0 + lane;
+                    const int t = t0 + lane;
                     int cxx = 0, cyy = 0;
                     bool ok = t < ncell;
                     if (ok) {
                         if (ring == 0) { cxx = qcx; cyy = qcy; }
                         else {
-                            int side = 2 * ring + 1;
+                            const int side = 2 * ring + 1;
                             if (t < side) { cxx = qcx - ring + t; cyy = qcy - ring; }
                             else if (t < 2 * side) { cxx = qcx - ring + (t - side); cyy = qcy + ring; }
                             else if (t < 2 * side + (2 * ring - 1)) { cxx = qcx - ring; cyy = qcy - ring + 1 + (t - 2 * side); }
@@ -515,9 +524,9 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                         cid = cyy * A.gf.gx + cxx;
                         ok = A.fstart[GX(cid + 1, NCF + 1, 102)] > A.fstart[GX(cid, NCF + 1, 102)];
                     }
-                    double key = ok ? rect_d2_64(qx, qy, A.fmbr[GX(cid, NCF, 103)]) : 0.0;
-                    unsigned m = __ballot_sync(FULL, ok);
-                    int rank = __popc(m & ((1u << lane) - 1));
+                    const double key = ok ? rect_d2_64(qx, qy, A.fmbr[GX(cid, NCF, 103)]) : 0.0;
+                    const unsigned m = __ballot_sync(FULL, ok);
+                    const int rank = __popc(m & ((1u << lane) - 1));
                     if (ok) { IX(S.tk, rank) = (uint64_t)__double_as_longlong(key); IX(S.tc, rank) = (uint32_t)cid; }
                     WSYNC();
                     if (lane == 0) {
@@ -552,7 +561,7 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             float4 mbr = make_float4(0, 0, 0, 0);
             if (is_point) {
                 if (id == qpos) continue;
-                float2 pf = A.fxy[GX(id, A.nf, 101)];
+                const float2 pf = A.fxy[GX(id, A.nf, 101)];
                 px = pf.x; py = pf.y;
                 if (A.skip_coincident && pf.x == qf.x && pf.y == qf.y) continue;
                 zs.pts++;
@@ -582,61 +591,95 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             else {
                 // ---- vertex test (inf.cpp:268-353, 466-551) -------------
                 if (nCons < 0) {
-                    // boundary vertices with count < k, in vertex order
-                    int nB = 0;
+                    // One pass in vertex order: vertices with count k-1 are
+                    // considered; boundary vertices with count < k are listed.
+                    int nC = 0, nB = 0;
                     for (int i0 = 0; i0 < nV; i0 += 32) {
-                        int i = i0 + lane;
-                        bool b = i < nV && (IX(S.vfl, i) & VB_BND) && IX(S.vcnt, i) < k;
-                        unsigned m = __ballot_sync(FULL, b);
-                        if (b) IX(S.cons, nB + __popc(m & ((1u << lane) - 1))) = i;
-                        nB += __popc(m);
+                        const int i = i0 + lane;
+                        uint32_t cnt = 0, fl = 0;
+                        const bool in = i < nV;
+                        if (in) {
+                            const float w = IX(S.v4, i).w;
+                            cnt = vcnt_of(w);
+                            fl = vfl_of(w);
+                        }
+                        const bool c = in && cnt == ku - 1;
+                        const bool b = in && (fl & VB_BND) && cnt < ku;
+                        const unsigned mc = __ballot_sync(FULL, c), mb = __ballot_sync(FULL, b);
+                        const unsigned below = (1u << lane) - 1;
+                        if (c) IX(S.cons, nC + __popc(mc & below)) = (uint16_t)i;
+                        if (b) IX(S.blist, nB + __popc(mb & below)) = (uint16_t)i;
+                        nC += __popc(mc);
+                        nB += __popc(mb);
                     }
                     WSYNC();
-                    // lane j < 8 scans them in order for extreme j (first strict
-                    // min / max wins, as the reference's pointer updates):
-                    // left min/max y, right min/max y, bottom min/max x, top min/max x
+                    // Extreme boundary points (inf.cpp:283-321): lane j < 8 keeps
+                    // extreme j over the list in vertex order, the first strict
+                    // min / max winning as the reference's pointer updates do:
+                    // left min/max y, right min/max y, bottom min/max x, top min/max x.
+                    // The list is read 32 entries at a time and broadcast.
                     int best = -1;
-                    if (lane < 8) {
+                    {
                         const bool byY = lane < 4;
                         const bool wantMin = (lane & 1) == 0;
-                        const uint8_t ebit = lane < 2 ? VB_EL : lane < 4 ? VB_ER : lane < 6 ? VB_EB : VB_ET;
+                        const uint32_t ebit = lane < 2 ? VB_EL : lane < 4 ? VB_ER : lane < 6 ? VB_EB : VB_ET;
                         long long bk = 0;
-                        for (int t = 0; t < nB; ++t) {
-                            const int i = IX(S.cons, t);
-                            if (!(IX(S.vfl, i) & ebit)) continue;
-                            const long long key = order_key(byY ? IX(S.vy, i) : IX(S.vx, i));
-                            if (best < 0 || (wantMin ? key < bk : key > bk)) { best = i; bk = key; }
-                        }
-                    }
-                    int ext[8];
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) ext[j] = __shfl_sync(FULL, best, j);
-                    WSYNC();
-                    // considered: count == k-1, or a boundary vertex (count < k)
-                    // within EPS of one of the extreme points (inf.cpp:326-346)
-                    int nC = 0;
-                    for (int i0 = 0; i0 < nV; i0 += 32) {
-                        int i = i0 + lane;
-                        bool c = false;
-                        if (i < nV) {
-                            int cnt = IX(S.vcnt, i);
-                            if (cnt == k - 1) c = true;
-                            else if ((IX(S.vfl, i) & VB_BND) && cnt < k) {
-                                // within EPS of an extreme point; coordinates within
-                                // EPS in double are within EPS + 2E as floats
-                                const float x32 = IX(S.vx32, i), y32 = IX(S.vy32, i);
-                                const float tol = (1e-9f + 2.0f * E) * (1.0f + 0x1p-20f);
-                                for (int j = 0; j < 8 && !c; ++j) {
-                                    const int b = ext[j];
-                                    if (b < 0 || fabsf(x32 - IX(S.vx32, b)) > tol || fabsf(y32 - IX(S.vy32, b)) > tol)
-                                        continue;
-                                    if (fabs(__dsub_rn(IX(S.vx, i), IX(S.vx, b))) < EPS &&
-                                        fabs(__dsub_rn(IX(S.vy, i), IX(S.vy, b))) < EPS) c = true;
+                        for (int t0 = 0; t0 < nB; t0 += 32) {
+                            const int t = t0 + lane;
+                            int vi = 0;
+                            uint32_t fl = 0;
+                            long long kx = 0, ky = 0;
+                            if (t < nB) {
+                                vi = IX(S.blist, t);
+                                fl = vfl_of(IX(S.v4, vi).w);
+                                const double2 p = IX(S.vd, vi);
+                                kx = order_key(p.x);
+                                ky = order_key(p.y);
+                            }
+                            const int n = min(32, nB - t0);
+                            for (int u = 0; u < n; ++u) {
+                                const int ui = __shfl_sync(FULL, vi, u);
+                                const uint32_t uf = __shfl_sync(FULL, fl, u);
+                                const long long ukx = __shfl_sync(FULL, kx, u);
+                                const long long uky = __shfl_sync(FULL, ky, u);
+                                if (lane < 8 && (uf & ebit)) {
+                                    const long long kk = byY ? uky : ukx;
+                                    if (best < 0 || (wantMin ? kk < bk : kk > bk)) { best = ui; bk = kk; }
                                 }
                             }
                         }
-                        unsigned m = __ballot_sync(FULL, c);
-                        if (c) IX(S.cons, nC + __popc(m & ((1u << lane) - 1))) = i;
+                    }
+                    int ext[8];
+                    float ex[8], ey[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        ext[j] = __shfl_sync(FULL, best, j);
+                        ex[j] = 0.0f; ey[j] = 0.0f;
+                        if (ext[j] >= 0) {
+                            const float4 e = IX(S.v4, ext[j]);
+                            ex[j] = e.x; ey[j] = e.y;
+                        }
+                    }
+                    // boundary vertices (count < k, not already considered)
+                    // within EPS of an extreme point (inf.cpp:326-346)
+                    for (int t0 = 0; t0 < nB; t0 += 32) {
+                        const int t = t0 + lane;
+                        bool c = false;
+                        int vi = 0;
+                        if (t < nB) {
+                            vi = IX(S.blist, t);
+                            const float4 v = IX(S.v4, vi);
+                            if (vcnt_of(v.w) != ku - 1) {
+#pragma unroll
+                                for (int j = 0; j < 8; ++j) {
+                                    if (c || ext[j] < 0 || fabsf(v.x - ex[j]) > tolE || fabsf(v.y - ey[j]) > tolE) continue;
+                                    const double2 a = IX(S.vd, vi), b = IX(S.vd, ext[j]);
+                                    if (fabs(__dsub_rn(a.x, b.x)) < EPS && fabs(__dsub_rn(a.y, b.y)) < EPS) c = true;
+                                }
+                            }
+                        }
+                        const unsigned m = __ballot_sync(FULL, c);
+                        if (c) IX(S.cons, nC + __popc(m & ((1u << lane) - 1))) = (uint16_t)vi;
                         nC += __popc(m);
                     }
                     nCons = nC;
@@ -647,23 +690,23 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                 const float px32 = (float)px, py32 = (float)py;
                 for (int t = lane; t < nC && !hit; t += 32) {
                     const int i = IX(S.cons, t);
-                    const float vx32 = IX(S.vx32, i), vy32 = IX(S.vy32, i);
+                    const float4 v = IX(S.v4, i);
                     int r;
-                    if (is_point) r = closer32(px32 - vx32, py32 - vy32, E, IX(S.vd2f, i));
-                    else r = closer32(rect_dx32(vx32, mbr.x, mbr.z), rect_dx32(vy32, mbr.y, mbr.w), E, IX(S.vd2f, i));
+                    if (is_point) r = closer32(px32 - v.x, py32 - v.y, E, v.z);
+                    else r = closer32(rect_dx32(v.x, mbr.x, mbr.z), rect_dx32(v.y, mbr.y, mbr.w), E, v.z);
                     if (r < 0) {
-                        const double vx = IX(S.vx, i), vy = IX(S.vy, i);
+                        const double2 p = IX(S.vd, i);
                         double dx64 = 0, dy64 = 0;
                         if (is_point) {
-                            dx64 = __dsub_rn(px, vx);
-                            dy64 = __dsub_rn(py, vy);
+                            dx64 = __dsub_rn(px, p.x);
+                            dy64 = __dsub_rn(py, p.y);
                         } else {
-                            if (vx < (double)mbr.x) dx64 = __dsub_rn((double)mbr.x, vx);
-                            else if (vx > (double)mbr.z) dx64 = __dsub_rn(vx, (double)mbr.z);
-                            if (vy < (double)mbr.y) dy64 = __dsub_rn((double)mbr.y, vy);
-                            else if (vy > (double)mbr.w) dy64 = __dsub_rn(vy, (double)mbr.w);
+                            if (p.x < (double)mbr.x) dx64 = __dsub_rn((double)mbr.x, p.x);
+                            else if (p.x > (double)mbr.z) dx64 = __dsub_rn(p.x, (double)mbr.z);
+                            if (p.y < (double)mbr.y) dy64 = __dsub_rn((double)mbr.y, p.y);
+                            else if (p.y > (double)mbr.w) dy64 = __dsub_rn(p.y, (double)mbr.w);
                         }
-                        r = closer64(dx64, dy64, vx, vy, qx, qy);
+                        r = closer64(dx64, dy64, p.x, p.y, qx, qy);
                     }
                     hit = r != 0;
                 }
@@ -676,16 +719,15 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                 // push the cell's facilities (inf.cpp:556-565)
                 const int p0 = A.fstart[GX(id, NCF + 1, 102)], p1 = A.fstart[GX(id + 1, NCF + 1, 102)];
                 for (int t0 = p0; t0 < p1; t0 += 32) {
-                    int t = t0 + lane;
-                    bool ok = t < p1;
-                    if (ok) {
-                        float2 pf = A.fxy[GX(t, A.nf, 101)];
+                    const int t = t0 + lane;
+                    if (t < p1) {
+                        const float2 pf = A.fxy[GX(t, A.nf, 101)];
                         IX(S.tk, lane) = (uint64_t)__double_as_longlong(d2_64(qx, qy, (double)pf.x, (double)pf.y));
                         IX(S.tc, lane) = KIND_POINT | (uint32_t)t;
                     }
                     WSYNC();
                     if (lane == 0) {
-                        int cnt = min(32, p1 - t0);
+                        const int cnt = min(32, p1 - t0);
                         for (int i = 0; i < cnt; ++i)
                             if (!pq_push(S.pqk.p, S.pqc.p, nP, PC, IX(S.tk, i), IX(S.tc, i))) { flags |= QF_ZONE_PQ_OVERFLOW; break; }
                     }
@@ -712,26 +754,28 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             // (1) count pass over the existing vertices (inf.cpp:359-364)
             const int nV0 = nV;
             for (int i = lane; i < nV0; i += 32) {
-                float x32 = IX(S.vx32, i), y32 = IX(S.vy32, i);
+                const float4 v = IX(S.v4, i);
                 float r32, err;
                 if (nb.vert) {
-                    r32 = x32 - nb32;
-                    err = 3.0f * kU32 * (fabsf(x32) + fabsf(nb32)) + 1e-37f;
+                    r32 = v.x - nb32;
+                    err = 3.0f * kU32 * (fabsf(v.x) + fabsf(nb32)) + 1e-37f;
                 } else {
-                    float t = nab * fabsf(x32);
-                    r32 = y32 - fmaf(na32, x32, nb32);
-                    err = 5.0f * kU32 * (fabsf(y32) + t + fabsf(nb32)) + 1e-37f;
+                    const float t = nab * fabsf(v.x);
+                    r32 = v.y - fmaf(na32, v.x, nb32);
+                    err = 5.0f * kU32 * (fabsf(v.y) + t + fabsf(nb32)) + 1e-37f;
                 }
                 bool valid;
                 if (r32 > err) valid = nb.valid == 1;
                 else if (r32 < -err) valid = nb.valid == 0;
-                else valid = valid64(nb.a, nb.b, nb.vert, nb.valid, IX(S.vx, i), IX(S.vy, i));
+                else {
+                    const double2 p = IX(S.vd, i);
+                    valid = valid64(nb.a, nb.b, nb.vert, nb.valid, p.x, p.y);
+                }
                 // near the new line: may coincide (within 1e-9) with one of its intersections
-                float tol = (1.0f + nab) * 1.2e-9f + err;
-                uint8_t fl = IX(S.vfl, i) & ~VB_ON;
+                const float tol = (1.0f + nab) * 1.2e-9f + err;
+                uint32_t fl = vfl_of(v.w) & ~VB_ON;
                 if (fabsf(r32) <= tol || !(fabsf(r32) < FLT_MAX)) fl |= VB_ON;
-                IX(S.vfl, i) = fl;
-                if (!valid) IX(S.vcnt, i) += 1;
+                IX(S.v4, i).w = vpack(vcnt_of(v.w) + (valid ? 0u : 1u), fl);
             }
             WSYNC();
 
@@ -747,8 +791,8 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                 bool ok = false;
                 uint8_t cf = 0;
                 if (c < 4) {
-                    double ea = 0, eb = (c == 0) ? sy0 : (c == 1) ? sy1 : (c == 2) ? sx0 : sx1;
-                    int ev = c >= 2;
+                    const double ea = 0, eb = (c == 0) ? sy0 : (c == 1) ? sy1 : (c == 2) ? sx0 : sx1;
+                    const int ev = c >= 2;
                     if (intersect64(nb.a, nb.b, nb.vert, ea, eb, ev, x, y)) {
                         ok = (c < 2) ? (x >= sx0 && x <= sx1) : (y >= sy0 && y <= sy1);
                     }
@@ -756,16 +800,16 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                     zs.cand += ok;
                 } else {
                     const int j = c - 4;
-                    const double ea = IX(S.la, j), eb = IX(S.lb, j);
-                    const int ev = IX(S.lfl, j) & LB_VERT;
+                    const double2 e = IX(S.ld, j);
+                    const float4 e4 = IX(S.l4, j);
+                    const int ev = (__float_as_uint(e4.w) & LB_VERT) ? 1 : 0;
                     bool need64 = true;
                     if (!nb.vert && !ev) {
                         // float interval of the intersection (directed rounding)
-                        const float ea32 = IX(S.la32, j), eb32 = IX(S.lb32, j);
-                        const float a2l = lo32(ea32), a2h = hi32(ea32);
-                        const float b2l = lo32(eb32), b2h = hi32(eb32);
-                        float dl = __fsub_rd(a1l, a2h), dh = __fsub_ru(a1h, a2l);
-                        float nl = __fsub_rd(b2l, b1h), nh = __fsub_ru(b2h, b1l);
+                        const float a2l = lo32(e4.x), a2h = hi32(e4.x);
+                        const float b2l = lo32(e4.y), b2h = hi32(e4.y);
+                        const float dl = __fsub_rd(a1l, a2h), dh = __fsub_ru(a1h, a2l);
+                        const float nl = __fsub_rd(b2l, b1h), nh = __fsub_ru(b2h, b1l);
                         if ((dl > 4e-9f || dh < -4e-9f) && fabsf(nl) < FLT_MAX && fabsf(nh) < FLT_MAX &&
                             fabsf(dl) < FLT_MAX && fabsf(dh) < FLT_MAX) {
                             // x = N / D, N in [nl, nh], D in [dl, dh] not containing 0
@@ -779,40 +823,35 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                                 xh = -__fdiv_rd(nl, nl >= 0.0f ? ph : pl);
                             }
                             // y = a1 x + b1 over the box
-                            float m1 = __fmul_rd(a1l, xl), m2 = __fmul_rd(a1l, xh), m3 = __fmul_rd(a1h, xl), m4 = __fmul_rd(a1h, xh);
-                            float n1 = __fmul_ru(a1l, xl), n2 = __fmul_ru(a1l, xh), n3 = __fmul_ru(a1h, xl), n4 = __fmul_ru(a1h, xh);
+                            const float m1 = __fmul_rd(a1l, xl), m2 = __fmul_rd(a1l, xh), m3 = __fmul_rd(a1h, xl), m4 = __fmul_rd(a1h, xh);
+                            const float n1 = __fmul_ru(a1l, xl), n2 = __fmul_ru(a1l, xh), n3 = __fmul_ru(a1h, xl), n4 = __fmul_ru(a1h, xh);
                             float yl = __fadd_rd(fminf(fminf(m1, m2), fminf(m3, m4)), b1l);
                             float yh = __fadd_ru(fmaxf(fmaxf(n1, n2), fmaxf(n3, n4)), b1h);
                             // pad for the FP64 rounding of the reference's evaluation
-                            float px_ = 1e-12f * fmaxf(fabsf(xl), fabsf(xh)) + 1e-37f;
-                            float py_ = 1e-12f * (fmaxf(fabsf(yl), fabsf(yh)) + fabsf(a1h) * fmaxf(fabsf(xl), fabsf(xh)) + fabsf(b1h)) + 1e-37f;
+                            const float px_ = 1e-12f * fmaxf(fabsf(xl), fabsf(xh)) + 1e-37f;
+                            const float py_ = 1e-12f * (fmaxf(fabsf(yl), fabsf(yh)) + fabsf(a1h) * fmaxf(fabsf(xl), fabsf(xh)) + fabsf(b1h)) + 1e-37f;
                             xl = __fsub_rd(xl, px_); xh = __fadd_ru(xh, px_);
                             yl = __fsub_rd(yl, py_); yh = __fadd_ru(yh, py_);
                             if (xl <= xh && yl <= yh && fabsf(xl) < FLT_MAX && fabsf(xh) < FLT_MAX &&
                                 fabsf(yl) < FLT_MAX && fabsf(yh) < FLT_MAX) {
                                 if (xh < fsx0 || xl > fsx1 || yh < fsy0 || yl > fsy1) need64 = false;  // outside
                                 else {
-                                    // certified violations of earlier bisectors
-                                    float xc = 0.5f * xl + 0.5f * xh, yc = 0.5f * yl + 0.5f * yh;
-                                    float rx = (0.5f * xh - 0.5f * xl) * (1.0f + 4.0f * kU32) + fabsf(xc) * 2.0f * kU32 + 1e-37f;
-                                    float ry = (0.5f * yh - 0.5f * yl) * (1.0f + 4.0f * kU32) + fabsf(yc) * 2.0f * kU32 + 1e-37f;
-                                    float K1 = rx * (1.0f + kU32) + 3.01f * kU32 * fabsf(xc);
-                                    float K0 = ry + 3.01f * kU32 * fabsf(yc) + 1e-37f;
+                                    // certified violations of earlier bisectors, four
+                                    // bisectors per step (overshooting k is harmless)
+                                    const float xc = 0.5f * xl + 0.5f * xh, yc = 0.5f * yl + 0.5f * yh;
+                                    const float rx = (0.5f * xh - 0.5f * xl) * (1.0f + 4.0f * kU32) + fabsf(xc) * 2.0f * kU32 + 1e-37f;
+                                    const float ry = (0.5f * yh - 0.5f * yl) * (1.0f + 4.0f * kU32) + fabsf(yc) * 2.0f * kU32 + 1e-37f;
+                                    const float KX = rx * (1.0f + kU32) + 3.01f * kU32 * fabsf(xc);
+                                    const float KY = ry + 3.01f * kU32 * fabsf(yc) + 1e-37f;
                                     int cert = 0;
-                                    for (int m = 0; m < nL && cert < k; ++m) {
-                                        uint8_t lf = IX(S.lfl, m);
-                                        float a = IX(S.la32, m), b = IX(S.lb32, m);
-                                        float sgn, err;
-                                        if (lf & LB_VERT) {
-                                            sgn = xc - b;
-                                            err = K1 + 3.01f * kU32 * fabsf(b);
-                                        } else {
-                                            sgn = yc - fmaf(a, xc, b);
-                                            err = fmaf(fabsf(a), K1, K0 + IX(S.lb3, m));
-                                        }
-                                        bool inval = (lf & LB_VALID) ? (sgn < -err) : (sgn > err);
-                                        cert += inval;
+                                    int m = 0;
+                                    for (; m + 4 <= nL && cert < k; m += 4) {
+                                        const float4 q0 = IX(S.l4, m), q1 = IX(S.l4, m + 1);
+                                        const float4 q2 = IX(S.l4, m + 2), q3 = IX(S.l4, m + 3);
+                                        cert += inval32(q0, xc, yc, KX, KY) + inval32(q1, xc, yc, KX, KY) +
+                                                inval32(q2, xc, yc, KX, KY) + inval32(q3, xc, yc, KX, KY);
                                     }
+                                    for (; m < nL && cert < k; ++m) cert += inval32(IX(S.l4, m), xc, yc, KX, KY);
                                     if (cert >= k) need64 = false;
                                 }
                             }
@@ -820,15 +859,13 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                     }
                     if (need64) {
                         zs.cand64++;
-                        if (intersect64(nb.a, nb.b, nb.vert, ea, eb, ev, x, y))
+                        if (intersect64(nb.a, nb.b, nb.vert, e.x, e.y, ev, x, y))
                             ok = x >= sx0 && x <= sx1 && y >= sy0 && y <= sy1;
                     }
                     zs.cand++;
                 }
-                IX(S.cx, c) = x;
-                IX(S.cy, c) = y;
-                IX(S.cx32, c) = (float)x;
-                IX(S.cy32, c) = (float)y;
+                IX(S.cd, c) = make_double2(x, y);
+                IX(S.c2, c) = make_float2((float)x, (float)y);
                 IX(S.cfl, c) = ok ? (uint8_t)(cf | 0x80) : (uint8_t)0;
             }
             WSYNC();
@@ -840,10 +877,10 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                 // online vertices
                 int nOn = 0;
                 for (int i0 = 0; i0 < nV0; i0 += 32) {
-                    int i = i0 + lane;
-                    bool on = i < nV0 && (IX(S.vfl, i) & VB_ON);
-                    unsigned m = __ballot_sync(FULL, on);
-                    if (on) IX(S.cons, nOn + __popc(m & ((1u << lane) - 1))) = i;   // cons reused as scratch
+                    const int i = i0 + lane;
+                    const bool on = i < nV0 && (vfl_of(IX(S.v4, i).w) & VB_ON);
+                    const unsigned m = __ballot_sync(FULL, on);
+                    if (on) IX(S.cons, nOn + __popc(m & ((1u << lane) - 1))) = (uint16_t)i;   // cons reused as scratch
                     nOn += __popc(m);
                 }
                 WSYNC();
@@ -851,11 +888,14 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                 if (nOn > 0) {
                     for (int c = lane; c < C; c += 32) {
                         if (!(IX(S.cfl, c) & 0x80)) continue;
-                        double x = IX(S.cx, c), y = IX(S.cy, c);
+                        const float2 c32 = IX(S.c2, c);
                         bool dup = false;
                         for (int t = 0; t < nOn && !dup; ++t) {
-                            int i = IX(S.cons, t);
-                            if (fabs(__dsub_rn(IX(S.vx, i), x)) < EPS && fabs(__dsub_rn(IX(S.vy, i), y)) < EPS) dup = true;
+                            const int i = IX(S.cons, t);
+                            const float4 v = IX(S.v4, i);
+                            if (fabsf(v.x - c32.x) > tolE || fabsf(v.y - c32.y) > tolE) continue;
+                            const double2 p = IX(S.vd, i), q = IX(S.cd, c);
+                            if (fabs(__dsub_rn(p.x, q.x)) < EPS && fabs(__dsub_rn(p.y, q.y)) < EPS) dup = true;
                         }
                         if (dup) IX(S.cfl, c) &= 0x7f;
                     }
@@ -864,40 +904,52 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             }
 
             PHASE(5);
-            // (4) counts of the surviving candidates over earlier bisectors
+            // (4) counts of the surviving candidates over earlier bisectors:
+            //     a float pass counts certain violations (and stops at k, which
+            //     erases the candidate anyway); bisectors it cannot decide are
+            //     evaluated in FP64 in a second pass
             for (int c = lane; c < C; c += 32) {
                 int cnt = k;
                 if (IX(S.cfl, c) & 0x80) {
-                    double x = IX(S.cx, c), y = IX(S.cy, c);
-                    float xc = IX(S.cx32, c), yc = IX(S.cy32, c);
-                    float K1 = kU32 * fabsf(xc) * (1.0f + kU32) + 3.01f * kU32 * fabsf(xc);
-                    float K0 = kU32 * fabsf(yc) + 3.01f * kU32 * fabsf(yc) + 1e-37f;
+                    const double2 p = IX(S.cd, c);
+                    const float2 c32 = IX(S.c2, c);
+                    const float KX = kU32 * fabsf(c32.x) * (1.0f + kU32) + 3.01f * kU32 * fabsf(c32.x);
+                    const float KY = kU32 * fabsf(c32.y) + 3.01f * kU32 * fabsf(c32.y) + 1e-37f;
                     cnt = 0;
                     // the bisector that generated this candidate passes through
                     // it: its side is a rounding question, decided in FP64
                     const int gen = c - 4;
                     if (gen >= 0) {
-                        uint8_t lf = IX(S.lfl, gen);
-                        cnt += !valid64(IX(S.la, gen), IX(S.lb, gen), lf & LB_VERT, (lf & LB_VALID) ? 1 : 0, x, y);
+                        const double2 g = IX(S.ld, gen);
+                        const uint32_t lf = __float_as_uint(IX(S.l4, gen).w);
+                        cnt += !valid64(g.x, g.y, lf & LB_VERT, (lf & LB_VALID) ? 1 : 0, p.x, p.y);
                     }
-                    // a count that reaches k erases the candidate: stop there
-                    for (int m = 0; m < nL && cnt < k; ++m) {
-                        if (m == gen) continue;
-                        uint8_t lf = IX(S.lfl, m);
-                        float a = IX(S.la32, m), b = IX(S.lb32, m);
-                        float sgn, err;
-                        if (lf & LB_VERT) {
-                            sgn = xc - b;
-                            err = K1 + 3.01f * kU32 * fabsf(b);
-                        } else {
-                            sgn = yc - fmaf(a, xc, b);
-                            err = fmaf(fabsf(a), K1, K0 + IX(S.lb3, m));
+                    int undec = 0;
+                    int m = 0;
+                    for (; m + 4 <= nL && cnt < k; m += 4) {
+                        const float4 q0 = IX(S.l4, m), q1 = IX(S.l4, m + 1);
+                        const float4 q2 = IX(S.l4, m + 2), q3 = IX(S.l4, m + 3);
+                        const int s0 = (m == gen) ? -1 : side32(q0, c32.x, c32.y, KX, KY);
+                        const int s1 = (m + 1 == gen) ? -1 : side32(q1, c32.x, c32.y, KX, KY);
+                        const int s2 = (m + 2 == gen) ? -1 : side32(q2, c32.x, c32.y, KX, KY);
+                        const int s3 = (m + 3 == gen) ? -1 : side32(q3, c32.x, c32.y, KX, KY);
+                        cnt += (s0 > 0) + (s1 > 0) + (s2 > 0) + (s3 > 0);
+                        undec += (s0 == 0) + (s1 == 0) + (s2 == 0) + (s3 == 0);
+                    }
+                    for (; m < nL && cnt < k; ++m) {
+                        const int sm = (m == gen) ? -1 : side32(IX(S.l4, m), c32.x, c32.y, KX, KY);
+                        cnt += sm > 0;
+                        undec += sm == 0;
+                    }
+                    if (cnt < k && undec > 0) {
+                        for (int j = 0; j < nL && cnt < k; ++j) {
+                            if (j == gen) continue;
+                            const float4 q = IX(S.l4, j);
+                            if (side32(q, c32.x, c32.y, KX, KY) != 0) continue;
+                            const double2 g = IX(S.ld, j);
+                            const uint32_t lf = __float_as_uint(q.w);
+                            cnt += !valid64(g.x, g.y, lf & LB_VERT, (lf & LB_VALID) ? 1 : 0, p.x, p.y);
                         }
-                        bool inval;
-                        if (sgn > err) inval = !(lf & LB_VALID);
-                        else if (sgn < -err) inval = (lf & LB_VALID) != 0;
-                        else inval = !valid64(IX(S.la, m), IX(S.lb, m), lf & LB_VERT, (lf & LB_VALID) ? 1 : 0, x, y);
-                        cnt += inval;
                     }
                 }
                 IX(S.ccnt, c) = cnt;
@@ -912,21 +964,23 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                 for (int c = lane; c < C; c += 32) {
                     if (!(IX(S.cfl, c) & 0x80) || IX(S.ccnt, c) >= k) continue;
                     // doubles within 1e-9 give floats within 1e-9 + u(|x1|+|x2|)
-                    float x32 = IX(S.cx32, c), y32 = IX(S.cy32, c);
-                    float tx = 3.0f * kU32 * fabsf(x32) + 2e-9f, ty = 3.0f * kU32 * fabsf(y32) + 2e-9f;
+                    const float2 c32 = IX(S.c2, c);
+                    const float tx = 3.0f * kU32 * fabsf(c32.x) + 2e-9f, ty = 3.0f * kU32 * fabsf(c32.y) + 2e-9f;
                     for (int c2 = 0; c2 < c; ++c2) {
                         if (!(IX(S.cfl, c2) & 0x80)) continue;
-                        if (fabsf(IX(S.cx32, c2) - x32) <= tx && fabsf(IX(S.cy32, c2) - y32) <= ty) { anyclose = true; break; }
+                        const float2 o = IX(S.c2, c2);
+                        if (fabsf(o.x - c32.x) <= tx && fabsf(o.y - c32.y) <= ty) { anyclose = true; break; }
                     }
                 }
                 if (__any_sync(FULL, anyclose)) {
                     if (lane == 0) {
                         for (int c = 0; c < C; ++c) {
                             if (!(IX(S.cfl, c) & 0x80)) continue;
+                            const double2 p = IX(S.cd, c);
                             for (int c2 = 0; c2 < c; ++c2) {
                                 if (!(IX(S.cfl, c2) & 0x80)) continue;
-                                if (fabs(__dsub_rn(IX(S.cx, c2), IX(S.cx, c))) < EPS &&
-                                    fabs(__dsub_rn(IX(S.cy, c2), IX(S.cy, c))) < EPS) { IX(S.cfl, c) &= 0x7f; break; }
+                                const double2 o = IX(S.cd, c2);
+                                if (fabs(__dsub_rn(o.x, p.x)) < EPS && fabs(__dsub_rn(o.y, p.y)) < EPS) { IX(S.cfl, c) &= 0x7f; break; }
                             }
                         }
                     }
@@ -938,39 +992,39 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             //     the new vertices with count < k in candidate order
             int w = 0;
             for (int i0 = 0; i0 < nV0; i0 += 32) {
-                int i = i0 + lane;
-                bool keep = i < nV0 && IX(S.vcnt, i) < k;
-                double x = 0, y = 0;
-                float x32 = 0, y32 = 0, d2f = 0;
-                int cnt = 0;
-                uint8_t fl = 0;
-                if (keep) {
-                    x = IX(S.vx, i); y = IX(S.vy, i); d2f = IX(S.vd2f, i);
-                    x32 = IX(S.vx32, i); y32 = IX(S.vy32, i); cnt = IX(S.vcnt, i); fl = IX(S.vfl, i) & ~VB_ON;
+                const int i = i0 + lane;
+                bool keep = false;
+                float4 v = make_float4(0, 0, 0, 0);
+                double2 p = make_double2(0, 0);
+                if (i < nV0) {
+                    v = IX(S.v4, i);
+                    keep = vcnt_of(v.w) < ku;
+                    if (keep) p = IX(S.vd, i);
                 }
-                unsigned m = __ballot_sync(FULL, keep);
+                const unsigned m = __ballot_sync(FULL, keep);
                 WSYNC();
                 if (keep) {
-                    int o = w + __popc(m & ((1u << lane) - 1));
-                    IX(S.vx, o) = x; IX(S.vy, o) = y; IX(S.vd2f, o) = d2f;
-                    IX(S.vx32, o) = x32; IX(S.vy32, o) = y32; IX(S.vcnt, o) = (uint16_t)cnt; IX(S.vfl, o) = fl;
+                    const int o = w + __popc(m & ((1u << lane) - 1));
+                    v.w = vpack(vcnt_of(v.w), vfl_of(v.w) & ~VB_ON);
+                    IX(S.vd, o) = p;
+                    IX(S.v4, o) = v;
                 }
                 w += __popc(m);
                 WSYNC();
             }
             int nnew = 0;
             for (int c0 = 0; c0 < C; c0 += 32) {
-                int c = c0 + lane;
-                bool keep = c < C && (IX(S.cfl, c) & 0x80) && IX(S.ccnt, c) < k;
-                unsigned m = __ballot_sync(FULL, keep);
-                int o = w + nnew + __popc(m & ((1u << lane) - 1));
+                const int c = c0 + lane;
+                const bool keep = c < C && (IX(S.cfl, c) & 0x80) && IX(S.ccnt, c) < k;
+                const unsigned m = __ballot_sync(FULL, keep);
+                const int o = w + nnew + __popc(m & ((1u << lane) - 1));
                 if (keep && o < VC) {
-                    double x = IX(S.cx, c), y = IX(S.cy, c);
-                    IX(S.vx, o) = x; IX(S.vy, o) = y;
-                    IX(S.vx32, o) = IX(S.cx32, c); IX(S.vy32, o) = IX(S.cy32, c);
-                    IX(S.vd2f, o) = (float)d2_64(x, y, qx, qy);
-                    IX(S.vcnt, o) = (uint16_t)IX(S.ccnt, c);
-                    IX(S.vfl, o) = (IX(S.cfl, c) & VB_BND) | edge_bits(x, y, sx0, sy0, sx1, sy1);
+                    const double2 p = IX(S.cd, c);
+                    const float2 c32 = IX(S.c2, c);
+                    IX(S.vd, o) = p;
+                    IX(S.v4, o) = make_float4(c32.x, c32.y, (float)d2_64(p.x, p.y, qx, qy),
+                                              vpack((uint32_t)IX(S.ccnt, c),
+                                                    (IX(S.cfl, c) & VB_BND) | edge_bits(p.x, p.y, sx0, sy0, sx1, sy1)));
                 }
                 nnew += __popc(m);
             }
@@ -1010,12 +1064,9 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                 }
             }
             if (lane == 0) {
-                IX(S.la, nL) = nb.a;
-                IX(S.lb, nL) = nb.b;
-                IX(S.lfl, nL) = (uint8_t)((nb.vert ? LB_VERT : 0) | (nb.valid ? LB_VALID : 0));
-                IX(S.la32, nL) = na32;
-                IX(S.lb32, nL) = nb32;
-                IX(S.lb3, nL) = 3.01f * kU32 * fabsf(nb32) + 1e-37f;
+                const uint32_t lf = (nb.vert ? LB_VERT : 0) | (nb.valid ? LB_VALID : 0);
+                IX(S.ld, nL) = make_double2(nb.a, nb.b);
+                IX(S.l4, nL) = make_float4(na32, nb32, 3.01f * kU32 * fabsf(nb32) + 1e-37f, __uint_as_float(lf));
                 IX(S.lpos, nL) = id;
             }
             nL += 1;
@@ -1028,13 +1079,15 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             //     float value is the float maximum.
             {
                 float m32 = 0.0f;
-                for (int i = lane; i < nV; i += 32) m32 = fmaxf(m32, IX(S.vd2f, i));
+                for (int i = lane; i < nV; i += 32) m32 = fmaxf(m32, IX(S.v4, i).z);
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) m32 = fmaxf(m32, __shfl_xor_sync(FULL, m32, o));
                 long long m = 0;
                 for (int i = lane; i < nV; i += 32)
-                    if (IX(S.vd2f, i) == m32)
-                        m = max(m, __double_as_longlong(d2_64(IX(S.vx, i), IX(S.vy, i), qx, qy)));
+                    if (IX(S.v4, i).z == m32) {
+                        const double2 p = IX(S.vd, i);
+                        m = max(m, __double_as_longlong(d2_64(p.x, p.y, qx, qy)));
+                    }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(FULL, m, o));
                 const double f = __dsqrt_rn(__longlong_as_double(m));
@@ -1213,6 +1266,6 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
 }
 #undef WSYNC
 
-__global__ void __launch_bounds__(ZONE_WARPS * 32) zone_kernel_smem(ZoneArgs a) { zone_body<false>(a); }
+__global__ void __launch_bounds__(ZONE_WARPS * 32) zone_kernel_smem(ZoneArgs a) { zone_body(a); }
 
 }  // namespace rknn

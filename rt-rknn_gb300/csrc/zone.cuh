@@ -16,11 +16,17 @@ struct ZoneCaps {
     int rm;   // user-cell ring scan radius (cells)
 };
 
+// Per-query state in shared memory.  Vertices and bisectors are kept as
+// 16-byte records so that one load brings everything a loop needs:
+//   vd   double2 (x, y)                           vertex coordinates (FP64)
+//   v4   float4  (x, y, d2 to q, count | flags<<16)  the same rounded to float
+//   ld   double2 (a, b)                           bisector y = a x + b (x = b if vertical)
+//   l4   float4  (a, b, 3.01u|b|, flags)          the same rounded to float
+//   cd   double2 / c2 float2                      candidate intersections
 struct ZoneLayout {
-    size_t vx, vy, vx32, vy32, vd2f, vcnt, vfl, cons;
-    size_t la, lb, la32, lb32, lb3, lfl, lpos;
+    size_t vd, v4, cons, ld, l4, lpos;
     size_t pqk, pqc;
-    size_t cx, cy, cx32, cy32, ccnt, cfl;
+    size_t cd, c2, ccnt, cfl;
     size_t tk, tc, sc;
     size_t bytes;
 };
@@ -33,6 +39,8 @@ constexpr size_t ZL_SPARE = 1;     // one spare element per array takes rejected
 constexpr size_t ZL_SPARE = 0;
 #endif
 
+__host__ __device__ inline size_t zl_max(size_t a, size_t b) { return a > b ? a : b; }
+
 __host__ __device__ inline ZoneLayout zone_layout(const ZoneCaps& c)
 {
     ZoneLayout L;
@@ -41,27 +49,19 @@ __host__ __device__ inline ZoneLayout zone_layout(const ZoneCaps& c)
     const size_t CC = (size_t)c.lc + 4 + ZL_SPARE;
     const size_t W = 2 * (size_t)c.rm + 1;
     const size_t bm = ((W * W + 31) / 32 + ZL_SPARE) * 4;
-    L.vx = o;   o = zl_align(o + (8 * VC > bm ? 8 * VC : bm));
-    L.vy = o;   o = zl_align(o + 8 * VC);
-    L.vx32 = o; o = zl_align(o + 4 * VC);
-    L.vy32 = o; o = zl_align(o + 4 * VC);
-    L.vd2f = o; o = zl_align(o + 4 * VC);
-    L.vcnt = o; o = zl_align(o + 2 * VC);      // counts <= bisectors < 65536
-    L.vfl = o;  o = zl_align(o + VC);
-    L.cons = o; o = zl_align(o + 2 * VC);      // vertex indices < 65536
-    L.la = o;   o = zl_align(o + 8 * LC);
-    L.lb = o;   o = zl_align(o + 8 * LC);
-    L.la32 = o; o = zl_align(o + 4 * LC);
-    L.lb32 = o; o = zl_align(o + 4 * LC);
-    L.lb3 = o;  o = zl_align(o + 4 * LC);
-    L.lfl = o;  o = zl_align(o + LC);
+    L.vd = o;   o = zl_align(o + zl_max(16 * VC, bm));     // also the epilogue's cell bitmap
+    L.v4 = o;   o = zl_align(o + 16 * VC);
+    L.cons = o; o = zl_align(o + 2 * VC);                  // vertex indices < 65536
+    L.ld = o;   o = zl_align(o + 16 * LC);
+    L.l4 = o;   o = zl_align(o + 16 * LC);
     L.lpos = o; o = zl_align(o + 4 * LC);
     L.pqk = o;  o = zl_align(o + 8 * PC);
     L.pqc = o;  o = zl_align(o + 4 * PC);
-    L.cx = o;   o = zl_align(o + (8 * CC > 16 * LC ? 8 * CC : 16 * LC));   // also float4 planes
-    L.cy = o;   o = zl_align(o + 8 * CC);
-    L.cx32 = o; o = zl_align(o + 4 * CC);
-    L.cy32 = o; o = zl_align(o + 4 * CC);
+    // candidates; between bisector additions the same bytes hold the list of
+    // boundary vertices (at most 4 + 4 x bisectors, uint16), and after the
+    // zone is built the float half-planes (lc float4)
+    L.cd = o;   o = zl_align(o + zl_max(16 * CC, 16 * LC));
+    L.c2 = o;   o = zl_align(o + 8 * CC);
     L.ccnt = o; o = zl_align(o + 4 * CC);
     L.cfl = o;  o = zl_align(o + CC);
     L.tk = o;   o = zl_align(o + 8 * (32 + ZL_SPARE));
