@@ -64,8 +64,20 @@ typedef struct {
     float usr_per_cell;     /* users per user-grid cell (0: default 8) */
     int32_t skip_coincident;/* 1 (default): a facility at q's exact position adds no
                                bisector (the reference adds a degenerate one) */
-    int32_t reserved[6];
+    int32_t filter;         /* candidate filter: RKNN_FILTER_AUTO (default), _INF, _SLICE */
+    int32_t slice_min_k;    /* AUTO: k classes whose largest k reaches this use the slice
+                               filter, smaller ones the influence zone (0: default 1) */
+    int32_t reserved[4];
 } rknn_index_opts;
+
+typedef enum {
+    RKNN_FILTER_AUTO = 0,   /* angular slices from slice_min_k on (the faster filter at every
+                               k measured), the influence zone below it and for k beyond the
+                               slices' shared-memory room (k ~ 1400) */
+    RKNN_FILTER_INF = 1,    /* always rknn-inf's influence zone (inf.cpp:201-585); beyond
+                               its shared-memory capacity (k ~ 35) the zone is cut short */
+    RKNN_FILTER_SLICE = 2   /* always the angular-slice filter (rknn-slice/slice.h) */
+} rknn_filter;
 
 typedef struct {
     int64_t queries;
@@ -178,6 +190,65 @@ rknn_status rknn_set_profiling(rknn_index* idx, int32_t on);
 /* Device time of each kernel of the last profiled call, in milliseconds:
  * ms[0] zone, ms[1] plan, ms[2] verify, ms[3] result offsets, ms[4] finalize. */
 rknn_status rknn_last_kernel_ms(rknn_index* idx, double* ms);
+
+/* ---- Serving: continuous batching over a resident index ----------------
+ * No counterpart in the reference (one query per process).  A server keeps
+ * the index on the device and runs a worker thread.  Requests queue as they
+ * are submitted; whenever one of the server's slots is free, the worker
+ * forms a batch from the queue (first come first served, one mode per batch,
+ * as many requests as max_batch and the slot's scratch budget admit, the
+ * budget charged by each request's scratch estimate from its k) and launches
+ * it on the slot's own stream while earlier batches are still running, so
+ * the work of several batches overlaps on the GPU.  A request's result does
+ * not depend on the batch it ran in. */
+typedef struct rknn_server rknn_server;
+
+typedef struct {
+    int32_t slots;          /* batches in flight at once (default 3) */
+    int32_t max_batch;      /* requests per batch (default 4096) */
+    int64_t scratch_bytes;  /* device scratch one batch may use (default 256 MiB) */
+    int32_t reserved[8];
+} rknn_serve_opts;
+
+typedef struct {
+    int64_t submitted, completed, failed;
+    int64_t batches;        /* batches launched */
+    double mean_batch;      /* requests per batch */
+    int32_t max_inflight;   /* most batches on the GPU at once */
+    int32_t pad;
+    double p50_ms, p99_ms, mean_ms, max_ms;   /* submit -> result ready */
+    double throughput_qps;  /* completed / (last completion - first submission) */
+} rknn_serve_stats;
+
+void rknn_serve_opts_default(rknn_serve_opts* opts);
+
+/* Start a server over idx (which must outlive it). */
+rknn_status rknn_serve_start(rknn_index* idx, const rknn_serve_opts* opts, rknn_server** out);
+
+/* Queue one request; *ticket identifies it in rknn_serve_wait.  Thread-safe. */
+rknn_status rknn_serve_submit(rknn_server* srv, int32_t q_index, int32_t k, int32_t mode,
+                              uint64_t* ticket);
+
+/* Wait up to timeout_ms (< 0: no limit) for a request, then copy its sorted
+ * ids and release it.  RKNN_ERR_TIMEOUT: not done yet (call again).
+ * RKNN_ERR_CAPACITY: cap too small, *n_out set, request kept.  latency_ms
+ * (may be null): submit to result ready.  Thread-safe. */
+rknn_status rknn_serve_wait(rknn_server* srv, uint64_t ticket, int32_t timeout_ms,
+                            int32_t* out_ids, int64_t cap, int64_t* n_out, double* latency_ms);
+
+/* Open-loop load: submit n requests, request i at arrival_s[i] seconds after
+ * the call starts (non-decreasing), wait for all, and write each request's
+ * latency (ms) and result size.  Results themselves are dropped. */
+rknn_status rknn_serve_replay(rknn_server* srv, int64_t n, const int32_t* q_index,
+                              const int32_t* k, const int32_t* mode, const double* arrival_s,
+                              double* latency_ms, int64_t* n_results);
+
+/* Counters and latency percentiles of requests completed since the start
+ * (or since the last call with reset != 0). */
+rknn_status rknn_serve_stats_get(rknn_server* srv, int32_t reset, rknn_serve_stats* stats);
+
+/* Finish queued and running requests, stop the worker, free the server. */
+rknn_status rknn_serve_stop(rknn_server* srv);
 
 /* Message of the last failure on this thread ("" if none). */
 const char* rknn_last_error(void);

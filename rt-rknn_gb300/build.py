@@ -32,6 +32,7 @@ UNITS = {
     "index.cu": [],
     "zone.cu": ["-fmad=false"],
     "verify.cu": [],
+    "slice.cu": [],
     "api.cu": [],
 }
 

@@ -64,15 +64,12 @@ ZoneCaps caps_for(int kmax)
     return c;
 }
 
-struct GraphKey {
-    int nq, mode, vc, lc, pc, rm, use_global;
-    long long pool;
-    bool operator<(const GraphKey& o) const
-    {
-        return std::tie(nq, mode, vc, lc, pc, rm, use_global, pool) <
-               std::tie(o.nq, o.mode, o.vc, o.lc, o.pc, o.rm, o.use_global, o.pool);
-    }
-};
+// A cached graph is keyed by everything its launches depend on: batch size,
+// mode, order, result-pool size and the (size, largest k) of each k class.
+using GraphKey = std::vector<long long>;
+
+constexpr int NAUX = 3;            // side streams for concurrent k-class zone launches
+constexpr int MAX_CLASSES = 16;
 
 struct Workspace {
     int nq_cap = 0, lc = 0, seg_cap = 0;
@@ -82,8 +79,12 @@ struct Workspace {
     int* d_bispos = nullptr;
     int2* d_segs = nullptr;
     ZStats* d_zst = nullptr;
-    int *d_cand_off = nullptr, *d_chunk_off = nullptr, *d_res_count = nullptr, *d_out_off = nullptr;
-    int* d_counters = nullptr;     // [0] zone work, [1] verify work, [4..8] zone fault record
+    long long* d_cand_off = nullptr;   // result region of each slot (64-bit offsets)
+    int *d_chunk_off = nullptr, *d_res_count = nullptr, *d_out_off = nullptr;
+    int rcap = 1 << 18;            // ids a slot's region holds at most (raised when exceeded)
+    int* d_counters = nullptr;     // [0] zone work, [1] verify work, [2] region exceeded,
+                                   // [4..8] zone fault record,
+                                   // [10..14] verify fault record, [16..31] zone work per k class
     VStats* d_vstats = nullptr;
     int *d_pool = nullptr, *d_out = nullptr;
     long long pool_cap = 0;
@@ -93,6 +94,8 @@ struct Workspace {
     int* h_ids = nullptr;
     long long h_ids_cap = 0;
     std::map<GraphKey, cudaGraphExec_t> graphs;
+    cudaStream_t aux[NAUX] = {};
+    cudaEvent_t fork = nullptr, join[NAUX] = {};
 };
 
 }  // namespace
@@ -110,6 +113,8 @@ struct rknn_index {
     int *d_uid = nullptr, *d_ustart = nullptr;
     std::vector<int> h_fidx;       // cell-sorted position -> facility input index
     int skip_coincident = 1;
+    int filter = RKNN_FILTER_AUTO;
+    int slice_min_k = 1;
     int num_sms = 0;
     size_t smem_optin = 0;
     Workspace ws;
@@ -123,6 +128,21 @@ struct rknn_index {
 
 namespace {
 
+// Where a batch runs: a workspace, a stream, timing events.  The index has
+// one (its own calls); a server owns one per in-flight slot.
+struct Ctx {
+    Workspace& w;
+    cudaStream_t st;
+    cudaEvent_t ev0, ev1;
+    cudaEvent_t* kev;          // per-kernel events (profiling), or null
+    double* device_ms;         // where run_sync stores the batch's device time
+};
+
+Ctx main_ctx(rknn_index* ix)
+{
+    return Ctx{ix->ws, ix->stream, ix->ev0, ix->ev1, ix->profiling ? ix->kev : nullptr, &ix->last.device_ms};
+}
+
 void free_ws(Workspace& w)
 {
     for (auto& g : w.graphs) cudaGraphExecDestroy(g.second);
@@ -134,6 +154,11 @@ void free_ws(Workspace& w)
     cudaFree(w.d_pool); cudaFree(w.d_out); cudaFree(w.d_zscratch);
     cudaFreeHost(w.h_q); cudaFreeHost(w.h_k); cudaFreeHost(w.h_order); cudaFreeHost(w.h_off);
     cudaFreeHost(w.h_ids);
+    for (int i = 0; i < NAUX; ++i) {
+        if (w.aux[i]) cudaStreamDestroy(w.aux[i]);
+        if (w.join[i]) cudaEventDestroy(w.join[i]);
+    }
+    if (w.fork) cudaEventDestroy(w.fork);
     w = Workspace();
 }
 
@@ -151,15 +176,14 @@ struct ZoneLaunch {
     int grid;
 };
 
-ZoneLaunch zone_launch(rknn_index* ix, const ZoneCaps& c, int nq)
+ZoneLaunch zone_launch(rknn_index* ix, const ZoneCaps& c, int nq, bool slice = false)
 {
     ZoneLaunch L;
-    L.slice = zone_layout(c).bytes;
+    L.slice = slice ? slice_layout(c).bytes : zone_layout(c).bytes;
     L.smem = L.slice * ZONE_WARPS;
     int per_sm = 1;
-    if (L.smem > 48 * 1024)
-        cudaFuncSetAttribute(zone_kernel_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zone_kernel_smem, 32 * ZONE_WARPS, L.smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, slice ? slice_kernel : zone_kernel_smem,
+                                                  32 * ZONE_WARPS, L.smem);
     if (per_sm < 1) per_sm = 1;
     long long want = (nq + ZONE_WARPS - 1) / ZONE_WARPS;
     L.grid = (int)std::max(1LL, std::min<long long>(want, (long long)per_sm * ix->num_sms));
@@ -181,17 +205,18 @@ ZoneCaps caps_fit(rknn_index* ix, ZoneCaps c)
     return c;
 }
 
-rknn_status ensure_ws(rknn_index* ix, int nq, const ZoneCaps& caps, long long pool_need)
+rknn_status ensure_ws(Workspace& w, int nq, const ZoneCaps& caps, long long pool_need)
 {
-    Workspace& w = ix->ws;
     const int seg_cap = 2 * caps.rm + 2;
     if (nq > w.nq_cap || caps.lc > w.lc || seg_cap > w.seg_cap) {
         int nqc = std::max(nq, w.nq_cap);
         int lc = std::max(caps.lc, w.lc);
         int sc = std::max(seg_cap, w.seg_cap);
         long long pool = w.pool_cap;
+        const int rcap = w.rcap;
         free_ws(w);
         w.pool_cap = pool;
+        w.rcap = rcap;
         w.nq_cap = nqc; w.lc = lc; w.seg_cap = sc;
         CK(dalloc(w.d_q, nqc)); CK(dalloc(w.d_k, nqc)); CK(dalloc(w.d_order, nqc));
         CK(dalloc(w.d_qd, nqc));
@@ -201,8 +226,13 @@ rknn_status ensure_ws(rknn_index* ix, int nq, const ZoneCaps& caps, long long po
         CK(dalloc(w.d_zst, nqc));
         CK(dalloc(w.d_cand_off, nqc + 1)); CK(dalloc(w.d_chunk_off, nqc + 1));
         CK(dalloc(w.d_res_count, nqc)); CK(dalloc(w.d_out_off, nqc + 1));
-        CK(dalloc(w.d_counters, 16));
-        CK(cudaMemset(w.d_counters, 0, sizeof(int) * 16));
+        CK(dalloc(w.d_counters, 64));
+        CK(cudaMemset(w.d_counters, 0, sizeof(int) * 64));
+        for (int i = 0; i < NAUX; ++i) {
+            CK(cudaStreamCreateWithFlags(&w.aux[i], cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&w.join[i], cudaEventDisableTiming));
+        }
+        CK(cudaEventCreateWithFlags(&w.fork, cudaEventDisableTiming));
         CK(dalloc(w.d_vstats, 1));
         CK(cudaMallocHost(&w.h_q, sizeof(int) * nqc));
         CK(cudaMallocHost(&w.h_k, sizeof(int) * nqc));
@@ -223,40 +253,127 @@ rknn_status ensure_ws(rknn_index* ix, int nq, const ZoneCaps& caps, long long po
     return RKNN_OK;
 }
 
-// Launch geometry of one batch; computed (and kernel attributes set) before
-// any stream capture.
-struct BatchLaunch {
+cudaError_t allow_dynamic_smem(const void* fn, int optin)
+{
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, fn);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)a.sharedSizeBytes);
+}
+
+// ceil(log2 k), capped: queries of one class share zone capacities
+int k_class(int k)
+{
+    int c = 0;
+    while ((1 << c) < k && c < MAX_CLASSES - 1) ++c;
+    return c;
+}
+
+// One zone launch per k class, with capacities sized for the class's
+// largest k: a batch of mixed k does not give every query the shared-memory
+// state (and the low occupancy) of its largest k.
+struct ZClass {
+    int off, n, kmax;
+    bool slice;                 // angular-slice filter instead of the influence zone
+    ZoneCaps caps;
     ZoneLaunch zl;
-    size_t vsmem;
-    int vgrid;
 };
 
-BatchLaunch batch_launch(rknn_index* ix, int nq, int mode, const ZoneCaps& caps)
+// Capacities of the slice filter: a k-entry heap per slice, half-planes of
+// the nearest facilities for the verification.
+ZoneCaps slice_caps(int kmax)
 {
-    BatchLaunch b;
-    b.zl = zone_launch(ix, caps, nq);
-    b.vsmem = (size_t)VERIFY_WARPS * caps.lc * (mode == MODE_FP32 ? 16 : 32);
-    if (b.vsmem > 48 * 1024)
-        cudaFuncSetAttribute(verify_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b.vsmem);
+    ZoneCaps c;
+    c.vc = std::max(1, kmax);
+    c.lc = (int)std::min<long long>(6LL * c.vc + 40, 512);
+    c.pc = 0;
+    c.rm = 64;
+    return c;
+}
+
+// Which filter a k class uses.
+bool use_slice(rknn_index* ix, int kmax)
+{
+    if (ix->filter == RKNN_FILTER_INF) return false;
+    const size_t budget = std::min<size_t>(ix->smem_optin, 200 * 1024) - 1024;
+    if (slice_layout(slice_caps(kmax)).bytes > budget) return false;    // k beyond the heaps' room
+    return ix->filter == RKNN_FILTER_SLICE || kmax >= ix->slice_min_k;
+}
+
+// Launch geometry of one batch, computed before any stream capture.
+struct BatchPlan {
+    int nq = 0, mode = 0;
+    bool use_order = false;
+    std::vector<ZClass> cls;
+    int pstride = 0;            // half-plane row stride: the largest class lc
+    int stage_cap = 0;          // half-planes the verification stages per warp
+    size_t vsmem = 0;
+    int vgrid = 0;
+    GraphKey key;
+};
+
+// k_sorted: the batch's k in processing order (descending) when use_order,
+// else null (every query in one class sized for kmax).
+BatchPlan plan_batch(rknn_index* ix, int nq, int mode, bool use_order, const int* k_sorted, int kmax)
+{
+    BatchPlan b;
+    b.nq = nq;
+    b.mode = mode;
+    b.use_order = use_order;
+    if (use_order && k_sorted) {
+        for (int i = 0; i < nq;) {
+            const int c = k_class(k_sorted[i]);
+            int j = i + 1;
+            while (j < nq && k_class(k_sorted[j]) == c) ++j;
+            b.cls.push_back(ZClass{i, j - i, std::max(1, k_sorted[i]), false, {}, {}});
+            i = j;
+        }
+    } else {
+        b.cls.push_back(ZClass{0, nq, std::max(1, kmax), false, {}, {}});
+    }
+    b.key = {nq, mode, use_order ? 1 : 0};
+    for (auto& c : b.cls) {
+        c.slice = use_slice(ix, c.kmax);
+        c.caps = c.slice ? slice_caps(c.kmax) : caps_fit(ix, caps_for(c.kmax));
+        c.zl = zone_launch(ix, c.caps, c.n, c.slice);
+        b.pstride = std::max(b.pstride, c.caps.lc);
+        b.key.push_back(c.n);
+        b.key.push_back(c.kmax);
+        b.key.push_back(c.slice ? 1 : 0);
+    }
+    // the verification stages each query's half-planes in shared memory, at
+    // most 96 KB per block (a longer list is cut: the filter weakens, the
+    // exact recount still decides)
+    const int bpp = mode == MODE_FP32 ? 16 : 32;
+    b.stage_cap = std::max(1, std::min(b.pstride, (96 << 10) / (VERIFY_WARPS * bpp)));
+    b.vsmem = (size_t)VERIFY_WARPS * b.stage_cap * bpp;
     int vper = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&vper, verify_kernel, VERIFY_WARPS * 32, b.vsmem);
     if (vper < 1) vper = 1;
     b.vgrid = vper * ix->num_sms;
-    cudaFuncSetAttribute(finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(SORT_CAP * sizeof(unsigned)));
     return b;
 }
 
-// Enqueue the five kernels (no synchronization, no non-stream CUDA calls:
-// this runs under stream capture).
-rknn_status enqueue(rknn_index* ix, int nq, int mode, const ZoneCaps& caps, bool use_order,
-                    const BatchLaunch& bl, bool events = false)
+// Workspace capacities a plan needs (lc = the half-plane stride).
+ZoneCaps plan_caps(const BatchPlan& b)
 {
-    Workspace& w = ix->ws;
-    cudaStream_t st = ix->stream;
-    auto mark = [&](int i) { if (events) cudaEventRecord(ix->kev[i], st); };
-    const ZoneLaunch& zl = bl.zl;
+    ZoneCaps c = b.cls[0].caps;
+    for (auto& z : b.cls) c.rm = std::max(c.rm, z.caps.rm);
+    c.lc = b.pstride;
+    return c;
+}
+
+// Enqueue the batch's kernels (no synchronization, no non-stream CUDA calls:
+// this runs under stream capture).  k classes after the first run on side
+// streams, forked from and joined back to the context's stream.
+rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = false)
+{
+    Workspace& w = c.w;
+    cudaStream_t st = c.st;
+    const int nq = b.nq;
+    auto mark = [&](int i) { if (events) cudaEventRecord(c.kev[i], st); };
     CK(cudaMemsetAsync(w.d_counters, 0, sizeof(int) * 4, st));
+    CK(cudaMemsetAsync(w.d_counters + 16, 0, sizeof(int) * MAX_CLASSES, st));
     CK(cudaMemsetAsync(w.d_res_count, 0, sizeof(int) * nq, st));
     CK(cudaMemsetAsync(w.d_vstats, 0, sizeof(VStats), st));
 
@@ -265,41 +382,57 @@ rknn_status enqueue(rknn_index* ix, int nq, int mode, const ZoneCaps& caps, bool
     za.gf = ix->gf; za.nf = (int)ix->nf;
     za.ustart = ix->d_ustart; za.gu = ix->gu; za.nu = (int)ix->nu;
     za.sx0 = ix->sx0; za.sy0 = ix->sy0; za.sx1 = ix->sx1; za.sy1 = ix->sy1;
-    za.q_in = w.d_q; za.k_in = w.d_k; za.order = use_order ? w.d_order : nullptr; za.nq = nq;
-    za.work_counter = w.d_counters + 0;
-    za.caps = caps;
-    za.use_global = 0;
-    za.gscratch = nullptr;
+    za.q_in = w.d_q; za.k_in = w.d_k;
     za.skip_coincident = ix->skip_coincident;
-    za.rmax = caps.rm;
     za.seg_cap = w.seg_cap;
     za.qd = w.d_qd; za.planes = w.d_planes; za.bis_pos = w.d_bispos; za.segs = w.d_segs; za.zst = w.d_zst;
+    za.pstride = b.pstride;
     za.fault = w.d_counters + 4;
-    // planes/bis_pos are strided by the workspace lc
-    za.caps.lc = caps.lc;
     mark(0);
-    zone_kernel_smem<<<zl.grid, 32 * ZONE_WARPS, zl.smem, st>>>(za);
-    CK(cudaGetLastError());
+    const int ncls = (int)b.cls.size();
+    if (ncls > 1) {
+        CK(cudaEventRecord(w.fork, st));
+        for (int i = 0; i < NAUX && i < ncls - 1; ++i) CK(cudaStreamWaitEvent(w.aux[i], w.fork, 0));
+    }
+    for (int i = 0; i < ncls; ++i) {
+        const ZClass& z = b.cls[i];
+        za.order = b.use_order ? w.d_order + z.off : nullptr;
+        za.nq = z.n;
+        za.caps = z.caps;
+        za.rmax = z.caps.rm;
+        za.work_counter = w.d_counters + 16 + i;
+        cudaStream_t zs = i == 0 ? st : w.aux[(i - 1) % NAUX];
+        if (z.slice) slice_kernel<<<z.zl.grid, 32, z.zl.smem, zs>>>(za);
+        else zone_kernel_smem<<<z.zl.grid, 32 * ZONE_WARPS, z.zl.smem, zs>>>(za);
+        CK(cudaGetLastError());
+    }
+    if (ncls > 1) {
+        for (int i = 0; i < NAUX && i < ncls - 1; ++i) {
+            CK(cudaEventRecord(w.join[i], w.aux[i]));
+            CK(cudaStreamWaitEvent(st, w.join[i], 0));
+        }
+    }
     mark(1);
 
-    plan_kernel<<<1, 1024, 0, st>>>(w.d_qd, nq, w.d_cand_off, w.d_chunk_off, (int)std::min<long long>(w.pool_cap, INT32_MAX));
+    plan_kernel<<<1, 1024, 0, st>>>(w.d_qd, nq, w.d_cand_off, w.d_chunk_off, w.pool_cap, w.rcap);
     CK(cudaGetLastError());
     mark(2);
 
     VerifyArgs va;
-    va.qd = w.d_qd; va.planes = w.d_planes; va.bis_pos = w.d_bispos; va.lc = caps.lc;
+    va.qd = w.d_qd; va.planes = w.d_planes; va.bis_pos = w.d_bispos; va.lc = b.pstride;
+    va.stage_cap = b.stage_cap;
     va.segs = w.d_segs; va.seg_cap = w.seg_cap;
     va.chunk_off = w.d_chunk_off; va.cand_off = w.d_cand_off; va.nq = nq;
     va.uxy = ix->d_uxy; va.uid = ix->d_uid; va.fxy = ix->d_fxy; va.fstart = ix->d_fstart; va.gf = ix->gf;
     va.res_count = w.d_res_count; va.res_pool = w.d_pool; va.work_counter = w.d_counters + 1;
-    va.vstats = w.d_vstats; va.mode = mode;
+    va.vstats = w.d_vstats; va.mode = b.mode;
     va.nu = (int)ix->nu; va.nf = (int)ix->nf; va.ncf = ix->gf.gx * ix->gf.gy;
-    va.pool_cap = w.pool_cap; va.fault = w.d_counters + 10;
-    verify_kernel<<<bl.vgrid, VERIFY_WARPS * 32, bl.vsmem, st>>>(va);
+    va.pool_cap = w.pool_cap; va.fault = w.d_counters + 10; va.dropped = w.d_counters + 2;
+    verify_kernel<<<b.vgrid, VERIFY_WARPS * 32, b.vsmem, st>>>(va);
     CK(cudaGetLastError());
     mark(3);
 
-    scan_counts_kernel<<<1, 1024, 0, st>>>(w.d_res_count, nq, w.d_out_off);
+    scan_counts_kernel<<<1, 1024, 0, st>>>(w.d_res_count, w.d_cand_off, nq, w.d_out_off);
     CK(cudaGetLastError());
     mark(4);
     finalize_kernel<<<nq, 256, SORT_CAP * sizeof(unsigned), st>>>(w.d_pool, w.d_cand_off, w.d_res_count,
@@ -309,21 +442,22 @@ rknn_status enqueue(rknn_index* ix, int nq, int mode, const ZoneCaps& caps, bool
     return RKNN_OK;
 }
 
-// Launch through a cached graph for this batch shape.
-rknn_status launch(rknn_index* ix, int nq, int mode, const ZoneCaps& caps, bool use_order)
+// Launch a batch: replay the graph cached for its plan (captured on first
+// use), or enqueue directly (profiling, or when graph is false).
+rknn_status launch(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = true)
 {
-    Workspace& w = ix->ws;
-    const BatchLaunch bl = batch_launch(ix, nq, mode, caps);
-    if (ix->profiling) return enqueue(ix, nq, mode, caps, use_order, bl, true);
-    const ZoneLaunch& zl = bl.zl;
-    GraphKey key{nq, mode, caps.vc, caps.lc, caps.pc, caps.rm, 0, w.pool_cap};
-    key.nq = use_order ? nq : -nq;
+    Workspace& w = c.w;
+    if (c.kev) return enqueue(ix, c, b, true);
+    if (!graph) return enqueue(ix, c, b);
+    GraphKey key = b.key;
+    key.push_back(w.pool_cap);
+    key.push_back(w.rcap);
     auto it = w.graphs.find(key);
     if (it == w.graphs.end()) {
         cudaGraph_t g;
-        CK(cudaStreamBeginCapture(ix->stream, cudaStreamCaptureModeThreadLocal));
-        rknn_status s = enqueue(ix, nq, mode, caps, use_order, bl);
-        cudaError_t e = cudaStreamEndCapture(ix->stream, &g);
+        CK(cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal));
+        rknn_status s = enqueue(ix, c, b);
+        cudaError_t e = cudaStreamEndCapture(c.st, &g);
         if (s != RKNN_OK) { if (e == cudaSuccess) cudaGraphDestroy(g); return s; }
         CK(e);
         cudaGraphExec_t ge;
@@ -332,20 +466,20 @@ rknn_status launch(rknn_index* ix, int nq, int mode, const ZoneCaps& caps, bool 
         CK(e);
         it = w.graphs.emplace(key, ge).first;
     }
-    CK(cudaGraphLaunch(it->second, ix->stream));
+    CK(cudaGraphLaunch(it->second, c.st));
     return RKNN_OK;
 }
 
-rknn_status collect_stats(rknn_index* ix, int nq, rknn_query_stats* out)
+rknn_status collect_stats(Ctx& c, int nq, rknn_query_stats* out)
 {
-    Workspace& w = ix->ws;
+    Workspace& w = c.w;
     std::vector<ZStats> z(nq);
     std::vector<QDesc> qd(nq);
     VStats v;
-    CK(cudaMemcpyAsync(z.data(), w.d_zst, sizeof(ZStats) * nq, cudaMemcpyDeviceToHost, ix->stream));
-    CK(cudaMemcpyAsync(qd.data(), w.d_qd, sizeof(QDesc) * nq, cudaMemcpyDeviceToHost, ix->stream));
-    CK(cudaMemcpyAsync(&v, w.d_vstats, sizeof(VStats), cudaMemcpyDeviceToHost, ix->stream));
-    CK(cudaStreamSynchronize(ix->stream));
+    CK(cudaMemcpyAsync(z.data(), w.d_zst, sizeof(ZStats) * nq, cudaMemcpyDeviceToHost, c.st));
+    CK(cudaMemcpyAsync(qd.data(), w.d_qd, sizeof(QDesc) * nq, cudaMemcpyDeviceToHost, c.st));
+    CK(cudaMemcpyAsync(&v, w.d_vstats, sizeof(VStats), cudaMemcpyDeviceToHost, c.st));
+    CK(cudaStreamSynchronize(c.st));
     rknn_query_stats s{};
     s.queries = nq;
     for (int i = 0; i < nq; ++i) {
@@ -364,36 +498,47 @@ rknn_status collect_stats(rknn_index* ix, int nq, rknn_query_stats* out)
     s.survivors = (int64_t)v.survivors;
     s.fac_checks = (int64_t)v.fac_checks;
     s.rechecks = (int64_t)v.rechecks;
-    s.device_ms = ix->last.device_ms;
+    s.device_ms = *c.device_ms;
     *out = s;
     return RKNN_OK;
 }
 
 // Run a batch whose q/k are already in ws.d_q / ws.d_k.  Grows the result
 // pool and reruns when a query's candidate region did not fit.
-rknn_status run_sync(rknn_index* ix, int nq, int mode, int kmax, bool use_order)
+rknn_status run_sync(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = true)
 {
-    Workspace& w = ix->ws;
-    ZoneCaps caps = caps_fit(ix, caps_for(kmax));
+    Workspace& w = c.w;
+    const int nq = b.nq;
+    const ZoneCaps caps = plan_caps(b);
     long long need = std::max<long long>(w.pool_cap, (long long)nq * 4096);
-    rknn_status s = ensure_ws(ix, nq, caps, need);
+    rknn_status s = ensure_ws(w, nq, caps, need);
     if (s != RKNN_OK) return s;
-    for (int attempt = 0; attempt < 3; ++attempt) {
-        CK(cudaEventRecord(ix->ev0, ix->stream));
-        s = launch(ix, nq, mode, caps, use_order);
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        CK(cudaEventRecord(c.ev0, c.st));
+        s = launch(ix, c, b, graph);
         if (s != RKNN_OK) return s;
-        CK(cudaEventRecord(ix->ev1, ix->stream));
-        int tot[2];
-        CK(cudaMemcpyAsync(&tot[0], w.d_cand_off + nq, sizeof(int), cudaMemcpyDeviceToHost, ix->stream));
-        CK(cudaMemcpyAsync(w.h_off, w.d_out_off, sizeof(int) * (nq + 1), cudaMemcpyDeviceToHost, ix->stream));
-        CK(cudaStreamSynchronize(ix->stream));
+        CK(cudaEventRecord(c.ev1, c.st));
+        long long region_total = 0;
+        int dropped = 0;
+        CK(cudaMemcpyAsync(&region_total, w.d_cand_off + nq, sizeof(long long), cudaMemcpyDeviceToHost, c.st));
+        CK(cudaMemcpyAsync(&dropped, w.d_counters + 2, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+        CK(cudaMemcpyAsync(w.h_off, w.d_out_off, sizeof(int) * (nq + 1), cudaMemcpyDeviceToHost, c.st));
+        CK(cudaStreamSynchronize(c.st));
         float ms = 0;
-        cudaEventElapsedTime(&ms, ix->ev0, ix->ev1);
-        ix->last.device_ms = ms;
-        long long cand_total = (unsigned)tot[0];
-        if (cand_total <= w.pool_cap) return RKNN_OK;
-        s = ensure_ws(ix, nq, caps, cand_total + cand_total / 4);
-        if (s != RKNN_OK) return s;
+        cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+        *c.device_ms = ms;
+        if (region_total > w.pool_cap) {
+            // some regions did not fit the pool (those slots were skipped)
+            s = ensure_ws(w, nq, caps, region_total + region_total / 4);
+            if (s != RKNN_OK) return s;
+            continue;
+        }
+        if (dropped) {
+            // a slot had more results than its region: give every slot more room
+            w.rcap = (int)std::min<long long>((long long)w.rcap * 8, std::max<long long>(ix->nu, 1));
+            continue;
+        }
+        return RKNN_OK;
     }
     return fail(RKNN_ERR_CAPACITY, "result pool could not be sized");
 }
@@ -464,6 +609,9 @@ rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf, 
     auto bail = [&](rknn_status s) { rknn_index_destroy(ix); return s; };
     ix->device = o.device;
     ix->skip_coincident = o.skip_coincident ? 1 : 0;
+    if (o.filter < RKNN_FILTER_AUTO || o.filter > RKNN_FILTER_SLICE) return bail(fail(RKNN_ERR_ARG, "bad filter"));
+    ix->filter = o.filter;
+    ix->slice_min_k = o.slice_min_k > 0 ? o.slice_min_k : 1;
     ix->nf = nf;
     ix->nu = nu;
     ix->sx0 = x0; ix->sy0 = y0; ix->sx1 = x1; ix->sy1 = y1;
@@ -488,6 +636,13 @@ rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf, 
     int optin = 0;
     CKB(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, o.device));
     ix->smem_optin = (size_t)optin;
+    // dynamic shared memory limit of the batch kernels: the device's opt-in
+    // maximum less the kernel's static shared memory, set once (each launch
+    // asks for what its plan needs)
+    CKB(allow_dynamic_smem((const void*)zone_kernel_smem, optin));
+    CKB(allow_dynamic_smem((const void*)slice_kernel, optin));
+    CKB(allow_dynamic_smem((const void*)verify_kernel, optin));
+    CKB(allow_dynamic_smem((const void*)finalize_kernel, optin));
 
     ix->gf = make_grid(x0, y0, x1, y1, nf, o.fac_per_cell, 4096);
     ix->gu = make_grid(x0, y0, x1, y1, nu, o.usr_per_cell, 8192);
@@ -628,30 +783,40 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
     if (s != RKNN_OK) return s;
     std::lock_guard<std::mutex> lk(ix->mu);
     CK(cudaSetDevice(ix->device));
-    s = ensure_ws(ix, nq, caps_fit(ix, caps_for(kmax)), ix->ws.pool_cap);
-    if (s != RKNN_OK) return s;
-    Workspace& w = ix->ws;
-    // descending k: the longest zones start first
+    // descending k: the longest zones start first, and each k class gets its
+    // own zone launch
     bool uniform = true;
     for (int i = 1; i < nq && uniform; ++i) uniform = k[i] == k[0];
+    std::vector<int> order, ksorted;
+    if (!uniform) {
+        order.resize(nq);
+        for (int i = 0; i < nq; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return k[a] > k[b]; });
+        ksorted.resize(nq);
+        for (int i = 0; i < nq; ++i) ksorted[i] = k[order[i]];
+    }
+    const BatchPlan b = plan_batch(ix, nq, mode, !uniform, uniform ? nullptr : ksorted.data(), kmax);
+    s = ensure_ws(ix->ws, nq, plan_caps(b), ix->ws.pool_cap);
+    if (s != RKNN_OK) return s;
+    Workspace& w = ix->ws;
+    Ctx c = main_ctx(ix);
     std::memcpy(w.h_q, q, sizeof(int) * nq);
     std::memcpy(w.h_k, k, sizeof(int) * nq);
     if (!uniform) {
-        for (int i = 0; i < nq; ++i) w.h_order[i] = i;
-        std::stable_sort(w.h_order, w.h_order + nq, [&](int a, int b) { return k[a] > k[b]; });
+        std::memcpy(w.h_order, order.data(), sizeof(int) * nq);
         CK(cudaMemcpyAsync(w.d_order, w.h_order, sizeof(int) * nq, cudaMemcpyHostToDevice, ix->stream));
     }
     CK(cudaMemcpyAsync(w.d_q, w.h_q, sizeof(int) * nq, cudaMemcpyHostToDevice, ix->stream));
     CK(cudaMemcpyAsync(w.d_k, w.h_k, sizeof(int) * nq, cudaMemcpyHostToDevice, ix->stream));
-    s = run_sync(ix, nq, mode, kmax, !uniform);
+    s = run_sync(ix, c, b);
     if (s != RKNN_OK) return s;
-    ix->last_lc = caps_fit(ix, caps_for(kmax)).lc;
+    ix->last_lc = b.pstride;
     const long long total = w.h_off[nq];
     for (int i = 0; i <= nq; ++i) offsets[i] = w.h_off[i];
     ix->last_nq = nq;
     ix->last_mode = mode;
     if (stats) {
-        s = collect_stats(ix, nq, stats);
+        s = collect_stats(c, nq, stats);
         if (s != RKNN_OK) return s;
     }
     if (total > cap || (!out_ids && total > 0))
@@ -682,13 +847,14 @@ rknn_status rknn_query_batch_device(rknn_index* ix, const int32_t* d_q, const in
     if (mode != RKNN_MODE_FP32 && mode != RKNN_MODE_FP64) return fail(RKNN_ERR_ARG, "bad mode");
     std::lock_guard<std::mutex> lk(ix->mu);
     Workspace& w = ix->ws;
-    ZoneCaps caps = caps_fit(ix, caps_for(kmax));
-    ix->last_lc = caps.lc;
-    rknn_status s = ensure_ws(ix, nq, caps, std::max<long long>(w.pool_cap, (long long)nq * 4096));
+    const BatchPlan b = plan_batch(ix, nq, mode, false, nullptr, kmax);
+    ix->last_lc = b.pstride;
+    rknn_status s = ensure_ws(w, nq, plan_caps(b), std::max<long long>(w.pool_cap, (long long)nq * 4096));
     if (s != RKNN_OK) return s;
     CK(cudaMemcpyAsync(w.d_q, d_q, sizeof(int) * nq, cudaMemcpyDeviceToDevice, ix->stream));
     CK(cudaMemcpyAsync(w.d_k, d_k, sizeof(int) * nq, cudaMemcpyDeviceToDevice, ix->stream));
-    s = launch(ix, nq, mode, caps, false);
+    Ctx c = main_ctx(ix);
+    s = launch(ix, c, b);
     ix->last_nq = nq;
     ix->last_mode = mode;
     return s;
@@ -707,7 +873,8 @@ rknn_status rknn_last_stats(rknn_index* ix, rknn_query_stats* stats)
     if (!ix || !stats) return fail(RKNN_ERR_ARG, "null argument");
     std::lock_guard<std::mutex> lk(ix->mu);
     if (ix->last_nq <= 0) return fail(RKNN_ERR_STATE, "no query has run");
-    return collect_stats(ix, ix->last_nq, stats);
+    Ctx c = main_ctx(ix);
+    return collect_stats(c, ix->last_nq, stats);
 }
 
 rknn_status rknn_last_zone(rknn_index* ix, int32_t slot, int32_t* bis_fac, int32_t cap, int32_t* n_bis,
@@ -756,7 +923,8 @@ std::mutex g_noalloc_mu;
 unsigned char* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
 
 struct NoallocLayout {
-    int *counters, *q, *k, *cand_off, *chunk_off, *res_count, *out_off, *bispos, *pool, *out;
+    int *counters, *q, *k, *chunk_off, *res_count, *out_off, *bispos, *pool, *out;
+    long long* cand_off;
     QDesc* qd;
     ZStats* zst;
     float4* planes;
@@ -775,7 +943,7 @@ NoallocLayout noalloc_layout(unsigned char* base, int lc, int seg_cap)
     L.counters = (int*)take(sizeof(int) * 16);
     L.q = (int*)take(sizeof(int));
     L.k = (int*)take(sizeof(int));
-    L.cand_off = (int*)take(sizeof(int) * 2);
+    L.cand_off = (long long*)take(sizeof(long long) * 2);
     L.chunk_off = (int*)take(sizeof(int) * 2);
     L.res_count = (int*)take(sizeof(int));
     L.out_off = (int*)take(sizeof(int) * 2);
@@ -837,51 +1005,48 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     za.q_in = L.q; za.k_in = L.k; za.order = nullptr; za.nq = 1;
     za.work_counter = L.counters + 0;
     za.caps = caps;
-    za.use_global = 0;
-    za.gscratch = nullptr;
     za.skip_coincident = ix->skip_coincident;
     za.rmax = caps.rm;
     za.seg_cap = seg_cap;
+    za.pstride = caps.lc;
     za.qd = L.qd; za.planes = L.planes; za.bis_pos = L.bispos; za.segs = L.segs; za.zst = L.zst;
     za.fault = L.counters + 4;
     const size_t zsmem = zone_layout(caps).bytes * ZONE_WARPS;
-    if (zsmem > 48 * 1024)
-        CK(cudaFuncSetAttribute(zone_kernel_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsmem));
     zone_kernel_smem<<<1, 32 * ZONE_WARPS, zsmem, st>>>(za);
     CK(cudaGetLastError());
-    plan_kernel<<<1, 1024, 0, st>>>(L.qd, 1, L.cand_off, L.chunk_off, (int)std::min<long long>(L.pool_cap, INT32_MAX));
+    plan_kernel<<<1, 1024, 0, st>>>(L.qd, 1, L.cand_off, L.chunk_off, L.pool_cap,
+                                    (int)std::min<long long>(L.pool_cap, INT32_MAX));
     CK(cudaGetLastError());
 
     VerifyArgs va;
     va.qd = L.qd; va.planes = L.planes; va.bis_pos = L.bispos; va.lc = caps.lc;
+    va.stage_cap = caps.lc;
     va.segs = L.segs; va.seg_cap = seg_cap;
     va.chunk_off = L.chunk_off; va.cand_off = L.cand_off; va.nq = 1;
     va.uxy = ix->d_uxy; va.uid = ix->d_uid; va.fxy = ix->d_fxy; va.fstart = ix->d_fstart; va.gf = ix->gf;
     va.res_count = L.res_count; va.res_pool = L.pool; va.work_counter = L.counters + 1;
     va.vstats = L.vstats; va.mode = mode;
     va.nu = (int)ix->nu; va.nf = (int)ix->nf; va.ncf = ix->gf.gx * ix->gf.gy;
-    va.pool_cap = L.pool_cap; va.fault = L.counters + 10;
+    va.pool_cap = L.pool_cap; va.fault = L.counters + 10; va.dropped = L.counters + 2;
     const size_t vsmem = (size_t)VERIFY_WARPS * caps.lc * (mode == MODE_FP32 ? 16 : 32);
-    if (vsmem > 48 * 1024)
-        CK(cudaFuncSetAttribute(verify_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem));
     verify_kernel<<<2 * ix->num_sms, VERIFY_WARPS * 32, vsmem, st>>>(va);
     CK(cudaGetLastError());
-    scan_counts_kernel<<<1, 1024, 0, st>>>(L.res_count, 1, L.out_off);
+    scan_counts_kernel<<<1, 1024, 0, st>>>(L.res_count, L.cand_off, 1, L.out_off);
     CK(cudaGetLastError());
-    CK(cudaFuncSetAttribute(finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)(SORT_CAP * sizeof(unsigned))));
     finalize_kernel<<<1, 256, SORT_CAP * sizeof(unsigned), st>>>(L.pool, L.cand_off, L.res_count, L.out_off,
                                                                   L.out, 1);
     CK(cudaGetLastError());
 
     QDesc d;
     int off[2] = {0, 0};
+    int dropped = 0;
     CK(cudaMemcpyAsync(&d, L.qd, sizeof(QDesc), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(off, L.out_off, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&dropped, L.counters + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (d.flags & QF_RESULT_OVERFLOW)
-        return fail(RKNN_ERR_CAPACITY, "rknn_query_noalloc: the query's candidate users exceed the fixed "
-                                       "scratch (about 2M); use rknn_query");
+    if ((d.flags & QF_RESULT_OVERFLOW) || dropped)
+        return fail(RKNN_ERR_CAPACITY, "rknn_query_noalloc: the query's results exceed the fixed "
+                                       "scratch (about 2M ids); use rknn_query");
     const int64_t n = off[1];
     *n_out = n;
     if (n > cap) return fail(RKNN_ERR_CAPACITY, "output buffer too small");
@@ -891,3 +1056,429 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     }
     return RKNN_OK;
 }
+
+// ====================================================================
+// Serving: continuous batching over a resident index.
+//
+// One worker thread per server.  Each slot owns a workspace, a stream and a
+// completion event.  The worker retires finished slots (copies their results
+// to the waiting requests) and fills free slots with batches formed from the
+// queue, so batches launched at different times run on the GPU together.
+// Batch sizes are padded to powers of two (padding slots carry an invalid
+// query index, which the zone kernel marks and every later kernel skips).
+// Batches are launched directly rather than through cached graphs: their
+// composition (size per k class) changes from batch to batch.
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <thread>
+#include <unordered_map>
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct ServeReq {
+    int32_t q = 0, k = 1, mode = 0;
+    uint64_t ticket = 0;
+    Clock::time_point t_sub, t_done;
+    std::vector<int32_t> ids;
+    rknn_status status = RKNN_OK;
+    std::string err;
+    bool done = false;
+};
+using ReqPtr = std::shared_ptr<ServeReq>;
+
+struct Slot {
+    Workspace ws;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, done = nullptr;
+    long long* h_tot = nullptr;      // pinned: [0] region total, [1] region exceeded
+    double device_ms = 0;
+    std::vector<ReqPtr> reqs;        // the batch in flight
+    BatchPlan plan;
+    bool busy = false;
+};
+
+int pad_pow2(int n)
+{
+    int p = 32;
+    while (p < n) p <<= 1;
+    return p;
+}
+
+// Scratch a batch slot uses per query at a given largest k: half-planes and
+// bisector positions, segments, descriptors and offsets, and the result
+// pool's starting share (two 4096-entry int arrays).
+long long scratch_per_query(rknn_index* ix, int kmax)
+{
+    const ZoneCaps c = caps_fit(ix, caps_for(kmax));
+    return 20LL * c.lc + 8LL * (2 * c.rm + 2) + (long long)sizeof(QDesc) + (long long)sizeof(ZStats) + 32 +
+           2LL * 4 * 4096;
+}
+
+}  // namespace
+
+struct rknn_server {
+    rknn_index* ix = nullptr;
+    rknn_serve_opts o{};
+    std::vector<Slot> slots;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<ReqPtr> pending;
+    std::unordered_map<uint64_t, ReqPtr> live;
+    uint64_t next_ticket = 1;
+    bool stopping = false;
+    std::thread th;
+    // statistics (under mu)
+    int64_t submitted = 0, completed = 0, failed = 0, batches = 0, batched = 0;
+    int inflight = 0, max_inflight = 0;
+    std::vector<double> lat;
+    bool have_first = false;
+    Clock::time_point t_first, t_last;
+};
+
+namespace {
+
+void finish(rknn_server* sv, const ReqPtr& r, rknn_status st, const std::string& err)
+{
+    r->status = st;
+    r->err = err;
+    r->t_done = Clock::now();
+    r->done = true;
+    if (st == RKNN_OK) {
+        sv->completed++;
+        sv->lat.push_back(std::chrono::duration<double, std::milli>(r->t_done - r->t_sub).count());
+        sv->t_last = r->t_done;
+    } else {
+        sv->failed++;
+    }
+}
+
+// Launch a batch on a free slot (worker thread, mu not held).
+rknn_status slot_launch(rknn_server* sv, Slot& sl)
+{
+    rknn_index* ix = sv->ix;
+    const int nq = (int)sl.reqs.size();
+    const int nqp = pad_pow2(nq);
+    // descending k: the longest zones start first; each k class gets its own
+    // zone launch.  Padding slots (invalid query, k = 1) come last.
+    std::vector<int> order(nqp), ksorted(nqp);
+    for (int i = 0; i < nqp; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.begin() + nq, [&](int a, int b) { return sl.reqs[a]->k > sl.reqs[b]->k; });
+    int kmax = 1;
+    for (int i = 0; i < nqp; ++i) {
+        ksorted[i] = order[i] < nq ? sl.reqs[order[i]]->k : 1;
+        kmax = std::max(kmax, ksorted[i]);
+    }
+    sl.plan = plan_batch(ix, nqp, sl.reqs[0]->mode, true, ksorted.data(), kmax);
+    Workspace& w = sl.ws;
+    rknn_status s = ensure_ws(w, nqp, plan_caps(sl.plan), std::max<long long>(w.pool_cap, (long long)nqp * 4096));
+    if (s != RKNN_OK) return s;
+    for (int i = 0; i < nqp; ++i) {
+        w.h_q[i] = i < nq ? sl.reqs[i]->q : -1;
+        w.h_k[i] = i < nq ? sl.reqs[i]->k : 1;
+        w.h_order[i] = order[i];
+    }
+    CK(cudaMemcpyAsync(w.d_q, w.h_q, sizeof(int) * nqp, cudaMemcpyHostToDevice, sl.st));
+    CK(cudaMemcpyAsync(w.d_k, w.h_k, sizeof(int) * nqp, cudaMemcpyHostToDevice, sl.st));
+    CK(cudaMemcpyAsync(w.d_order, w.h_order, sizeof(int) * nqp, cudaMemcpyHostToDevice, sl.st));
+    Ctx c{w, sl.st, sl.ev0, sl.ev1, nullptr, &sl.device_ms};
+    CK(cudaEventRecord(sl.ev0, sl.st));
+    s = launch(ix, c, sl.plan, false);
+    if (s != RKNN_OK) return s;
+    CK(cudaEventRecord(sl.ev1, sl.st));
+    sl.h_tot[1] = 0;
+    CK(cudaMemcpyAsync(sl.h_tot, w.d_cand_off + nqp, sizeof(long long), cudaMemcpyDeviceToHost, sl.st));
+    CK(cudaMemcpyAsync(sl.h_tot + 1, w.d_counters + 2, sizeof(int), cudaMemcpyDeviceToHost, sl.st));
+    CK(cudaMemcpyAsync(w.h_off, w.d_out_off, sizeof(int) * (nqp + 1), cudaMemcpyDeviceToHost, sl.st));
+    CK(cudaEventRecord(sl.done, sl.st));
+    return RKNN_OK;
+}
+
+// Collect a finished slot's results (worker thread, mu not held).
+rknn_status slot_collect(rknn_server* sv, Slot& sl)
+{
+    Workspace& w = sl.ws;
+    const int nq = (int)sl.reqs.size();
+    if (sl.h_tot[0] > w.pool_cap || sl.h_tot[1] != 0) {
+        // a result region did not fit the pool, or held too few ids: rerun
+        Ctx c{w, sl.st, sl.ev0, sl.ev1, nullptr, &sl.device_ms};
+        rknn_status s = run_sync(sv->ix, c, sl.plan, false);
+        if (s != RKNN_OK) return s;
+    }
+    const long long total = w.h_off[nq];
+    if (total > w.h_ids_cap) {
+        cudaFreeHost(w.h_ids);
+        w.h_ids = nullptr;
+        w.h_ids_cap = 0;
+        long long cap = std::max<long long>(total, 1 << 16);
+        CK(cudaMallocHost(&w.h_ids, sizeof(int) * cap));
+        w.h_ids_cap = cap;
+    }
+    if (total > 0) {
+        CK(cudaMemcpyAsync(w.h_ids, w.d_out, sizeof(int) * total, cudaMemcpyDeviceToHost, sl.st));
+        CK(cudaStreamSynchronize(sl.st));
+    }
+    for (int i = 0; i < nq; ++i) sl.reqs[i]->ids.assign(w.h_ids + w.h_off[i], w.h_ids + w.h_off[i + 1]);
+    return RKNN_OK;
+}
+
+void serve_loop(rknn_server* sv)
+{
+    cudaSetDevice(sv->ix->device);
+    const long long budget = sv->o.scratch_bytes;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    for (;;) {
+        // retire finished batches
+        for (auto& sl : sv->slots) {
+            if (!sl.busy) continue;
+            cudaError_t q = cudaEventQuery(sl.done);
+            if (q == cudaErrorNotReady) continue;
+            lk.unlock();
+            rknn_status s = q == cudaSuccess ? slot_collect(sv, sl) : RKNN_ERR_CUDA;
+            std::string err = s == RKNN_OK ? "" : (q == cudaSuccess ? g_err : std::string(cudaGetErrorString(q)));
+            lk.lock();
+            for (auto& r : sl.reqs) finish(sv, r, s, err);
+            sl.reqs.clear();
+            sl.busy = false;
+            sv->inflight--;
+            sv->cv_done.notify_all();
+        }
+        // fill free slots from the queue
+        for (auto& sl : sv->slots) {
+            if (sl.busy || sv->pending.empty()) continue;
+            const int mode = sv->pending.front()->mode;
+            int kmax = 1;
+            for (auto it = sv->pending.begin(); it != sv->pending.end() && (int)sl.reqs.size() < sv->o.max_batch;) {
+                ReqPtr r = *it;
+                if (r->mode != mode) { ++it; continue; }
+                const int km = std::max(kmax, (int)r->k);
+                const long long need = (long long)pad_pow2((int)sl.reqs.size() + 1) * scratch_per_query(sv->ix, km);
+                if (!sl.reqs.empty() && need > budget) break;
+                sl.reqs.push_back(r);
+                kmax = km;
+                it = sv->pending.erase(it);
+            }
+            lk.unlock();
+            rknn_status s = slot_launch(sv, sl);
+            std::string err = s == RKNN_OK ? "" : g_err;
+            lk.lock();
+            sv->batches++;
+            sv->batched += (int64_t)sl.reqs.size();
+            if (s != RKNN_OK) {
+                cudaStreamSynchronize(sl.st);
+                for (auto& r : sl.reqs) finish(sv, r, s, err);
+                sl.reqs.clear();
+                sv->cv_done.notify_all();
+                continue;
+            }
+            sl.busy = true;
+            sv->inflight++;
+            sv->max_inflight = std::max(sv->max_inflight, sv->inflight);
+        }
+        if (sv->inflight == 0 && sv->pending.empty()) {
+            if (sv->stopping) break;
+            sv->cv_work.wait(lk);
+        } else {
+            // batches on the GPU: look again shortly (new arrivals wake us at once)
+            sv->cv_work.wait_for(lk, std::chrono::microseconds(20));
+        }
+    }
+}
+
+void destroy_server(rknn_server* sv)
+{
+    for (auto& sl : sv->slots) {
+        if (sl.st) cudaStreamSynchronize(sl.st);
+        free_ws(sl.ws);
+        if (sl.h_tot) cudaFreeHost(sl.h_tot);
+        if (sl.ev0) cudaEventDestroy(sl.ev0);
+        if (sl.ev1) cudaEventDestroy(sl.ev1);
+        if (sl.done) cudaEventDestroy(sl.done);
+        if (sl.st) cudaStreamDestroy(sl.st);
+    }
+    delete sv;
+}
+
+}  // namespace
+
+extern "C" {
+
+void rknn_serve_opts_default(rknn_serve_opts* o)
+{
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->slots = 3;
+    o->max_batch = 4096;
+    o->scratch_bytes = 256LL << 20;
+}
+
+rknn_status rknn_serve_start(rknn_index* ix, const rknn_serve_opts* opts, rknn_server** out)
+{
+    g_err.clear();
+    if (!ix || !out) return fail(RKNN_ERR_ARG, "null argument");
+    *out = nullptr;
+    rknn_serve_opts o;
+    rknn_serve_opts_default(&o);
+    if (opts) o = *opts;
+    if (o.slots < 1 || o.slots > 64) return fail(RKNN_ERR_ARG, "slots must be in [1, 64]");
+    if (o.max_batch < 1 || o.max_batch > (1 << 20)) return fail(RKNN_ERR_ARG, "max_batch must be in [1, 2^20]");
+    if (o.scratch_bytes <= 0) return fail(RKNN_ERR_ARG, "scratch_bytes must be positive");
+    CK(cudaSetDevice(ix->device));
+    rknn_server* sv = new (std::nothrow) rknn_server();
+    if (!sv) return fail(RKNN_ERR_OOM, "host allocation failed");
+    sv->ix = ix;
+    sv->o = o;
+    sv->slots.resize(o.slots);
+    for (auto& sl : sv->slots) {
+        cudaError_t e = cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreate(&sl.ev0);
+        if (e == cudaSuccess) e = cudaEventCreate(&sl.ev1);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_tot, 2 * sizeof(long long));
+        if (e != cudaSuccess) {
+            destroy_server(sv);
+            return fail(RKNN_ERR_CUDA, std::string("server setup: ") + cudaGetErrorString(e));
+        }
+    }
+    sv->th = std::thread(serve_loop, sv);
+    *out = sv;
+    return RKNN_OK;
+}
+
+rknn_status rknn_serve_submit(rknn_server* sv, int32_t q, int32_t k, int32_t mode, uint64_t* ticket)
+{
+    if (!sv || !ticket) return fail(RKNN_ERR_ARG, "null argument");
+    if (q < 0 || q >= sv->ix->nf)
+        return fail(RKNN_ERR_ARG, "query index " + std::to_string(q) + " out of range [0, " +
+                                      std::to_string(sv->ix->nf) + ")");
+    if (k <= 0) return fail(RKNN_ERR_ARG, "k must be a positive integer");
+    if (mode != RKNN_MODE_FP32 && mode != RKNN_MODE_FP64) return fail(RKNN_ERR_ARG, "bad mode");
+    auto r = std::make_shared<ServeReq>();
+    r->q = q;
+    r->k = k;
+    r->mode = mode;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        if (sv->stopping) return fail(RKNN_ERR_STATE, "server is stopping");
+        r->ticket = sv->next_ticket++;
+        r->t_sub = Clock::now();
+        if (!sv->have_first) { sv->have_first = true; sv->t_first = r->t_sub; }
+        sv->submitted++;
+        sv->pending.push_back(r);
+        sv->live.emplace(r->ticket, r);
+        *ticket = r->ticket;
+    }
+    sv->cv_work.notify_one();
+    return RKNN_OK;
+}
+
+rknn_status rknn_serve_wait(rknn_server* sv, uint64_t ticket, int32_t timeout_ms, int32_t* out_ids,
+                            int64_t cap, int64_t* n_out, double* latency_ms)
+{
+    if (!sv || !n_out) return fail(RKNN_ERR_ARG, "null argument");
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->live.find(ticket);
+    if (it == sv->live.end()) return fail(RKNN_ERR_ARG, "unknown ticket " + std::to_string(ticket));
+    ReqPtr r = it->second;
+    auto ready = [&] { return r->done; };
+    if (timeout_ms < 0) sv->cv_done.wait(lk, ready);
+    else if (!sv->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready))
+        return fail(RKNN_ERR_TIMEOUT, "request not finished");
+    if (r->status != RKNN_OK) {
+        sv->live.erase(ticket);
+        return fail(r->status, r->err);
+    }
+    *n_out = (int64_t)r->ids.size();
+    if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_sub).count();
+    if ((int64_t)r->ids.size() > cap || (!out_ids && !r->ids.empty()))
+        return fail(RKNN_ERR_CAPACITY, "output buffer holds " + std::to_string(cap) + " ids, " +
+                                           std::to_string(r->ids.size()) + " needed");
+    if (!r->ids.empty()) std::memcpy(out_ids, r->ids.data(), sizeof(int32_t) * r->ids.size());
+    sv->live.erase(ticket);
+    return RKNN_OK;
+}
+
+rknn_status rknn_serve_replay(rknn_server* sv, int64_t n, const int32_t* q, const int32_t* k,
+                              const int32_t* mode, const double* arrival_s, double* latency_ms,
+                              int64_t* n_results)
+{
+    if (!sv || n < 0 || (n > 0 && (!q || !k || !mode || !arrival_s))) return fail(RKNN_ERR_ARG, "null argument");
+    std::vector<uint64_t> tickets((size_t)n);
+    const Clock::time_point t0 = Clock::now();
+    for (int64_t i = 0; i < n; ++i) {
+        const auto due = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(arrival_s[i]));
+        while (Clock::now() < due) {
+            const auto left = due - Clock::now();
+            if (left > std::chrono::microseconds(200)) std::this_thread::sleep_for(left - std::chrono::microseconds(100));
+        }
+        rknn_status s = rknn_serve_submit(sv, q[i], k[i], mode[i], &tickets[(size_t)i]);
+        if (s != RKNN_OK) return s;
+    }
+    rknn_status first = RKNN_OK;
+    std::string first_err;
+    for (int64_t i = 0; i < n; ++i) {
+        std::unique_lock<std::mutex> lk(sv->mu);
+        auto it = sv->live.find(tickets[(size_t)i]);
+        if (it == sv->live.end()) continue;
+        ReqPtr r = it->second;
+        sv->cv_done.wait(lk, [&] { return r->done; });
+        if (latency_ms) latency_ms[i] = std::chrono::duration<double, std::milli>(r->t_done - r->t_sub).count();
+        if (n_results) n_results[i] = (int64_t)r->ids.size();
+        if (r->status != RKNN_OK && first == RKNN_OK) { first = r->status; first_err = r->err; }
+        sv->live.erase(it);
+    }
+    if (first != RKNN_OK) return fail(first, first_err);
+    return RKNN_OK;
+}
+
+rknn_status rknn_serve_stats_get(rknn_server* sv, int32_t reset, rknn_serve_stats* st)
+{
+    if (!sv || !st) return fail(RKNN_ERR_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    rknn_serve_stats s{};
+    s.submitted = sv->submitted;
+    s.completed = sv->completed;
+    s.failed = sv->failed;
+    s.batches = sv->batches;
+    s.mean_batch = sv->batches ? (double)sv->batched / (double)sv->batches : 0.0;
+    s.max_inflight = sv->max_inflight;
+    if (!sv->lat.empty()) {
+        std::vector<double> v = sv->lat;
+        std::sort(v.begin(), v.end());
+        auto pct = [&](double p) { return v[std::min(v.size() - 1, (size_t)(p * (double)v.size()))]; };
+        s.p50_ms = pct(0.50);
+        s.p99_ms = pct(0.99);
+        s.max_ms = v.back();
+        double sum = 0;
+        for (double x : v) sum += x;
+        s.mean_ms = sum / (double)v.size();
+        const double span = std::chrono::duration<double>(sv->t_last - sv->t_first).count();
+        s.throughput_qps = span > 0 ? (double)v.size() / span : 0.0;
+    }
+    *st = s;
+    if (reset) {
+        sv->lat.clear();
+        sv->submitted = sv->completed = sv->failed = sv->batches = sv->batched = 0;
+        sv->max_inflight = sv->inflight;
+        sv->have_first = false;
+    }
+    return RKNN_OK;
+}
+
+rknn_status rknn_serve_stop(rknn_server* sv)
+{
+    if (!sv) return RKNN_OK;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stopping = true;
+    }
+    sv->cv_work.notify_all();
+    if (sv->th.joinable()) sv->th.join();
+    destroy_server(sv);
+    return RKNN_OK;
+}
+
+}  // extern "C"

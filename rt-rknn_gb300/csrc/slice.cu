@@ -1,0 +1,469 @@
+// Angular-slice filter: one warp per query, for large k.
+//
+// The influence zone of rknn-inf keeps every arrangement vertex below level
+// k (about 3.4 k^2 of them), which outgrows shared memory beyond k ~ 35.
+// This kernel restates the SLICE filter of rknn-slice (rknn-slice/slice.h:
+// 306-367 pruneSpace, 465-551 isCompletelyPruned, 574-586 the user test)
+// with state linear in k:
+//   * the plane around q is cut into 32 equal angular slices, one per lane
+//     (the reference uses 12);
+//   * a facility f bounds slice P by its upper arc |f-q| / (2 cos a), a the
+//     largest angle between f-q and a direction of P (infinite when a >= 90
+//     degrees): every point of P farther than that from q is strictly nearer
+//     to f than to q.  With unit directions e1, e2 at the slice's edges the
+//     arc is |f-q|^2 / (2 min((f-q).e1, (f-q).e2));
+//   * each lane keeps the k smallest arcs of its slice in a max-heap; the
+//     k-th smallest, R(P), bounds the results: a user of P farther than R(P)
+//     from q has k facilities strictly nearer than q;
+//   * facilities stream in ring by ring from q's cell; a facility at
+//     distance d has arcs >= d/2, so the stream stops once half a ring's
+//     lower distance bound exceeds every slice's min(R(P), C(P)), C(P) the
+//     farthest point of the data's bounding box inside P (no user lies
+//     beyond it, so a smaller arc there changes nothing).
+// Rounding: slices are widened by 2^-14 rad on each side, arcs are computed
+// in float and rounded up by explicit error bounds, and R is inflated before
+// the user test, so the kept region contains every result.  The verification
+// kernel decides exactly; this filter only bounds its work.
+//
+// Outputs are those of the zone kernel: half-planes of the nearest
+// facilities (the first caps.lc streamed) for the verification's filter, and
+// the user-cell segments of the kept region (a ring scan over user cells; the
+// region {u : |u-q| <= R(slice of u)} is star-shaped around q, so a full ring
+// of pruned cells closes it).
+#include "rknn_common.cuh"
+#include "zone.cuh"
+#include <cfloat>
+
+namespace rknn {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int NS = 32;                                  // slices: one per lane
+constexpr float SLICE_W = 6.28318530717958647692f / NS;
+constexpr float WIDEN = 6.103515625e-05f;               // 2^-14 rad
+constexpr float TWO_PI_F = 6.28318530717958647692f;
+
+#ifdef RKNN_CHECKED
+__device__ int* s_fault;
+__device__ __forceinline__ long long sck(long long i, long long n, int id, int line)
+{
+    if (i < 0 || i >= n) {
+        if (s_fault && atomicCAS(s_fault, 0, 1) == 0) {
+            s_fault[1] = id; s_fault[2] = (int)i; s_fault[3] = (int)n; s_fault[4] = line;
+        }
+        return 0;
+    }
+    return i;
+}
+#define SX(i, n, id) sck((i), (n), (id), __LINE__)
+#else
+#define SX(i, n, id) (i)
+#endif
+
+// Upper arc of slice (e1, e2) for facility offset (vx, vy), rounded up.
+__device__ __forceinline__ float upper_arc(float vx, float vy, float e1x, float e1y, float e2x, float e2y)
+{
+    const float d1 = fmaf(vx, e1x, vy * e1y), d2 = fmaf(vx, e2x, vy * e2y);
+    const float l1 = fabsf(vx) + fabsf(vy);
+    const float dmin = fminf(d1, d2) - 8.0f * kU32 * l1 - 1e-37f;
+    if (!(dmin > 0.0f)) return INFINITY;
+    const float num = fmaf(vx, vx, vy * vy) * (1.0f + 8.0f * kU32);
+    return __fdiv_ru(num, 2.0f * dmin) * (1.0f + 4.0f * kU32);
+}
+
+// Distance from q along unit direction (ex, ey) to the box's boundary,
+// rounded up (q lies inside the box).
+__device__ __forceinline__ float exit_dist(float qx, float qy, float ex, float ey,
+                                           float x0, float y0, float x1, float y1)
+{
+    float t = INFINITY;
+    if (ex > 0.0f) t = fminf(t, __fdiv_ru(__fsub_ru(x1, qx), ex));
+    else if (ex < 0.0f) t = fminf(t, __fdiv_ru(__fsub_rd(x0, qx), ex));
+    if (ey > 0.0f) t = fminf(t, __fdiv_ru(__fsub_ru(y1, qy), ey));
+    else if (ey < 0.0f) t = fminf(t, __fdiv_ru(__fsub_rd(y0, qy), ey));
+    return t;
+}
+
+// Max-heap of one slice, interleaved across lanes: entry i of lane l at
+// H[i * 32 + l] (all lanes touching the same level hit distinct banks).
+__device__ __forceinline__ void heap_insert(float* H, int lane, int& n, int cap, float v)
+{
+    if (n < cap) {
+        int i = n++;
+        while (i > 0) {
+            const int p = (i - 1) >> 1;
+            const float pv = H[SX(p * 32 + lane, 32LL * cap, 301)];
+            if (!(pv < v)) break;
+            H[SX(i * 32 + lane, 32LL * cap, 302)] = pv;
+            i = p;
+        }
+        H[SX(i * 32 + lane, 32LL * cap, 303)] = v;
+        return;
+    }
+    if (!(v < H[lane])) return;
+    int i = 0;
+    for (;;) {
+        const int l = 2 * i + 1;
+        if (l >= n) break;
+        int c = l;
+        float cv = H[SX(l * 32 + lane, 32LL * cap, 304)];
+        if (l + 1 < n) {
+            const float rv = H[SX((l + 1) * 32 + lane, 32LL * cap, 305)];
+            if (rv > cv) { c = l + 1; cv = rv; }
+        }
+        if (!(cv > v)) break;
+        H[SX(i * 32 + lane, 32LL * cap, 306)] = cv;
+        i = c;
+    }
+    H[SX(i * 32 + lane, 32LL * cap, 307)] = v;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
+{
+    extern __shared__ __align__(16) char smem[];
+    const int lane = threadIdx.x & 31;
+#ifdef RKNN_CHECKED
+    if (threadIdx.x == 0 && blockIdx.x == 0) s_fault = A.fault;
+    __syncthreads();
+    if (!s_fault) s_fault = A.fault;
+#endif
+    const SliceLayout LY = slice_layout(A.caps);
+    float* H = (float*)(smem + LY.heap);
+    float* Rs = (float*)(smem + LY.R);
+    int* lpos = (int*)(smem + LY.lpos);
+    uint32_t* bitmap = (uint32_t*)(smem + LY.bitmap);
+    const int KC = A.caps.vc, LC = A.caps.lc;
+    const long long NCF = (long long)A.gf.gx * A.gf.gy, NCU = (long long)A.gu.gx * A.gu.gy;
+    (void)NCF; (void)NCU;
+    // this lane's slice, widened: directions from a0 to b0
+    float e1x, e1y, e2x, e2y;
+    sincosf((float)lane * SLICE_W - WIDEN, &e1y, &e1x);
+    sincosf((float)(lane + 1) * SLICE_W + WIDEN, &e2y, &e2x);
+    const double slack = 1e-5 * ((double)A.gf.cs + fmax(fmax(fabs(A.sx0), fabs(A.sx1)), fmax(fabs(A.sy0), fabs(A.sy1))));
+
+    for (;;) {
+        int slot = 0;
+        if (lane == 0) slot = atomicAdd(A.work_counter, 1);
+        slot = __shfl_sync(FULL, slot, 0);
+        if (slot >= A.nq) break;
+        const int s = A.order ? A.order[slot] : slot;
+        const int qin = A.q_in[s];
+        const int k = A.k_in[s];
+        QDesc* qd = A.qd + s;
+        ZStats zs = {};
+        if (qin < 0 || qin >= A.nf || k <= 0 || k > KC) {
+            if (lane == 0) {
+                QDesc d = {};
+                d.qpos = -1;
+                d.k = k;
+                d.flags = QF_BAD_QUERY;
+                *qd = d;
+                A.zst[s] = zs;
+                A.segs[(size_t)s * A.seg_cap] = make_int2(0, 0);
+            }
+            continue;
+        }
+        const int qpos = A.fpos[SX(qin, A.nf, 310)];
+        const float2 qf = A.fxy[SX(qpos, A.nf, 311)];
+        const double qx = qf.x, qy = qf.y;
+        long long tph = clock64();
+
+        // C(P): farthest point of the box inside this slice, a vertex of the
+        // slice's cone clipped to the box (an edge ray's exit or a box corner
+        // inside the cone), rounded up
+        float clip;
+        {
+            const float bx0 = __double2float_rd(A.sx0), by0 = __double2float_rd(A.sy0);
+            const float bx1 = __double2float_ru(A.sx1), by1 = __double2float_ru(A.sy1);
+            clip = fmaxf(exit_dist(qf.x, qf.y, e1x, e1y, bx0, by0, bx1, by1),
+                         exit_dist(qf.x, qf.y, e2x, e2y, bx0, by0, bx1, by1));
+            const float cxs[4] = {bx0, bx1, bx0, bx1}, cys[4] = {by0, by0, by1, by1};
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4) {
+                const float dx = cxs[c4] - qf.x, dy = cys[c4] - qf.y;
+                // inside the cone (or near its edges: then the corner only raises the bound)
+                const float c1 = e1x * dy - e1y * dx, c2 = dx * e2y - dy * e2x;
+                const float tol = 1e-5f * (fabsf(dx) + fabsf(dy));
+                if (c1 >= -tol && c2 >= -tol) clip = fmaxf(clip, sqrtf(fmaf(dx, dx, dy * dy)));
+            }
+            clip = clip * (1.0f + 1e-5f) + 1e-30f;
+        }
+
+        // ---- stream facilities ring by ring -------------------------------
+        int n = 0;              // this slice's heap size
+        int nL = 0;             // half-planes kept (warp-uniform)
+        const int qcx = cell_coord(qf.x, A.gf.x0, A.gf.inv, A.gf.gx);
+        const int qcy = cell_coord(qf.y, A.gf.y0, A.gf.inv, A.gf.gy);
+        const int rmaxf = max(max(qcx, A.gf.gx - 1 - qcx), max(qcy, A.gf.gy - 1 - qcy));
+        const int gx = A.gf.gx, gy = A.gf.gy;
+        int ring = 0;
+        for (; ring <= rmaxf; ++ring) {
+            // stop when no facility at or beyond this ring can change a
+            // slice's effective bound min(R, C)
+            const float Rl = fminf((n < k) ? INFINITY : H[lane], clip);
+            float Rmax = Rl;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) Rmax = fmaxf(Rmax, __shfl_xor_sync(FULL, Rmax, o));
+            if (ring > 0 && Rmax < INFINITY) {
+                const double Lr = (double)(ring - 1) * (double)A.gf.cs - slack;
+                if (Lr > 0.0 && 0.5 * Lr > (double)Rmax * (1.0 + 1e-6)) break;
+            }
+            // the ring as facility ranges (cells are row-major): its top and
+            // bottom rows, then the left and right cells of the rows between
+            const int nrange = ring == 0 ? 1 : 2 + 2 * (2 * ring - 1);
+            for (int r0 = 0; r0 < nrange; r0 += 32) {
+                const int ri = r0 + lane;
+                int fs = 0, fe = 0;
+                if (ri < nrange) {
+                    int y = 0, x0 = 0, x1 = -1;
+                    if (ring == 0) { y = qcy; x0 = x1 = qcx; }
+                    else if (ri == 0) { y = qcy - ring; x0 = qcx - ring; x1 = qcx + ring; }
+                    else if (ri == 1) { y = qcy + ring; x0 = qcx - ring; x1 = qcx + ring; }
+                    else {
+                        const int m = ri - 2;              // 0 .. 2(2 ring - 1) - 1
+                        y = qcy - ring + 1 + (m >> 1);
+                        x0 = x1 = (m & 1) ? qcx + ring : qcx - ring;
+                    }
+                    x0 = max(x0, 0);
+                    x1 = min(x1, gx - 1);
+                    if (y >= 0 && y < gy && x0 <= x1) {
+                        fs = A.fstart[SX((long long)y * gx + x0, NCF + 1, 312)];
+                        fe = A.fstart[SX((long long)y * gx + x1 + 1, NCF + 1, 313)];
+                    }
+                }
+                // flatten the ranges: inclusive prefix of their lengths
+                const int len = fe - fs;
+                int incl = len;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                const int total = __shfl_sync(FULL, incl, 31);
+                for (int t0 = 0; t0 < total; t0 += 32) {
+                    const int j = t0 + lane;
+                    // range holding item j: first lane with incl > j
+                    int lo = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const int probe = __shfl_sync(FULL, incl, lo + step - 1);
+                        if (probe <= j) lo += step;
+                    }
+                    const int rs = __shfl_sync(FULL, fs, lo);
+                    const int rincl = __shfl_sync(FULL, incl, lo);
+                    const int rlen = __shfl_sync(FULL, len, lo);
+                    const int fidx = rs + (j - (rincl - rlen));
+                    bool ok = j < total && fidx != qpos;
+                    float vx = 0.0f, vy = 0.0f;
+                    if (ok) {
+                        const float2 f = A.fxy[SX(fidx, A.nf, 314)];
+                        vx = f.x - qf.x;
+                        vy = f.y - qf.y;
+                        // a facility at q's position is never strictly nearer
+                        // (float differences are zero only for equal floats)
+                        ok = vx != 0.0f || vy != 0.0f;
+                    }
+                    // half-planes: the first LC facilities streamed
+                    const unsigned pm = __ballot_sync(FULL, ok);
+                    if (ok) {
+                        const int at = nL + __popc(pm & ((1u << lane) - 1));
+                        if (at < LC) lpos[SX(at, LC, 315)] = fidx;
+                    }
+                    nL = min(LC, nL + __popc(pm));
+                    zs.pts += __popc(pm);
+                    // every lane offers every streamed facility to its slice
+                    unsigned m = pm;
+                    while (m) {
+                        const int src = __ffs(m) - 1;
+                        m &= m - 1;
+                        const float ux = __shfl_sync(FULL, vx, src), uy = __shfl_sync(FULL, vy, src);
+                        const float u = upper_arc(ux, uy, e1x, e1y, e2x, e2y);
+                        if (n < k || u < H[lane]) heap_insert(H, lane, n, k, u);
+                    }
+                }
+            }
+            zs.cells += nrange;
+        }
+        zs.rings = ring;
+        __syncwarp();
+        // R(P): k-th smallest arc, rounded up for the user test, and clipped
+        // to the box (no user lies farther)
+        {
+            const float R = (n < k) ? INFINITY : H[lane];
+            Rs[lane] = fminf(R < INFINITY ? R * (1.0f + 1e-5f) + 1e-30f : INFINITY, clip);
+        }
+        __syncwarp();
+        zs.cyc[0] += clock64() - tph;
+        tph = clock64();
+
+        // ---- half-planes relative to q (as the zone kernel's epilogue) -----
+        float4* planes = A.planes + (size_t)s * A.pstride;
+        double cmax = 0.0;
+        for (int m = lane; m < nL; m += 32) {
+            const int pos = lpos[SX(m, LC, 316)];
+            const float2 f = A.fxy[SX(pos, A.nf, 317)];
+            const double dx = (double)f.x - qx, dy = (double)f.y - qy;
+            const double c = dx * dx + dy * dy;
+            planes[SX(m, A.pstride, 318)] = make_float4((float)(-2.0 * dx), (float)(-2.0 * dy), (float)c, 0.0f);
+            A.bis_pos[(size_t)s * A.pstride + SX(m, A.pstride, 319)] = pos;
+            cmax = fmax(cmax, c);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cmax = fmax(cmax, __shfl_xor_sync(FULL, cmax, o));
+        const double Fp = sqrt(cmax) * (1.0 + 1e-6) + 1e-30;
+        const float k2f = (float)(8.0 * (double)kU32 * 2.0 * Fp * (1.0 + 1e-6));
+        const float kf2 = (float)(8.0 * (double)kU32 * Fp * Fp * (1.0 + 1e-6)) + 1e-30f;
+        const double k2f64 = 8.0 * kU64 * 2.0 * Fp * (1.0 + 1e-6);
+        const double kf264 = 8.0 * kU64 * Fp * Fp * (1.0 + 1e-6) + 1e-300;
+
+        // ---- ring scan over user cells --------------------------------------
+        const Grid gu = A.gu;
+        const int ucx = cell_coord(qf.x, gu.x0, gu.inv, gu.gx);
+        const int ucy = cell_coord(qf.y, gu.y0, gu.inv, gu.gy);
+        const int RM = A.rmax;
+        const int W = 2 * RM + 1;
+        const int nwords = (W * W + 31) / 32;
+        for (int i = lane; i < nwords; i += 32) bitmap[SX(i, nwords, 320)] = 0u;
+        __syncwarp();
+        const float delta = 8.0f * kU32 * (fabsf(gu.x0) + fabsf(gu.y0) + gu.cs * (float)max(gu.gx, gu.gy) + fabsf(qf.x) + fabsf(qf.y) + gu.cs) + 1e-30f;
+        const int rmaxu = max(max(ucx, gu.gx - 1 - ucx), max(ucy, gu.gy - 1 - ucy));
+        bool all_users = false;
+        int rend = -1;
+        if (A.nu > 0) {
+            for (int r = 0;; ++r) {
+                if (r > rmaxu) { rend = r - 1; break; }
+                if (r > RM) { all_users = true; break; }
+                const int ncell = r == 0 ? 1 : 8 * r;
+                bool anykeep = false;
+                for (int t0 = 0; t0 < ncell; t0 += 32) {
+                    const int t = t0 + lane;
+                    int dx = 0, dy = 0;
+                    bool ok = t < ncell;
+                    if (ok && r > 0) {
+                        const int side = 2 * r + 1;
+                        if (t < side) { dx = -r + t; dy = -r; }
+                        else if (t < 2 * side) { dx = -r + (t - side); dy = r; }
+                        else if (t < 2 * side + (2 * r - 1)) { dx = -r; dy = -r + 1 + (t - 2 * side); }
+                        else { dx = r; dy = -r + 1 + (t - 2 * side - (2 * r - 1)); }
+                    }
+                    const int cxx = ucx + dx, cyy = ucy + dy;
+                    ok = ok && cxx >= 0 && cxx < gu.gx && cyy >= 0 && cyy < gu.gy;
+                    bool keep = false;
+                    if (ok) {
+                        const float X0 = (gu.x0 + (float)cxx * gu.cs) - qf.x - delta;
+                        const float X1 = (gu.x0 + (float)(cxx + 1) * gu.cs) - qf.x + delta;
+                        const float Y0 = (gu.y0 + (float)cyy * gu.cs) - qf.y - delta;
+                        const float Y1 = (gu.y0 + (float)(cyy + 1) * gu.cs) - qf.y + delta;
+                        if (X0 <= 0.0f && X1 >= 0.0f && Y0 <= 0.0f && Y1 >= 0.0f) keep = true;
+                        else {
+                            // nearest point of the cell, and the slices the cell spans
+                            const float ddx = fmaxf(fmaxf(X0, -X1), 0.0f), ddy = fmaxf(fmaxf(Y0, -Y1), 0.0f);
+                            const float dmin2 = fmaf(ddx, ddx, ddy * ddy) * (1.0f - 4.0f * kU32);
+                            const float pc = atan2f(0.5f * (Y0 + Y1), 0.5f * (X0 + X1));
+                            float lo = 0.0f, hi = 0.0f;
+                            const float cxs[4] = {X0, X1, X0, X1}, cys[4] = {Y0, Y0, Y1, Y1};
+#pragma unroll
+                            for (int c4 = 0; c4 < 4; ++c4) {
+                                float d = atan2f(cys[c4], cxs[c4]) - pc;
+                                if (d > 3.14159265f) d -= TWO_PI_F;
+                                if (d < -3.14159265f) d += TWO_PI_F;
+                                lo = fminf(lo, d);
+                                hi = fmaxf(hi, d);
+                            }
+                            const int s0 = (int)floorf((pc + lo - WIDEN) / SLICE_W);
+                            const int s1 = (int)floorf((pc + hi + WIDEN) / SLICE_W);
+                            float Rmax = 0.0f;
+                            for (int sl = s0; sl <= s1 && sl <= s0 + NS; ++sl) Rmax = fmaxf(Rmax, Rs[((sl % NS) + NS) % NS]);
+                            keep = !(dmin2 > Rmax * Rmax);
+                        }
+                    }
+                    if (keep) {
+                        const int bit = (dy + RM) * W + (dx + RM);
+                        atomicOr(&bitmap[SX(bit >> 5, nwords, 321)], 1u << (bit & 31));
+                    }
+                    anykeep |= keep;
+                }
+                anykeep = __any_sync(FULL, anykeep);
+                if (!anykeep && r >= 1) { rend = r - 1; break; }
+                rend = r;
+            }
+            zs.rings = rend + 1;
+        }
+        __syncwarp();
+
+        // ---- segments: one user range per row ------------------------------
+        int2* seg = A.segs + (size_t)s * A.seg_cap;
+        int nseg = 0, ncand = 0;
+        int qflags = 0;
+        if (all_users) {
+            seg[0] = make_int2(0, 0);
+            seg[1] = make_int2(0, A.nu);
+            nseg = 1;
+            ncand = A.nu;
+            qflags |= QF_ALL_USERS;
+        } else if (rend >= 0) {
+            const int y0 = max(0, ucy - rend), y1 = min(gu.gy - 1, ucy + rend);
+            const int xl0 = max(0, ucx - rend), xl1 = min(gu.gx - 1, ucx + rend);
+            for (int r0 = y0; r0 <= y1; r0 += 32) {
+                const int row = r0 + lane;
+                int st = 0, len = 0;
+                if (row <= y1) {
+                    const int dy = row - ucy;
+                    int xmin = INT_MAX, xmax = -1;
+                    for (int cxx = xl0; cxx <= xl1; ++cxx) {
+                        const int bit = (dy + RM) * W + (cxx - ucx + RM);
+                        if (bitmap[SX(bit >> 5, nwords, 322)] & (1u << (bit & 31))) {
+                            xmin = min(xmin, cxx);
+                            xmax = cxx;
+                        }
+                    }
+                    if (xmax >= 0) {
+                        st = A.ustart[SX((long long)row * gu.gx + xmin, NCU + 1, 323)];
+                        len = A.ustart[SX((long long)row * gu.gx + xmax + 1, NCU + 1, 324)] - st;
+                    }
+                }
+                const bool has = len > 0;
+                const unsigned m = __ballot_sync(FULL, has);
+                const int pre = __popc(m & ((1u << lane) - 1));
+                int incl = has ? len : 0;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                const int excl = incl - (has ? len : 0);
+                if (has) seg[SX(nseg + pre, A.seg_cap, 325)] = make_int2(st, ncand + excl);
+                nseg += __popc(m);
+                ncand += __shfl_sync(FULL, incl, 31);
+            }
+            if (lane == 0) seg[SX(nseg, A.seg_cap, 326)] = make_int2(0, ncand);
+        } else if (lane == 0) {
+            seg[0] = make_int2(0, 0);
+        }
+        zs.cyc[7] += clock64() - tph;
+        zs.nb = nL;
+        if (lane == 0) {
+            QDesc d;
+            d.qx = qf.x;
+            d.qy = qf.y;
+            d.qpos = qpos;
+            d.k = k;
+            d.nb = nL;
+            d.nseg = nseg;
+            d.k2f = k2f;
+            d.kf2 = kf2;
+            d.k2f64 = k2f64;
+            d.kf264 = kf264;
+            d.ncand = ncand;
+            d.flags = qflags;
+            *qd = d;
+            A.zst[s] = zs;
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace rknn

@@ -89,7 +89,7 @@ __device__ __forceinline__ int exact_count(float ux, float uy, const QDesc& d, c
 }
 
 template <typename T>
-__device__ __forceinline__ void filter_users(const QDesc& d, const char* sp, const int* pos,
+__device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char* sp, const int* pos,
                                              const float2* u, const bool* valid, int* cnt,
                                              unsigned long long& evals)
 {
@@ -109,7 +109,7 @@ __device__ __forceinline__ void filter_users(const QDesc& d, const char* sp, con
             bu[t] = (T)fma(d.k2f64, fabs(xx) + fabs(yy), d.kf264);
         }
     }
-    const int nb = d.nb, k = d.k;
+    const int k = d.k;
     int m = 0;
     for (; m < nb; ++m) {
         T a, b, c;
@@ -142,7 +142,7 @@ verify_kernel(VerifyArgs A)
 {
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const size_t per_warp = (size_t)A.lc * (A.mode == MODE_FP32 ? 16 : 32);
+    const size_t per_warp = (size_t)A.stage_cap * (A.mode == MODE_FP32 ? 16 : 32);
     char* sp = smem + w * per_warp;
     int cur = -1;
     unsigned long long s_cand = 0, s_evals = 0, s_surv = 0, s_fac = 0, s_rech = 0, s_res = 0;
@@ -163,10 +163,10 @@ verify_kernel(VerifyArgs A)
             __syncwarp();
             if (A.mode == MODE_FP32) {
                 const float4* src = A.planes + (size_t)s * A.lc;
-                for (int m = lane; m < d.nb; m += 32) ((float4*)sp)[m] = src[m];
+                for (int m = lane; m < min(d.nb, A.stage_cap); m += 32) ((float4*)sp)[m] = src[m];
             } else {
                 const int* bp = A.bis_pos + (size_t)s * A.lc;
-                for (int m = lane; m < d.nb; m += 32) {
+                for (int m = lane; m < min(d.nb, A.stage_cap); m += 32) {
                     float2 f = A.fxy[VX(bp[m], A.nf, 204)];
                     double dx = (double)f.x - (double)d.qx, dy = (double)f.y - (double)d.qy;
                     double* p = (double*)sp + 4 * m;
@@ -209,8 +209,9 @@ verify_kernel(VerifyArgs A)
             s_cand += valid[t];
         }
         int cnt[VERIFY_UPT];
-        if (A.mode == MODE_FP32) filter_users<float>(d, sp, pos, u, valid, cnt, s_evals);
-        else filter_users<double>(d, sp, pos, u, valid, cnt, s_evals);
+        const int nbs = min(d.nb, A.stage_cap);
+        if (A.mode == MODE_FP32) filter_users<float>(d, nbs, sp, pos, u, valid, cnt, s_evals);
+        else filter_users<double>(d, nbs, sp, pos, u, valid, cnt, s_evals);
 
         // stage 2: exact count for the survivors, one user at a time per warp
         bool acc[VERIFY_UPT];
@@ -237,11 +238,15 @@ verify_kernel(VerifyArgs A)
             int base = 0;
             if (lane == 0) base = atomicAdd(A.res_count + s, tot);
             base = __shfl_sync(FULL, base, 0);
-            int* dst = A.res_pool + A.cand_off[s] + base;
+            // the slot's region holds min(candidates, rcap) ids; results
+            // beyond it are counted, not stored, and the host reruns
+            const long long r0 = A.cand_off[s], region = A.cand_off[s + 1] - r0;
+            if (lane == 0 && base + tot > region) atomicOr(A.dropped, 1);
             int o = 0;
 #pragma unroll
             for (int t = 0; t < VERIFY_UPT; ++t) {
-                if (acc[t]) A.res_pool[VX((long long)A.cand_off[s] + base + o + __popc(am[t] & ((1u << lane) - 1)), A.pool_cap, 206)] = A.uid[VX(pos[t], A.nu, 207)];
+                const long long at = (long long)base + o + __popc(am[t] & ((1u << lane) - 1));
+                if (acc[t] && at < region) A.res_pool[VX(r0 + at, A.pool_cap, 206)] = A.uid[VX(pos[t], A.nu, 207)];
                 o += __popc(am[t]);
             }
             s_res += (lane == 0) ? tot : 0;
@@ -265,80 +270,78 @@ verify_kernel(VerifyArgs A)
 
 // ---------------------------------------------------------------- scans
 namespace {
-// exclusive scan over one block of 1024 threads; returns the total
-__device__ int block_scan_excl(int v, int* tmp)
+// Exclusive block-wide prefix sum; *total receives the block's sum.
+template <typename T>
+__device__ T block_scan_excl(T v, T* tmp, T* total)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int x = v;
+    T x = v;
     for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(FULL, x, o);
+        T y = __shfl_up_sync(FULL, x, o);
         if (lane >= o) x += y;
     }
     if (lane == 31) tmp[w] = x;
     __syncthreads();
     if (w == 0) {
-        int t = lane < (int)(blockDim.x >> 5) ? tmp[lane] : 0;
+        T t = lane < (int)(blockDim.x >> 5) ? tmp[lane] : (T)0;
         for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(FULL, t, o);
+            T y = __shfl_up_sync(FULL, t, o);
             if (lane >= o) t += y;
         }
         tmp[lane] = t;
     }
     __syncthreads();
-    int total = tmp[(blockDim.x >> 5) - 1];
-    int excl = x - v + (w > 0 ? tmp[w - 1] : 0);
+    *total = tmp[(blockDim.x >> 5) - 1];
+    const T excl = x - v + (w > 0 ? tmp[w - 1] : (T)0);
     __syncthreads();
-    return excl | 0 ? excl : excl + 0 * total;   // keep total live for callers below
+    return excl;
 }
 }  // namespace
 
-__global__ void plan_kernel(QDesc* qd, int nq, int* cand_off, int* chunk_off, int pool_cap)
+// Result region of each slot: min(candidates, rcap) entries, at 64-bit
+// offsets; slots whose region does not fit the pool are flagged and skipped
+// (the host grows the pool and runs the batch again).  Work items cover
+// every candidate of the slots that fit.
+__global__ void plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_off, long long pool_cap, int rcap)
 {
+    __shared__ long long tmp64[32];
     __shared__ int tmp[32];
-    __shared__ int tot;
     const int T = blockDim.x;
     const int per = (nq + T - 1) / T;
     const int b = threadIdx.x * per, e = min(nq, b + per);
-    // pass 1: candidate offsets
-    int sum = 0;
-    for (int i = b; i < e; ++i) sum += qd[i].ncand;
-    int run = block_scan_excl(sum, tmp);
-    if (threadIdx.x == T - 1) tot = run + sum;
-    for (int i = b; i < e; ++i) { cand_off[i] = run; run += qd[i].ncand; }
-    __syncthreads();
-    if (threadIdx.x == 0) cand_off[nq] = tot;
-    // pass 2: chunk offsets, skipping slots whose region overflows the pool
-    sum = 0;
+    long long sum = 0, tot64 = 0;
+    for (int i = b; i < e; ++i) sum += min(qd[i].ncand, rcap);
+    long long run = block_scan_excl<long long>(sum, tmp64, &tot64);
+    for (int i = b; i < e; ++i) { cand_off[i] = run; run += min(qd[i].ncand, rcap); }
+    if (threadIdx.x == 0) cand_off[nq] = tot64;
+    int csum = 0, ctot = 0;
     for (int i = b; i < e; ++i) {
-        int n = qd[i].ncand;
-        bool fits = cand_off[i] + n <= pool_cap;
+        const int n = qd[i].ncand;
+        const bool fits = cand_off[i] + min(n, rcap) <= pool_cap;
         if (!fits) qd[i].flags |= QF_RESULT_OVERFLOW;
-        sum += fits ? (n + VERIFY_CHUNK - 1) / VERIFY_CHUNK : 0;
+        csum += fits ? (n + VERIFY_CHUNK - 1) / VERIFY_CHUNK : 0;
     }
-    run = block_scan_excl(sum, tmp);
-    if (threadIdx.x == T - 1) tot = run + sum;
+    int crun = block_scan_excl<int>(csum, tmp, &ctot);
     for (int i = b; i < e; ++i) {
-        chunk_off[i] = run;
-        int n = qd[i].ncand;
-        if (!(qd[i].flags & QF_RESULT_OVERFLOW)) run += (n + VERIFY_CHUNK - 1) / VERIFY_CHUNK;
+        chunk_off[i] = crun;
+        const int n = qd[i].ncand;
+        if (!(qd[i].flags & QF_RESULT_OVERFLOW)) crun += (n + VERIFY_CHUNK - 1) / VERIFY_CHUNK;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) chunk_off[nq] = tot;
+    if (threadIdx.x == 0) chunk_off[nq] = ctot;
 }
 
-__global__ void scan_counts_kernel(const int* res_count, int nq, int* out_off)
+// Output offsets of the stored results (a slot stores at most its region).
+__global__ void scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int* out_off)
 {
     __shared__ int tmp[32];
-    __shared__ int tot;
     const int T = blockDim.x;
     const int per = (nq + T - 1) / T;
     const int b = threadIdx.x * per, e = min(nq, b + per);
-    int sum = 0;
-    for (int i = b; i < e; ++i) sum += res_count[i];
-    int run = block_scan_excl(sum, tmp);
-    if (threadIdx.x == T - 1) tot = run + sum;
-    for (int i = b; i < e; ++i) { out_off[i] = run; run += res_count[i]; }
-    __syncthreads();
+    auto stored = [&](int i) { return (int)min((long long)res_count[i], cand_off[i + 1] - cand_off[i]); };
+    int sum = 0, tot = 0;
+    for (int i = b; i < e; ++i) sum += stored(i);
+    int run = block_scan_excl<int>(sum, tmp, &tot);
+    for (int i = b; i < e; ++i) { out_off[i] = run; run += stored(i); }
     if (threadIdx.x == 0) out_off[nq] = tot;
 }
 
@@ -393,13 +396,13 @@ __device__ void block_radix_pass(const unsigned* in, unsigned* out, int n, int s
 }  // namespace
 
 __global__ void __launch_bounds__(256)
-finalize_kernel(int* res_pool, const int* cand_off, const int* res_count, const int* out_off,
+finalize_kernel(int* res_pool, const long long* cand_off, const int* res_count, const int* out_off,
                 int* out, int nq)
 {
     extern __shared__ unsigned skeys[];
     const int s = blockIdx.x;
     if (s >= nq) return;
-    const int n = res_count[s];
+    const int n = (int)min((long long)res_count[s], cand_off[s + 1] - cand_off[s]);
     unsigned* src = (unsigned*)(res_pool + cand_off[s]);
     unsigned* dst = (unsigned*)(out + out_off[s]);
     const int tid = threadIdx.x;

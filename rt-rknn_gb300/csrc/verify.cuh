@@ -15,11 +15,13 @@ struct VerifyArgs {
     const QDesc* qd;
     const float4* planes;    // [slot][lc] float half-planes relative to q
     const int* bis_pos;      // [slot][lc] facility positions (FP64 planes are rebuilt from these)
-    int lc;
+    int lc;                  // row stride of planes / bis_pos
+    int stage_cap;           // half-planes staged per warp (the filter uses the first ones;
+                             // fewer only means more users reach the exact recount)
     const int2* segs;        // [slot][seg_cap]
     int seg_cap;
     const int* chunk_off;    // [nq+1]
-    const int* cand_off;     // [nq+1] result region of each slot
+    const long long* cand_off;   // [nq+1] result region of each slot
     int nq;
     const float2* uxy;       // cell-sorted users
     const int* uid;          // their ids
@@ -33,20 +35,23 @@ struct VerifyArgs {
     int mode;
     int nu, nf, ncf;         // array sizes (bounds-checked builds)
     long long pool_cap;
+    int* dropped;            // set when a slot had more results than its region
     int* fault;              // checked builds: {flag, array id, index, size, line}
 };
 
 __global__ void verify_kernel(VerifyArgs a);
 
-// single block: cand_off / chunk_off from QDesc.ncand; flags slots whose
-// region does not fit the pool
-__global__ void plan_kernel(QDesc* qd, int nq, int* cand_off, int* chunk_off, int pool_cap);
+// single block: result regions (min(candidates, rcap) ids, 64-bit offsets)
+// and work-item offsets from QDesc.ncand; flags slots whose region does not
+// fit the pool
+__global__ void plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_off, long long pool_cap,
+                            int rcap);
 
-// single block: exclusive scan of res_count into out_off
-__global__ void scan_counts_kernel(const int* res_count, int nq, int* out_off);
+// single block: exclusive scan of the stored result counts into out_off
+__global__ void scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int* out_off);
 
 // one block per slot: sort the slot's results into out[out_off[s] ...]
-__global__ void finalize_kernel(int* res_pool, const int* cand_off, const int* res_count,
+__global__ void finalize_kernel(int* res_pool, const long long* cand_off, const int* res_count,
                                 const int* out_off, int* out, int nq);
 
 }  // namespace rknn

@@ -1110,7 +1110,7 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
         // ---- epilogue 1: exact half-planes relative to q -------------------
         // m(u) = a (ux - qx) + b (uy - qy) + c = d2(u,f) - d2(u,q);  f strictly
         // nearer than q  <=>  m < 0.
-        float4* planes = A.planes + (size_t)s * LC;
+        float4* planes = A.planes + (size_t)s * A.pstride;
         double cmax = 0.0;
         for (int m = lane; m < nL; m += 32) {
             int pos = IX(S.lpos, m);
@@ -1118,9 +1118,9 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             double dx = (double)f.x - qx, dy = (double)f.y - qy;
             double c = dx * dx + dy * dy;
             float4 p = make_float4((float)(-2.0 * dx), (float)(-2.0 * dy), (float)c, 0.0f);
-            planes[GX(m, LC, 106)] = p;
+            planes[GX(m, A.pstride, 106)] = p;
             IX(S.splanes, m) = p;
-            A.bis_pos[(size_t)s * LC + GX(m, LC, 107)] = pos;
+            A.bis_pos[(size_t)s * A.pstride + GX(m, A.pstride, 107)] = pos;
             cmax = fmax(cmax, c);
         }
         cmax = warp_max(cmax);

@@ -71,6 +71,26 @@ __host__ __device__ inline ZoneLayout zone_layout(const ZoneCaps& c)
     return L;
 }
 
+// Angular-slice filter (slice_kernel): 32 slices around q, one per lane.
+// caps.vc = heap entries per slice (the batch class's largest k), caps.lc =
+// half-planes kept for the verification, caps.rm = user ring scan radius.
+struct SliceLayout {
+    size_t heap, R, lpos, bitmap, bytes;
+};
+
+__host__ __device__ inline SliceLayout slice_layout(const ZoneCaps& c)
+{
+    SliceLayout L;
+    size_t o = 0;
+    const size_t W = 2 * (size_t)c.rm + 1;
+    L.heap = o;   o = zl_align(o + 4 * 32 * ((size_t)c.vc + ZL_SPARE));
+    L.R = o;      o = zl_align(o + 4 * 32);
+    L.lpos = o;   o = zl_align(o + 4 * ((size_t)c.lc + ZL_SPARE));
+    L.bitmap = o; o = zl_align(o + 4 * ((W * W + 31) / 32 + ZL_SPARE));
+    L.bytes = o;
+    return L;
+}
+
 struct ZoneArgs {
     // facility index
     const float2* fxy;       // cell-sorted facility coordinates
@@ -91,15 +111,14 @@ struct ZoneArgs {
     int nq;
     int* work_counter;
     ZoneCaps caps;
-    int use_global;          // zone state in global scratch instead of shared memory
-    char* gscratch;
     int skip_coincident;
     int rmax;                // == caps.rm
     int seg_cap;             // segments per query slot (>= 2*rmax+2)
     // outputs (per slot)
     QDesc* qd;
-    float4* planes;          // [slot][caps.lc]
-    int* bis_pos;            // [slot][caps.lc] facility positions of the bisectors
+    float4* planes;          // [slot][pstride]
+    int* bis_pos;            // [slot][pstride] facility positions of the bisectors
+    int pstride;             // >= caps.lc: row stride of planes / bis_pos
     int2* segs;              // [slot][seg_cap]: (user start, candidate offset)
     ZStats* zst;
     int* fault;              // checked builds: {flag, array id, index, capacity, line}
@@ -107,5 +126,8 @@ struct ZoneArgs {
 
 // zone state in shared memory, one warp (one query at a time) per block
 __global__ void zone_kernel_smem(ZoneArgs a);
+
+// angular-slice filter for large k, same arguments and outputs
+__global__ void slice_kernel(ZoneArgs a);
 
 }  // namespace rknn

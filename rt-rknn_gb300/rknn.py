@@ -36,7 +36,24 @@ EXPORTS = ["rknn_index_opts_default", "rknn_index_create", "rknn_index_destroy",
            "rknn_index_size", "rknn_index_get_info", "rknn_query", "rknn_query_noalloc", "rknn_query_batch", "rknn_query_batch_device",
            "rknn_batch_device_results", "rknn_sync", "rknn_set_stream", "rknn_last_stats",
            "rknn_last_zone", "rknn_set_profiling", "rknn_last_kernel_ms",
+           "rknn_serve_opts_default", "rknn_serve_start", "rknn_serve_submit", "rknn_serve_wait",
+           "rknn_serve_replay", "rknn_serve_stats_get", "rknn_serve_stop",
            "rknn_last_error", "rknn_version"]
+
+
+class ServeOpts(C.Structure):
+    _fields_ = [("slots", C.c_int32), ("max_batch", C.c_int32), ("scratch_bytes", C.c_int64),
+                ("reserved", C.c_int32 * 8)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+                ("batches", C.c_int64), ("mean_batch", C.c_double), ("max_inflight", C.c_int32),
+                ("pad", C.c_int32), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("mean_ms", C.c_double), ("max_ms", C.c_double), ("throughput_qps", C.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "pad"}
 
 
 class RkNNError(RuntimeError):
@@ -47,7 +64,8 @@ class RkNNError(RuntimeError):
 
 class Opts(C.Structure):
     _fields_ = [("device", C.c_int32), ("fac_per_cell", C.c_float), ("usr_per_cell", C.c_float),
-                ("skip_coincident", C.c_int32), ("reserved", C.c_int32 * 6)]
+                ("skip_coincident", C.c_int32), ("filter", C.c_int32), ("slice_min_k", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class Info(C.Structure):
@@ -105,11 +123,20 @@ def load(path: str = LIB_PATH):
     L.rknn_last_zone.argtypes = [vp, i32, vp, i32, C.POINTER(i32), C.POINTER(i32)]
     L.rknn_set_profiling.argtypes = [vp, i32]
     L.rknn_last_kernel_ms.argtypes = [vp, vp]
+    L.rknn_serve_opts_default.argtypes = [C.POINTER(ServeOpts)]
+    L.rknn_serve_opts_default.restype = None
+    L.rknn_serve_start.argtypes = [vp, C.POINTER(ServeOpts), C.POINTER(vp)]
+    L.rknn_serve_submit.argtypes = [vp, i32, i32, i32, C.POINTER(C.c_uint64)]
+    L.rknn_serve_wait.argtypes = [vp, C.c_uint64, i32, vp, i64, C.POINTER(i64), C.POINTER(C.c_double)]
+    L.rknn_serve_replay.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp]
+    L.rknn_serve_stats_get.argtypes = [vp, i32, C.POINTER(ServeStats)]
+    L.rknn_serve_stop.argtypes = [vp]
     L.rknn_last_error.restype = C.c_char_p
     L.rknn_version.restype = C.c_char_p
     for name in EXPORTS:
         fn = getattr(L, name)
-        if name not in ("rknn_last_error", "rknn_version", "rknn_index_opts_default"):
+        if name not in ("rknn_last_error", "rknn_version", "rknn_index_opts_default",
+                        "rknn_serve_opts_default"):
             fn.restype = C.c_int
     _lib = L
     return L
@@ -129,7 +156,7 @@ class Index:
 
     def __init__(self, fxy, uxy, fid=None, uid=None, device: int = 0,
                  fac_per_cell: float = 0.0, usr_per_cell: float = 0.0,
-                 skip_coincident: bool = True):
+                 skip_coincident: bool = True, filter: str = "auto", slice_min_k: int = 0):
         L = load()
         self.fxy = np.ascontiguousarray(fxy, dtype=np.float32).reshape(-1, 2)
         self.uxy = np.ascontiguousarray(uxy, dtype=np.float32).reshape(-1, 2)
@@ -146,6 +173,8 @@ class Index:
         if usr_per_cell:
             o.usr_per_cell = usr_per_cell
         o.skip_coincident = 1 if skip_coincident else 0
+        o.filter = {"auto": 0, "inf": 1, "slice": 2}[filter]
+        o.slice_min_k = int(slice_min_k)
         h = C.c_void_p()
         _check(L.rknn_index_create(_ptr(self.fxy), _ptr(self.fid), nf, _ptr(self.uxy),
                                    _ptr(self.uid), nu, C.byref(o), C.byref(h)))
@@ -262,6 +291,80 @@ class Index:
         st = Stats()
         _check(load().rknn_last_stats(self.h, C.byref(st)))
         return st.as_dict()
+
+
+class Server:
+    """Continuous-batching server over a resident index (rknn_serve_*).
+
+    submit() queues a request and returns a ticket; wait() returns its sorted
+    ids.  Requests from any number of threads are batched as they arrive and
+    run while earlier batches are still on the GPU."""
+
+    def __init__(self, index: "Index", slots: int = 3, max_batch: int = 4096,
+                 scratch_bytes: int = 256 << 20):
+        L = load()
+        o = ServeOpts()
+        L.rknn_serve_opts_default(C.byref(o))
+        o.slots, o.max_batch, o.scratch_bytes = int(slots), int(max_batch), int(scratch_bytes)
+        self.index = index
+        self.h = C.c_void_p()
+        _check(L.rknn_serve_start(index.h, C.byref(o), C.byref(self.h)))
+
+    def submit(self, q: int, k: int, mode="fp32") -> int:
+        t = C.c_uint64(0)
+        _check(load().rknn_serve_submit(self.h, int(q), int(k), _MODES[mode], C.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1, latency: bool = False):
+        L = load()
+        n = C.c_int64(0)
+        lat = C.c_double(0)
+        cap = 1024
+        while True:
+            out = np.empty(cap, np.int32)
+            rc = L.rknn_serve_wait(self.h, C.c_uint64(ticket), int(timeout_ms), out.ctypes.data, cap,
+                                   C.byref(n), C.byref(lat))
+            if rc == 5 and n.value > cap:            # RKNN_ERR_CAPACITY: request kept
+                cap = int(n.value)
+                continue
+            _check(rc)
+            ids = out[: n.value].copy()
+            return (ids, lat.value) if latency else ids
+
+    def replay(self, q, k, mode, arrival_s):
+        """Open-loop load: request i at arrival_s[i] s; returns (latency_ms, n_results)."""
+        q = np.ascontiguousarray(q, np.int32)
+        n = q.size
+        k = np.ascontiguousarray(np.broadcast_to(k, n), np.int32)
+        m = np.ascontiguousarray(np.broadcast_to(np.asarray([_MODES[x] for x in np.atleast_1d(mode)]), n), np.int32)
+        t = np.ascontiguousarray(arrival_s, np.float64)
+        lat = np.zeros(n, np.float64)
+        nr = np.zeros(n, np.int64)
+        _check(load().rknn_serve_replay(self.h, n, q.ctypes.data, k.ctypes.data, m.ctypes.data,
+                                        t.ctypes.data, lat.ctypes.data, nr.ctypes.data))
+        return lat, nr
+
+    def stats(self, reset: bool = False) -> dict:
+        st = ServeStats()
+        _check(load().rknn_serve_stats_get(self.h, 1 if reset else 0, C.byref(st)))
+        return st.as_dict()
+
+    def stop(self):
+        if self.h:
+            load().rknn_serve_stop(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.stop()
+
+    def __del__(self):
+        try:
+            self.stop()
+        except Exception:
+            pass
 
 
 def main(argv=None) -> int:
