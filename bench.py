@@ -5,17 +5,21 @@
 Workload (the reference's headline configuration): 100,000 facilities and
 1,000,000 users, float32 uniform in [0,1000]^2 (seeded synthetic data), k=10.
 One step = one batch of 1,000 random facility queries through the engine:
-zone kernel -> plan -> verification -> result offsets -> finalize (one CUDA
-graph).  Prints one JSON line (rank 0).
+candidate filter (angular slices, the default) -> plan -> verification ->
+result offsets -> finalize (one CUDA graph), FP32-filtered predicates with
+exact fallback; result sets are bit-exact.  Prints one JSON line (rank 0).
 
   value      queries/s with the facility/user index and the query batch
              resident in HBM, device time from CUDA events on the engine's
              stream, L2 flushed (256 MB write) before every timed step
   e2e        queries/s through rknn_query_batch (the C ABI with host
              buffers): query ids H2D, result offsets and ids D2H, per step
-  roofline   the zone kernel (the dominant one), timed live per launch with
-             CUDA events in profiling mode; roofline_verify: the same for the
-             verification kernel
+  roofline   the dominant kernel (of the filter and the verification),
+             timed live per launch with CUDA events in profiling mode;
+             roofline_other: the same for the other one
+  fp64_single_query  the plain form: one query per launch, FP64 predicates,
+             rknn-inf's influence zone (the drop-in); p50/p99 latency
+  serving    open-loop Poisson arrivals through the continuous batcher
   cpu_baseline  the C restatement of rknn-inf's query path (R-tree,
              influence-zone filter + verification) on the host's cores,
              over a bounded sample of the same workload
@@ -44,7 +48,7 @@ NF, NU, K, NQ = 100_000, 1_000_000, 10, 1000
 
 # DRAM bytes (read + write) per launch of each kernel on this workload, from
 # one ncu capture of the same 1000-query batch (profiles/zone_verify_config2_k10.md)
-TRAFFIC = {"zone_kernel_smem": 2189312, "verify_kernel": 4915200}
+TRAFFIC = {}
 
 
 def peaks():
@@ -175,18 +179,23 @@ def run_ours(args):
     torch.cuda.set_device(local)
     build.build()
     ds = dataset()
+    # the chosen form: batched, FP32-filtered predicates, default candidate
+    # filter (angular slices); the plain form: rknn-inf's influence zone
     idx = rknn.Index.of(ds, device=local)
+    idx_inf = rknn.Index.of(ds, device=local, filter="inf")
     stream = torch.cuda.Stream(device=local)
     idx.set_stream(stream.cuda_stream)
+    idx_inf.set_stream(stream.cuda_stream)
     rng = np.random.default_rng(17 + rank)
     nsteps = args.steps
     qsets = [rng.choice(ds.nf, size=NQ, replace=False).astype(np.int32)
              for _ in range(nsteps + args.warmup)]
     ks = np.full(NQ, K, np.int32)
 
-    # correctness of the timed configuration (host path, sizes the pools)
+    # correctness of the timed configuration (host path, sizes the pools):
+    # FP32 and FP64 predicates, both filters, give the same id sets
     res = idx.query_batch(qsets[0], ks, "fp32")
-    res64 = idx.query_batch(qsets[0][:100], ks[:100], "fp64")
+    res64 = idx_inf.query_batch(qsets[0][:100], ks[:100], "fp64")
     assert all(np.array_equal(a, b) for a, b in zip(res[:100], res64))
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -237,14 +246,14 @@ def run_ours(args):
         d2h = 4 * (NQ + 1) + 4 * sum(len(o) for o in out)
     e2e = NQ / statistics.mean(e2e_times) * ws
 
-    # ---- plain FP64 single-query form (one query per launch) --------------
+    # ---- plain FP64 single-query form (one query per launch, influence zone)
     single = qsets[0][:200]
     lat = []
     for q in single[:10]:
-        idx.query(int(q), K, "fp64")
+        idx_inf.query(int(q), K, "fp64")
     for q in single:
         t1 = time.perf_counter()
-        idx.query(int(q), K, "fp64")
+        idx_inf.query(int(q), K, "fp64")
         lat.append(1e3 * (time.perf_counter() - t1))
     fp64_single_qps = 1e3 / statistics.mean(lat)
     lat.sort()
@@ -260,6 +269,36 @@ def run_ours(args):
         e1.record(stream)
     torch.cuda.synchronize()
     fp64_batch_qps = NQ / (e0.elapsed_time(e1) / 1e3)
+    # the influence-zone filter batched in FP32 (same device timing)
+    def dev_qps(ix, mode, reps=3):
+        ms = []
+        for r in range(reps + 1):
+            with torch.cuda.stream(stream):
+                flush.fill_(3.0 + r)
+                e0.record(stream)
+                ix.query_batch_device(d_qs[r % len(d_qs)].data_ptr(), d_k.data_ptr(), NQ, K, mode)
+                e1.record(stream)
+            torch.cuda.synchronize()
+            if r:
+                ms.append(e0.elapsed_time(e1))
+        return NQ / (statistics.mean(ms) / 1e3)
+    inf_batch_qps = dev_qps(idx_inf, "fp32")
+
+    # ---- serving: open-loop Poisson arrivals through the continuous batcher
+    srv_rate, srv_n = 100_000.0, 20_000
+    srng = np.random.default_rng(23)
+    sq = srng.integers(0, ds.nf, srv_n).astype(np.int32)
+    arrival = np.cumsum(srng.exponential(1.0 / srv_rate, srv_n))
+    serving = {}
+    with rknn.Server(idx, slots=3, max_batch=2048) as srv:
+        for mode in ("fp32", "fp64"):
+            srv.replay(sq[:2000], K, mode, arrival[:2000])            # warm the slots
+            srv.stats(reset=True)
+            lat_s, _ = srv.replay(sq, K, mode, arrival)
+            st_s = srv.stats(reset=True)
+            serving[mode] = {"offered_qps": srv_rate, "throughput_qps": st_s["throughput_qps"],
+                             "p50_ms": st_s["p50_ms"], "p99_ms": st_s["p99_ms"],
+                             "mean_batch": st_s["mean_batch"], "max_inflight": st_s["max_inflight"]}
 
     # ---- rooflines (live, profiling mode: per-kernel CUDA events) ----------
     idx.set_profiling(True)
@@ -276,20 +315,17 @@ def run_ours(args):
     hbm_peak, kind = peaks()
     props = torch.cuda.get_device_properties(local)
     fp32_peak = props.multi_processor_count * 128 * 2 * 2.07e9 / 1e12     # nominal
-    # zone kernel, the dominant one: bytes it must move per launch = facility
-    # cells taken from the queue (16 B box + 8 B start pair), facilities taken
-    # (8 B), half-planes and bisector positions written (20 B), one 64 B query
-    # descriptor per query
+    # filter kernel (angular slices for this workload): bytes it must move
+    # per launch = facilities streamed (8 B), facility cell-range starts read
+    # (8 B per ring range), half-planes and their positions written (20 B),
+    # one 64 B query descriptor and its user segments (8 B per row) per query
     zms = kavg["zone"]
-    zbytes = 24 * st["zone_cells"] + 8 * st["zone_points"] + 20 * st["bisectors"] + 64 * NQ
+    zbytes = 8 * st["zone_points"] + 8 * st["zone_cells"] + 20 * st["bisectors"] + 64 * NQ
     zgbs = zbytes / (zms / 1e3) / 1e9
-    roof = {"bound": "hbm", "achieved": zgbs, "peak": hbm_peak, "unit": "GB/s",
-            "frac": zgbs / hbm_peak, "peak_kind": kind, "kernel": "zone_kernel_smem",
-            "launch_ms": zms, "alg_bytes": zbytes,
-            "traffic": TRAFFIC.get("zone_kernel_smem"),
-            "note": "latency-bound: one warp per query runs the sequential best-first search; "
-                    "neither HBM nor FP32 issue bounds it",
-            "kernel_ms": kavg, "share": {n: v / sum(kavg.values()) for n, v in kavg.items()}}
+    froof = {"bound": "hbm", "achieved": zgbs, "peak": hbm_peak, "unit": "GB/s",
+             "frac": zgbs / hbm_peak, "peak_kind": kind, "kernel": "slice_kernel", "launch_ms": zms,
+             "alg_bytes": zbytes, "traffic": TRAFFIC.get("slice_kernel"),
+             "note": "latency-bound: one warp per query streams facilities ring by ring"}
     # verification kernel: users read (8 B), half-planes staged (16 B each
     # per query), result ids written (4 B), facilities read by the exact
     # recount (8 B); FLOP = 4 per (user, half-plane) evaluation executed
@@ -298,12 +334,14 @@ def run_ours(args):
     vflops = 4 * st["plane_evals"]
     vgbs = vbytes / (vms / 1e3) / 1e9
     vtfs = vflops / (vms / 1e3) / 1e12
-    vroof = {"bound": "hbm" if vgbs / hbm_peak >= vtfs / fp32_peak else "fp32",
-             "achieved": vgbs, "peak": hbm_peak, "unit": "GB/s", "frac": vgbs / hbm_peak,
+    vroof = {"bound": "hbm", "achieved": vgbs, "peak": hbm_peak, "unit": "GB/s", "frac": vgbs / hbm_peak,
              "peak_kind": kind, "kernel": "verify_kernel", "launch_ms": vms,
              "alg_bytes": vbytes, "alg_flop": vflops, "traffic": TRAFFIC.get("verify_kernel"),
              "fp32": {"achieved_tflops": vtfs, "frac": vtfs / fp32_peak, "peak": fp32_peak,
                       "peak_kind": "nominal (SMs x 128 FMA x 2.07 GHz)"}}
+    # the dominant kernel's roofline leads; the other rides beside it
+    roof, other = (froof, vroof) if zms >= vms else (vroof, froof)
+    roof = dict(roof, kernel_ms=kavg, share={n: v / sum(kavg.values()) for n, v in kavg.items()})
 
     # ---- CPU baseline (rank 0, N=1 only) ---------------------------------
     cpu = None
@@ -322,15 +360,19 @@ def run_ours(args):
         "data": "synthetic (seeded uniform float32 in [0,1000]^2)",
         "config": {"workload": "uniform 100k facilities / 1M users, k=10, 1000 queries per step",
                    "nf": NF, "nu": NU, "k": K, "queries_per_step": NQ, "mode": "fp32 batched",
+                   "filter": "angular slices (rknn-slice rule, 32 slices); plain form: influence zone",
                    "l2": "256 MB flush before each timed step", "parallelism": f"replicas x{ws}"},
         "wall_s": wall,
         "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": 5 * nsteps,
-        "fp64_single_query": {"qps": fp64_single_qps, "p50_ms": p50, "p99_ms": p99},
+        "fp64_single_query": {"qps": fp64_single_qps, "p50_ms": p50, "p99_ms": p99,
+                              "filter": "influence zone (rknn-inf rules)"},
         "fp64_batched_qps": fp64_batch_qps,
+        "inf_zone_fp32_batched_qps": inf_batch_qps,
+        "serving": dict(serving, workload=f"{srv_n} Poisson requests at {srv_rate:.0f}/s, k={K}"),
         "speedup_fp32_batched_vs_fp64_single": value / ws / fp64_single_qps,
         "roofline": roof,
-        "roofline_verify": vroof,
+        "roofline_other": other,
         "stats": {k2: st[k2] for k2 in ("bisectors", "zone_vertices_max", "zone_candidates", "zone_fp64",
                                         "zone_points", "zone_cells",
                                         "candidates", "plane_evals", "survivors", "fac_checks",

@@ -41,6 +41,8 @@ double wall()
                  "         -q <index>                  query facility index (default 0)\n"
                  "         --algorithm | -al <name>    accepted and ignored\n"
                  "         --mode fp64|fp32            predicate filter precision (default fp64)\n"
+                 "         --filter inf|slice|auto     candidate filter (default inf: rknn-inf's\n"
+                 "                                     influence zone; slice: angular slices)\n"
                  "         --queries i,j,...           several query indices in one batch\n"
                  "         --log <dir>                 result directory (default log)\n"
                  "         --no-log                    do not write result files\n"
@@ -105,7 +107,7 @@ bool parse_points(Parser& ps, long long n, std::vector<float>& xy, std::vector<i
 
 int main(int argc, char** argv)
 {
-    std::string infile, logdir = "log", mode_s = "fp64";
+    std::string infile, logdir = "log", mode_s = "fp64", filter_s = "inf";
     long long k = 4, q = 0;
     std::vector<long long> queries;
     bool write_log = true;
@@ -131,6 +133,7 @@ int main(int argc, char** argv)
                 return 1;
             }
         } else if (a == "--mode") mode_s = val();
+        else if (a == "--filter") filter_s = val();
         else if (a == "--queries") {
             std::string s = val();
             size_t b = 0;
@@ -152,6 +155,13 @@ int main(int argc, char** argv)
         return 1;
     }
     const int mode = mode_s == "fp32" ? RKNN_MODE_FP32 : RKNN_MODE_FP64;
+    if (filter_s != "inf" && filter_s != "slice" && filter_s != "auto") {
+        std::fprintf(stderr, "Unknown filter '%s'\n", filter_s.c_str());
+        return 1;
+    }
+    rknn_index_opts opts;
+    rknn_index_opts_default(&opts);
+    opts.filter = filter_s == "inf" ? RKNN_FILTER_INF : filter_s == "slice" ? RKNN_FILTER_SLICE : RKNN_FILTER_AUTO;
     if (queries.empty()) queries.push_back(q);
 
     std::printf("Loading data...\n");
@@ -182,7 +192,7 @@ int main(int argc, char** argv)
     std::printf("building grid index...\n");
     double t0 = wall();
     rknn_index* ix = nullptr;
-    if (rknn_index_create(fxy.data(), fid.data(), nf, uxy.data(), uid.data(), nu, nullptr, &ix) != RKNN_OK) {
+    if (rknn_index_create(fxy.data(), fid.data(), nf, uxy.data(), uid.data(), nu, &opts, &ix) != RKNN_OK) {
         std::fprintf(stderr, "index build failed: %s\n", rknn_last_error());
         return 1;
     }

@@ -380,6 +380,7 @@ def main(argv=None) -> int:
     p.add_argument("-q", type=int, default=0)
     p.add_argument("-al", "--algorithm", default="all")
     p.add_argument("--mode", default="fp64", choices=["fp64", "fp32"])
+    p.add_argument("--filter", default="inf", choices=["inf", "slice", "auto"])
     p.add_argument("--log", default="log")
     a = p.parse_args(argv)
     if a.k <= 0:
@@ -389,7 +390,7 @@ def main(argv=None) -> int:
     ds = datagen.read_text(a.infile)
     print(f"Loaded {ds.nf} facilities and {ds.nu} users.")
     t0 = time.time()
-    with Index.of(ds) as idx:
+    with Index.of(ds, filter=a.filter) as idx:
         print(f"Grid index is built in {time.time() - t0:g}[s].\n")
         t0 = time.time()
         ids, st = idx.query(a.q, a.k, a.mode, stats=True)

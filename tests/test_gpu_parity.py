@@ -112,7 +112,7 @@ def test_zone_bisectors_match_port(engine):
     in the same order as the CPU restatement does."""
     for nf, nu, k in ((1000, 10000, 5), (20000, 200000, 10), (20000, 200000, 3)):
         ds = datagen.uniform(nf, nu, seed=31 + k, nq=40, k=k)
-        idx = engine.Index.of(ds)
+        idx = engine.Index.of(ds, filter="inf")
         info = idx.info()
         port = O.InfPort(ds.fxy, ds.uxy, grid=(info["fgrid_x0"], info["fgrid_y0"], info["fgrid_inv"],
                                                info["fgrid_gx"], info["fgrid_gy"]))
