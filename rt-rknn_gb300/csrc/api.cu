@@ -88,6 +88,8 @@ struct Workspace {
     VStats* d_vstats = nullptr;
     int *d_pool = nullptr, *d_out = nullptr;
     long long pool_cap = 0;
+    int2* d_surv = nullptr;        // survivors of the half-plane filter, for recount_kernel
+    long long surv_cap = 0;
     char* d_zscratch = nullptr;
     size_t zscratch_bytes = 0;
     int *h_q = nullptr, *h_k = nullptr, *h_order = nullptr, *h_off = nullptr;
@@ -151,7 +153,7 @@ void free_ws(Workspace& w)
     cudaFree(w.d_qd); cudaFree(w.d_planes); cudaFree(w.d_bispos); cudaFree(w.d_segs); cudaFree(w.d_zst);
     cudaFree(w.d_cand_off); cudaFree(w.d_chunk_off); cudaFree(w.d_res_count); cudaFree(w.d_out_off);
     cudaFree(w.d_counters); cudaFree(w.d_vstats);
-    cudaFree(w.d_pool); cudaFree(w.d_out); cudaFree(w.d_zscratch);
+    cudaFree(w.d_pool); cudaFree(w.d_out); cudaFree(w.d_zscratch); cudaFree(w.d_surv);
     cudaFreeHost(w.h_q); cudaFreeHost(w.h_k); cudaFreeHost(w.h_order); cudaFreeHost(w.h_off);
     cudaFreeHost(w.h_ids);
     for (int i = 0; i < NAUX; ++i) {
@@ -214,9 +216,11 @@ rknn_status ensure_ws(Workspace& w, int nq, const ZoneCaps& caps, long long pool
         int sc = std::max(seg_cap, w.seg_cap);
         long long pool = w.pool_cap;
         const int rcap = w.rcap;
+        const long long scap = w.surv_cap;
         free_ws(w);
         w.pool_cap = pool;
         w.rcap = rcap;
+        w.surv_cap = scap;
         w.nq_cap = nqc; w.lc = lc; w.seg_cap = sc;
         CK(dalloc(w.d_q, nqc)); CK(dalloc(w.d_k, nqc)); CK(dalloc(w.d_order, nqc));
         CK(dalloc(w.d_qd, nqc));
@@ -239,6 +243,11 @@ rknn_status ensure_ws(Workspace& w, int nq, const ZoneCaps& caps, long long pool
         CK(cudaMallocHost(&w.h_order, sizeof(int) * nqc));
         CK(cudaMallocHost(&w.h_off, sizeof(int) * (nqc + 1)));
         w.pool_cap = 0;
+    }
+    if (!w.d_surv) {
+        const long long cap = std::max<long long>(w.surv_cap, 1 << 22);
+        CK(dalloc(w.d_surv, (size_t)cap));
+        w.surv_cap = cap;
     }
     if (pool_need > w.pool_cap) {
         drop_graphs(w);
@@ -428,7 +437,10 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     va.vstats = w.d_vstats; va.mode = b.mode;
     va.nu = (int)ix->nu; va.nf = (int)ix->nf; va.ncf = ix->gf.gx * ix->gf.gy;
     va.pool_cap = w.pool_cap; va.fault = w.d_counters + 10; va.dropped = w.d_counters + 2;
+    va.surv = w.d_surv; va.surv_cap = (int)std::min<long long>(w.surv_cap, INT32_MAX); va.surv_count = w.d_counters + 3;
     verify_kernel<<<b.vgrid, VERIFY_WARPS * 32, b.vsmem, st>>>(va);
+    CK(cudaGetLastError());
+    recount_kernel<<<ix->num_sms * 8, 256, 0, st>>>(va);
     CK(cudaGetLastError());
     mark(3);
 
@@ -452,6 +464,7 @@ rknn_status launch(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = true
     GraphKey key = b.key;
     key.push_back(w.pool_cap);
     key.push_back(w.rcap);
+    key.push_back(w.surv_cap);
     auto it = w.graphs.find(key);
     if (it == w.graphs.end()) {
         cudaGraph_t g;
@@ -519,14 +532,25 @@ rknn_status run_sync(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = tr
         if (s != RKNN_OK) return s;
         CK(cudaEventRecord(c.ev1, c.st));
         long long region_total = 0;
-        int dropped = 0;
+        int flags[2] = {0, 0};      // region exceeded, survivors listed
         CK(cudaMemcpyAsync(&region_total, w.d_cand_off + nq, sizeof(long long), cudaMemcpyDeviceToHost, c.st));
-        CK(cudaMemcpyAsync(&dropped, w.d_counters + 2, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+        CK(cudaMemcpyAsync(flags, w.d_counters + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.st));
+        const int& dropped = flags[0];
         CK(cudaMemcpyAsync(w.h_off, w.d_out_off, sizeof(int) * (nq + 1), cudaMemcpyDeviceToHost, c.st));
         CK(cudaStreamSynchronize(c.st));
         float ms = 0;
         cudaEventElapsedTime(&ms, c.ev0, c.ev1);
         *c.device_ms = ms;
+        if ((unsigned)flags[1] > (unsigned long long)w.surv_cap) {
+            // survivors overflowed the list (they were recounted in-warp):
+            // give the next batch room for all of them
+            drop_graphs(w);
+            cudaFree(w.d_surv);
+            w.d_surv = nullptr;
+            w.surv_cap = (long long)(unsigned)flags[1] + (long long)(unsigned)flags[1] / 4;
+            s = ensure_ws(w, nq, caps, w.pool_cap);
+            if (s != RKNN_OK) return s;
+        }
         if (region_total > w.pool_cap) {
             // some regions did not fit the pool (those slots were skipped)
             s = ensure_ws(w, nq, caps, region_total + region_total / 4);
@@ -1028,6 +1052,7 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     va.vstats = L.vstats; va.mode = mode;
     va.nu = (int)ix->nu; va.nf = (int)ix->nf; va.ncf = ix->gf.gx * ix->gf.gy;
     va.pool_cap = L.pool_cap; va.fault = L.counters + 10; va.dropped = L.counters + 2;
+    va.surv = nullptr; va.surv_cap = 0; va.surv_count = L.counters + 3;
     const size_t vsmem = (size_t)VERIFY_WARPS * caps.lc * (mode == MODE_FP32 ? 16 : 32);
     verify_kernel<<<2 * ix->num_sms, VERIFY_WARPS * 32, vsmem, st>>>(va);
     CK(cudaGetLastError());

@@ -38,6 +38,9 @@ struct QDesc {
     double k2f64, kf264;
     int ncand;         // users in all segments
     int flags;         // RKNN_QF_* bits
+    float rho;         // every facility nearer to q than rho is one of the half-planes
+                       // (0 when unknown): a user with 2|u-q| <= rho is decided by them
+    int pad;
 };
 
 // QDesc.flags

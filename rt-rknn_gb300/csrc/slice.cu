@@ -69,7 +69,11 @@ __device__ __forceinline__ float upper_arc(float vx, float vy, float e1x, float 
     const float dmin = fminf(d1, d2) - 8.0f * kU32 * l1 - 1e-37f;
     if (!(dmin > 0.0f)) return INFINITY;
     const float num = fmaf(vx, vx, vy * vy) * (1.0f + 8.0f * kU32);
-    return __fdiv_ru(num, 2.0f * dmin) * (1.0f + 4.0f * kU32);
+    const float den = 2.0f * dmin;
+    // __fdividef is within 2 ulp for denominators in [2^-126, 2^126]: a
+    // 2^-20 relative inflation covers it; outside that range divide exactly
+    if (den > 0x1p-126f && den < 0x1p126f) return __fdividef(num, den) * (1.0f + 0x1p-20f);
+    return __fdiv_ru(num, den) * (1.0f + 4.0f * kU32);
 }
 
 // Distance from q along unit direction (ex, ey) to the box's boundary,
@@ -195,6 +199,7 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
         // ---- stream facilities ring by ring -------------------------------
         int n = 0;              // this slice's heap size
         int nL = 0;             // half-planes kept (warp-uniform)
+        int rho_ring = -1;      // first ring with a streamed facility left out of the half-planes
         const int qcx = cell_coord(qf.x, A.gf.x0, A.gf.inv, A.gf.gx);
         const int qcy = cell_coord(qf.y, A.gf.y0, A.gf.inv, A.gf.gy);
         const int rmaxf = max(max(qcx, A.gf.gx - 1 - qcx), max(qcy, A.gf.gy - 1 - qcy));
@@ -272,6 +277,7 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
                         const int at = nL + __popc(pm & ((1u << lane) - 1));
                         if (at < LC) lpos[SX(at, LC, 315)] = fidx;
                     }
+                    if (nL + __popc(pm) > LC && rho_ring < 0) rho_ring = ring;
                     nL = min(LC, nL + __popc(pm));
                     zs.pts += __popc(pm);
                     // every lane offers every streamed facility to its slice
@@ -288,6 +294,17 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
             zs.cells += nrange;
         }
         zs.rings = ring;
+        // rho: every facility outside the half-planes lies in ring rho_ring or
+        // beyond, at least (rho_ring - 1) cs from q (less the rounding slack)
+        float rho;
+        {
+            if (rho_ring < 0) rho_ring = ring;          // every streamed facility is a half-plane
+            if (rho_ring > rmaxf) rho = INFINITY;
+            else {
+                const double Lr = (double)(rho_ring - 1) * (double)A.gf.cs - slack;
+                rho = Lr > 0.0 ? __double2float_rd(Lr) : 0.0f;
+            }
+        }
         __syncwarp();
         // R(P): k-th smallest arc, rounded up for the user test, and clipped
         // to the box (no user lies farther)
@@ -459,6 +476,8 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
             d.kf264 = kf264;
             d.ncand = ncand;
             d.flags = qflags;
+            d.rho = rho;
+            d.pad = 0;
             *qd = d;
             A.zst[s] = zs;
         }

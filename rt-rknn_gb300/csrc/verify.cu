@@ -14,14 +14,18 @@
 // four per lane); the warp leaves the half-plane loop as soon as every lane
 // has k certified violations for all its users (__all_sync).
 //
-// Stage 2 (exact count).  Users that survive stage 1 are counted exactly
-// over the facility grid: the whole warp scans, row by row, the facility
-// cells covering the disc of radius d(u,q) around u (one contiguous range
-// of the cell-sorted facility array per row, coalesced), counting
-// d2(u,f) < d2(u,q) with __ballot_sync/__popc and stopping at k.  Each
-// comparison is decided in float (or double) with its error bound, and the
-// undecided ones by the exact expansion predicate.  Accepted users are
-// appended with one warp-aggregated atomic per work item.
+// Stage 2 (exact count).  Users that survive stage 1 go to a survivor list,
+// and recount_kernel counts each one exactly, one thread per survivor (many
+// independent chains of facility loads in flight): the facility cells
+// covering the disc of radius d(u,q) around u, row by row (one contiguous
+// range of the cell-sorted facility array per row, trimmed to the disc's
+// chord), counting d2(u,f) < d2(u,q) and stopping at k.  Each comparison is
+// decided in float (or double) with its error bound, and the undecided ones
+// by the exact expansion predicate.  Accepted users are appended with
+// warp-aggregated atomics (lanes grouped by query with __match_any_sync).
+// When the survivor list is full, the warp recounts its own survivors, the
+// whole warp scanning one survivor's rows at a time with
+// __ballot_sync/__popc.
 #include "verify.cuh"
 #include <climits>
 
@@ -88,9 +92,12 @@ __device__ __forceinline__ int exact_count(float ux, float uy, const QDesc& d, c
     return cnt;
 }
 
+// Stage 1 over the first nb staged half-planes: cnt = certified
+// violations (the loop leaves once every lane's users reached k), und =
+// half-planes the bound could not decide.
 template <typename T>
 __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char* sp, const int* pos,
-                                             const float2* u, const bool* valid, int* cnt,
+                                             const float2* u, const bool* valid, int* cnt, int* und,
                                              unsigned long long& evals)
 {
     T x[VERIFY_UPT], y[VERIFY_UPT], bu[VERIFY_UPT];
@@ -98,6 +105,7 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
 #pragma unroll
     for (int t = 0; t < VERIFY_UPT; ++t) {
         cnt[t] = valid[t] ? 0 : INT_MAX / 2;
+        und[t] = 0;
         nvalid += valid[t];
         if (sizeof(T) == 4) {
             float xx = u[t].x - d.qx, yy = u[t].y - d.qy;
@@ -124,6 +132,7 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
         for (int t = 0; t < VERIFY_UPT; ++t) {
             T mv = fma(a, x[t], fma(b, y[t], c));
             cnt[t] += (mv < -bu[t]);
+            und[t] += (mv <= bu[t]) & (mv >= -bu[t]);
         }
         if ((m & 7) == 7) {
             bool done = true;
@@ -208,18 +217,60 @@ verify_kernel(VerifyArgs A)
             }
             s_cand += valid[t];
         }
-        int cnt[VERIFY_UPT];
+        int cnt[VERIFY_UPT], und[VERIFY_UPT];
         const int nbs = min(d.nb, A.stage_cap);
-        if (A.mode == MODE_FP32) filter_users<float>(d, nbs, sp, pos, u, valid, cnt, s_evals);
-        else filter_users<double>(d, nbs, sp, pos, u, valid, cnt, s_evals);
+        if (A.mode == MODE_FP32) filter_users<float>(d, nbs, sp, pos, u, valid, cnt, und, s_evals);
+        else filter_users<double>(d, nbs, sp, pos, u, valid, cnt, und, s_evals);
+        // A user within rho/2 of q is decided by the half-planes alone: every
+        // facility strictly nearer to it than q lies within 2|u-q| <= rho of
+        // q, so it is a half-plane.  With no undecided half-plane the
+        // certified count is the exact count.  (All half-planes must be
+        // staged for this.)
+        bool direct[VERIFY_UPT];
+        {
+            const float rho2 = (nbs == d.nb) ? d.rho * d.rho * (1.0f - 1e-5f) : 0.0f;
+#pragma unroll
+            for (int t = 0; t < VERIFY_UPT; ++t) {
+                const float xx = u[t].x - d.qx, yy = u[t].y - d.qy;
+                const float du2 = 4.0f * fmaf(xx, xx, yy * yy) * (1.0f + 1e-5f);
+                direct[t] = valid[t] && cnt[t] < d.k && und[t] == 0 && du2 <= rho2;
+            }
+        }
 
-        // stage 2: exact count for the survivors, one user at a time per warp
+        // stage 2: survivors go to the list for recount_kernel; when it is
+        // full, the warp counts them itself, one user at a time
+        unsigned sm[VERIFY_UPT];
+        int ns = 0;
+#pragma unroll
+        for (int t = 0; t < VERIFY_UPT; ++t) {
+            sm[t] = __ballot_sync(FULL, valid[t] && cnt[t] < d.k && !direct[t]);
+            ns += __popc(sm[t]);
+        }
+        s_surv += (lane == 0) ? ns : 0;
+        bool listed = false;
+        if (ns && A.surv_cap > 0) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(A.surv_count, ns);
+            base = __shfl_sync(FULL, base, 0);
+            if ((long long)base + ns <= A.surv_cap) {
+                int o = 0;
+#pragma unroll
+                for (int t = 0; t < VERIFY_UPT; ++t) {
+                    if (sm[t] & (1u << lane))
+                        A.surv[VX((long long)base + o + __popc(sm[t] & ((1u << lane) - 1)), A.surv_cap, 214)] = make_int2(s, pos[t]);
+                    o += __popc(sm[t]);
+                }
+                listed = true;
+            } else {
+                // the reservation straddles the end: mark its listed part empty
+                for (int i = base + lane; i < A.surv_cap && i < base + ns; i += 32) A.surv[i] = make_int2(-1, 0);
+            }
+        }
         bool acc[VERIFY_UPT];
 #pragma unroll
         for (int t = 0; t < VERIFY_UPT; ++t) {
-            acc[t] = false;
-            unsigned m = __ballot_sync(FULL, valid[t] && cnt[t] < d.k);
-            s_surv += (lane == 0) ? __popc(m) : 0;
+            acc[t] = direct[t];
+            unsigned m = listed ? 0u : sm[t];
             while (m) {
                 int l = __ffs(m) - 1;
                 m &= m - 1;
@@ -262,6 +313,108 @@ verify_kernel(VerifyArgs A)
         atomicAdd(&A.vstats->cand, s_cand);
         atomicAdd(&A.vstats->plane_evals, s_evals);
         atomicAdd(&A.vstats->survivors, s_surv);
+        atomicAdd(&A.vstats->fac_checks, s_fac);
+        atomicAdd(&A.vstats->rechecks, s_rech);
+        atomicAdd(&A.vstats->results, s_res);
+    }
+}
+
+// One warp per listed survivor.  Lane r computes the facility range of
+// disc row r (trimmed to the chord), a warp prefix sum flattens the rows,
+// and each round tests 32 facilities (__ballot_sync/__popc), stopping at k:
+// the survivor costs a couple of load latencies, not one per facility.
+__device__ __forceinline__ int warp_exact_count(float ux, float uy, const QDesc& d, const VerifyArgs& A,
+                                                unsigned long long& fac, unsigned long long& rech)
+{
+    const int lane = threadIdx.x & 31;
+    const float qx = d.qx, qy = d.qy;
+    const bool f32 = A.mode == MODE_FP32;
+    float Dq32 = 0.0f;
+    double Dq64 = 0.0;
+    float r;
+    const float slack = 4.0f * kU32 * (fabsf(ux) + fabsf(uy) + fabsf(qx) + fabsf(qy)) + 1e-30f;
+    if (f32) {
+        const float dx = ux - qx, dy = uy - qy;
+        Dq32 = fmaf(dx, dx, dy * dy);
+        r = sqrtf(Dq32) * (1.0f + 4e-6f) + slack;
+    } else {
+        const double dx = (double)ux - (double)qx, dy = (double)uy - (double)qy;
+        Dq64 = fma(dx, dx, dy * dy);
+        r = (float)sqrt(Dq64) * (1.0f + 4e-6f) + slack;
+    }
+    const Grid& g = A.gf;
+    const float ym = 1e-5f * g.cs + 8.0f * kU32 * (fabsf(g.y0) + fabsf(uy) + g.cs * (float)g.gy);
+    const int cy0 = cell_coord(uy - r, g.y0, g.inv, g.gy), cy1 = cell_coord(uy + r, g.y0, g.inv, g.gy);
+    int cnt = 0;
+    for (int rb = cy0; rb <= cy1; rb += 32) {
+        const int cy = rb + lane;
+        int f0 = 0, len = 0;
+        if (cy <= cy1) {
+            const float ylo = g.y0 + (float)cy * g.cs - ym, yhi = g.y0 + (float)(cy + 1) * g.cs + ym;
+            const float dyn = fmaxf(fmaxf(ylo - uy, uy - yhi), 0.0f) * (1.0f - 1e-6f);
+            const float w = sqrtf(fmaxf(fmaf(r, r, -dyn * dyn), 0.0f)) * (1.0f + 1e-6f) + slack;
+            const int cx0 = cell_coord(ux - w, g.x0, g.inv, g.gx), cx1 = cell_coord(ux + w, g.x0, g.inv, g.gx);
+            f0 = A.fstart[VX(cy * g.gx + cx0, A.ncf + 1, 211)];
+            len = A.fstart[VX(cy * g.gx + cx1 + 1, A.ncf + 1, 212)] - f0;
+        }
+        int incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(FULL, incl, 31);
+        for (int t0 = 0; t0 < total; t0 += 32) {
+            const int j = t0 + lane;
+            int lo = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const int probe = __shfl_sync(FULL, incl, lo + step - 1);
+                if (probe <= j) lo += step;
+            }
+            const int rs = __shfl_sync(FULL, f0, lo & 31);
+            const int ri = __shfl_sync(FULL, incl, lo & 31);
+            const int rl = __shfl_sync(FULL, len, lo & 31);
+            const int i = rs + (j - (ri - rl));
+            bool c = false;
+            if (j < total && i != d.qpos) {
+                const float2 f = A.fxy[VX(i, A.nf, 213)];
+                c = f32 ? closer_f32(ux, uy, f.x, f.y, qx, qy, Dq32, &rech)
+                        : closer_f64(ux, uy, f.x, f.y, qx, qy, Dq64, &rech);
+            }
+            cnt += __popc(__ballot_sync(FULL, c));
+            fac += (unsigned long long)min(32, total - t0);
+            if (cnt >= d.k) return cnt;
+        }
+    }
+    return cnt;
+}
+
+// Exact recount of the listed survivors, one warp each; accepted users are
+// appended with one atomic per survivor.
+__global__ void __launch_bounds__(256) recount_kernel(VerifyArgs A)
+{
+    const int lane = threadIdx.x & 31;
+    const int n = min(*A.surv_count, A.surv_cap);
+    unsigned long long s_fac = 0, s_rech = 0, s_res = 0;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nw) {
+        const int2 e = A.surv[VX(i, A.surv_cap, 215)];
+        if (e.x < 0) continue;
+        const int slot = e.x, pos = e.y;
+        const QDesc d = A.qd[slot];
+        const float2 u = A.uxy[VX(pos, A.nu, 216)];
+        const int c = warp_exact_count(u.x, u.y, d, A, s_fac, s_rech);
+        if (c < d.k && lane == 0) {
+            const int at = atomicAdd(A.res_count + slot, 1);
+            const long long r0 = A.cand_off[slot], region = A.cand_off[slot + 1] - r0;
+            if (at < region) A.res_pool[VX(r0 + at, A.pool_cap, 217)] = A.uid[VX(pos, A.nu, 218)];
+            else atomicOr(A.dropped, 1);
+            s_res += 1;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) s_rech += __shfl_xor_sync(FULL, s_rech, o);
+    if (lane == 0 && A.vstats && (s_fac | s_res | s_rech)) {
         atomicAdd(&A.vstats->fac_checks, s_fac);
         atomicAdd(&A.vstats->rechecks, s_rech);
         atomicAdd(&A.vstats->results, s_res);

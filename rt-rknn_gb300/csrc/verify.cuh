@@ -36,10 +36,16 @@ struct VerifyArgs {
     int nu, nf, ncf;         // array sizes (bounds-checked builds)
     long long pool_cap;
     int* dropped;            // set when a slot had more results than its region
+    int2* surv;              // survivors of the half-plane filter: (slot, user position)
+    int surv_cap;            // 0: no list (the verification kernel recounts in-warp)
+    int* surv_count;
     int* fault;              // checked builds: {flag, array id, index, size, line}
 };
 
 __global__ void verify_kernel(VerifyArgs a);
+
+// exact recount of the listed survivors, one thread each
+__global__ void recount_kernel(VerifyArgs a);
 
 // single block: result regions (min(candidates, rcap) ids, 64-bit offsets)
 // and work-item offsets from QDesc.ncand; flags slots whose region does not

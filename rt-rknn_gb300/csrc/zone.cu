@@ -1258,6 +1258,8 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             d.kf264 = kf264;
             d.ncand = ncand;
             d.flags = qflags;
+            d.rho = 0.0f;           // the zone's bisectors need not cover any disc
+            d.pad = 0;
             *qd = d;
             A.zst[s] = zs;
         }
