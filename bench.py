@@ -47,8 +47,9 @@ METRIC = "RkNN queries/s (1M users,100k fac,k=10) FP32-filtered vs FP64; p99 ms"
 NF, NU, K, NQ = 100_000, 1_000_000, 10, 1000
 
 # DRAM bytes (read + write) per launch of each kernel on this workload, from
-# one ncu capture of the same 1000-query batch (profiles/zone_verify_config2_k10.md)
-TRAFFIC = {}
+# one ncu capture of the same 1000-query batch
+# (profiles/slice_verify_recount_config2_k10.md)
+TRAFFIC = {"slice_kernel": 1528832, "verify_kernel": 4856064 + 1889280}
 
 
 def peaks():
@@ -237,13 +238,14 @@ def run_ours(args):
 
     # ---- end to end through the C ABI with host buffers ------------------
     e2e_times, h2d, d2h = [], 0, 0
+    idx.query_batch_flat(qsets[0], ks, "fp32")                      # sizes the output buffers
     for i in range(nsteps):
         q = qsets[args.warmup + i]
         t1 = time.perf_counter()
-        out = idx.query_batch(q, ks, "fp32")
+        ids, offs = idx.query_batch_flat(q, ks, "fp32")
         e2e_times.append(time.perf_counter() - t1)
         h2d = q.nbytes + ks.nbytes
-        d2h = 4 * (NQ + 1) + 4 * sum(len(o) for o in out)
+        d2h = 4 * (NQ + 1) + 4 * int(ids.shape[0])
     e2e = NQ / statistics.mean(e2e_times) * ws
 
     # ---- plain FP64 single-query form (one query per launch, influence zone)
@@ -335,7 +337,8 @@ def run_ours(args):
     vgbs = vbytes / (vms / 1e3) / 1e9
     vtfs = vflops / (vms / 1e3) / 1e12
     vroof = {"bound": "hbm", "achieved": vgbs, "peak": hbm_peak, "unit": "GB/s", "frac": vgbs / hbm_peak,
-             "peak_kind": kind, "kernel": "verify_kernel", "launch_ms": vms,
+             "peak_kind": kind, "kernel": "verify_kernel", "kernels": "verify_kernel + recount_kernel",
+             "launch_ms": vms,
              "alg_bytes": vbytes, "alg_flop": vflops, "traffic": TRAFFIC.get("verify_kernel"),
              "fp32": {"achieved_tflops": vtfs, "frac": vtfs / fp32_peak, "peak": fp32_peak,
                       "peak_kind": "nominal (SMs x 128 FMA x 2.07 GHz)"}}

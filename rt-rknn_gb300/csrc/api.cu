@@ -847,8 +847,27 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
         return fail(RKNN_ERR_CAPACITY, "output buffer holds " + std::to_string(cap) + " ids, " +
                                            std::to_string(total) + " needed");
     if (total > 0) {
-        CK(cudaMemcpyAsync(out_ids, w.d_out, sizeof(int) * total, cudaMemcpyDeviceToHost, ix->stream));
-        CK(cudaStreamSynchronize(ix->stream));
+        // page-locked caller buffers take the copy directly; pageable ones
+        // through the workspace's page-locked staging buffer
+        cudaPointerAttributes pa;
+        const bool locked = cudaPointerGetAttributes(&pa, out_ids) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+        if (locked) {
+            CK(cudaMemcpyAsync(out_ids, w.d_out, sizeof(int) * total, cudaMemcpyDeviceToHost, ix->stream));
+            CK(cudaStreamSynchronize(ix->stream));
+        } else {
+            if (total > w.h_ids_cap) {
+                cudaFreeHost(w.h_ids);
+                w.h_ids = nullptr;
+                w.h_ids_cap = 0;
+                const long long hc = std::max<long long>(total + total / 4, 1 << 16);
+                CK(cudaMallocHost(&w.h_ids, sizeof(int) * hc));
+                w.h_ids_cap = hc;
+            }
+            CK(cudaMemcpyAsync(w.h_ids, w.d_out, sizeof(int) * total, cudaMemcpyDeviceToHost, ix->stream));
+            CK(cudaStreamSynchronize(ix->stream));
+            std::memcpy(out_ids, w.h_ids, sizeof(int) * total);
+        }
     }
     return RKNN_OK;
 }

@@ -247,6 +247,29 @@ class Index:
         res = [out[off[i]:off[i + 1]].copy() for i in range(nq)]
         return (res, st.as_dict()) if stats else res
 
+    def query_batch_flat(self, qs, ks, mode="fp32"):
+        """(ids, offsets): the batch's results as one id array, query i's
+        sorted ids at ids[offsets[i]:offsets[i+1]] (no per-query copies; the
+        output buffers are reused between calls)."""
+        L = load()
+        qs = np.ascontiguousarray(qs, dtype=np.int32)
+        ks = np.ascontiguousarray(np.broadcast_to(np.asarray(ks, np.int32), qs.shape), dtype=np.int32)
+        nq = qs.shape[0]
+        off = getattr(self, "_flat_off", None)
+        if off is None or off.shape[0] < nq + 1:
+            off = self._flat_off = np.zeros(nq + 1, np.int64)
+        out = getattr(self, "_flat_out", None)
+        if out is None:
+            out = self._flat_out = np.empty(1 << 16, np.int32)
+        while True:
+            rc = L.rknn_query_batch(self.h, _ptr(qs), _ptr(ks), nq, _MODES[mode], out.ctypes.data,
+                                    out.shape[0], off.ctypes.data, None)
+            if rc == 5 and off[nq] > out.shape[0]:
+                out = self._flat_out = np.empty(int(off[nq] * 5 // 4), np.int32)
+                continue
+            _check(rc)
+            return out[: off[nq]], off[: nq + 1]
+
     def last_zone(self, slot: int = 0):
         """(facility indices of the bisectors in creation order, flags)."""
         L = load()

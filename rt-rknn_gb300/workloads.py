@@ -1,0 +1,155 @@
+"""The five benchmark workloads of the engine, one JSON line each.
+
+    python rt-rknn_gb300/workloads.py [--configs 1,2,3,4,5] [--out FILE]
+
+  1  1,000 facilities / 10,000 users uniform, k=5, 10 queries
+  2  100,000 / 1,000,000 uniform, k in {1,5,10,25}, 1,000 queries: the plain
+     form (one query per launch, FP64 predicates, influence zone) and the
+     chosen form (one batch, FP32-filtered predicates, default filter)
+  3  200,000 / 4,000,000 Gaussian mixture with 1% bisector ties and 0.1%
+     duplicates, k=10, 2,000 queries: FP32 and FP64 batches, recheck fraction,
+     FP32 == FP64 on every query
+  4  20,000 / 2,000,000 street layout, 16,384 queries with k log-uniform in
+     [1,100], one batch
+  5  1,000,000 / 10,000,000 uniform resident, Poisson arrivals at 1k-100k
+     requests/s with k log-uniform in [1,64] through the serving loop: p50/p99
+     latency and throughput for FP32 and FP64
+
+Device times come from the engine's own CUDA events (rknn_query_stats
+.device_ms); every batch is run once untimed first.  Parity with the exact
+oracle is checked by tests/test_configs.py, not here.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+import build  # noqa: E402
+import datagen  # noqa: E402
+import rknn  # noqa: E402
+
+
+def _batch(idx, qs, ks, mode, reps=3):
+    idx.query_batch_flat(qs, ks, mode)
+    ms = []
+    st = None
+    for _ in range(reps):
+        res, st = idx.query_batch(qs, ks, mode, stats=True)
+        ms.append(st["device_ms"])
+    return float(np.median(ms)), st, res
+
+
+def config1():
+    ds = datagen.config(1)
+    with rknn.Index.of(ds) as idx:
+        ms, st, _ = _batch(idx, ds.queries, ds.ks, "fp32")
+        t = []
+        for q in ds.queries:
+            t0 = time.perf_counter()
+            idx.query(int(q), 5, "fp64")
+            t.append(time.perf_counter() - t0)
+    return {"config": 1, "fp32_batch_ms": ms, "fp64_single_ms_median": 1e3 * float(np.median(t)),
+            "results": st["results"]}
+
+
+def config2():
+    ds = datagen.config(2)
+    out = {"config": 2, "k": {}}
+    qs = ds.queries.astype(np.int32)
+    with rknn.Index.of(ds) as idx, rknn.Index.of(ds, filter="inf") as inf:
+        for k in (1, 5, 10, 25):
+            ms, st, res = _batch(idx, qs, k, "fp32")
+            ms_inf, _, res_inf = _batch(inf, qs, k, "fp32")
+            same = all(np.array_equal(a, b) for a, b in zip(res, res_inf))
+            lat = []
+            for q in qs[:100]:
+                t0 = time.perf_counter()
+                inf.query(int(q), k, "fp64")
+                lat.append(1e3 * (time.perf_counter() - t0))
+            lat.sort()
+            out["k"][k] = {"fp32_batched_qps": len(qs) / (ms / 1e3), "inf_zone_fp32_batched_qps": len(qs) / (ms_inf / 1e3),
+                           "fp64_single_qps": 1e3 / float(np.mean(lat)), "fp64_single_p50_ms": lat[len(lat) // 2],
+                           "fp64_single_p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                           "filters_agree": same, "results_per_query": st["results"] / len(qs),
+                           "candidates_per_query": st["candidates"] / len(qs)}
+    return out
+
+
+def config3():
+    ds = datagen.config(3)
+    qs = ds.queries.astype(np.int32)
+    with rknn.Index.of(ds) as idx:
+        ms32, st32, r32 = _batch(idx, qs, 10, "fp32", reps=2)
+        ms64, st64, r64 = _batch(idx, qs, 10, "fp64", reps=2)
+    same = sum(np.array_equal(a, b) for a, b in zip(r32, r64))
+    return {"config": 3, "fp32_batched_qps": len(qs) / (ms32 / 1e3), "fp64_batched_qps": len(qs) / (ms64 / 1e3),
+            "recheck_fraction_fp32": st32["rechecks"] / max(1, st32["fac_checks"]),
+            "recheck_fraction_fp64": st64["rechecks"] / max(1, st64["fac_checks"]),
+            "rechecks_fp32": st32["rechecks"], "rechecks_fp64": st64["rechecks"],
+            "fp32_equals_fp64_queries": int(same), "queries": len(qs), "results": st32["results"]}
+
+
+def config4():
+    ds = datagen.config(4)
+    qs, ks = ds.queries.astype(np.int32), ds.ks.astype(np.int32)
+    out = {"config": 4, "queries": len(qs)}
+    with rknn.Index.of(ds) as idx:
+        for mode in ("fp32", "fp64"):
+            ms, st, _ = _batch(idx, qs, ks, mode, reps=2)
+            out[mode] = {"device_ms": ms, "qps": len(qs) / (ms / 1e3), "results": st["results"],
+                         "candidates": st["candidates"], "survivors": st["survivors"]}
+    return out
+
+
+def config5():
+    ds = datagen.config(5)
+    rng = np.random.default_rng(55)
+    out = {"config": 5, "rates": {}}
+    with rknn.Index.of(ds) as idx, rknn.Server(idx, slots=3, max_batch=4096) as srv:
+        for rate in (1_000, 10_000, 50_000, 100_000):
+            n = int(min(200_000, max(2_000, rate * 2)))
+            qs = rng.integers(0, ds.nf, n).astype(np.int32)
+            ks = (np.floor(np.exp(rng.uniform(0, np.log(65), n)))).clip(1, 64).astype(np.int32)
+            arr = np.cumsum(rng.exponential(1.0 / rate, n))
+            row = {}
+            for mode in ("fp32", "fp64"):
+                srv.replay(qs[:1000], ks[:1000], mode, arr[:1000])
+                srv.stats(reset=True)
+                lat, _ = srv.replay(qs, ks, mode, arr)
+                st = srv.stats(reset=True)
+                row[mode] = {"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "throughput_qps": st["throughput_qps"],
+                             "mean_batch": st["mean_batch"], "requests": n}
+            out["rates"][rate] = row
+    return out
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--configs", default="1,2,3,4,5")
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args(argv)
+    build.build()
+    fns = {1: config1, 2: config2, 3: config3, 4: config4, 5: config5}
+    fh = open(a.out, "w") if a.out else None
+    for c in (int(x) for x in a.configs.split(",")):
+        t0 = time.perf_counter()
+        r = fns[c]()
+        r["wall_s"] = time.perf_counter() - t0
+        line = json.dumps(r)
+        print(line, flush=True)
+        if fh:
+            fh.write(line + "\n")
+            fh.flush()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
