@@ -67,7 +67,9 @@ typedef struct {
     int32_t filter;         /* candidate filter: RKNN_FILTER_AUTO (default), _INF, _SLICE */
     int32_t slice_min_k;    /* AUTO: k classes whose largest k reaches this use the slice
                                filter, smaller ones the influence zone (0: default 1) */
-    int32_t reserved[4];
+    int32_t users_per_thread;   /* verification: users per lane per work item, 2/4/8 (0: 4) */
+    int32_t verify_warps;       /* verification: warps per block, 4/8/16 (0: 8) */
+    int32_t reserved[2];
 } rknn_index_opts;
 
 typedef enum {
@@ -249,6 +251,26 @@ rknn_status rknn_serve_stats_get(rknn_server* srv, int32_t reset, rknn_serve_sta
 
 /* Finish queued and running requests, stop the worker, free the server. */
 rknn_status rknn_serve_stop(rknn_server* srv);
+
+/* ---- Autotuning ---------------------------------------------------------
+ * No counterpart in the reference.  Times a sample batch (the caller's
+ * queries, in the given mode) under every combination of facility-grid
+ * density {1, 2, 4} and user-grid density {4, 8, 16} (points per cell: the
+ * grids are rebuilt on the device), users per lane {2, 4, 8} and warps per
+ * block {4, 8, 16} of the verification kernel, and leaves the index set to
+ * the fastest.  Results never depend on these settings.  Not to be called
+ * while a server over the index is running. */
+typedef struct {
+    float fac_per_cell, usr_per_cell;   /* chosen grid densities */
+    int32_t users_per_thread, verify_warps;
+    double default_ms;      /* device time of the sample batch with the settings on entry */
+    double best_ms;         /* ... with the chosen settings */
+    int32_t trials;         /* settings timed */
+    int32_t reserved[5];
+} rknn_tune_result;
+
+rknn_status rknn_index_tune(rknn_index* idx, const int32_t* q_index, const int32_t* k, int32_t nq,
+                            int32_t mode, rknn_tune_result* result);
 
 /* Message of the last failure on this thread ("" if none). */
 const char* rknn_last_error(void);

@@ -114,6 +114,13 @@ struct rknn_index {
     float2* d_uxy = nullptr;
     int *d_uid = nullptr, *d_ustart = nullptr;
     std::vector<int> h_fidx;       // cell-sorted position -> facility input index
+    // the input points, kept on the device so the grids can be rebuilt
+    // with other cell sizes (rknn_index_tune)
+    float2 *d_fin = nullptr, *d_uin = nullptr;
+    int* d_uidin = nullptr;
+    float fac_per_cell = 2.0f, usr_per_cell = 8.0f;
+    int vupt = VERIFY_UPT;         // verification: users per lane per work item
+    int vwarps = VERIFY_WARPS;     // verification: warps per block
     int skip_coincident = 1;
     int filter = RKNN_FILTER_AUTO;
     int slice_min_k = 1;
@@ -270,6 +277,12 @@ cudaError_t allow_dynamic_smem(const void* fn, int optin)
     return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)a.sharedSizeBytes);
 }
 
+// The verification kernel for a users-per-lane setting.
+void (*verify_fn(int upt))(VerifyArgs)
+{
+    return upt == 2 ? verify_kernel_u2 : upt == 8 ? verify_kernel_u8 : verify_kernel;
+}
+
 // ceil(log2 k), capped: queries of one class share zone capacities
 int k_class(int k)
 {
@@ -316,6 +329,7 @@ struct BatchPlan {
     std::vector<ZClass> cls;
     int pstride = 0;            // half-plane row stride: the largest class lc
     int stage_cap = 0;          // half-planes the verification stages per warp
+    int vupt = VERIFY_UPT, vwarps = VERIFY_WARPS;
     size_t vsmem = 0;
     int vgrid = 0;
     GraphKey key;
@@ -354,12 +368,16 @@ BatchPlan plan_batch(rknn_index* ix, int nq, int mode, bool use_order, const int
     // most 96 KB per block (a longer list is cut: the filter weakens, the
     // exact recount still decides)
     const int bpp = mode == MODE_FP32 ? 16 : 32;
-    b.stage_cap = std::max(1, std::min(b.pstride, (96 << 10) / (VERIFY_WARPS * bpp)));
-    b.vsmem = (size_t)VERIFY_WARPS * b.stage_cap * bpp;
+    b.vupt = ix->vupt;
+    b.vwarps = ix->vwarps;
+    b.stage_cap = std::max(1, std::min(b.pstride, (96 << 10) / (b.vwarps * bpp)));
+    b.vsmem = (size_t)b.vwarps * b.stage_cap * bpp;
     int vper = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&vper, verify_kernel, VERIFY_WARPS * 32, b.vsmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&vper, verify_fn(b.vupt), b.vwarps * 32, b.vsmem);
     if (vper < 1) vper = 1;
     b.vgrid = vper * ix->num_sms;
+    b.key.push_back(b.vupt);
+    b.key.push_back(b.vwarps);
     return b;
 }
 
@@ -423,7 +441,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     }
     mark(1);
 
-    plan_kernel<<<1, 1024, 0, st>>>(w.d_qd, nq, w.d_cand_off, w.d_chunk_off, w.pool_cap, w.rcap);
+    plan_kernel<<<1, 1024, 0, st>>>(w.d_qd, nq, w.d_cand_off, w.d_chunk_off, w.pool_cap, w.rcap, 32 * b.vupt);
     CK(cudaGetLastError());
     mark(2);
 
@@ -438,7 +456,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     va.nu = (int)ix->nu; va.nf = (int)ix->nf; va.ncf = ix->gf.gx * ix->gf.gy;
     va.pool_cap = w.pool_cap; va.fault = w.d_counters + 10; va.dropped = w.d_counters + 2;
     va.surv = w.d_surv; va.surv_cap = (int)std::min<long long>(w.surv_cap, INT32_MAX); va.surv_count = w.d_counters + 3;
-    verify_kernel<<<b.vgrid, VERIFY_WARPS * 32, b.vsmem, st>>>(va);
+    verify_fn(b.vupt)<<<b.vgrid, b.vwarps * 32, b.vsmem, st>>>(va);
     CK(cudaGetLastError());
     recount_kernel<<<ix->num_sms * 8, 256, 0, st>>>(va);
     CK(cudaGetLastError());
@@ -580,6 +598,40 @@ rknn_status check_queries(rknn_index* ix, const int32_t* q, const int32_t* k, in
     return RKNN_OK;
 }
 
+// (Re)build the facility and user grids from the device copies of the input
+// points: cell ids, stable radix sort, cell starts, per-cell facility boxes.
+rknn_status build_grids(rknn_index* ix, float fac_per_cell, float usr_per_cell)
+{
+    cudaStream_t st = ix->stream;
+    CK(cudaStreamSynchronize(st));
+    cudaFree(ix->d_fxy); cudaFree(ix->d_fidx); cudaFree(ix->d_fpos); cudaFree(ix->d_fstart);
+    cudaFree(ix->d_fmbr); cudaFree(ix->d_uxy); cudaFree(ix->d_uid); cudaFree(ix->d_ustart);
+    ix->d_fxy = nullptr; ix->d_fidx = ix->d_fpos = ix->d_fstart = nullptr; ix->d_fmbr = nullptr;
+    ix->d_uxy = nullptr; ix->d_uid = ix->d_ustart = nullptr;
+    drop_graphs(ix->ws);                        // graphs hold the old grids' pointers
+    const long long nf = ix->nf, nu = ix->nu;
+    ix->fac_per_cell = fac_per_cell;
+    ix->usr_per_cell = usr_per_cell;
+    ix->gf = make_grid(ix->sx0, ix->sy0, ix->sx1, ix->sy1, nf, fac_per_cell, 4096);
+    ix->gu = make_grid(ix->sx0, ix->sy0, ix->sx1, ix->sy1, nu, usr_per_cell, 8192);
+    const long long ncf = (long long)ix->gf.gx * ix->gf.gy, ncu = (long long)ix->gu.gx * ix->gu.gy;
+    CK(dalloc(ix->d_fxy, nf));
+    CK(dalloc(ix->d_fidx, nf));
+    CK(dalloc(ix->d_fpos, nf));
+    CK(dalloc(ix->d_fstart, ncf + 1));
+    CK(dalloc(ix->d_fmbr, ncf));
+    CK(dalloc(ix->d_uxy, nu));
+    CK(dalloc(ix->d_uid, nu));
+    CK(dalloc(ix->d_ustart, ncu + 1));
+    CK(grid_sort(ix->d_fin, nullptr, (int)nf, ix->gf, ix->d_fxy, nullptr, ix->d_fidx, ix->d_fpos, ix->d_fstart, st));
+    CK(cell_mbrs(ix->d_fxy, ix->d_fstart, ix->gf, ix->d_fmbr, st));
+    CK(grid_sort(ix->d_uin, ix->d_uidin, (int)nu, ix->gu, ix->d_uxy, ix->d_uid, nullptr, nullptr, ix->d_ustart, st));
+    ix->h_fidx.resize(nf);
+    CK(cudaMemcpyAsync(ix->h_fidx.data(), ix->d_fidx, sizeof(int) * nf, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return RKNN_OK;
+}
+
 }  // namespace
 
 // ============================================================== public API
@@ -666,39 +718,29 @@ rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf, 
     CKB(allow_dynamic_smem((const void*)zone_kernel_smem, optin));
     CKB(allow_dynamic_smem((const void*)slice_kernel, optin));
     CKB(allow_dynamic_smem((const void*)verify_kernel, optin));
+    CKB(allow_dynamic_smem((const void*)verify_kernel_u2, optin));
+    CKB(allow_dynamic_smem((const void*)verify_kernel_u8, optin));
     CKB(allow_dynamic_smem((const void*)finalize_kernel, optin));
 
-    ix->gf = make_grid(x0, y0, x1, y1, nf, o.fac_per_cell, 4096);
-    ix->gu = make_grid(x0, y0, x1, y1, nu, o.usr_per_cell, 8192);
+    if (o.users_per_thread != 0 && o.users_per_thread != 2 && o.users_per_thread != 4 && o.users_per_thread != 8)
+        return bail(fail(RKNN_ERR_ARG, "users_per_thread must be 2, 4 or 8"));
+    if (o.verify_warps != 0 && o.verify_warps != 4 && o.verify_warps != 8 && o.verify_warps != 16)
+        return bail(fail(RKNN_ERR_ARG, "verify_warps must be 4, 8 or 16"));
+    if (o.users_per_thread) ix->vupt = o.users_per_thread;
+    if (o.verify_warps) ix->vwarps = o.verify_warps;
     cudaStream_t st = ix->stream;
-    float2 *tf = nullptr, *tu = nullptr;
-    int* tuid = nullptr;
-    CKB(dalloc(tf, nf));
-    CKB(cudaMemcpyAsync(tf, fxy, sizeof(float2) * nf, cudaMemcpyHostToDevice, st));
+    CKB(dalloc(ix->d_fin, nf));
+    CKB(cudaMemcpyAsync(ix->d_fin, fxy, sizeof(float2) * nf, cudaMemcpyHostToDevice, st));
     if (nu > 0) {
-        CKB(dalloc(tu, nu));
-        CKB(dalloc(tuid, nu));
-        CKB(cudaMemcpyAsync(tu, uxy, sizeof(float2) * nu, cudaMemcpyHostToDevice, st));
-        CKB(cudaMemcpyAsync(tuid, uid, sizeof(int) * nu, cudaMemcpyHostToDevice, st));
+        CKB(dalloc(ix->d_uin, nu));
+        CKB(dalloc(ix->d_uidin, nu));
+        CKB(cudaMemcpyAsync(ix->d_uin, uxy, sizeof(float2) * nu, cudaMemcpyHostToDevice, st));
+        CKB(cudaMemcpyAsync(ix->d_uidin, uid, sizeof(int) * nu, cudaMemcpyHostToDevice, st));
     }
-    long long ncf = (long long)ix->gf.gx * ix->gf.gy, ncu = (long long)ix->gu.gx * ix->gu.gy;
-    CKB(dalloc(ix->d_fxy, nf));
-    CKB(dalloc(ix->d_fidx, nf));
-    CKB(dalloc(ix->d_fpos, nf));
-    CKB(dalloc(ix->d_fstart, ncf + 1));
-    CKB(dalloc(ix->d_fmbr, ncf));
-    CKB(dalloc(ix->d_uxy, nu));
-    CKB(dalloc(ix->d_uid, nu));
-    CKB(dalloc(ix->d_ustart, ncu + 1));
-    CKB(grid_sort(tf, nullptr, (int)nf, ix->gf, ix->d_fxy, nullptr, ix->d_fidx, ix->d_fpos, ix->d_fstart, st));
-    CKB(cell_mbrs(ix->d_fxy, ix->d_fstart, ix->gf, ix->d_fmbr, st));
-    CKB(grid_sort(tu, tuid, (int)nu, ix->gu, ix->d_uxy, ix->d_uid, nullptr, nullptr, ix->d_ustart, st));
-    ix->h_fidx.resize(nf);
-    CKB(cudaMemcpyAsync(ix->h_fidx.data(), ix->d_fidx, sizeof(int) * nf, cudaMemcpyDeviceToHost, st));
-    CKB(cudaStreamSynchronize(st));
-    cudaFree(tf);
-    cudaFree(tu);
-    cudaFree(tuid);
+    {
+        rknn_status bs = build_grids(ix, o.fac_per_cell, o.usr_per_cell);
+        if (bs != RKNN_OK) return bail(bs);
+    }
 #undef CKB
     *out = ix;
     return RKNN_OK;
@@ -712,6 +754,7 @@ rknn_status rknn_index_destroy(rknn_index* ix)
     free_ws(ix->ws);
     cudaFree(ix->d_fxy); cudaFree(ix->d_fidx); cudaFree(ix->d_fpos); cudaFree(ix->d_fstart);
     cudaFree(ix->d_fmbr); cudaFree(ix->d_uxy); cudaFree(ix->d_uid); cudaFree(ix->d_ustart);
+    cudaFree(ix->d_fin); cudaFree(ix->d_uin); cudaFree(ix->d_uidin);
     if (ix->ev0) cudaEventDestroy(ix->ev0);
     if (ix->ev1) cudaEventDestroy(ix->ev1);
     for (int i = 0; i < 6; ++i) if (ix->kev[i]) cudaEventDestroy(ix->kev[i]);
@@ -1058,7 +1101,7 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     zone_kernel_smem<<<1, 32 * ZONE_WARPS, zsmem, st>>>(za);
     CK(cudaGetLastError());
     plan_kernel<<<1, 1024, 0, st>>>(L.qd, 1, L.cand_off, L.chunk_off, L.pool_cap,
-                                    (int)std::min<long long>(L.pool_cap, INT32_MAX));
+                                    (int)std::min<long long>(L.pool_cap, INT32_MAX), VERIFY_CHUNK);
     CK(cudaGetLastError());
 
     VerifyArgs va;
@@ -1526,3 +1569,69 @@ rknn_status rknn_serve_stop(rknn_server* sv)
 }
 
 }  // extern "C"
+
+// ====================================================================
+// Autotuning: grid densities and the verification kernel's shape, timed on
+// the caller's sample batch with the engine's own events.
+extern "C" rknn_status rknn_index_tune(rknn_index* ix, const int32_t* q, const int32_t* k, int32_t nq,
+                                       int32_t mode, rknn_tune_result* result)
+{
+    g_err.clear();
+    if (!ix || !q || !k || nq <= 0 || !result) return fail(RKNN_ERR_ARG, "bad argument");
+    if (mode != RKNN_MODE_FP32 && mode != RKNN_MODE_FP64) return fail(RKNN_ERR_ARG, "bad mode");
+    int kmax = 1;
+    rknn_status s = check_queries(ix, q, k, nq, &kmax);
+    if (s != RKNN_OK) return s;
+    std::vector<int64_t> off((size_t)nq + 1);
+    // device time of the sample batch: best of two runs after one untimed run
+    auto time_batch = [&](double& ms) -> rknn_status {
+        ms = 1e300;
+        for (int r = 0; r < 3; ++r) {
+            rknn_query_stats st;
+            rknn_status e = rknn_query_batch(ix, q, k, nq, mode, nullptr, 0, off.data(), &st);
+            if (e != RKNN_OK && e != RKNN_ERR_CAPACITY) return e;
+            if (r > 0) ms = std::min(ms, st.device_ms);
+        }
+        g_err.clear();
+        return RKNN_OK;
+    };
+    const float fpc0 = ix->fac_per_cell, upc0 = ix->usr_per_cell;
+    const int upt0 = ix->vupt, vw0 = ix->vwarps;
+    rknn_tune_result r{};
+    r.fac_per_cell = fpc0; r.usr_per_cell = upc0; r.users_per_thread = upt0; r.verify_warps = vw0;
+    s = time_batch(r.default_ms);
+    if (s != RKNN_OK) return s;
+    r.best_ms = r.default_ms;
+    const float fpcs[3] = {1.0f, 2.0f, 4.0f}, upcs[3] = {4.0f, 8.0f, 16.0f};
+    const int upts[3] = {2, 4, 8}, vws[3] = {4, 8, 16};
+    for (float fpc : fpcs)
+        for (float upc : upcs) {
+            {
+                std::lock_guard<std::mutex> lk(ix->mu);
+                s = build_grids(ix, fpc, upc);
+            }
+            if (s != RKNN_OK) return s;
+            for (int upt : upts)
+                for (int vw : vws) {
+                    ix->vupt = upt;
+                    ix->vwarps = vw;
+                    double ms = 0;
+                    s = time_batch(ms);
+                    if (s != RKNN_OK) return s;
+                    r.trials++;
+                    if (ms < r.best_ms) {
+                        r.best_ms = ms;
+                        r.fac_per_cell = fpc; r.usr_per_cell = upc; r.users_per_thread = upt; r.verify_warps = vw;
+                    }
+                }
+        }
+    {
+        std::lock_guard<std::mutex> lk(ix->mu);
+        s = build_grids(ix, r.fac_per_cell, r.usr_per_cell);
+    }
+    if (s != RKNN_OK) return s;
+    ix->vupt = r.users_per_thread;
+    ix->vwarps = r.verify_warps;
+    *result = r;
+    return RKNN_OK;
+}

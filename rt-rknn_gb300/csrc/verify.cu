@@ -95,15 +95,15 @@ __device__ __forceinline__ int exact_count(float ux, float uy, const QDesc& d, c
 // Stage 1 over the first nb staged half-planes: cnt = certified
 // violations (the loop leaves once every lane's users reached k), und =
 // half-planes the bound could not decide.
-template <typename T>
+template <typename T, int UPT>
 __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char* sp, const int* pos,
                                              const float2* u, const bool* valid, int* cnt, int* und,
                                              unsigned long long& evals)
 {
-    T x[VERIFY_UPT], y[VERIFY_UPT], bu[VERIFY_UPT];
+    T x[UPT], y[UPT], bu[UPT];
     int nvalid = 0;
 #pragma unroll
-    for (int t = 0; t < VERIFY_UPT; ++t) {
+    for (int t = 0; t < UPT; ++t) {
         cnt[t] = valid[t] ? 0 : INT_MAX / 2;
         und[t] = 0;
         nvalid += valid[t];
@@ -129,7 +129,7 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
             a = (T)p[0]; b = (T)p[1]; c = (T)p[2];
         }
 #pragma unroll
-        for (int t = 0; t < VERIFY_UPT; ++t) {
+        for (int t = 0; t < UPT; ++t) {
             T mv = fma(a, x[t], fma(b, y[t], c));
             cnt[t] += (mv < -bu[t]);
             und[t] += (mv <= bu[t]) & (mv >= -bu[t]);
@@ -137,7 +137,7 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
         if ((m & 7) == 7) {
             bool done = true;
 #pragma unroll
-            for (int t = 0; t < VERIFY_UPT; ++t) done &= cnt[t] >= k;
+            for (int t = 0; t < UPT; ++t) done &= cnt[t] >= k;
             if (__all_sync(FULL, done)) { ++m; break; }
         }
     }
@@ -146,8 +146,8 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
 
 }  // namespace
 
-__global__ void __launch_bounds__(VERIFY_WARPS * 32)
-verify_kernel(VerifyArgs A)
+template <int UPT>
+__device__ __forceinline__ void verify_body(const VerifyArgs& A)
 {
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -188,7 +188,7 @@ verify_kernel(VerifyArgs A)
             cur = s;
             __syncwarp();
         }
-        const int v0 = (g - A.chunk_off[s]) * VERIFY_CHUNK;
+        const int v0 = (g - A.chunk_off[s]) * (32 * UPT);
         const int2* sg = A.segs + (size_t)s * A.seg_cap;
         // segment holding v0: largest i < nseg with sg[i].y <= v0
         int i0 = 0;
@@ -200,12 +200,12 @@ verify_kernel(VerifyArgs A)
             }
             i0 = l;
         }
-        int pos[VERIFY_UPT];
-        float2 u[VERIFY_UPT];
-        bool valid[VERIFY_UPT];
+        int pos[UPT];
+        float2 u[UPT];
+        bool valid[UPT];
         int si = i0;
 #pragma unroll
-        for (int t = 0; t < VERIFY_UPT; ++t) {
+        for (int t = 0; t < UPT; ++t) {
             int v = v0 + t * 32 + lane;
             valid[t] = v < d.ncand;
             pos[t] = 0;
@@ -217,20 +217,20 @@ verify_kernel(VerifyArgs A)
             }
             s_cand += valid[t];
         }
-        int cnt[VERIFY_UPT], und[VERIFY_UPT];
+        int cnt[UPT], und[UPT];
         const int nbs = min(d.nb, A.stage_cap);
-        if (A.mode == MODE_FP32) filter_users<float>(d, nbs, sp, pos, u, valid, cnt, und, s_evals);
-        else filter_users<double>(d, nbs, sp, pos, u, valid, cnt, und, s_evals);
+        if (A.mode == MODE_FP32) filter_users<float, UPT>(d, nbs, sp, pos, u, valid, cnt, und, s_evals);
+        else filter_users<double, UPT>(d, nbs, sp, pos, u, valid, cnt, und, s_evals);
         // A user within rho/2 of q is decided by the half-planes alone: every
         // facility strictly nearer to it than q lies within 2|u-q| <= rho of
         // q, so it is a half-plane.  With no undecided half-plane the
         // certified count is the exact count.  (All half-planes must be
         // staged for this.)
-        bool direct[VERIFY_UPT];
+        bool direct[UPT];
         {
             const float rho2 = (nbs == d.nb) ? d.rho * d.rho * (1.0f - 1e-5f) : 0.0f;
 #pragma unroll
-            for (int t = 0; t < VERIFY_UPT; ++t) {
+            for (int t = 0; t < UPT; ++t) {
                 const float xx = u[t].x - d.qx, yy = u[t].y - d.qy;
                 const float du2 = 4.0f * fmaf(xx, xx, yy * yy) * (1.0f + 1e-5f);
                 direct[t] = valid[t] && cnt[t] < d.k && und[t] == 0 && du2 <= rho2;
@@ -239,10 +239,10 @@ verify_kernel(VerifyArgs A)
 
         // stage 2: survivors go to the list for recount_kernel; when it is
         // full, the warp counts them itself, one user at a time
-        unsigned sm[VERIFY_UPT];
+        unsigned sm[UPT];
         int ns = 0;
 #pragma unroll
-        for (int t = 0; t < VERIFY_UPT; ++t) {
+        for (int t = 0; t < UPT; ++t) {
             sm[t] = __ballot_sync(FULL, valid[t] && cnt[t] < d.k && !direct[t]);
             ns += __popc(sm[t]);
         }
@@ -255,7 +255,7 @@ verify_kernel(VerifyArgs A)
             if ((long long)base + ns <= A.surv_cap) {
                 int o = 0;
 #pragma unroll
-                for (int t = 0; t < VERIFY_UPT; ++t) {
+                for (int t = 0; t < UPT; ++t) {
                     if (sm[t] & (1u << lane))
                         A.surv[VX((long long)base + o + __popc(sm[t] & ((1u << lane) - 1)), A.surv_cap, 214)] = make_int2(s, pos[t]);
                     o += __popc(sm[t]);
@@ -266,9 +266,9 @@ verify_kernel(VerifyArgs A)
                 for (int i = base + lane; i < A.surv_cap && i < base + ns; i += 32) A.surv[i] = make_int2(-1, 0);
             }
         }
-        bool acc[VERIFY_UPT];
+        bool acc[UPT];
 #pragma unroll
-        for (int t = 0; t < VERIFY_UPT; ++t) {
+        for (int t = 0; t < UPT; ++t) {
             acc[t] = direct[t];
             unsigned m = listed ? 0u : sm[t];
             while (m) {
@@ -281,10 +281,10 @@ verify_kernel(VerifyArgs A)
             }
         }
         // warp-aggregated append of the accepted users
-        unsigned am[VERIFY_UPT];
+        unsigned am[UPT];
         int tot = 0;
 #pragma unroll
-        for (int t = 0; t < VERIFY_UPT; ++t) { am[t] = __ballot_sync(FULL, acc[t]); tot += __popc(am[t]); }
+        for (int t = 0; t < UPT; ++t) { am[t] = __ballot_sync(FULL, acc[t]); tot += __popc(am[t]); }
         if (tot) {
             int base = 0;
             if (lane == 0) base = atomicAdd(A.res_count + s, tot);
@@ -295,7 +295,7 @@ verify_kernel(VerifyArgs A)
             if (lane == 0 && base + tot > region) atomicOr(A.dropped, 1);
             int o = 0;
 #pragma unroll
-            for (int t = 0; t < VERIFY_UPT; ++t) {
+            for (int t = 0; t < UPT; ++t) {
                 const long long at = (long long)base + o + __popc(am[t] & ((1u << lane) - 1));
                 if (acc[t] && at < region) A.res_pool[VX(r0 + at, A.pool_cap, 206)] = A.uid[VX(pos[t], A.nu, 207)];
                 o += __popc(am[t]);
@@ -318,6 +318,12 @@ verify_kernel(VerifyArgs A)
         atomicAdd(&A.vstats->results, s_res);
     }
 }
+
+// The verification kernel with 2, 4 or 8 users per lane per work item
+// (32 * UPT users per item); blocks of up to 16 warps.
+__global__ void __launch_bounds__(512) verify_kernel(VerifyArgs a) { verify_body<4>(a); }
+__global__ void __launch_bounds__(512) verify_kernel_u2(VerifyArgs a) { verify_body<2>(a); }
+__global__ void __launch_bounds__(512) verify_kernel_u8(VerifyArgs a) { verify_body<8>(a); }
 
 // One warp per listed survivor.  Lane r computes the facility range of
 // disc row r (trimmed to the chord), a warp prefix sum flattens the rows,
@@ -455,7 +461,8 @@ __device__ T block_scan_excl(T v, T* tmp, T* total)
 // offsets; slots whose region does not fit the pool are flagged and skipped
 // (the host grows the pool and runs the batch again).  Work items cover
 // every candidate of the slots that fit.
-__global__ void plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_off, long long pool_cap, int rcap)
+__global__ void plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_off, long long pool_cap, int rcap,
+                            int chunk)
 {
     __shared__ long long tmp64[32];
     __shared__ int tmp[32];
@@ -472,13 +479,13 @@ __global__ void plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_o
         const int n = qd[i].ncand;
         const bool fits = cand_off[i] + min(n, rcap) <= pool_cap;
         if (!fits) qd[i].flags |= QF_RESULT_OVERFLOW;
-        csum += fits ? (n + VERIFY_CHUNK - 1) / VERIFY_CHUNK : 0;
+        csum += fits ? (n + chunk - 1) / chunk : 0;
     }
     int crun = block_scan_excl<int>(csum, tmp, &ctot);
     for (int i = b; i < e; ++i) {
         chunk_off[i] = crun;
         const int n = qd[i].ncand;
-        if (!(qd[i].flags & QF_RESULT_OVERFLOW)) crun += (n + VERIFY_CHUNK - 1) / VERIFY_CHUNK;
+        if (!(qd[i].flags & QF_RESULT_OVERFLOW)) crun += (n + chunk - 1) / chunk;
     }
     if (threadIdx.x == 0) chunk_off[nq] = ctot;
 }

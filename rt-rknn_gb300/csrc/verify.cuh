@@ -4,9 +4,9 @@
 
 namespace rknn {
 
-constexpr int VERIFY_UPT = 4;                       // users per lane per chunk
-constexpr int VERIFY_CHUNK = 32 * VERIFY_UPT;       // users per work item
-constexpr int VERIFY_WARPS = 8;                     // warps per block
+constexpr int VERIFY_UPT = 4;                       // default users per lane per work item
+constexpr int VERIFY_CHUNK = 32 * VERIFY_UPT;       // default users per work item
+constexpr int VERIFY_WARPS = 8;                     // default warps per block
 constexpr int SORT_CAP = 16384;                     // results sorted in shared memory
 
 enum { MODE_FP64 = 0, MODE_FP32 = 1 };
@@ -42,7 +42,9 @@ struct VerifyArgs {
     int* fault;              // checked builds: {flag, array id, index, size, line}
 };
 
-__global__ void verify_kernel(VerifyArgs a);
+__global__ void verify_kernel(VerifyArgs a);        // 4 users per lane per work item
+__global__ void verify_kernel_u2(VerifyArgs a);     // 2
+__global__ void verify_kernel_u8(VerifyArgs a);     // 8
 
 // exact recount of the listed survivors, one thread each
 __global__ void recount_kernel(VerifyArgs a);
@@ -51,7 +53,7 @@ __global__ void recount_kernel(VerifyArgs a);
 // and work-item offsets from QDesc.ncand; flags slots whose region does not
 // fit the pool
 __global__ void plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_off, long long pool_cap,
-                            int rcap);
+                            int rcap, int chunk);
 
 // single block: exclusive scan of the stored result counts into out_off
 __global__ void scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int* out_off);

@@ -37,7 +37,7 @@ EXPORTS = ["rknn_index_opts_default", "rknn_index_create", "rknn_index_destroy",
            "rknn_batch_device_results", "rknn_sync", "rknn_set_stream", "rknn_last_stats",
            "rknn_last_zone", "rknn_set_profiling", "rknn_last_kernel_ms",
            "rknn_serve_opts_default", "rknn_serve_start", "rknn_serve_submit", "rknn_serve_wait",
-           "rknn_serve_replay", "rknn_serve_stats_get", "rknn_serve_stop",
+           "rknn_serve_replay", "rknn_serve_stats_get", "rknn_serve_stop", "rknn_index_tune",
            "rknn_last_error", "rknn_version"]
 
 
@@ -65,7 +65,17 @@ class RkNNError(RuntimeError):
 class Opts(C.Structure):
     _fields_ = [("device", C.c_int32), ("fac_per_cell", C.c_float), ("usr_per_cell", C.c_float),
                 ("skip_coincident", C.c_int32), ("filter", C.c_int32), ("slice_min_k", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("users_per_thread", C.c_int32), ("verify_warps", C.c_int32), ("reserved", C.c_int32 * 2)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("fac_per_cell", C.c_float), ("usr_per_cell", C.c_float),
+                ("users_per_thread", C.c_int32), ("verify_warps", C.c_int32),
+                ("default_ms", C.c_double), ("best_ms", C.c_double), ("trials", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
 
 
 class Info(C.Structure):
@@ -131,6 +141,7 @@ def load(path: str = LIB_PATH):
     L.rknn_serve_replay.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp]
     L.rknn_serve_stats_get.argtypes = [vp, i32, C.POINTER(ServeStats)]
     L.rknn_serve_stop.argtypes = [vp]
+    L.rknn_index_tune.argtypes = [vp, vp, vp, i32, i32, C.POINTER(TuneResult)]
     L.rknn_last_error.restype = C.c_char_p
     L.rknn_version.restype = C.c_char_p
     for name in EXPORTS:
@@ -156,7 +167,8 @@ class Index:
 
     def __init__(self, fxy, uxy, fid=None, uid=None, device: int = 0,
                  fac_per_cell: float = 0.0, usr_per_cell: float = 0.0,
-                 skip_coincident: bool = True, filter: str = "auto", slice_min_k: int = 0):
+                 skip_coincident: bool = True, filter: str = "auto", slice_min_k: int = 0,
+                 users_per_thread: int = 0, verify_warps: int = 0):
         L = load()
         self.fxy = np.ascontiguousarray(fxy, dtype=np.float32).reshape(-1, 2)
         self.uxy = np.ascontiguousarray(uxy, dtype=np.float32).reshape(-1, 2)
@@ -175,6 +187,8 @@ class Index:
         o.skip_coincident = 1 if skip_coincident else 0
         o.filter = {"auto": 0, "inf": 1, "slice": 2}[filter]
         o.slice_min_k = int(slice_min_k)
+        o.users_per_thread = int(users_per_thread)
+        o.verify_warps = int(verify_warps)
         h = C.c_void_p()
         _check(L.rknn_index_create(_ptr(self.fxy), _ptr(self.fid), nf, _ptr(self.uxy),
                                    _ptr(self.uid), nu, C.byref(o), C.byref(h)))
@@ -246,6 +260,15 @@ class Index:
             break
         res = [out[off[i]:off[i + 1]].copy() for i in range(nq)]
         return (res, st.as_dict()) if stats else res
+
+    def tune(self, qs, ks, mode="fp32") -> dict:
+        """Autotune grid densities and the verification kernel's shape on a
+        sample batch (rknn_index_tune); the index keeps the fastest."""
+        qs = np.ascontiguousarray(qs, dtype=np.int32)
+        ks = np.ascontiguousarray(np.broadcast_to(np.asarray(ks, np.int32), qs.shape), dtype=np.int32)
+        r = TuneResult()
+        _check(load().rknn_index_tune(self.h, _ptr(qs), _ptr(ks), qs.shape[0], _MODES[mode], C.byref(r)))
+        return r.as_dict()
 
     def query_batch_flat(self, qs, ks, mode="fp32"):
         """(ids, offsets): the batch's results as one id array, query i's

@@ -179,3 +179,39 @@ def test_edge_cases(engine):
     for q in (0, 2, 31, 33):
         for k in (1, 2, 6):
             assert np.array_equal(idx.query(q, k), o.query(q, k)), (q, k)
+
+
+def test_command_line_drop_in(engine, golden_dir, tmp_path):
+    """`rknn-gb300 -if <file> -k <k> -q <index>` as the reference's binaries are
+    called: the reference's text format in, its summary lines out, and the
+    result set in log/<mode>_k<k>_q<q>.txt (sorted user ids, one per line)."""
+    import subprocess
+    z = np.load(os.path.join(golden_dir, "uniform_int_1k10k.npz"))
+    g = json.load(open(os.path.join(golden_dir, "naive_int_1k10k.json")))
+    ds = datagen.Dataset(z["fxy"], z["uxy"], z["fid"], z["uid"], z["queries"], z["ks"], "golden_int")
+    path = tmp_path / "points.txt"
+    datagen.write_text(str(path), ds)
+    o = O.Oracle(z["fxy"], z["uxy"], z["fid"], z["uid"])
+    cli = os.path.join(os.path.dirname(engine.__file__), "rknn-gb300")
+    k = g["k"]
+    qs = [int(q) for q in g["ids"]][:4]
+    for mode in MODES:
+        for q in qs:
+            r = subprocess.run([cli, "-if", str(path), "-k", str(k), "-q", str(q), "-al", "inf",
+                                "--mode", mode, "--log", str(tmp_path / "log")],
+                               capture_output=True, text=True)
+            assert r.returncode == 0, r.stderr
+            assert f"Loaded {ds.nf} facilities and {ds.nu} users." in r.stdout
+            want = o.query(q, k)
+            assert f"Found {want.size} RkNN results." in r.stdout
+            got = np.loadtxt(tmp_path / "log" / f"{mode}_k{k}_q{q}.txt", dtype=np.int64, ndmin=1)
+            assert np.array_equal(got, want), (q, mode)
+            assert set(g["ids"][str(q)]) <= set(got.tolist())
+    # several queries in one batch, slice filter
+    r = subprocess.run([cli, "-if", str(path), "-k", str(k), "--queries", ",".join(map(str, qs)),
+                        "--filter", "slice", "--mode", "fp32", "--log", str(tmp_path / "log2")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for q in qs:
+        got = np.loadtxt(tmp_path / "log2" / f"fp32_k{k}_q{q}.txt", dtype=np.int64, ndmin=1)
+        assert np.array_equal(got, o.query(q, k)), q

@@ -79,3 +79,25 @@ def test_slice_on_ties_and_street(engine):
         assert np.array_equal(r, os_.query(int(q), int(k))), (int(q), int(k))
     idx.close()
     idx2.close()
+
+
+def test_autotune_keeps_results(engine, uni):
+    """Tuning rebuilds the grids and reshapes the verification; the answers
+    stay the same."""
+    ds, o = uni
+    idx = engine.Index.of(ds, users_per_thread=2, verify_warps=16)
+    rng = np.random.default_rng(7)
+    qs = rng.integers(0, ds.nf, 300).astype(np.int32)
+    ks = rng.integers(1, 40, 300).astype(np.int32)
+    before = idx.query_batch(qs, ks, "fp32")
+    r = idx.tune(qs, ks, "fp32")
+    assert r["trials"] == 81 and r["best_ms"] <= r["default_ms"]
+    assert r["users_per_thread"] in (2, 4, 8) and r["verify_warps"] in (4, 8, 16)
+    after = idx.query_batch(qs, ks, "fp32")
+    after64 = idx.query_batch(qs[:50], ks[:50], "fp64")
+    for i in range(300):
+        assert np.array_equal(before[i], after[i]), i
+    for i in range(0, 50, 5):
+        want = o.query(int(qs[i]), int(ks[i]))
+        assert np.array_equal(after[i], want) and np.array_equal(after64[i], want), i
+    idx.close()
