@@ -302,12 +302,13 @@ struct ZClass {
 };
 
 // Capacities of the slice filter: a k-entry heap per slice, half-planes of
-// the nearest facilities for the verification.
-ZoneCaps slice_caps(int kmax)
+// the nearest facilities for the verification (no more than it stages, so
+// that all of them take part in its exact shortcut).
+ZoneCaps slice_caps(int kmax, int lc_cap = 512)
 {
     ZoneCaps c;
     c.vc = std::max(1, kmax);
-    c.lc = (int)std::min<long long>(6LL * c.vc + 40, 512);
+    c.lc = (int)std::max<long long>(1, std::min<long long>(6LL * c.vc + 40, lc_cap));
     c.pc = 0;
     c.rm = 64;
     return c;
@@ -355,9 +356,12 @@ BatchPlan plan_batch(rknn_index* ix, int nq, int mode, bool use_order, const int
         b.cls.push_back(ZClass{0, nq, std::max(1, kmax), false, {}, {}});
     }
     b.key = {nq, mode, use_order ? 1 : 0};
+    // half-planes the verification can stage per warp (96 KB per block)
+    const int bpp = mode == MODE_FP32 ? 16 : 32;
+    const int stage_max = std::max(1, (96 << 10) / (ix->vwarps * bpp));
     for (auto& c : b.cls) {
         c.slice = use_slice(ix, c.kmax);
-        c.caps = c.slice ? slice_caps(c.kmax) : caps_fit(ix, caps_for(c.kmax));
+        c.caps = c.slice ? slice_caps(c.kmax, std::min(512, stage_max)) : caps_fit(ix, caps_for(c.kmax));
         c.zl = zone_launch(ix, c.caps, c.n, c.slice);
         b.pstride = std::max(b.pstride, c.caps.lc);
         b.key.push_back(c.n);
@@ -367,10 +371,9 @@ BatchPlan plan_batch(rknn_index* ix, int nq, int mode, bool use_order, const int
     // the verification stages each query's half-planes in shared memory, at
     // most 96 KB per block (a longer list is cut: the filter weakens, the
     // exact recount still decides)
-    const int bpp = mode == MODE_FP32 ? 16 : 32;
     b.vupt = ix->vupt;
     b.vwarps = ix->vwarps;
-    b.stage_cap = std::max(1, std::min(b.pstride, (96 << 10) / (b.vwarps * bpp)));
+    b.stage_cap = std::max(1, std::min(b.pstride, stage_max));
     b.vsmem = (size_t)b.vwarps * b.stage_cap * bpp;
     int vper = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&vper, verify_fn(b.vupt), b.vwarps * 32, b.vsmem);
