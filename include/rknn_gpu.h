@@ -254,12 +254,13 @@ rknn_status rknn_serve_stop(rknn_server* srv);
 
 /* ---- Autotuning ---------------------------------------------------------
  * No counterpart in the reference.  Times a sample batch (the caller's
- * queries, in the given mode) under every combination of facility-grid
- * density {1, 2, 4} and user-grid density {4, 8, 16} (points per cell: the
- * grids are rebuilt on the device), users per lane {2, 4, 8} and warps per
- * block {4, 8, 16} of the verification kernel, and leaves the index set to
- * the fastest.  Results never depend on these settings.  Not to be called
- * while a server over the index is running. */
+ * queries, in the given mode): first every combination of facility-grid
+ * density {0.25, 0.5, 1, 2, 4} and user-grid density {1, 2, 4, 8, 16}
+ * (points per cell: the grids are rebuilt on the device), then with the best
+ * grids every combination of users per lane {2, 4, 8} and warps per block
+ * {4, 8, 16} of the verification kernel (34 settings), and leaves the index
+ * set to the fastest.  Results never depend on these settings.  Not to be
+ * called while a server over the index is running. */
 typedef struct {
     float fac_per_cell, usr_per_cell;   /* chosen grid densities */
     int32_t users_per_thread, verify_warps;

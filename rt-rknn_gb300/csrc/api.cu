@@ -76,6 +76,7 @@ struct Workspace {
     int *d_q = nullptr, *d_k = nullptr, *d_order = nullptr;
     QDesc* d_qd = nullptr;
     float4* d_planes = nullptr;
+    float* d_slice_r = nullptr;    // [slot][32] slice filter bounds
     int* d_bispos = nullptr;
     int2* d_segs = nullptr;
     ZStats* d_zst = nullptr;
@@ -158,6 +159,7 @@ void free_ws(Workspace& w)
     w.graphs.clear();
     cudaFree(w.d_q); cudaFree(w.d_k); cudaFree(w.d_order);
     cudaFree(w.d_qd); cudaFree(w.d_planes); cudaFree(w.d_bispos); cudaFree(w.d_segs); cudaFree(w.d_zst);
+    cudaFree(w.d_slice_r);
     cudaFree(w.d_cand_off); cudaFree(w.d_chunk_off); cudaFree(w.d_res_count); cudaFree(w.d_out_off);
     cudaFree(w.d_counters); cudaFree(w.d_vstats);
     cudaFree(w.d_pool); cudaFree(w.d_out); cudaFree(w.d_zscratch); cudaFree(w.d_surv);
@@ -232,6 +234,7 @@ rknn_status ensure_ws(Workspace& w, int nq, const ZoneCaps& caps, long long pool
         CK(dalloc(w.d_q, nqc)); CK(dalloc(w.d_k, nqc)); CK(dalloc(w.d_order, nqc));
         CK(dalloc(w.d_qd, nqc));
         CK(dalloc(w.d_planes, (size_t)nqc * lc));
+        CK(dalloc(w.d_slice_r, (size_t)nqc * 32));
         CK(dalloc(w.d_bispos, (size_t)nqc * lc));
         CK(dalloc(w.d_segs, (size_t)nqc * sc));
         CK(dalloc(w.d_zst, nqc));
@@ -416,6 +419,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     za.skip_coincident = ix->skip_coincident;
     za.seg_cap = w.seg_cap;
     za.qd = w.d_qd; za.planes = w.d_planes; za.bis_pos = w.d_bispos; za.segs = w.d_segs; za.zst = w.d_zst;
+    za.slice_r = w.d_slice_r;
     za.pstride = b.pstride;
     za.fault = w.d_counters + 4;
     mark(0);
@@ -450,6 +454,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
 
     VerifyArgs va;
     va.qd = w.d_qd; va.planes = w.d_planes; va.bis_pos = w.d_bispos; va.lc = b.pstride;
+    va.slice_r = w.d_slice_r;
     va.stage_cap = b.stage_cap;
     va.segs = w.d_segs; va.seg_cap = w.seg_cap;
     va.chunk_off = w.d_chunk_off; va.cand_off = w.d_cand_off; va.nq = nq;
@@ -1098,6 +1103,7 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     za.rmax = caps.rm;
     za.seg_cap = seg_cap;
     za.pstride = caps.lc;
+    za.slice_r = nullptr;
     za.qd = L.qd; za.planes = L.planes; za.bis_pos = L.bispos; za.segs = L.segs; za.zst = L.zst;
     za.fault = L.counters + 4;
     const size_t zsmem = zone_layout(caps).bytes * ZONE_WARPS;
@@ -1109,6 +1115,7 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
 
     VerifyArgs va;
     va.qd = L.qd; va.planes = L.planes; va.bis_pos = L.bispos; va.lc = caps.lc;
+    va.slice_r = nullptr;
     va.stage_cap = caps.lc;
     va.segs = L.segs; va.seg_cap = seg_cap;
     va.chunk_off = L.chunk_off; va.cand_off = L.cand_off; va.nq = 1;
@@ -1605,7 +1612,9 @@ extern "C" rknn_status rknn_index_tune(rknn_index* ix, const int32_t* q, const i
     s = time_batch(r.default_ms);
     if (s != RKNN_OK) return s;
     r.best_ms = r.default_ms;
-    const float fpcs[3] = {1.0f, 2.0f, 4.0f}, upcs[3] = {4.0f, 8.0f, 16.0f};
+    // stage 1: grid densities (finer ones pay off on clustered data), with
+    // the verification shape on entry; stage 2: the verification shape
+    const float fpcs[5] = {0.25f, 0.5f, 1.0f, 2.0f, 4.0f}, upcs[5] = {1.0f, 2.0f, 4.0f, 8.0f, 16.0f};
     const int upts[3] = {2, 4, 8}, vws[3] = {4, 8, 16};
     for (float fpc : fpcs)
         for (float upc : upcs) {
@@ -1614,19 +1623,34 @@ extern "C" rknn_status rknn_index_tune(rknn_index* ix, const int32_t* q, const i
                 s = build_grids(ix, fpc, upc);
             }
             if (s != RKNN_OK) return s;
-            for (int upt : upts)
-                for (int vw : vws) {
-                    ix->vupt = upt;
-                    ix->vwarps = vw;
-                    double ms = 0;
-                    s = time_batch(ms);
-                    if (s != RKNN_OK) return s;
-                    r.trials++;
-                    if (ms < r.best_ms) {
-                        r.best_ms = ms;
-                        r.fac_per_cell = fpc; r.usr_per_cell = upc; r.users_per_thread = upt; r.verify_warps = vw;
-                    }
-                }
+            double ms = 0;
+            s = time_batch(ms);
+            if (s != RKNN_OK) return s;
+            r.trials++;
+            if (ms < r.best_ms) {
+                r.best_ms = ms;
+                r.fac_per_cell = fpc;
+                r.usr_per_cell = upc;
+            }
+        }
+    {
+        std::lock_guard<std::mutex> lk(ix->mu);
+        s = build_grids(ix, r.fac_per_cell, r.usr_per_cell);
+    }
+    if (s != RKNN_OK) return s;
+    for (int upt : upts)
+        for (int vw : vws) {
+            ix->vupt = upt;
+            ix->vwarps = vw;
+            double ms = 0;
+            s = time_batch(ms);
+            if (s != RKNN_OK) return s;
+            r.trials++;
+            if (ms < r.best_ms) {
+                r.best_ms = ms;
+                r.users_per_thread = upt;
+                r.verify_warps = vw;
+            }
         }
     {
         std::lock_guard<std::mutex> lk(ix->mu);

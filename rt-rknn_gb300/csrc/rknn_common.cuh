@@ -48,6 +48,7 @@ constexpr int QF_ZONE_V_OVERFLOW = 1;    // vertex capacity reached: zone stoppe
 constexpr int QF_ZONE_L_OVERFLOW = 2;    // bisector capacity reached
 constexpr int QF_ZONE_PQ_OVERFLOW = 4;   // priority queue full
 constexpr int QF_ALL_USERS = 8;          // cell scan gave up: every user is a candidate
+constexpr int QF_SLICE_R = 64;           // slice bounds of the query are in slice_r (32 floats)
 constexpr int QF_RESULT_OVERFLOW = 16;   // result pool too small
 constexpr int QF_BAD_QUERY = 32;         // q or k out of range
 

@@ -200,6 +200,11 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
         int n = 0;              // this slice's heap size
         int nL = 0;             // half-planes kept (warp-uniform)
         int rho_ring = -1;      // first ring with a streamed facility left out of the half-planes
+        float rho_skip = INFINITY;   // nearest skipped cell
+        const int fbudget = max(8192, 128 * k);
+        // cell boxes widened for the rounding of the cell function
+        const float cmargin = 1e-5f * A.gf.cs + 8.0f * kU32 * (fabsf(A.gf.x0) + fabsf(A.gf.y0) + fabsf(qf.x) + fabsf(qf.y) +
+                                                               A.gf.cs * (float)max(A.gf.gx, A.gf.gy));
         const int qcx = cell_coord(qf.x, A.gf.x0, A.gf.inv, A.gf.gx);
         const int qcy = cell_coord(qf.y, A.gf.y0, A.gf.inv, A.gf.gy);
         const int rmaxf = max(max(qcx, A.gf.gx - 1 - qcx), max(qcy, A.gf.gy - 1 - qcy));
@@ -209,6 +214,7 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
             // stop when no facility at or beyond this ring can change a
             // slice's effective bound min(R, C)
             const float Rl = fminf((n < k) ? INFINITY : H[lane], clip);
+            __syncwarp();
             float Rmax = Rl;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) Rmax = fmaxf(Rmax, __shfl_xor_sync(FULL, Rmax, o));
@@ -216,28 +222,73 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
                 const double Lr = (double)(ring - 1) * (double)A.gf.cs - slack;
                 if (Lr > 0.0 && 0.5 * Lr > (double)Rmax * (1.0 + 1e-6)) break;
             }
-            // the ring as facility ranges (cells are row-major): its top and
-            // bottom rows, then the left and right cells of the rows between
-            const int nrange = ring == 0 ? 1 : 2 + 2 * (2 * ring - 1);
+            // Every heap top is an upper bound at any time, so the stream may
+            // stop early; past a budget the remaining (sparse-direction)
+            // slices keep their bounds and the kept region grows instead.
+            if (zs.pts >= fbudget) break;
+            // Window maxima of the bounds for the ring: a facility helps only
+            // slices within 8 of its own, so a cell whose facilities are all
+            // farther than twice the largest bound of the slices within 8 of
+            // those the cell spans can enter no heap and is skipped.  (Rs
+            // serves as scratch until the stream ends.)
+            {
+                float Rw = Rl;
+#pragma unroll
+                for (int dd = 1; dd <= 8; ++dd)
+                    Rw = fmaxf(Rw, fmaxf(__shfl_sync(FULL, Rl, (lane + dd) & 31), __shfl_sync(FULL, Rl, (lane - dd) & 31)));
+                Rs[lane] = Rw;
+                __syncwarp();
+            }
+            // the ring's cells (8 ring of them, 1 for ring 0), one range each
+            const int nrange = ring == 0 ? 1 : 8 * ring;
             for (int r0 = 0; r0 < nrange; r0 += 32) {
                 const int ri = r0 + lane;
                 int fs = 0, fe = 0;
+                float skipped_at = INFINITY;
                 if (ri < nrange) {
-                    int y = 0, x0 = 0, x1 = -1;
-                    if (ring == 0) { y = qcy; x0 = x1 = qcx; }
-                    else if (ri == 0) { y = qcy - ring; x0 = qcx - ring; x1 = qcx + ring; }
-                    else if (ri == 1) { y = qcy + ring; x0 = qcx - ring; x1 = qcx + ring; }
-                    else {
-                        const int m = ri - 2;              // 0 .. 2(2 ring - 1) - 1
-                        y = qcy - ring + 1 + (m >> 1);
-                        x0 = x1 = (m & 1) ? qcx + ring : qcx - ring;
+                    int cxx = qcx, cyy = qcy;
+                    if (ring > 0) {
+                        const int side = 2 * ring + 1;
+                        if (ri < side) { cxx = qcx - ring + ri; cyy = qcy - ring; }
+                        else if (ri < 2 * side) { cxx = qcx - ring + (ri - side); cyy = qcy + ring; }
+                        else if (ri < 2 * side + (2 * ring - 1)) { cxx = qcx - ring; cyy = qcy - ring + 1 + (ri - 2 * side); }
+                        else { cxx = qcx + ring; cyy = qcy - ring + 1 + (ri - 2 * side - (2 * ring - 1)); }
                     }
-                    x0 = max(x0, 0);
-                    x1 = min(x1, gx - 1);
-                    if (y >= 0 && y < gy && x0 <= x1) {
-                        fs = A.fstart[SX((long long)y * gx + x0, NCF + 1, 312)];
-                        fe = A.fstart[SX((long long)y * gx + x1 + 1, NCF + 1, 313)];
+                    if (cxx >= 0 && cxx < gx && cyy >= 0 && cyy < gy) {
+                        const long long cid = (long long)cyy * gx + cxx;
+                        fs = A.fstart[SX(cid, NCF + 1, 312)];
+                        fe = A.fstart[SX(cid + 1, NCF + 1, 313)];
+                        if (ring > 0 && fe > fs) {
+                            // the cell's box widened for the cell function's rounding
+                            const float X0 = A.gf.x0 + (float)cxx * A.gf.cs - cmargin, X1 = A.gf.x0 + (float)(cxx + 1) * A.gf.cs + cmargin;
+                            const float Y0 = A.gf.y0 + (float)cyy * A.gf.cs - cmargin, Y1 = A.gf.y0 + (float)(cyy + 1) * A.gf.cs + cmargin;
+                            const float ddx = fmaxf(fmaxf(X0 - qf.x, qf.x - X1), 0.0f), ddy = fmaxf(fmaxf(Y0 - qf.y, qf.y - Y1), 0.0f);
+                            const float Lc = sqrtf(fmaf(ddx, ddx, ddy * ddy)) * (1.0f - 1e-6f);
+                            const float cxm = 0.5f * (X0 + X1) - qf.x, cym = 0.5f * (Y0 + Y1) - qf.y;
+                            const float dc = sqrtf(fmaf(cxm, cxm, cym * cym));
+                            const float hd = 0.5f * sqrtf(fmaf(X1 - X0, X1 - X0, (Y1 - Y0) * (Y1 - Y0)));
+                            if (dc > 1.01f * hd) {
+                                float th = atan2f(cym, cxm);
+                                if (th < 0.0f) th += TWO_PI_F;
+                                const float al = asinf(fminf(1.0f, hd / dc)) * 1.001f + WIDEN;
+                                const int s0 = (int)floorf((th - al) * (1.0f / SLICE_W));
+                                const int s1 = (int)floorf((th + al) * (1.0f / SLICE_W));
+                                float Rc = 0.0f;
+                                for (int sl = s0; sl <= s1 && sl <= s0 + NS; ++sl) Rc = fmaxf(Rc, Rs[((sl % NS) + NS) % NS]);
+                                if (0.5f * Lc > Rc * (1.0f + 1e-6f)) {
+                                    skipped_at = Lc;
+                                    fe = fs;
+                                }
+                            }
+                        }
                     }
+                }
+                // every facility outside the half-planes stays at least rho from q
+                {
+                    float m = skipped_at;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(FULL, m, o));
+                    rho_skip = fminf(rho_skip, m);
                 }
                 // flatten the ranges: inclusive prefix of their lengths
                 const int len = fe - fs;
@@ -280,8 +331,31 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
                     if (nL + __popc(pm) > LC && rho_ring < 0) rho_ring = ring;
                     nL = min(LC, nL + __popc(pm));
                     zs.pts += __popc(pm);
-                    // every lane offers every streamed facility to its slice
+                    // A facility has finite arcs only for slices within 90 degrees
+                    // of its direction (the 8 slices on either side of its own,
+                    // counting the widening) and every arc is at least half its
+                    // distance: when that exceeds the largest bound R among
+                    // them it can enter no heap.  Bounds only shrink, so the
+                    // window maxima taken before the batch are conservative.
                     unsigned m = pm;
+                    {
+                        const float Rl = (n < k) ? INFINITY : H[lane];
+                        float Rw = Rl;
+#pragma unroll
+                        for (int dd = 1; dd <= 8; ++dd)
+                            Rw = fmaxf(Rw, fmaxf(__shfl_sync(FULL, Rl, (lane + dd) & 31),
+                                                 __shfl_sync(FULL, Rl, (lane - dd) & 31)));
+                        int sj = 0;
+                        if (ok) {
+                            float th = atan2f(vy, vx);
+                            if (th < 0.0f) th += TWO_PI_F;
+                            sj = min(NS - 1, max(0, (int)(th * (1.0f / SLICE_W))));
+                        }
+                        const float Rwj = __shfl_sync(FULL, Rw, sj);
+                        const bool useful = ok && !(0.25f * fmaf(vx, vx, vy * vy) * (1.0f - 4.0f * kU32) >= Rwj * Rwj);
+                        m = __ballot_sync(FULL, useful);
+                    }
+                    // every lane offers every useful facility to its slice
                     while (m) {
                         const int src = __ffs(m) - 1;
                         m &= m - 1;
@@ -304,6 +378,7 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
                 const double Lr = (double)(rho_ring - 1) * (double)A.gf.cs - slack;
                 rho = Lr > 0.0 ? __double2float_rd(Lr) : 0.0f;
             }
+            rho = fminf(rho, rho_skip);
         }
         __syncwarp();
         // R(P): k-th smallest arc, rounded up for the user test, and clipped
@@ -311,6 +386,7 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
         {
             const float R = (n < k) ? INFINITY : H[lane];
             Rs[lane] = fminf(R < INFINITY ? R * (1.0f + 1e-5f) + 1e-30f : INFINITY, clip);
+            A.slice_r[(size_t)s * 32 + lane] = Rs[lane];
         }
         __syncwarp();
         zs.cyc[0] += clock64() - tph;
@@ -376,24 +452,23 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
                         const float Y1 = (gu.y0 + (float)(cyy + 1) * gu.cs) - qf.y + delta;
                         if (X0 <= 0.0f && X1 >= 0.0f && Y0 <= 0.0f && Y1 >= 0.0f) keep = true;
                         else {
-                            // nearest point of the cell, and the slices the cell spans
+                            // nearest point of the cell, and the slices the cell
+                            // spans: its box lies in the disc of the half-diagonal
+                            // hd around its centre, which subtends asin(hd/dc)
                             const float ddx = fmaxf(fmaxf(X0, -X1), 0.0f), ddy = fmaxf(fmaxf(Y0, -Y1), 0.0f);
                             const float dmin2 = fmaf(ddx, ddx, ddy * ddy) * (1.0f - 4.0f * kU32);
-                            const float pc = atan2f(0.5f * (Y0 + Y1), 0.5f * (X0 + X1));
-                            float lo = 0.0f, hi = 0.0f;
-                            const float cxs[4] = {X0, X1, X0, X1}, cys[4] = {Y0, Y0, Y1, Y1};
-#pragma unroll
-                            for (int c4 = 0; c4 < 4; ++c4) {
-                                float d = atan2f(cys[c4], cxs[c4]) - pc;
-                                if (d > 3.14159265f) d -= TWO_PI_F;
-                                if (d < -3.14159265f) d += TWO_PI_F;
-                                lo = fminf(lo, d);
-                                hi = fmaxf(hi, d);
+                            const float cxm = 0.5f * (X0 + X1), cym = 0.5f * (Y0 + Y1);
+                            const float dc = sqrtf(fmaf(cxm, cxm, cym * cym));
+                            const float hd = 0.5f * sqrtf(fmaf(X1 - X0, X1 - X0, (Y1 - Y0) * (Y1 - Y0)));
+                            float Rmax = INFINITY;
+                            if (dc > 1.01f * hd) {
+                                const float pc = atan2f(cym, cxm);
+                                const float al = asinf(fminf(1.0f, hd / dc)) * 1.001f + WIDEN;
+                                const int s0 = (int)floorf((pc - al) / SLICE_W);
+                                const int s1 = (int)floorf((pc + al) / SLICE_W);
+                                Rmax = 0.0f;
+                                for (int sl = s0; sl <= s1 && sl <= s0 + NS; ++sl) Rmax = fmaxf(Rmax, Rs[((sl % NS) + NS) % NS]);
                             }
-                            const int s0 = (int)floorf((pc + lo - WIDEN) / SLICE_W);
-                            const int s1 = (int)floorf((pc + hi + WIDEN) / SLICE_W);
-                            float Rmax = 0.0f;
-                            for (int sl = s0; sl <= s1 && sl <= s0 + NS; ++sl) Rmax = fmaxf(Rmax, Rs[((sl % NS) + NS) % NS]);
                             keep = !(dmin2 > Rmax * Rmax);
                         }
                     }
@@ -414,7 +489,7 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
         // ---- segments: one user range per row ------------------------------
         int2* seg = A.segs + (size_t)s * A.seg_cap;
         int nseg = 0, ncand = 0;
-        int qflags = 0;
+        int qflags = QF_SLICE_R;
         if (all_users) {
             seg[0] = make_int2(0, 0);
             seg[1] = make_int2(0, A.nu);

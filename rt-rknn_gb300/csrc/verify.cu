@@ -217,6 +217,23 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
             }
             s_cand += valid[t];
         }
+        // a user beyond its slice's bound R(P) has k facilities strictly nearer
+        // than q (the slice filter's rule): drop it before the half-planes.
+        // Slices were widened by 2^-14 rad, far beyond atan2f's error, so the
+        // computed angle's slice is one whose bound holds for the user.
+        if (d.flags & QF_SLICE_R) {
+            const float* Rq = A.slice_r + (size_t)s * 32;
+#pragma unroll
+            for (int t = 0; t < UPT; ++t) {
+                if (!valid[t]) continue;
+                const float dx = u[t].x - d.qx, dy = u[t].y - d.qy;
+                float th = atan2f(dy, dx);
+                if (th < 0.0f) th += 6.28318530717958647692f;
+                const int si = min(31, max(0, (int)(th * (32.0f / 6.28318530717958647692f))));
+                const float Rs = Rq[si];
+                if (fmaf(dx, dx, dy * dy) * (1.0f - 1e-6f) > Rs * Rs) valid[t] = false;
+            }
+        }
         int cnt[UPT], und[UPT];
         const int nbs = min(d.nb, A.stage_cap);
         if (A.mode == MODE_FP32) filter_users<float, UPT>(d, nbs, sp, pos, u, valid, cnt, und, s_evals);

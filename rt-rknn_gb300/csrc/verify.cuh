@@ -36,6 +36,7 @@ struct VerifyArgs {
     int nu, nf, ncf;         // array sizes (bounds-checked builds)
     long long pool_cap;
     int* dropped;            // set when a slot had more results than its region
+    const float* slice_r;    // [slot][32] slice bounds (queries flagged QF_SLICE_R)
     int2* surv;              // survivors of the half-plane filter: (slot, user position)
     int surv_cap;            // 0: no list (the verification kernel recounts in-warp)
     int* surv_count;

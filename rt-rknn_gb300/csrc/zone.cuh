@@ -119,6 +119,7 @@ struct ZoneArgs {
     float4* planes;          // [slot][pstride]
     int* bis_pos;            // [slot][pstride] facility positions of the bisectors
     int pstride;             // >= caps.lc: row stride of planes / bis_pos
+    float* slice_r;          // [slot][32]: the slice filter's bounds R(P) (slice kernel)
     int2* segs;              // [slot][seg_cap]: (user start, candidate offset)
     ZStats* zst;
     int* fault;              // checked builds: {flag, array id, index, capacity, line}
