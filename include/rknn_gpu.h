@@ -86,7 +86,8 @@ typedef struct {
     int64_t results;        /* result ids returned */
     int64_t bisectors;      /* influence-zone bisectors created */
     int64_t zone_vertices_max;
-    int64_t zone_candidates;/* bisector intersections considered */
+    int64_t zone_candidates;/* bisector intersections considered (slice filter:
+                               facilities offered to the slice heaps) */
     int64_t zone_fp64;      /* intersections computed in double precision */
     int64_t candidates;     /* users tested against the half-planes */
     int64_t plane_evals;    /* (user, half-plane) evaluations */
@@ -97,7 +98,9 @@ typedef struct {
     double device_ms;       /* device time of the last launch sequence */
     int64_t zone_cycles[8]; /* zone kernel SM cycles by phase, summed over queries: ring
                                expansion, pop + rules, vertex test, vertex count pass,
-                               candidate intersections, dedup, counts/erase/append, epilogue */
+                               candidate intersections, dedup, counts/erase/append, epilogue.
+                               The slice filter fills 0 facility stream, 1 heap offers (part
+                               of 0), 2 user-cell ring scan, 7 half-planes and segments */
     int64_t zone_points;    /* facilities taken from the zone search's queue */
     int64_t zone_cells;     /* facility grid cells taken from the queue */
 } rknn_query_stats;
@@ -157,6 +160,15 @@ rknn_status rknn_query_batch(rknn_index* idx, const int32_t* q_index, const int3
                              int32_t nq, int32_t mode, int32_t* out_ids, int64_t cap,
                              int64_t* offsets, rknn_query_stats* stats);
 
+/* Page-locked host memory for rknn_query_batch's out_ids (and any other
+ * buffer).  The batch call copies result ids straight into a page-locked
+ * out_ids, in the same stream round trip as the offsets when the batch
+ * returns no more ids than the previous batch plus a quarter plus 4096;
+ * pageable buffers go through a staging copy.  No counterpart in the
+ * reference (its host arrays are std::vector). */
+rknn_status rknn_host_alloc(int64_t bytes, void** out);
+rknn_status rknn_host_free(void* p);
+
 /* Device-resident form: q_index/k are device pointers; results stay on the
  * device (see rknn_batch_device_results).  kmax bounds every k[i] (it sizes
  * the zone state; a larger k is still answered exactly, with the zone cut
@@ -166,7 +178,10 @@ rknn_status rknn_query_batch_device(rknn_index* idx, const int32_t* d_q_index,
                                     const int32_t* d_k, int32_t nq, int32_t kmax, int32_t mode);
 
 /* Device pointers to the last device batch's results: ids and nq+1 int32
- * offsets.  Valid until the next query call on this index. */
+ * offsets.  Synchronizes the index's stream; when a query's results outgrew
+ * the room the batch gave them, runs the batch again (from the workspace's
+ * copies of q and k) so that the results are complete.  Valid until the next
+ * query call on this index. */
 rknn_status rknn_batch_device_results(rknn_index* idx, const int32_t** d_ids,
                                       const int32_t** d_offsets);
 
@@ -190,7 +205,8 @@ rknn_status rknn_last_zone(rknn_index* idx, int32_t slot, int32_t* bis_fac, int3
 rknn_status rknn_set_profiling(rknn_index* idx, int32_t on);
 
 /* Device time of each kernel of the last profiled call, in milliseconds:
- * ms[0] zone, ms[1] plan, ms[2] verify, ms[3] result offsets, ms[4] finalize. */
+ * ms[0] zone (or slice filter), ms[1] plan, ms[2] verify, ms[3] exact
+ * recount of the survivors, ms[4] result offsets, ms[5] finalize. */
 rknn_status rknn_last_kernel_ms(rknn_index* idx, double* ms);
 
 /* ---- Serving: continuous batching over a resident index ----------------

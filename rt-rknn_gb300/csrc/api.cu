@@ -9,7 +9,8 @@
 //   verify_kernel    persistent warps over 128-user work items: half-plane
 //                    filter, exact recount, warp-aggregated result append
 //   scan_counts      result offsets
-//   finalize_kernel  one block per query: sort its ids into the output
+//   finalize_kernel  one warp per query (the block for large sets): sort its
+//                    ids into the output
 #include "../../include/rknn_gpu.h"
 #include "index.cuh"
 #include "rknn_common.cuh"
@@ -131,9 +132,11 @@ struct rknn_index {
     std::mutex mu;
     rknn_query_stats last{};
     int last_nq = 0, last_mode = 0, last_lc = 0;
+    long long last_total = 0;   // ids the previous host batch returned
+    int dev_nq = 0, dev_kmax = 0, dev_mode = 0;   // the last device batch (0: none pending a check)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int profiling = 0;
-    cudaEvent_t kev[6] = {};
+    cudaEvent_t kev[7] = {};
 };
 
 namespace {
@@ -187,13 +190,20 @@ struct ZoneLaunch {
     int grid;
 };
 
-ZoneLaunch zone_launch(rknn_index* ix, const ZoneCaps& c, int nq, bool slice = false)
+// The slice filter's kernel for a class whose largest k is kmax.
+using ZoneFn = void (*)(ZoneArgs);
+ZoneFn slice_fn(int kmax)
+{
+    return kmax <= 16 ? slice_kernel_r16 : kmax <= 32 ? slice_kernel_r32 : slice_kernel;
+}
+
+ZoneLaunch zone_launch(rknn_index* ix, const ZoneCaps& c, int nq, bool slice = false, int kmax = 0)
 {
     ZoneLaunch L;
     L.slice = slice ? slice_layout(c).bytes : zone_layout(c).bytes;
     L.smem = L.slice * ZONE_WARPS;
     int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, slice ? slice_kernel : zone_kernel_smem,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, slice ? slice_fn(kmax) : zone_kernel_smem,
                                                   32 * ZONE_WARPS, L.smem);
     if (per_sm < 1) per_sm = 1;
     long long want = (nq + ZONE_WARPS - 1) / ZONE_WARPS;
@@ -365,7 +375,7 @@ BatchPlan plan_batch(rknn_index* ix, int nq, int mode, bool use_order, const int
     for (auto& c : b.cls) {
         c.slice = use_slice(ix, c.kmax);
         c.caps = c.slice ? slice_caps(c.kmax, std::min(512, stage_max)) : caps_fit(ix, caps_for(c.kmax));
-        c.zl = zone_launch(ix, c.caps, c.n, c.slice);
+        c.zl = zone_launch(ix, c.caps, c.n, c.slice, c.kmax);
         b.pstride = std::max(b.pstride, c.caps.lc);
         b.key.push_back(c.n);
         b.key.push_back(c.kmax);
@@ -436,7 +446,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
         za.rmax = z.caps.rm;
         za.work_counter = w.d_counters + 16 + i;
         cudaStream_t zs = i == 0 ? st : w.aux[(i - 1) % NAUX];
-        if (z.slice) slice_kernel<<<z.zl.grid, 32, z.zl.smem, zs>>>(za);
+        if (z.slice) slice_fn(z.kmax)<<<z.zl.grid, 32, z.zl.smem, zs>>>(za);
         else zone_kernel_smem<<<z.zl.grid, 32 * ZONE_WARPS, z.zl.smem, zs>>>(za);
         CK(cudaGetLastError());
     }
@@ -466,17 +476,18 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     va.surv = w.d_surv; va.surv_cap = (int)std::min<long long>(w.surv_cap, INT32_MAX); va.surv_count = w.d_counters + 3;
     verify_fn(b.vupt)<<<b.vgrid, b.vwarps * 32, b.vsmem, st>>>(va);
     CK(cudaGetLastError());
+    mark(3);
     recount_kernel<<<ix->num_sms * 8, 256, 0, st>>>(va);
     CK(cudaGetLastError());
-    mark(3);
+    mark(4);
 
     scan_counts_kernel<<<1, 1024, 0, st>>>(w.d_res_count, w.d_cand_off, nq, w.d_out_off);
     CK(cudaGetLastError());
-    mark(4);
-    finalize_kernel<<<nq, 256, SORT_CAP * sizeof(unsigned), st>>>(w.d_pool, w.d_cand_off, w.d_res_count,
-                                                                  w.d_out_off, w.d_out, nq);
-    CK(cudaGetLastError());
     mark(5);
+    finalize_kernel<<<(nq + FIN_WARPS - 1) / FIN_WARPS, 32 * FIN_WARPS, 0, st>>>(
+        w.d_pool, w.d_cand_off, w.d_res_count, w.d_out_off, w.d_out, nq);
+    CK(cudaGetLastError());
+    mark(6);
     return RKNN_OK;
 }
 
@@ -544,7 +555,12 @@ rknn_status collect_stats(Ctx& c, int nq, rknn_query_stats* out)
 
 // Run a batch whose q/k are already in ws.d_q / ws.d_k.  Grows the result
 // pool and reruns when a query's candidate region did not fit.
-rknn_status run_sync(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = true)
+// Launch, read the offsets and counters back, and rerun when a region or the
+// pool was too small.  spec (page-locked, spec_n ids) takes a speculative copy
+// of the first spec_n result ids in the same stream round trip: when the batch
+// returned at most spec_n ids the caller needs no second copy.
+rknn_status run_sync(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = true, int* spec = nullptr,
+                     long long spec_n = 0)
 {
     Workspace& w = c.w;
     const int nq = b.nq;
@@ -563,6 +579,8 @@ rknn_status run_sync(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = tr
         CK(cudaMemcpyAsync(flags, w.d_counters + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.st));
         const int& dropped = flags[0];
         CK(cudaMemcpyAsync(w.h_off, w.d_out_off, sizeof(int) * (nq + 1), cudaMemcpyDeviceToHost, c.st));
+        const long long sn = std::min(spec_n, w.pool_cap);
+        if (spec && sn > 0) CK(cudaMemcpyAsync(spec, w.d_out, sizeof(int) * sn, cudaMemcpyDeviceToHost, c.st));
         CK(cudaStreamSynchronize(c.st));
         float ms = 0;
         cudaEventElapsedTime(&ms, c.ev0, c.ev1);
@@ -725,10 +743,11 @@ rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf, 
     // asks for what its plan needs)
     CKB(allow_dynamic_smem((const void*)zone_kernel_smem, optin));
     CKB(allow_dynamic_smem((const void*)slice_kernel, optin));
+    CKB(allow_dynamic_smem((const void*)slice_kernel_r16, optin));
+    CKB(allow_dynamic_smem((const void*)slice_kernel_r32, optin));
     CKB(allow_dynamic_smem((const void*)verify_kernel, optin));
     CKB(allow_dynamic_smem((const void*)verify_kernel_u2, optin));
     CKB(allow_dynamic_smem((const void*)verify_kernel_u8, optin));
-    CKB(allow_dynamic_smem((const void*)finalize_kernel, optin));
 
     if (o.users_per_thread != 0 && o.users_per_thread != 2 && o.users_per_thread != 4 && o.users_per_thread != 8)
         return bail(fail(RKNN_ERR_ARG, "users_per_thread must be 2, 4 or 8"));
@@ -765,7 +784,7 @@ rknn_status rknn_index_destroy(rknn_index* ix)
     cudaFree(ix->d_fin); cudaFree(ix->d_uin); cudaFree(ix->d_uidin);
     if (ix->ev0) cudaEventDestroy(ix->ev0);
     if (ix->ev1) cudaEventDestroy(ix->ev1);
-    for (int i = 0; i < 6; ++i) if (ix->kev[i]) cudaEventDestroy(ix->kev[i]);
+    for (int i = 0; i < 7; ++i) if (ix->kev[i]) cudaEventDestroy(ix->kev[i]);
     if (ix->own_stream) cudaStreamDestroy(ix->own_stream);
     delete ix;
     return RKNN_OK;
@@ -797,7 +816,7 @@ rknn_status rknn_set_profiling(rknn_index* ix, int32_t on)
     if (!ix) return fail(RKNN_ERR_ARG, "index is null");
     std::lock_guard<std::mutex> lk(ix->mu);
     if (on && !ix->kev[0])
-        for (int i = 0; i < 6; ++i) CK(cudaEventCreate(&ix->kev[i]));
+        for (int i = 0; i < 7; ++i) CK(cudaEventCreate(&ix->kev[i]));
     ix->profiling = on ? 1 : 0;
     return RKNN_OK;
 }
@@ -806,8 +825,8 @@ rknn_status rknn_last_kernel_ms(rknn_index* ix, double* ms)
 {
     if (!ix || !ms) return fail(RKNN_ERR_ARG, "null argument");
     if (!ix->kev[0]) return fail(RKNN_ERR_STATE, "profiling was never enabled");
-    CK(cudaEventSynchronize(ix->kev[5]));
-    for (int i = 0; i < 5; ++i) {
+    CK(cudaEventSynchronize(ix->kev[6]));
+    for (int i = 0; i < 6; ++i) {
         float t = 0;
         CK(cudaEventElapsedTime(&t, ix->kev[i], ix->kev[i + 1]));
         ms[i] = t;
@@ -823,6 +842,19 @@ rknn_status rknn_debug_zone_fault(rknn_index* ix, int32_t* out5)
     if (!ix || !out5 || !ix->ws.d_counters) return fail(RKNN_ERR_ARG, "no workspace");
     CK(cudaMemcpy(out5, ix->ws.d_counters + 4, sizeof(int) * 5, cudaMemcpyDeviceToHost));
     if (!out5[0]) CK(cudaMemcpy(out5, ix->ws.d_counters + 10, sizeof(int) * 5, cudaMemcpyDeviceToHost));
+    return RKNN_OK;
+}
+
+// Per-query zone statistics of the last call (nq records of the kernel's
+// ZStats layout: 8 ints, then 8 int64 cycle counters).  Not part of the
+// public header; used by profiling runs.
+rknn_status rknn_debug_zone_stats(rknn_index* ix, void* out, int32_t nq)
+{
+    if (!ix || !out || nq < 0 || !ix->ws.d_zst) return fail(RKNN_ERR_ARG, "no workspace");
+    std::lock_guard<std::mutex> lk(ix->mu);
+    if (nq > ix->last_nq) return fail(RKNN_ERR_ARG, "more records than the last call's queries");
+    CK(cudaStreamSynchronize(ix->stream));
+    CK(cudaMemcpy(out, ix->ws.d_zst, sizeof(ZStats) * (size_t)nq, cudaMemcpyDeviceToHost));
     return RKNN_OK;
 }
 
@@ -858,6 +890,7 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
     if (s != RKNN_OK) return s;
     std::lock_guard<std::mutex> lk(ix->mu);
     CK(cudaSetDevice(ix->device));
+    ix->dev_nq = 0;     // the workspace now holds this batch
     // descending k: the longest zones start first, and each k class gets its
     // own zone launch
     bool uniform = true;
@@ -883,13 +916,40 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
     }
     CK(cudaMemcpyAsync(w.d_q, w.h_q, sizeof(int) * nq, cudaMemcpyHostToDevice, ix->stream));
     CK(cudaMemcpyAsync(w.d_k, w.h_k, sizeof(int) * nq, cudaMemcpyHostToDevice, ix->stream));
-    s = run_sync(ix, c, b);
+    // The ids come back with the offsets when the batch returns no more than
+    // the previous one plus a margin: page-locked caller buffers take them
+    // directly, pageable ones through the workspace's page-locked staging.
+    bool locked = false;
+    if (out_ids && cap > 0) {
+        cudaPointerAttributes pa;
+        locked = cudaPointerGetAttributes(&pa, out_ids) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+    }
+    long long guess = ix->last_total + ix->last_total / 4 + 4096;
+    int* spec = nullptr;
+    if (locked) {
+        guess = std::min<long long>(guess, cap);
+        spec = out_ids;
+    } else if (out_ids && cap > 0) {
+        guess = std::min<long long>(guess, cap);
+        if (guess > w.h_ids_cap) {
+            cudaFreeHost(w.h_ids);
+            w.h_ids = nullptr;
+            w.h_ids_cap = 0;
+            const long long hc = std::max<long long>(guess, 1 << 16);
+            CK(cudaMallocHost(&w.h_ids, sizeof(int) * hc));
+            w.h_ids_cap = hc;
+        }
+        spec = w.h_ids;
+    }
+    s = run_sync(ix, c, b, true, spec, spec ? guess : 0);
     if (s != RKNN_OK) return s;
     ix->last_lc = b.pstride;
     const long long total = w.h_off[nq];
     for (int i = 0; i <= nq; ++i) offsets[i] = w.h_off[i];
     ix->last_nq = nq;
     ix->last_mode = mode;
+    ix->last_total = total;
     if (stats) {
         s = collect_stats(c, nq, stats);
         if (s != RKNN_OK) return s;
@@ -897,29 +957,37 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
     if (total > cap || (!out_ids && total > 0))
         return fail(RKNN_ERR_CAPACITY, "output buffer holds " + std::to_string(cap) + " ids, " +
                                            std::to_string(total) + " needed");
-    if (total > 0) {
-        // page-locked caller buffers take the copy directly; pageable ones
-        // through the workspace's page-locked staging buffer
-        cudaPointerAttributes pa;
-        const bool locked = cudaPointerGetAttributes(&pa, out_ids) == cudaSuccess && pa.type == cudaMemoryTypeHost;
-        cudaGetLastError();
-        if (locked) {
-            CK(cudaMemcpyAsync(out_ids, w.d_out, sizeof(int) * total, cudaMemcpyDeviceToHost, ix->stream));
-            CK(cudaStreamSynchronize(ix->stream));
-        } else {
-            if (total > w.h_ids_cap) {
-                cudaFreeHost(w.h_ids);
-                w.h_ids = nullptr;
-                w.h_ids_cap = 0;
-                const long long hc = std::max<long long>(total + total / 4, 1 << 16);
-                CK(cudaMallocHost(&w.h_ids, sizeof(int) * hc));
-                w.h_ids_cap = hc;
-            }
-            CK(cudaMemcpyAsync(w.h_ids, w.d_out, sizeof(int) * total, cudaMemcpyDeviceToHost, ix->stream));
-            CK(cudaStreamSynchronize(ix->stream));
-            std::memcpy(out_ids, w.h_ids, sizeof(int) * total);
+    if (total > 0 && total > std::min(guess, w.pool_cap)) {
+        // more ids than the speculative copy held: fetch them all
+        if (!locked && total > w.h_ids_cap) {
+            cudaFreeHost(w.h_ids);
+            w.h_ids = nullptr;
+            w.h_ids_cap = 0;
+            const long long hc = std::max<long long>(total + total / 4, 1 << 16);
+            CK(cudaMallocHost(&w.h_ids, sizeof(int) * hc));
+            w.h_ids_cap = hc;
         }
+        CK(cudaMemcpyAsync(locked ? out_ids : w.h_ids, w.d_out, sizeof(int) * total, cudaMemcpyDeviceToHost,
+                           ix->stream));
+        CK(cudaStreamSynchronize(ix->stream));
     }
+    if (total > 0 && !locked) std::memcpy(out_ids, w.h_ids, sizeof(int) * total);
+    return RKNN_OK;
+}
+
+rknn_status rknn_host_alloc(int64_t bytes, void** out)
+{
+    g_err.clear();
+    if (!out || bytes <= 0) return fail(RKNN_ERR_ARG, "bad argument");
+    *out = nullptr;
+    CK(cudaMallocHost(out, (size_t)bytes));
+    return RKNN_OK;
+}
+
+rknn_status rknn_host_free(void* p)
+{
+    g_err.clear();
+    if (p) CK(cudaFreeHost(p));
     return RKNN_OK;
 }
 
@@ -940,6 +1008,7 @@ rknn_status rknn_query_batch_device(rknn_index* ix, const int32_t* d_q, const in
     if (!ix || !d_q || !d_k || nq <= 0 || kmax <= 0) return fail(RKNN_ERR_ARG, "bad argument");
     if (mode != RKNN_MODE_FP32 && mode != RKNN_MODE_FP64) return fail(RKNN_ERR_ARG, "bad mode");
     std::lock_guard<std::mutex> lk(ix->mu);
+    CK(cudaSetDevice(ix->device));
     Workspace& w = ix->ws;
     const BatchPlan b = plan_batch(ix, nq, mode, false, nullptr, kmax);
     ix->last_lc = b.pstride;
@@ -951,12 +1020,38 @@ rknn_status rknn_query_batch_device(rknn_index* ix, const int32_t* d_q, const in
     s = launch(ix, c, b);
     ix->last_nq = nq;
     ix->last_mode = mode;
+    ix->dev_nq = s == RKNN_OK ? nq : 0;
+    ix->dev_kmax = kmax;
+    ix->dev_mode = mode;
     return s;
 }
 
 rknn_status rknn_batch_device_results(rknn_index* ix, const int32_t** d_ids, const int32_t** d_offsets)
 {
+    g_err.clear();
     if (!ix || !d_ids || !d_offsets) return fail(RKNN_ERR_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(ix->mu);
+    CK(cudaSetDevice(ix->device));
+    if (ix->dev_nq > 0) {
+        // a slot whose results outgrew its region, or regions that outgrew
+        // the pool, left the device batch incomplete: run it again (its q
+        // and k are still in the workspace) with room for all of them
+        Workspace& w = ix->ws;
+        const int nq = ix->dev_nq;
+        long long region_total = 0;
+        int dropped = 0;
+        CK(cudaMemcpyAsync(&region_total, w.d_cand_off + nq, sizeof(long long), cudaMemcpyDeviceToHost, ix->stream));
+        CK(cudaMemcpyAsync(&dropped, w.d_counters + 2, sizeof(int), cudaMemcpyDeviceToHost, ix->stream));
+        CK(cudaStreamSynchronize(ix->stream));
+        if (region_total > w.pool_cap || dropped) {
+            if (dropped) w.rcap = (int)std::min<long long>((long long)w.rcap * 8, std::max<long long>(ix->nu, 1));
+            const BatchPlan b = plan_batch(ix, nq, ix->dev_mode, false, nullptr, ix->dev_kmax);
+            Ctx c = main_ctx(ix);
+            rknn_status s = run_sync(ix, c, b);
+            if (s != RKNN_OK) return s;
+        }
+        ix->dev_nq = 0;
+    }
     *d_ids = ix->ws.d_out;
     *d_offsets = ix->ws.d_out_off;
     return RKNN_OK;
@@ -1130,8 +1225,7 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     CK(cudaGetLastError());
     scan_counts_kernel<<<1, 1024, 0, st>>>(L.res_count, L.cand_off, 1, L.out_off);
     CK(cudaGetLastError());
-    finalize_kernel<<<1, 256, SORT_CAP * sizeof(unsigned), st>>>(L.pool, L.cand_off, L.res_count, L.out_off,
-                                                                  L.out, 1);
+    finalize_kernel<<<1, 32 * FIN_WARPS, 0, st>>>(L.pool, L.cand_off, L.res_count, L.out_off, L.out, 1);
     CK(cudaGetLastError());
 
     QDesc d;

@@ -89,6 +89,26 @@ __device__ __forceinline__ float exit_dist(float qx, float qy, float ex, float e
     return t;
 }
 
+// Cell ri of the square ring at Chebyshev distance ring around (qcx, qcy):
+// bottom row, top row, then the left and right columns without corners.
+__device__ __forceinline__ void ring_cell(int ring, int ri, int qcx, int qcy, int& cxx, int& cyy)
+{
+    cxx = qcx;
+    cyy = qcy;
+    if (ring > 0) {
+        const int side = 2 * ring + 1;
+        if (ri < side) { cxx = qcx - ring + ri; cyy = qcy - ring; }
+        else if (ri < 2 * side) { cxx = qcx - ring + (ri - side); cyy = qcy + ring; }
+        else if (ri < 2 * side + (2 * ring - 1)) { cxx = qcx - ring; cyy = qcy - ring + 1 + (ri - 2 * side); }
+        else { cxx = qcx + ring; cyy = qcy - ring + 1 + (ri - 2 * side - (2 * ring - 1)); }
+    }
+}
+
+__device__ __forceinline__ void prefetch_l1(const void* p)
+{
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 // Max-heap of one slice, interleaved across lanes: entry i of lane l at
 // H[i * 32 + l] (all lanes touching the same level hit distinct banks).
 __device__ __forceinline__ void heap_insert(float* H, int lane, int& n, int cap, float v)
@@ -123,9 +143,25 @@ __device__ __forceinline__ void heap_insert(float* H, int lane, int& n, int cap,
     H[SX(i * 32 + lane, 32LL * cap, 307)] = v;
 }
 
+// The k smallest arcs of one slice as an ascending list of KR registers
+// (k <= KR): the first KR - k entries hold -inf and never move, the last k
+// the k smallest arcs so far (+inf while unfilled), so the k-th smallest is
+// always L[KR-1].  Inserting v and dropping the largest is branch-free:
+// entry i becomes min(old[i], max(old[i-1], v)).
+template <int KR>
+__device__ __forceinline__ void list_insert(float (&L)[KR], float v)
+{
+#pragma unroll
+    for (int i = KR - 1; i > 0; --i) L[i] = fminf(L[i], fmaxf(L[i - 1], v));
+    L[0] = fminf(L[0], v);
+}
+
 }  // namespace
 
-__global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
+// KR > 0: the slice bounds live in a register list (k <= KR); KR == 0: in a
+// shared-memory max-heap per lane (any k up to the class's capacity).
+template <int KR>
+__device__ __forceinline__ void slice_body(const ZoneArgs& A)
 {
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31;
@@ -158,7 +194,7 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
         const int k = A.k_in[s];
         QDesc* qd = A.qd + s;
         ZStats zs = {};
-        if (qin < 0 || qin >= A.nf || k <= 0 || k > KC) {
+        if (qin < 0 || qin >= A.nf || k <= 0) {
             if (lane == 0) {
                 QDesc d = {};
                 d.qpos = -1;
@@ -173,6 +209,29 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
         const int qpos = A.fpos[SX(qin, A.nf, 310)];
         const float2 qf = A.fxy[SX(qpos, A.nf, 311)];
         const double qx = qf.x, qy = qf.y;
+        if (k > KC || (KR > 0 && k > KR)) {
+            // k beyond the slice bounds' capacity (a device batch whose kmax
+            // understates a k): every user is a candidate and the
+            // verification counts exactly
+            if (lane == 0) {
+                QDesc d = {};
+                d.qx = qf.x;
+                d.qy = qf.y;
+                d.qpos = qpos;
+                d.k = k;
+                d.nseg = 1;
+                d.kf2 = 1e-30f;
+                d.kf264 = 1e-300;
+                d.ncand = A.nu;
+                d.flags = QF_ALL_USERS;
+                *qd = d;
+                A.zst[s] = zs;
+                int2* seg = A.segs + (size_t)s * A.seg_cap;
+                seg[0] = make_int2(0, 0);
+                seg[1] = make_int2(0, A.nu);
+            }
+            continue;
+        }
         long long tph = clock64();
 
         // C(P): farthest point of the box inside this slice, a vertex of the
@@ -184,10 +243,9 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
             const float bx1 = __double2float_ru(A.sx1), by1 = __double2float_ru(A.sy1);
             clip = fmaxf(exit_dist(qf.x, qf.y, e1x, e1y, bx0, by0, bx1, by1),
                          exit_dist(qf.x, qf.y, e2x, e2y, bx0, by0, bx1, by1));
-            const float cxs[4] = {bx0, bx1, bx0, bx1}, cys[4] = {by0, by0, by1, by1};
 #pragma unroll
             for (int c4 = 0; c4 < 4; ++c4) {
-                const float dx = cxs[c4] - qf.x, dy = cys[c4] - qf.y;
+                const float dx = ((c4 & 1) ? bx1 : bx0) - qf.x, dy = ((c4 & 2) ? by1 : by0) - qf.y;
                 // inside the cone (or near its edges: then the corner only raises the bound)
                 const float c1 = e1x * dy - e1y * dx, c2 = dx * e2y - dy * e2x;
                 const float tol = 1e-5f * (fabsf(dx) + fabsf(dy));
@@ -197,7 +255,12 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
         }
 
         // ---- stream facilities ring by ring -------------------------------
-        int n = 0;              // this slice's heap size
+        int n = 0;              // this slice's heap size (KR == 0)
+        float RL[KR > 0 ? KR : 1];   // this slice's k smallest arcs (KR > 0)
+#pragma unroll
+        for (int i = 0; i < (KR > 0 ? KR : 1); ++i) RL[i] = i < KR - k ? -INFINITY : INFINITY;
+        // the slice's current bound R: its k-th smallest arc (infinite below k)
+#define SLICE_KTH() (KR > 0 ? RL[(KR > 0 ? KR : 1) - 1] : ((n < k) ? INFINITY : H[lane]))
         int nL = 0;             // half-planes kept (warp-uniform)
         int rho_ring = -1;      // first ring with a streamed facility left out of the half-planes
         float rho_skip = INFINITY;   // nearest skipped cell
@@ -209,11 +272,34 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
         const int qcy = cell_coord(qf.y, A.gf.y0, A.gf.inv, A.gf.gy);
         const int rmaxf = max(max(qcx, A.gf.gx - 1 - qcx), max(qcy, A.gf.gy - 1 - qcy));
         const int gx = A.gf.gx, gy = A.gf.gy;
+        // Rings of up to 32 cells have their cell ranges loaded one ring
+        // ahead (lane = range index), so that the load latency overlaps the
+        // previous ring's work; ring 0's before the loop.
+        int pf_fs = 0, pf_fe = 0;
+        if (lane == 0) {
+            const long long cid = (long long)qcy * gx + qcx;
+            pf_fs = A.fstart[SX(cid, NCF + 1, 330)];
+            pf_fe = A.fstart[SX(cid + 1, NCF + 1, 331)];
+        }
         int ring = 0;
         for (; ring <= rmaxf; ++ring) {
+            const int cur_fs = pf_fs, cur_fe = pf_fe;
+            {
+                const int nr1 = 8 * (ring + 1);
+                pf_fs = pf_fe = 0;
+                if (nr1 <= 32 && ring + 1 <= rmaxf && lane < nr1) {
+                    int cxx, cyy;
+                    ring_cell(ring + 1, lane, qcx, qcy, cxx, cyy);
+                    if (cxx >= 0 && cxx < gx && cyy >= 0 && cyy < gy) {
+                        const long long cid = (long long)cyy * gx + cxx;
+                        pf_fs = A.fstart[SX(cid, NCF + 1, 332)];
+                        pf_fe = A.fstart[SX(cid + 1, NCF + 1, 333)];
+                    }
+                }
+            }
             // stop when no facility at or beyond this ring can change a
             // slice's effective bound min(R, C)
-            const float Rl = fminf((n < k) ? INFINITY : H[lane], clip);
+            const float Rl = fminf(SLICE_KTH(), clip);
             __syncwarp();
             float Rmax = Rl;
 #pragma unroll
@@ -246,18 +332,17 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
                 int fs = 0, fe = 0;
                 float skipped_at = INFINITY;
                 if (ri < nrange) {
-                    int cxx = qcx, cyy = qcy;
-                    if (ring > 0) {
-                        const int side = 2 * ring + 1;
-                        if (ri < side) { cxx = qcx - ring + ri; cyy = qcy - ring; }
-                        else if (ri < 2 * side) { cxx = qcx - ring + (ri - side); cyy = qcy + ring; }
-                        else if (ri < 2 * side + (2 * ring - 1)) { cxx = qcx - ring; cyy = qcy - ring + 1 + (ri - 2 * side); }
-                        else { cxx = qcx + ring; cyy = qcy - ring + 1 + (ri - 2 * side - (2 * ring - 1)); }
-                    }
+                    int cxx, cyy;
+                    ring_cell(ring, ri, qcx, qcy, cxx, cyy);
                     if (cxx >= 0 && cxx < gx && cyy >= 0 && cyy < gy) {
                         const long long cid = (long long)cyy * gx + cxx;
-                        fs = A.fstart[SX(cid, NCF + 1, 312)];
-                        fe = A.fstart[SX(cid + 1, NCF + 1, 313)];
+                        if (nrange <= 32) {
+                            fs = cur_fs;
+                            fe = cur_fe;
+                        } else {
+                            fs = A.fstart[SX(cid, NCF + 1, 312)];
+                            fe = A.fstart[SX(cid + 1, NCF + 1, 313)];
+                        }
                         if (ring > 0 && fe > fs) {
                             // the cell's box widened for the cell function's rounding
                             const float X0 = A.gf.x0 + (float)cxx * A.gf.cs - cmargin, X1 = A.gf.x0 + (float)(cxx + 1) * A.gf.cs + cmargin;
@@ -289,6 +374,11 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(FULL, m, o));
                     rho_skip = fminf(rho_skip, m);
+                }
+                // the next ring's facility lines, while this ring is streamed
+                if (r0 == 0 && pf_fe > pf_fs) {
+                    prefetch_l1(A.fxy + pf_fs);
+                    prefetch_l1(A.fxy + (pf_fe - 1));
                 }
                 // flatten the ranges: inclusive prefix of their lengths
                 const int len = fe - fs;
@@ -339,7 +429,7 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
                     // window maxima taken before the batch are conservative.
                     unsigned m = pm;
                     {
-                        const float Rl = (n < k) ? INFINITY : H[lane];
+                        const float Rl = SLICE_KTH();
                         float Rw = Rl;
 #pragma unroll
                         for (int dd = 1; dd <= 8; ++dd)
@@ -356,13 +446,35 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
                         m = __ballot_sync(FULL, useful);
                     }
                     // every lane offers every useful facility to its slice
-                    while (m) {
-                        const int src = __ffs(m) - 1;
-                        m &= m - 1;
-                        const float ux = __shfl_sync(FULL, vx, src), uy = __shfl_sync(FULL, vy, src);
-                        const float u = upper_arc(ux, uy, e1x, e1y, e2x, e2y);
-                        if (n < k || u < H[lane]) heap_insert(H, lane, n, k, u);
+                    zs.cand += __popc(m);
+                    const long long t_offer = clock64();
+                    if constexpr (KR > 0) {
+                        // two facilities per step: their arcs are independent
+                        while (m) {
+                            const int s1 = __ffs(m) - 1;
+                            m &= m - 1;
+                            const bool two = m != 0;
+                            const int s2 = two ? __ffs(m) - 1 : s1;
+                            m &= m - 1;
+                            const float ax = __shfl_sync(FULL, vx, s1), ay = __shfl_sync(FULL, vy, s1);
+                            const float bx = __shfl_sync(FULL, vx, s2), by = __shfl_sync(FULL, vy, s2);
+                            const float u1 = upper_arc(ax, ay, e1x, e1y, e2x, e2y);
+                            const float u2 = two ? upper_arc(bx, by, e1x, e1y, e2x, e2y) : INFINITY;
+                            if (__any_sync(FULL, fminf(u1, u2) < RL[(KR > 0 ? KR : 1) - 1])) {
+                                list_insert<KR>(RL, u1);
+                                list_insert<KR>(RL, u2);
+                            }
+                        }
+                    } else {
+                        while (m) {
+                            const int src = __ffs(m) - 1;
+                            m &= m - 1;
+                            const float ux = __shfl_sync(FULL, vx, src), uy = __shfl_sync(FULL, vy, src);
+                            const float u = upper_arc(ux, uy, e1x, e1y, e2x, e2y);
+                            if (n < k || u < H[lane]) heap_insert(H, lane, n, k, u);
+                        }
                     }
+                    zs.cyc[1] += clock64() - t_offer;
                 }
             }
             zs.cells += nrange;
@@ -384,7 +496,7 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
         // R(P): k-th smallest arc, rounded up for the user test, and clipped
         // to the box (no user lies farther)
         {
-            const float R = (n < k) ? INFINITY : H[lane];
+            const float R = SLICE_KTH();
             Rs[lane] = fminf(R < INFINITY ? R * (1.0f + 1e-5f) + 1e-30f : INFINITY, clip);
             A.slice_r[(size_t)s * 32 + lane] = Rs[lane];
         }
@@ -411,6 +523,9 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
         const float kf2 = (float)(8.0 * (double)kU32 * Fp * Fp * (1.0 + 1e-6)) + 1e-30f;
         const double k2f64 = 8.0 * kU64 * 2.0 * Fp * (1.0 + 1e-6);
         const double kf264 = 8.0 * kU64 * Fp * Fp * (1.0 + 1e-6) + 1e-300;
+
+        zs.cyc[7] += clock64() - tph;
+        tph = clock64();
 
         // ---- ring scan over user cells --------------------------------------
         const Grid gu = A.gu;
@@ -485,6 +600,8 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
             zs.rings = rend + 1;
         }
         __syncwarp();
+        zs.cyc[2] += clock64() - tph;
+        tph = clock64();
 
         // ---- segments: one user range per row ------------------------------
         int2* seg = A.segs + (size_t)s * A.seg_cap;
@@ -559,5 +676,11 @@ __global__ void __launch_bounds__(32) slice_kernel(ZoneArgs A)
         __syncwarp();
     }
 }
+
+#undef SLICE_KTH
+
+__global__ void __launch_bounds__(32, 1) slice_kernel(ZoneArgs A) { slice_body<0>(A); }
+__global__ void __launch_bounds__(32, 1) slice_kernel_r16(ZoneArgs A) { slice_body<16>(A); }
+__global__ void __launch_bounds__(32, 1) slice_kernel_r32(ZoneArgs A) { slice_body<32>(A); }
 
 }  // namespace rknn

@@ -119,6 +119,46 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
     }
     const int k = d.k;
     int m = 0;
+    if constexpr (sizeof(T) == 4) {
+        // FP32: users in pairs through the packed FMA (each half rounds as
+        // fmaf).  mv < -bu exactly when fl(mv + bu) is negative, and
+        // |mv| <= bu exactly when fl(|mv| - bu) <= 0: a nonzero exact sum of
+        // two floats never rounds to zero, and bu > 0 rules out -0.
+        constexpr int H2 = UPT / 2;
+        float2 X[H2], Y[H2], B[H2];
+        float umin[UPT];
+#pragma unroll
+        for (int h = 0; h < H2; ++h) {
+            X[h] = make_float2((float)x[2 * h], (float)x[2 * h + 1]);
+            Y[h] = make_float2((float)y[2 * h], (float)y[2 * h + 1]);
+            B[h] = make_float2((float)bu[2 * h], (float)bu[2 * h + 1]);
+        }
+#pragma unroll
+        for (int t = 0; t < UPT; ++t) umin[t] = INFINITY;
+        for (; m < nb; ++m) {
+            const float4 p = ((const float4*)sp)[m];
+            const float2 a2 = make_float2(p.x, p.x), b2 = make_float2(p.y, p.y), c2 = make_float2(p.z, p.z);
+#pragma unroll
+            for (int h = 0; h < H2; ++h) {
+                const float2 mv = __ffma2_rn(a2, X[h], __ffma2_rn(b2, Y[h], c2));
+                const float2 r = __fadd2_rn(mv, B[h]);
+                cnt[2 * h] += (int)(__float_as_uint(r.x) >> 31);
+                cnt[2 * h + 1] += (int)(__float_as_uint(r.y) >> 31);
+                umin[2 * h] = fminf(umin[2 * h], fabsf(mv.x) - B[h].x);
+                umin[2 * h + 1] = fminf(umin[2 * h + 1], fabsf(mv.y) - B[h].y);
+            }
+            if ((m & 7) == 7) {
+                bool done = true;
+#pragma unroll
+                for (int t = 0; t < UPT; ++t) done &= cnt[t] >= k;
+                if (__all_sync(FULL, done)) { ++m; break; }
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < UPT; ++t) und[t] = umin[t] <= 0.0f;
+        evals += (unsigned long long)m * nvalid;
+        return;
+    }
     for (; m < nb; ++m) {
         T a, b, c;
         if (sizeof(T) == 4) {
@@ -572,52 +612,107 @@ __device__ void block_radix_pass(const unsigned* in, unsigned* out, int n, int s
 }
 }  // namespace
 
-__global__ void __launch_bounds__(256)
+namespace {
+// ascending bitonic sort of n keys (padded to a power of two with the largest
+// key) by one warp in its shared segment
+__device__ void warp_bitonic(unsigned* seg, const unsigned* src, unsigned* dst, int n, int lane)
+{
+    int P = 64;
+    while (P < n) P <<= 1;
+    for (int i = lane; i < P; i += 32) seg[i] = i < n ? okey((int)src[i]) : 0xffffffffu;
+    __syncwarp();
+    for (int kk = 2; kk <= P; kk <<= 1) {
+        for (int j = kk >> 1; j > 0; j >>= 1) {
+            for (int t = lane; t < (P >> 1); t += 32) {
+                const int i = 2 * t - (t & (j - 1));     // lower index of the pair
+                const unsigned x = seg[i], y = seg[i + j];
+                if ((x > y) == ((i & kk) == 0)) { seg[i] = y; seg[i + j] = x; }
+            }
+            __syncwarp();
+        }
+    }
+    for (int i = lane; i < n; i += 32) dst[i] = seg[i] ^ 0x80000000u;
+    __syncwarp();
+}
+}  // namespace
+
+// One warp per slot sorts the slot's stored ids into its output range: up to
+// 32 ids by rank counting in registers, up to FIN_WCAP by a bitonic sort in
+// the warp's shared segment.  Larger sets are sorted by the whole block
+// afterwards: in shared memory up to FIN_BCAP ids, by four stable radix
+// passes through the pool region above that.
+__global__ void __launch_bounds__(32 * FIN_WARPS)
 finalize_kernel(int* res_pool, const long long* cand_off, const int* res_count, const int* out_off,
                 int* out, int nq)
 {
-    extern __shared__ unsigned skeys[];
-    const int s = blockIdx.x;
-    if (s >= nq) return;
-    const int n = (int)min((long long)res_count[s], cand_off[s + 1] - cand_off[s]);
-    unsigned* src = (unsigned*)(res_pool + cand_off[s]);
-    unsigned* dst = (unsigned*)(out + out_off[s]);
-    const int tid = threadIdx.x;
-    if (n <= SORT_CAP) {
-        int P = 1;
-        while (P < n) P <<= 1;
-        for (int i = tid; i < P; i += blockDim.x) skeys[i] = i < n ? okey((int)src[i]) : 0xffffffffu;
-        __syncthreads();
-        for (int kk = 2; kk <= P; kk <<= 1) {
-            for (int j = kk >> 1; j > 0; j >>= 1) {
-                for (int i = tid; i < P; i += blockDim.x) {
-                    int ixj = i ^ j;
-                    if (ixj > i) {
-                        unsigned a = skeys[i], b = skeys[ixj];
-                        bool up = (i & kk) == 0;
-                        if ((a > b) == up) { skeys[i] = b; skeys[ixj] = a; }
-                    }
-                }
-                __syncthreads();
+    __shared__ unsigned skeys[FIN_BCAP];
+    __shared__ int big[FIN_WARPS];
+    __shared__ int nbig;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) nbig = 0;
+    __syncthreads();
+    const int s = blockIdx.x * FIN_WARPS + w;
+    if (s < nq) {
+        const int n = (int)min((long long)res_count[s], cand_off[s + 1] - cand_off[s]);
+        const unsigned* src = (const unsigned*)(res_pool + cand_off[s]);
+        unsigned* dst = (unsigned*)(out + out_off[s]);
+        if (n <= 32) {
+            // stable rank: smaller keys, and equal keys in lower lanes
+            const unsigned key = lane < n ? okey((int)src[lane]) : 0xffffffffu;
+            int rank = 0;
+            for (int j = 0; j < 32; ++j) {
+                const unsigned o = __shfl_sync(FULL, key, j);
+                rank += (o < key) || (o == key && j < lane);
             }
+            if (lane < n) dst[rank] = key ^ 0x80000000u;
+        } else if (n <= FIN_WCAP) {
+            warp_bitonic(skeys + w * FIN_WCAP, src, dst, n, lane);
+        } else if (lane == 0) {
+            big[atomicAdd(&nbig, 1)] = s;
         }
-        for (int i = tid; i < n; i += blockDim.x) dst[i] = skeys[i] ^ 0x80000000u;
-        return;
     }
-    // large result set: four stable LSD passes between the pool region and out
+    __syncthreads();
+    const int nb = nbig;
     __shared__ unsigned hist[256];
     __shared__ unsigned wc[8][256];
-    for (int i = tid; i < n; i += blockDim.x) src[i] = okey((int)src[i]);
-    __syncthreads();
-    block_radix_pass(src, dst, n, 0, hist, wc);
-    __syncthreads();
-    block_radix_pass(dst, src, n, 8, hist, wc);
-    __syncthreads();
-    block_radix_pass(src, dst, n, 16, hist, wc);
-    __syncthreads();
-    block_radix_pass(dst, src, n, 24, hist, wc);
-    __syncthreads();
-    for (int i = tid; i < n; i += blockDim.x) dst[i] = src[i] ^ 0x80000000u;
+    for (int bi = 0; bi < nb; ++bi) {
+        const int t = big[bi];
+        const int n = (int)min((long long)res_count[t], cand_off[t + 1] - cand_off[t]);
+        unsigned* src = (unsigned*)(res_pool + cand_off[t]);
+        unsigned* dst = (unsigned*)(out + out_off[t]);
+        if (n <= FIN_BCAP) {
+            int P = 1;
+            while (P < n) P <<= 1;
+            for (int i = tid; i < P; i += blockDim.x) skeys[i] = i < n ? okey((int)src[i]) : 0xffffffffu;
+            __syncthreads();
+            for (int kk = 2; kk <= P; kk <<= 1) {
+                for (int j = kk >> 1; j > 0; j >>= 1) {
+                    for (int i = tid; i < P; i += blockDim.x) {
+                        const int ixj = i ^ j;
+                        if (ixj > i) {
+                            const unsigned x = skeys[i], y = skeys[ixj];
+                            if ((x > y) == ((i & kk) == 0)) { skeys[i] = y; skeys[ixj] = x; }
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            for (int i = tid; i < n; i += blockDim.x) dst[i] = skeys[i] ^ 0x80000000u;
+        } else {
+            for (int i = tid; i < n; i += blockDim.x) src[i] = okey((int)src[i]);
+            __syncthreads();
+            block_radix_pass(src, dst, n, 0, hist, wc);
+            __syncthreads();
+            block_radix_pass(dst, src, n, 8, hist, wc);
+            __syncthreads();
+            block_radix_pass(src, dst, n, 16, hist, wc);
+            __syncthreads();
+            block_radix_pass(dst, src, n, 24, hist, wc);
+            __syncthreads();
+            for (int i = tid; i < n; i += blockDim.x) dst[i] = src[i] ^ 0x80000000u;
+        }
+        __syncthreads();
+    }
 }
 
 }  // namespace rknn

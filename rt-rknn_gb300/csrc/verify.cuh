@@ -7,7 +7,9 @@ namespace rknn {
 constexpr int VERIFY_UPT = 4;                       // default users per lane per work item
 constexpr int VERIFY_CHUNK = 32 * VERIFY_UPT;       // default users per work item
 constexpr int VERIFY_WARPS = 8;                     // default warps per block
-constexpr int SORT_CAP = 16384;                     // results sorted in shared memory
+constexpr int FIN_WARPS = 8;                        // finalize: slots per block (one warp each)
+constexpr int FIN_WCAP = 512;                       // ids one warp sorts in shared memory
+constexpr int FIN_BCAP = FIN_WARPS * FIN_WCAP;      // ids the block sorts in shared memory
 
 enum { MODE_FP64 = 0, MODE_FP32 = 1 };
 

@@ -128,7 +128,10 @@ struct ZoneArgs {
 // zone state in shared memory, one warp (one query at a time) per block
 __global__ void zone_kernel_smem(ZoneArgs a);
 
-// angular-slice filter for large k, same arguments and outputs
+// angular-slice filter, same arguments and outputs: slice bounds in a
+// shared-memory heap (any k), or in registers for k <= 16 / k <= 32
 __global__ void slice_kernel(ZoneArgs a);
+__global__ void slice_kernel_r16(ZoneArgs a);
+__global__ void slice_kernel_r32(ZoneArgs a);
 
 }  // namespace rknn

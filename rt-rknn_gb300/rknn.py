@@ -38,7 +38,7 @@ EXPORTS = ["rknn_index_opts_default", "rknn_index_create", "rknn_index_destroy",
            "rknn_last_zone", "rknn_set_profiling", "rknn_last_kernel_ms",
            "rknn_serve_opts_default", "rknn_serve_start", "rknn_serve_submit", "rknn_serve_wait",
            "rknn_serve_replay", "rknn_serve_stats_get", "rknn_serve_stop", "rknn_index_tune",
-           "rknn_last_error", "rknn_version"]
+           "rknn_host_alloc", "rknn_host_free", "rknn_last_error", "rknn_version"]
 
 
 class ServeOpts(C.Structure):
@@ -54,6 +54,30 @@ class ServeStats(C.Structure):
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "pad"}
+
+
+class _HostBlock:
+    """Owns one rknn_host_alloc block; freed when the last array over it goes."""
+
+    def __init__(self, nbytes: int):
+        p = C.c_void_p()
+        _check(load().rknn_host_alloc(int(nbytes), C.byref(p)))
+        self.p = p.value
+
+    def __del__(self):
+        if self.p:
+            load().rknn_host_free(C.c_void_p(self.p))
+            self.p = None
+
+
+def pinned_ids(n: int) -> np.ndarray:
+    """An int32 array of n ids in page-locked host memory: rknn_query_batch
+    copies results into it directly.  Views keep the block alive."""
+    blk = _HostBlock(4 * max(1, int(n)))
+    arr_t = C.c_int32 * max(1, int(n))
+    cobj = arr_t.from_address(blk.p)
+    cobj._owner = blk
+    return np.ctypeslib.as_array(cobj)
 
 
 class RkNNError(RuntimeError):
@@ -125,6 +149,8 @@ def load(path: str = LIB_PATH):
     L.rknn_query.argtypes = [vp, i32, i32, i32, vp, i64, C.POINTER(i64), C.POINTER(Stats)]
     L.rknn_query_batch.argtypes = [vp, vp, vp, i32, i32, vp, i64, vp, C.POINTER(Stats)]
     L.rknn_query_noalloc.argtypes = [vp, i32, i32, i32, vp, i64, C.POINTER(i64)]
+    L.rknn_host_alloc.argtypes = [i64, C.POINTER(vp)]
+    L.rknn_host_free.argtypes = [vp]
     L.rknn_query_batch_device.argtypes = [vp, vp, vp, i32, i32, i32]
     L.rknn_batch_device_results.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
     L.rknn_sync.argtypes = [vp]
@@ -203,6 +229,7 @@ class Index:
         if getattr(self, "h", None):
             load().rknn_index_destroy(self.h)
             self.h = None
+        self._flat_out = None
 
     def __del__(self):
         try:
@@ -281,14 +308,15 @@ class Index:
         off = getattr(self, "_flat_off", None)
         if off is None or off.shape[0] < nq + 1:
             off = self._flat_off = np.zeros(nq + 1, np.int64)
-        out = getattr(self, "_flat_out", None)
-        if out is None:
-            out = self._flat_out = np.empty(1 << 16, np.int32)
+        buf = getattr(self, "_flat_out", None)
+        if buf is None:
+            buf = self._flat_out = pinned_ids(1 << 16)
         while True:
+            out = buf
             rc = L.rknn_query_batch(self.h, _ptr(qs), _ptr(ks), nq, _MODES[mode], out.ctypes.data,
                                     out.shape[0], off.ctypes.data, None)
             if rc == 5 and off[nq] > out.shape[0]:
-                out = self._flat_out = np.empty(int(off[nq] * 5 // 4), np.int32)
+                buf = self._flat_out = pinned_ids(int(off[nq] * 5 // 4))
                 continue
             _check(rc)
             return out[: off[nq]], off[: nq + 1]
@@ -306,11 +334,11 @@ class Index:
         _check(load().rknn_set_profiling(self.h, 1 if on else 0))
 
     def kernel_ms(self):
-        """Per-kernel device ms of the last profiled call: zone, plan, verify,
-        result offsets, finalize."""
-        ms = np.zeros(5, np.float64)
+        """Per-kernel device ms of the last profiled call: zone (or slice
+        filter), plan, verify, recount, result offsets, finalize."""
+        ms = np.zeros(6, np.float64)
         _check(load().rknn_last_kernel_ms(self.h, ms.ctypes.data))
-        return dict(zip(("zone", "plan", "verify", "offsets", "finalize"), ms.tolist()))
+        return dict(zip(("zone", "plan", "verify", "recount", "offsets", "finalize"), ms.tolist()))
 
     def set_stream(self, stream_handle: int | None):
         _check(load().rknn_set_stream(self.h, C.c_void_p(stream_handle or 0)))

@@ -107,6 +107,68 @@ def test_street_large_k(engine):
         assert np.array_equal(res, o.query(int(q), int(k))), (q, k)
 
 
+def test_result_set_sizes(engine):
+    """Few facilities, many users: result sets of tens to tens of thousands of
+    ids, sorted by a warp in registers (<= 32), by a warp in shared memory
+    (<= 512), by the block in shared memory (<= 4096) and by radix passes
+    through the result pool above that."""
+    ds = datagen.uniform(200, 100_000, seed=21, nq=60, k=1)
+    o = O.Oracle.of(ds)
+    ks = np.array([1, 8, 20, 2] * 15, np.int32)
+    idx = engine.Index.of(ds)
+    got = idx.query_batch(ds.queries, ks, "fp32")
+    sizes = [r.size for r in got]
+    assert min(sizes) <= 512 < max(sizes) and max(sizes) > 4096
+    for q, k, res in zip(ds.queries, ks, got):
+        assert np.array_equal(res, o.query(int(q), int(k))), (int(q), int(k))
+    small = datagen.uniform(20_000, 100_000, seed=22, nq=40, k=1)
+    os_ = O.Oracle.of(small)
+    idx2 = engine.Index.of(small)
+    got = idx2.query_batch(small.queries, 3, "fp32")
+    assert max(r.size for r in got) <= 32
+    for q, res in zip(small.queries, got):
+        assert np.array_equal(res, os_.query(int(q), 3)), int(q)
+    idx.close()
+    idx2.close()
+
+
+def _device_results(idx, nq):
+    """The last device batch's (ids, offsets) copied to the host."""
+    import torch
+
+    class _Dev:
+        def __init__(self, ptr, n, typestr):
+            self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False),
+                                             "version": 3, "strides": None}
+
+    idx.sync()
+    ids_p, off_p = idx.device_results()
+    off = torch.as_tensor(_Dev(off_p, nq + 1, "<i4"), device="cuda").cpu().numpy().astype(np.int64)
+    n = int(off[-1])
+    ids = torch.as_tensor(_Dev(ids_p, max(n, 1), "<i4"), device="cuda").cpu().numpy()[:n] if n else np.zeros(0, np.int32)
+    return [ids[off[i]:off[i + 1]] for i in range(nq)]
+
+
+@pytest.mark.parametrize("filt", ["slice", "inf"])
+def test_device_batch_with_understated_kmax(engine, filt):
+    """rknn_query_batch_device: q and k already on the device; a k above the
+    stated kmax is still answered exactly."""
+    import torch
+    ds = datagen.uniform(3000, 40000, seed=31, nq=120, k=1)
+    o = O.Oracle.of(ds)
+    rng = np.random.default_rng(5)
+    ks = rng.integers(1, 41, ds.queries.shape[0]).astype(np.int32)
+    idx = engine.Index.of(ds, filter=filt)
+    d_q = torch.from_numpy(ds.queries.astype(np.int32)).cuda()
+    d_k = torch.from_numpy(ks).cuda()
+    for kmax in (40, 8):
+        idx.query_batch_device(d_q.data_ptr(), d_k.data_ptr(), len(ks), kmax, "fp32")
+        got = _device_results(idx, len(ks))
+        for q, k, res in zip(ds.queries, ks, got):
+            assert np.array_equal(res, o.query(int(q), int(k))), (int(q), int(k), kmax)
+    idx.close()
+
+
 def test_zone_bisectors_match_port(engine):
     """Same grid, same rules: the zone kernel builds rknn-inf's bisector set
     in the same order as the CPU restatement does."""
