@@ -412,6 +412,7 @@ def run_ours(args):
 
 
 def main():
+    global NQ
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -419,8 +420,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=400000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--queries", type=int, default=NQ,
+                    help="queries per step (default 1000, the headline workload; larger batches for profiling)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    NQ = args.queries
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

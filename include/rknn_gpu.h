@@ -99,8 +99,10 @@ typedef struct {
     int64_t zone_cycles[8]; /* zone kernel SM cycles by phase, summed over queries: ring
                                expansion, pop + rules, vertex test, vertex count pass,
                                candidate intersections, dedup, counts/erase/append, epilogue.
-                               The slice filter fills 0 facility stream, 1 heap offers (part
-                               of 0), 2 user-cell ring scan, 7 half-planes and segments */
+                               The slice filter fills 0 facility stream, and within it 1
+                               slice-bound offers, 3 ring stop tests, 4 cell ranges, 5 facility
+                               items (with 1); 2 user-cell ring scan, 7 half-planes and
+                               segments */
     int64_t zone_points;    /* facilities taken from the zone search's queue */
     int64_t zone_cells;     /* facility grid cells taken from the queue */
 } rknn_query_stats;

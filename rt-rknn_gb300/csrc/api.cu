@@ -127,6 +127,7 @@ struct rknn_index {
     int filter = RKNN_FILTER_AUTO;
     int slice_min_k = 1;
     int num_sms = 0;
+    int recount_grid = 0;       // one wave of recount_kernel blocks
     size_t smem_optin = 0;
     Workspace ws;
     std::mutex mu;
@@ -343,6 +344,7 @@ struct BatchPlan {
     std::vector<ZClass> cls;
     int pstride = 0;            // half-plane row stride: the largest class lc
     int stage_cap = 0;          // half-planes the verification stages per warp
+    int seg_stage = 0;          // user segments it stages per warp
     int vupt = VERIFY_UPT, vwarps = VERIFY_WARPS;
     size_t vsmem = 0;
     int vgrid = 0;
@@ -387,7 +389,10 @@ BatchPlan plan_batch(rknn_index* ix, int nq, int mode, bool use_order, const int
     b.vupt = ix->vupt;
     b.vwarps = ix->vwarps;
     b.stage_cap = std::max(1, std::min(b.pstride, stage_max));
-    b.vsmem = (size_t)b.vwarps * b.stage_cap * bpp;
+    int rm = 0;
+    for (auto& c : b.cls) rm = std::max(rm, c.caps.rm);
+    b.seg_stage = std::min(2 * rm + 2, 512);
+    b.vsmem = (size_t)b.vwarps * ((size_t)b.stage_cap * bpp + (size_t)b.seg_stage * sizeof(int2));
     int vper = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&vper, verify_fn(b.vupt), b.vwarps * 32, b.vsmem);
     if (vper < 1) vper = 1;
@@ -466,7 +471,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     va.qd = w.d_qd; va.planes = w.d_planes; va.bis_pos = w.d_bispos; va.lc = b.pstride;
     va.slice_r = w.d_slice_r;
     va.stage_cap = b.stage_cap;
-    va.segs = w.d_segs; va.seg_cap = w.seg_cap;
+    va.segs = w.d_segs; va.seg_cap = w.seg_cap; va.seg_stage = b.seg_stage;
     va.chunk_off = w.d_chunk_off; va.cand_off = w.d_cand_off; va.nq = nq;
     va.uxy = ix->d_uxy; va.uid = ix->d_uid; va.fxy = ix->d_fxy; va.fstart = ix->d_fstart; va.gf = ix->gf;
     va.res_count = w.d_res_count; va.res_pool = w.d_pool; va.work_counter = w.d_counters + 1;
@@ -477,7 +482,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     verify_fn(b.vupt)<<<b.vgrid, b.vwarps * 32, b.vsmem, st>>>(va);
     CK(cudaGetLastError());
     mark(3);
-    recount_kernel<<<ix->num_sms * 8, 256, 0, st>>>(va);
+    recount_kernel<<<ix->recount_grid, 256, 0, st>>>(va);
     CK(cudaGetLastError());
     mark(4);
 
@@ -742,6 +747,11 @@ rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf, 
     // maximum less the kernel's static shared memory, set once (each launch
     // asks for what its plan needs)
     CKB(allow_dynamic_smem((const void*)zone_kernel_smem, optin));
+    {
+        int per = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, recount_kernel, 256, 0);
+        ix->recount_grid = std::max(1, per) * ix->num_sms;
+    }
     CKB(allow_dynamic_smem((const void*)slice_kernel, optin));
     CKB(allow_dynamic_smem((const void*)slice_kernel_r16, optin));
     CKB(allow_dynamic_smem((const void*)slice_kernel_r32, optin));

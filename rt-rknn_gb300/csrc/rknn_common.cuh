@@ -19,6 +19,23 @@ struct Grid {
     int gx, gy;        // cells per axis
 };
 
+// Angular slice (of 32 around the origin, slice i spanning [i, i+1) * 11.25
+// degrees counter-clockwise from +x) of direction (vx, vy): the octant from
+// signs and |vx| <= |vy|, then the quarter of the octant from the ratio
+// min/max against tan(11.25), tan(22.5), tan(33.75) degrees.  The products
+// carry float rounding only, so the index is exact except within about
+// 1e-7 rad of a slice edge, where it may name the neighbour.  (0, 0) gives 0.
+__host__ __device__ __forceinline__ int slice_of(float vx, float vy)
+{
+    const float ax = fabsf(vx), ay = fabsf(vy);
+    const float mn = fminf(ax, ay), mx = fmaxf(ax, ay);
+    const int sub = (mn > 0.198912367f * mx) + (mn > 0.414213562f * mx) + (mn > 0.668178638f * mx);
+    int s = ay <= ax ? sub : 7 - sub;       // slice of the first-quadrant reflection
+    if (vx < 0.0f) s = vy >= 0.0f ? 15 - s : 16 + s;
+    else if (vy < 0.0f) s = 31 - s;
+    return s;
+}
+
 __host__ __device__ __forceinline__ int cell_coord(float v, float o, float inv, int g)
 {
     float t = floorf((v - o) * inv);

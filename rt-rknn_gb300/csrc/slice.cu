@@ -76,6 +76,20 @@ __device__ __forceinline__ float upper_arc(float vx, float vy, float e1x, float 
     return __fdiv_ru(num, den) * (1.0f + 4.0f * kU32);
 }
 
+// upper_arc without branches for the common case: ok is false when the
+// denominator lies outside [2^-126, 2^126] (then call upper_arc).
+__device__ __forceinline__ float upper_arc_fast(float vx, float vy, float e1x, float e1y, float e2x, float e2y, bool& ok)
+{
+    const float d1 = fmaf(vx, e1x, vy * e1y), d2 = fmaf(vx, e2x, vy * e2y);
+    const float l1 = fabsf(vx) + fabsf(vy);
+    const float dmin = fminf(d1, d2) - 8.0f * kU32 * l1 - 1e-37f;
+    const float num = fmaf(vx, vx, vy * vy) * (1.0f + 8.0f * kU32);
+    const float den = 2.0f * dmin;
+    const bool pos = dmin > 0.0f;
+    ok = !pos || (den > 0x1p-126f && den < 0x1p126f);
+    return pos ? __fdividef(num, den) * (1.0f + 0x1p-20f) : INFINITY;
+}
+
 // Distance from q along unit direction (ex, ey) to the box's boundary,
 // rounded up (q lies inside the box).
 __device__ __forceinline__ float exit_dist(float qx, float qy, float ex, float ey,
@@ -183,6 +197,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
     sincosf((float)lane * SLICE_W - WIDEN, &e1y, &e1x);
     sincosf((float)(lane + 1) * SLICE_W + WIDEN, &e2y, &e2x);
     const double slack = 1e-5 * ((double)A.gf.cs + fmax(fmax(fabs(A.sx0), fabs(A.sx1)), fmax(fabs(A.sy0), fabs(A.sy1))));
+    const float slack_f = __double2float_ru(slack);
 
     for (;;) {
         int slot = 0;
@@ -283,6 +298,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
         }
         int ring = 0;
         for (; ring <= rmaxf; ++ring) {
+            long long tp = clock64();
             const int cur_fs = pf_fs, cur_fe = pf_fe;
             {
                 const int nr1 = 8 * (ring + 1);
@@ -305,8 +321,9 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) Rmax = fmaxf(Rmax, __shfl_xor_sync(FULL, Rmax, o));
             if (ring > 0 && Rmax < INFINITY) {
-                const double Lr = (double)(ring - 1) * (double)A.gf.cs - slack;
-                if (Lr > 0.0 && 0.5 * Lr > (double)Rmax * (1.0 + 1e-6)) break;
+                // in float, rounded toward stopping later
+                const float Lr = __fsub_rd(__fmul_rd((float)(ring - 1), A.gf.cs), slack_f);
+                if (Lr > 0.0f && 0.5f * Lr > __fmul_ru(Rmax, 1.0f + 1e-6f)) break;
             }
             // Every heap top is an upper bound at any time, so the stream may
             // stop early; past a budget the remaining (sparse-direction)
@@ -325,6 +342,8 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                 Rs[lane] = Rw;
                 __syncwarp();
             }
+            zs.cyc[3] += clock64() - tp;
+            tp = clock64();
             // the ring's cells (8 ring of them, 1 for ring 0), one range each
             const int nrange = ring == 0 ? 1 : 8 * ring;
             for (int r0 = 0; r0 < nrange; r0 += 32) {
@@ -380,6 +399,8 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                     prefetch_l1(A.fxy + pf_fs);
                     prefetch_l1(A.fxy + (pf_fe - 1));
                 }
+                zs.cyc[4] += clock64() - tp;
+                tp = clock64();
                 // flatten the ranges: inclusive prefix of their lengths
                 const int len = fe - fs;
                 int incl = len;
@@ -435,12 +456,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                         for (int dd = 1; dd <= 8; ++dd)
                             Rw = fmaxf(Rw, fmaxf(__shfl_sync(FULL, Rl, (lane + dd) & 31),
                                                  __shfl_sync(FULL, Rl, (lane - dd) & 31)));
-                        int sj = 0;
-                        if (ok) {
-                            float th = atan2f(vy, vx);
-                            if (th < 0.0f) th += TWO_PI_F;
-                            sj = min(NS - 1, max(0, (int)(th * (1.0f / SLICE_W))));
-                        }
+                        const int sj = ok ? slice_of(vx, vy) : 0;
                         const float Rwj = __shfl_sync(FULL, Rw, sj);
                         const bool useful = ok && !(0.25f * fmaf(vx, vx, vy * vy) * (1.0f - 4.0f * kU32) >= Rwj * Rwj);
                         m = __ballot_sync(FULL, useful);
@@ -458,8 +474,14 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                             m &= m - 1;
                             const float ax = __shfl_sync(FULL, vx, s1), ay = __shfl_sync(FULL, vy, s1);
                             const float bx = __shfl_sync(FULL, vx, s2), by = __shfl_sync(FULL, vy, s2);
-                            const float u1 = upper_arc(ax, ay, e1x, e1y, e2x, e2y);
-                            const float u2 = two ? upper_arc(bx, by, e1x, e1y, e2x, e2y) : INFINITY;
+                            bool ok1, ok2;
+                            float u1 = upper_arc_fast(ax, ay, e1x, e1y, e2x, e2y, ok1);
+                            float u2 = upper_arc_fast(bx, by, e1x, e1y, e2x, e2y, ok2);
+                            if (!__all_sync(FULL, ok1 && ok2)) {
+                                if (!ok1) u1 = upper_arc(ax, ay, e1x, e1y, e2x, e2y);
+                                if (!ok2) u2 = upper_arc(bx, by, e1x, e1y, e2x, e2y);
+                            }
+                            if (!two) u2 = INFINITY;
                             if (__any_sync(FULL, fminf(u1, u2) < RL[(KR > 0 ? KR : 1) - 1])) {
                                 list_insert<KR>(RL, u1);
                                 list_insert<KR>(RL, u2);
@@ -476,6 +498,8 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                     }
                     zs.cyc[1] += clock64() - t_offer;
                 }
+                zs.cyc[5] += clock64() - tp;
+                tp = clock64();
             }
             zs.cells += nrange;
         }

@@ -190,10 +190,18 @@ template <int UPT>
 __device__ __forceinline__ void verify_body(const VerifyArgs& A)
 {
     extern __shared__ __align__(16) char smem[];
+    // every st-th work-item offset, for the item -> slot lookup
+    __shared__ int csmp[VERIFY_SAMPLES];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const size_t per_warp = (size_t)A.stage_cap * (A.mode == MODE_FP32 ? 16 : 32);
-    char* sp = smem + w * per_warp;
+    const size_t plane_bytes = (size_t)A.stage_cap * (A.mode == MODE_FP32 ? 16 : 32);
+    char* sp = smem + w * (plane_bytes + (size_t)A.seg_stage * sizeof(int2));
+    int2* ssg = (int2*)(sp + plane_bytes);
+    const int st = max(1, (A.nq + VERIFY_SAMPLES) / VERIFY_SAMPLES);     // ceil((nq + 1) / samples)
+    const int nsmp = A.nq / st + 1;                                       // samples i * st <= nq
+    for (int i = threadIdx.x; i < nsmp; i += blockDim.x) csmp[i] = A.chunk_off[i * st];
+    __syncthreads();
     int cur = -1;
+    bool seg_staged = false;
     unsigned long long s_cand = 0, s_evals = 0, s_surv = 0, s_fac = 0, s_rech = 0, s_res = 0;
     const int total = A.chunk_off[A.nq];
     for (;;) {
@@ -201,12 +209,30 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
         if (lane == 0) g = atomicAdd(A.work_counter, 1);
         g = __shfl_sync(FULL, g, 0);
         if (g >= total) break;
-        int lo = 0, hi = A.nq;          // chunk_off[lo] <= g < chunk_off[hi]
+        // slot s of item g: chunk_off[s] <= g < chunk_off[s+1].  The samples
+        // narrow it to [ws, ws + st); there the count of offsets <= g places
+        // it (offsets never decrease).
+        int lo = 0, hi = nsmp;
         while (hi - lo > 1) {
-            int mid = (lo + hi) >> 1;
-            if (A.chunk_off[mid] <= g) lo = mid; else hi = mid;
+            const int mid = (lo + hi) >> 1;
+            if (csmp[mid] <= g) lo = mid; else hi = mid;
         }
-        const int s = lo;
+        int s = lo;
+        if (st > 1) {
+            const int ws = lo * st, we = min(ws + st, A.nq);
+            if (st <= 31) {
+                const int j = ws + lane;
+                const bool le = j <= we && A.chunk_off[VX(j, A.nq + 1, 215)] <= g;
+                s = ws + __popc(__ballot_sync(FULL, le)) - 1;
+            } else {
+                int l = ws, h = we;
+                while (h - l > 1) {
+                    const int mid = (l + h) >> 1;
+                    if (A.chunk_off[mid] <= g) l = mid; else h = mid;
+                }
+                s = l;
+            }
+        }
         const QDesc d = A.qd[s];
         if (s != cur) {
             __syncwarp();
@@ -225,11 +251,17 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
                     p[3] = 0.0;
                 }
             }
+            // the slot's user segments (nseg ranges and the terminal entry)
+            seg_staged = d.nseg + 1 <= A.seg_stage;
+            if (seg_staged) {
+                const int2* gsg = A.segs + (size_t)s * A.seg_cap;
+                for (int m = lane; m <= d.nseg; m += 32) ssg[m] = gsg[m];
+            }
             cur = s;
             __syncwarp();
         }
         const int v0 = (g - A.chunk_off[s]) * (32 * UPT);
-        const int2* sg = A.segs + (size_t)s * A.seg_cap;
+        const int2* sg = seg_staged ? ssg : A.segs + (size_t)s * A.seg_cap;
         // segment holding v0: largest i < nseg with sg[i].y <= v0
         int i0 = 0;
         {
@@ -259,18 +291,15 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
         }
         // a user beyond its slice's bound R(P) has k facilities strictly nearer
         // than q (the slice filter's rule): drop it before the half-planes.
-        // Slices were widened by 2^-14 rad, far beyond atan2f's error, so the
-        // computed angle's slice is one whose bound holds for the user.
+        // Slices were widened by 2^-14 rad, far beyond slice_of's 1e-7 rad
+        // edge uncertainty, so the computed slice's bound holds for the user.
         if (d.flags & QF_SLICE_R) {
             const float* Rq = A.slice_r + (size_t)s * 32;
 #pragma unroll
             for (int t = 0; t < UPT; ++t) {
                 if (!valid[t]) continue;
                 const float dx = u[t].x - d.qx, dy = u[t].y - d.qy;
-                float th = atan2f(dy, dx);
-                if (th < 0.0f) th += 6.28318530717958647692f;
-                const int si = min(31, max(0, (int)(th * (32.0f / 6.28318530717958647692f))));
-                const float Rs = Rq[si];
+                const float Rs = Rq[slice_of(dx, dy)];
                 if (fmaf(dx, dx, dy * dy) * (1.0f - 1e-6f) > Rs * Rs) valid[t] = false;
             }
         }
@@ -514,52 +543,98 @@ __device__ T block_scan_excl(T v, T* tmp, T* total)
 }
 }  // namespace
 
+// Scans over the batch's slots run in one block of SCAN_THREADS threads, a
+// tile of SCAN_TILE slots per round: values are read coalesced into shared
+// memory, each thread scans SCAN_PT consecutive slots of the tile, and a
+// block scan of the per-thread sums plus the running carry places them.
+constexpr int SCAN_THREADS = 1024, SCAN_PT = 4, SCAN_TILE = SCAN_THREADS * SCAN_PT;
+
 // Result region of each slot: min(candidates, rcap) entries, at 64-bit
 // offsets; slots whose region does not fit the pool are flagged and skipped
 // (the host grows the pool and runs the batch again).  Work items cover
 // every candidate of the slots that fit.
-__global__ void plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_off, long long pool_cap, int rcap,
-                            int chunk)
+__global__ void __launch_bounds__(SCAN_THREADS)
+plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_off, long long pool_cap, int rcap, int chunk)
 {
+    __shared__ int sn[SCAN_TILE];
     __shared__ long long tmp64[32];
     __shared__ int tmp[32];
-    const int T = blockDim.x;
-    const int per = (nq + T - 1) / T;
-    const int b = threadIdx.x * per, e = min(nq, b + per);
-    long long sum = 0, tot64 = 0;
-    for (int i = b; i < e; ++i) sum += min(qd[i].ncand, rcap);
-    long long run = block_scan_excl<long long>(sum, tmp64, &tot64);
-    for (int i = b; i < e; ++i) { cand_off[i] = run; run += min(qd[i].ncand, rcap); }
-    if (threadIdx.x == 0) cand_off[nq] = tot64;
-    int csum = 0, ctot = 0;
-    for (int i = b; i < e; ++i) {
-        const int n = qd[i].ncand;
-        const bool fits = cand_off[i] + min(n, rcap) <= pool_cap;
-        if (!fits) qd[i].flags |= QF_RESULT_OVERFLOW;
-        csum += fits ? (n + chunk - 1) / chunk : 0;
+    const int tid = threadIdx.x;
+    long long carry64 = 0;
+    int carryc = 0;
+    for (int base = 0; base < nq; base += SCAN_TILE) {
+        for (int j = tid; j < SCAN_TILE; j += SCAN_THREADS) sn[j] = base + j < nq ? qd[base + j].ncand : 0;
+        __syncthreads();
+        int n[SCAN_PT];
+        long long r[SCAN_PT], rs = 0;
+#pragma unroll
+        for (int t = 0; t < SCAN_PT; ++t) {
+            n[t] = sn[tid * SCAN_PT + t];
+            r[t] = min(n[t], rcap);
+            rs += r[t];
+        }
+        long long tot64 = 0;
+        long long off = carry64 + block_scan_excl<long long>(rs, tmp64, &tot64);
+        int cs = 0;
+        bool fits[SCAN_PT];
+#pragma unroll
+        for (int t = 0; t < SCAN_PT; ++t) {
+            const int i = base + tid * SCAN_PT + t;
+            fits[t] = off + r[t] <= pool_cap;
+            if (i < nq) {
+                cand_off[i] = off;
+                if (!fits[t]) qd[i].flags |= QF_RESULT_OVERFLOW;
+            }
+            off += r[t];
+            cs += fits[t] ? (n[t] + chunk - 1) / chunk : 0;
+        }
+        int ctot = 0;
+        int coff = carryc + block_scan_excl<int>(cs, tmp, &ctot);
+#pragma unroll
+        for (int t = 0; t < SCAN_PT; ++t) {
+            const int i = base + tid * SCAN_PT + t;
+            if (i < nq) chunk_off[i] = coff;
+            coff += fits[t] ? (n[t] + chunk - 1) / chunk : 0;
+        }
+        carry64 += tot64;
+        carryc += ctot;
+        __syncthreads();
     }
-    int crun = block_scan_excl<int>(csum, tmp, &ctot);
-    for (int i = b; i < e; ++i) {
-        chunk_off[i] = crun;
-        const int n = qd[i].ncand;
-        if (!(qd[i].flags & QF_RESULT_OVERFLOW)) crun += (n + chunk - 1) / chunk;
+    if (tid == 0) {
+        cand_off[nq] = carry64;
+        chunk_off[nq] = carryc;
     }
-    if (threadIdx.x == 0) chunk_off[nq] = ctot;
 }
 
 // Output offsets of the stored results (a slot stores at most its region).
-__global__ void scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int* out_off)
+__global__ void __launch_bounds__(SCAN_THREADS)
+scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int* out_off)
 {
+    __shared__ int sn[SCAN_TILE];
     __shared__ int tmp[32];
-    const int T = blockDim.x;
-    const int per = (nq + T - 1) / T;
-    const int b = threadIdx.x * per, e = min(nq, b + per);
-    auto stored = [&](int i) { return (int)min((long long)res_count[i], cand_off[i + 1] - cand_off[i]); };
-    int sum = 0, tot = 0;
-    for (int i = b; i < e; ++i) sum += stored(i);
-    int run = block_scan_excl<int>(sum, tmp, &tot);
-    for (int i = b; i < e; ++i) { out_off[i] = run; run += stored(i); }
-    if (threadIdx.x == 0) out_off[nq] = tot;
+    const int tid = threadIdx.x;
+    int carry = 0;
+    for (int base = 0; base < nq; base += SCAN_TILE) {
+        for (int j = tid; j < SCAN_TILE; j += SCAN_THREADS) {
+            const int i = base + j;
+            sn[j] = i < nq ? (int)min((long long)res_count[i], cand_off[i + 1] - cand_off[i]) : 0;
+        }
+        __syncthreads();
+        int v[SCAN_PT], vs = 0;
+#pragma unroll
+        for (int t = 0; t < SCAN_PT; ++t) { v[t] = sn[tid * SCAN_PT + t]; vs += v[t]; }
+        int tot = 0;
+        int off = carry + block_scan_excl<int>(vs, tmp, &tot);
+#pragma unroll
+        for (int t = 0; t < SCAN_PT; ++t) {
+            const int i = base + tid * SCAN_PT + t;
+            if (i < nq) out_off[i] = off;
+            off += v[t];
+        }
+        carry += tot;
+        __syncthreads();
+    }
+    if (tid == 0) out_off[nq] = carry;
 }
 
 // ---------------------------------------------------------------- finalize
@@ -613,35 +688,64 @@ __device__ void block_radix_pass(const unsigned* in, unsigned* out, int n, int s
 }  // namespace
 
 namespace {
-// ascending bitonic sort of n keys (padded to a power of two with the largest
-// key) by one warp in its shared segment
-__device__ void warp_bitonic(unsigned* seg, const unsigned* src, unsigned* dst, int n, int lane)
+// Ascending bitonic sort of 32*E keys held by one warp in registers, key
+// t*32 + lane in x[t] (coalesced loads and stores).  Pairs 32 or more apart
+// sit in one lane's registers; nearer pairs are exchanged by shuffles.
+template <int E>
+__device__ __forceinline__ void warp_sort_regs(unsigned (&x)[E], int lane)
 {
-    int P = 64;
-    while (P < n) P <<= 1;
-    for (int i = lane; i < P; i += 32) seg[i] = i < n ? okey((int)src[i]) : 0xffffffffu;
-    __syncwarp();
-    for (int kk = 2; kk <= P; kk <<= 1) {
+#pragma unroll
+    for (int kk = 2; kk <= 32 * E; kk <<= 1) {
+#pragma unroll
         for (int j = kk >> 1; j > 0; j >>= 1) {
-            for (int t = lane; t < (P >> 1); t += 32) {
-                const int i = 2 * t - (t & (j - 1));     // lower index of the pair
-                const unsigned x = seg[i], y = seg[i + j];
-                if ((x > y) == ((i & kk) == 0)) { seg[i] = y; seg[i + j] = x; }
+            if (j >= 32) {
+                const int tj = j >> 5;
+#pragma unroll
+                for (int t = 0; t < E; ++t) {
+                    if ((t & tj) == 0) {
+                        const bool up = (((t << 5) | lane) & kk) == 0;
+                        const unsigned a = x[t], b = x[t | tj];
+                        x[t] = up ? min(a, b) : max(a, b);
+                        x[t | tj] = up ? max(a, b) : min(a, b);
+                    }
+                }
+            } else {
+                const bool lower = (lane & j) == 0;
+#pragma unroll
+                for (int t = 0; t < E; ++t) {
+                    const unsigned o = __shfl_xor_sync(FULL, x[t], j);
+                    const bool up = (((t << 5) | lane) & kk) == 0;
+                    x[t] = (lower == up) ? min(x[t], o) : max(x[t], o);
+                }
             }
-            __syncwarp();
         }
     }
-    for (int i = lane; i < n; i += 32) dst[i] = seg[i] ^ 0x80000000u;
-    __syncwarp();
+}
+
+template <int E>
+__device__ __forceinline__ void warp_sort_slot(const unsigned* src, unsigned* dst, int n, int lane)
+{
+    unsigned x[E];
+#pragma unroll
+    for (int t = 0; t < E; ++t) {
+        const int i = (t << 5) | lane;
+        x[t] = i < n ? okey((int)src[i]) : 0xffffffffu;
+    }
+    warp_sort_regs<E>(x, lane);
+#pragma unroll
+    for (int t = 0; t < E; ++t) {
+        const int i = (t << 5) | lane;
+        if (i < n) dst[i] = x[t] ^ 0x80000000u;
+    }
 }
 }  // namespace
 
 // One warp per slot sorts the slot's stored ids into its output range: up to
-// 32 ids by rank counting in registers, up to FIN_WCAP by a bitonic sort in
-// the warp's shared segment.  Larger sets are sorted by the whole block
-// afterwards: in shared memory up to FIN_BCAP ids, by four stable radix
-// passes through the pool region above that.
-__global__ void __launch_bounds__(32 * FIN_WARPS)
+// 32 ids by rank counting in registers, up to FIN_WCAP by a bitonic network
+// in registers.  Larger sets are sorted by the whole block afterwards: in
+// shared memory up to FIN_BCAP ids, by four stable radix passes through the
+// pool region above that.
+__global__ void __launch_bounds__(32 * FIN_WARPS, 1)
 finalize_kernel(int* res_pool, const long long* cand_off, const int* res_count, const int* out_off,
                 int* out, int nq)
 {
@@ -665,8 +769,14 @@ finalize_kernel(int* res_pool, const long long* cand_off, const int* res_count, 
                 rank += (o < key) || (o == key && j < lane);
             }
             if (lane < n) dst[rank] = key ^ 0x80000000u;
+        } else if (n <= 64) {
+            warp_sort_slot<2>(src, dst, n, lane);
+        } else if (n <= 128) {
+            warp_sort_slot<4>(src, dst, n, lane);
+        } else if (n <= 256) {
+            warp_sort_slot<8>(src, dst, n, lane);
         } else if (n <= FIN_WCAP) {
-            warp_bitonic(skeys + w * FIN_WCAP, src, dst, n, lane);
+            warp_sort_slot<16>(src, dst, n, lane);
         } else if (lane == 0) {
             big[atomicAdd(&nbig, 1)] = s;
         }

@@ -7,8 +7,9 @@ namespace rknn {
 constexpr int VERIFY_UPT = 4;                       // default users per lane per work item
 constexpr int VERIFY_CHUNK = 32 * VERIFY_UPT;       // default users per work item
 constexpr int VERIFY_WARPS = 8;                     // default warps per block
+constexpr int VERIFY_SAMPLES = 4096;                // work-item offsets cached per block
 constexpr int FIN_WARPS = 8;                        // finalize: slots per block (one warp each)
-constexpr int FIN_WCAP = 512;                       // ids one warp sorts in shared memory
+constexpr int FIN_WCAP = 512;                       // ids one warp sorts in registers
 constexpr int FIN_BCAP = FIN_WARPS * FIN_WCAP;      // ids the block sorts in shared memory
 
 enum { MODE_FP64 = 0, MODE_FP32 = 1 };
@@ -22,6 +23,8 @@ struct VerifyArgs {
                              // fewer only means more users reach the exact recount)
     const int2* segs;        // [slot][seg_cap]
     int seg_cap;
+    int seg_stage = 0;       // user segments staged per warp beside the half-planes
+                             // (a slot with more reads them from global memory)
     const int* chunk_off;    // [nq+1]
     const long long* cand_off;   // [nq+1] result region of each slot
     int nq;

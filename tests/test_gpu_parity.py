@@ -121,6 +121,17 @@ def test_result_set_sizes(engine):
     assert min(sizes) <= 512 < max(sizes) and max(sizes) > 4096
     for q, k, res in zip(ds.queries, ks, got):
         assert np.array_equal(res, o.query(int(q), int(k))), (int(q), int(k))
+    mid = datagen.uniform(2000, 100_000, seed=23, nq=60, k=1)
+    om = O.Oracle.of(mid)
+    idx3 = engine.Index.of(mid)
+    km = np.array([1, 2, 3, 5] * 15, np.int32)
+    got = idx3.query_batch(mid.queries, km, "fp32")
+    sizes = [r.size for r in got]
+    for lo, hi in ((32, 64), (64, 128), (128, 256), (256, 512)):
+        assert any(lo < n <= hi for n in sizes), (lo, hi, sorted(sizes))
+    for q, k, res in zip(mid.queries, km, got):
+        assert np.array_equal(res, om.query(int(q), int(k))), (int(q), int(k))
+    idx3.close()
     small = datagen.uniform(20_000, 100_000, seed=22, nq=40, k=1)
     os_ = O.Oracle.of(small)
     idx2 = engine.Index.of(small)
