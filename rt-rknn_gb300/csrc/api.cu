@@ -12,6 +12,7 @@
 //   finalize_kernel  one warp per query (the block for large sets): sort its
 //                    ids into the output
 #include "../../include/rknn_gpu.h"
+#include <utility>
 #include "index.cuh"
 #include "rknn_common.cuh"
 #include "verify.cuh"
@@ -128,6 +129,7 @@ struct rknn_index {
     int slice_min_k = 1;
     int num_sms = 0;
     int recount_grid = 0;       // one wave of recount_kernel blocks
+    bool pdl = true;            // programmatic dependent launch between the batch kernels
     size_t smem_optin = 0;
     Workspace ws;
     std::mutex mu;
@@ -411,10 +413,29 @@ ZoneCaps plan_caps(const BatchPlan& b)
     return c;
 }
 
+// Launch with programmatic stream serialization when pdl is set: the kernel
+// may start while its predecessor in the stream drains, and waits for it with
+// pdl_wait() before reading its outputs.
+template <typename... Exp, typename... Act>
+cudaError_t launch_k(void (*k)(Exp...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool pdl, Act&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, std::forward<Act>(args)...);
+}
+
 // Enqueue the batch's kernels (no synchronization, no non-stream CUDA calls:
 // this runs under stream capture).  k classes after the first run on side
 // streams, forked from and joined back to the context's stream.
-rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = false)
+rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = false, bool chain = false)
 {
     Workspace& w = c.w;
     cudaStream_t st = c.st;
@@ -463,8 +484,13 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     }
     mark(1);
 
-    plan_kernel<<<1, 1024, 0, st>>>(w.d_qd, nq, w.d_cand_off, w.d_chunk_off, w.pool_cap, w.rcap, 32 * b.vupt);
-    CK(cudaGetLastError());
+    // the kernels after the filter start while their predecessor drains
+    // (captured batches only: not between profiling events, nor after a
+    // cross-stream join, nor in serving, where blocks waiting early would
+    // hold resources that other slots' kernels need)
+    const bool pdl = chain && !events && ix->pdl;
+    CK(launch_k(plan_kernel, 1, 1024, 0, st, pdl && ncls == 1, w.d_qd, nq, w.d_cand_off, w.d_chunk_off, w.pool_cap,
+                w.rcap, 32 * b.vupt));
     mark(2);
 
     VerifyArgs va;
@@ -479,19 +505,16 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     va.nu = (int)ix->nu; va.nf = (int)ix->nf; va.ncf = ix->gf.gx * ix->gf.gy;
     va.pool_cap = w.pool_cap; va.fault = w.d_counters + 10; va.dropped = w.d_counters + 2;
     va.surv = w.d_surv; va.surv_cap = (int)std::min<long long>(w.surv_cap, INT32_MAX); va.surv_count = w.d_counters + 3;
-    verify_fn(b.vupt)<<<b.vgrid, b.vwarps * 32, b.vsmem, st>>>(va);
-    CK(cudaGetLastError());
+    CK(launch_k(verify_fn(b.vupt), b.vgrid, b.vwarps * 32, b.vsmem, st, pdl, va));
     mark(3);
-    recount_kernel<<<ix->recount_grid, 256, 0, st>>>(va);
-    CK(cudaGetLastError());
+    CK(launch_k(recount_kernel, ix->recount_grid, 256, 0, st, pdl, va));
     mark(4);
 
-    scan_counts_kernel<<<1, 1024, 0, st>>>(w.d_res_count, w.d_cand_off, nq, w.d_out_off);
-    CK(cudaGetLastError());
+    CK(launch_k(scan_counts_kernel, 1, 1024, 0, st, pdl, (const int*)w.d_res_count, (const long long*)w.d_cand_off,
+                nq, w.d_out_off));
     mark(5);
-    finalize_kernel<<<(nq + FIN_WARPS - 1) / FIN_WARPS, 32 * FIN_WARPS, 0, st>>>(
-        w.d_pool, w.d_cand_off, w.d_res_count, w.d_out_off, w.d_out, nq);
-    CK(cudaGetLastError());
+    CK(launch_k(finalize_kernel, (nq + FIN_WARPS - 1) / FIN_WARPS, 32 * FIN_WARPS, 0, st, pdl, w.d_pool,
+                (const long long*)w.d_cand_off, (const int*)w.d_res_count, (const int*)w.d_out_off, w.d_out, nq));
     mark(6);
     return RKNN_OK;
 }
@@ -511,7 +534,7 @@ rknn_status launch(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = true
     if (it == w.graphs.end()) {
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal));
-        rknn_status s = enqueue(ix, c, b);
+        rknn_status s = enqueue(ix, c, b, false, true);
         cudaError_t e = cudaStreamEndCapture(c.st, &g);
         if (s != RKNN_OK) { if (e == cudaSuccess) cudaGraphDestroy(g); return s; }
         CK(e);

@@ -19,6 +19,14 @@ struct Grid {
     int gx, gy;        // cells per axis
 };
 
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialization may start while its predecessor in the stream still runs:
+// pdl_wait() blocks until that grid has completed and its memory operations
+// are visible (a no-op for an ordinary launch), and pdl_trigger() lets the
+// successor launch once every block of this grid has issued it.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Angular slice (of 32 around the origin, slice i spanning [i, i+1) * 11.25
 // degrees counter-clockwise from +x) of direction (vx, vy): the octant from
 // signs and |vx| <= |vy|, then the quarter of the octant from the ratio

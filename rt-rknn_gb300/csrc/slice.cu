@@ -177,6 +177,7 @@ __device__ __forceinline__ void list_insert(float (&L)[KR], float v)
 template <int KR>
 __device__ __forceinline__ void slice_body(const ZoneArgs& A)
 {
+    pdl_trigger();
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31;
 #ifdef RKNN_CHECKED
@@ -539,9 +540,30 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
             planes[SX(m, A.pstride, 318)] = make_float4((float)(-2.0 * dx), (float)(-2.0 * dy), (float)c, 0.0f);
             A.bis_pos[(size_t)s * A.pstride + SX(m, A.pstride, 319)] = pos;
             cmax = fmax(cmax, c);
+            lpos[SX(m, LC, 316)] = __float_as_int(__double2float_rd(c));    // the slot is free now
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) cmax = fmax(cmax, __shfl_xor_sync(FULL, cmax, o));
+        __syncwarp();
+        // Fourth component of half-plane m: the least |f - q|^2 (rounded
+        // down) over half-planes m, m+1, ...  Only a facility within 2|u - q|
+        // of q can be strictly nearer to u than q, so the verification may
+        // stop a user's half-planes once this exceeds 4|u - q|^2.
+        {
+            float carry = INFINITY;
+            for (int t0 = ((nL - 1) >> 5) << 5; t0 >= 0; t0 -= 32) {
+                const int m = t0 + lane;
+                float v = m < nL ? __int_as_float(lpos[SX(m, LC, 316)]) : INFINITY;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const float h = __shfl_down_sync(FULL, v, o);
+                    if (lane + o < 32) v = fminf(v, h);
+                }
+                v = fminf(v, carry);
+                if (m < nL) planes[SX(m, A.pstride, 318)].w = v;
+                carry = __shfl_sync(FULL, v, 0);
+            }
+        }
         const double Fp = sqrt(cmax) * (1.0 + 1e-6) + 1e-30;
         const float k2f = (float)(8.0 * (double)kU32 * 2.0 * Fp * (1.0 + 1e-6));
         const float kf2 = (float)(8.0 * (double)kU32 * Fp * Fp * (1.0 + 1e-6)) + 1e-30f;

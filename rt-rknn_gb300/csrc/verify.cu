@@ -98,19 +98,30 @@ __device__ __forceinline__ int exact_count(float ux, float uy, const QDesc& d, c
 template <typename T, int UPT>
 __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char* sp, const int* pos,
                                              const float2* u, const bool* valid, int* cnt, int* und,
-                                             unsigned long long& evals)
+                                             unsigned& evals, float rho2)
 {
     T x[UPT], y[UPT], bu[UPT];
+    // und[t] on return: the half-planes alone do not decide user t, because
+    // one was too close to call or the user lies beyond rho/2 of q (then a
+    // facility strictly nearer to it need not be a half-plane; rho2 is
+    // (rho/2)^2 scaled by 4, or 0 when not every half-plane was staged).
+    // lim: above 4|u - q|^2 with margin.  The fourth component w of half-plane
+    // m bounds |f - q|^2 from below for it and every later one; once w > lim,
+    // none of them lies within 2|u - q| of q, so none is strictly nearer to u
+    // than q and the user's remaining half-planes are skipped.  (Half-planes
+    // whose w is 0 never cut a user short.)
+    float lim[UPT];
     int nvalid = 0;
 #pragma unroll
     for (int t = 0; t < UPT; ++t) {
         cnt[t] = valid[t] ? 0 : INT_MAX / 2;
         und[t] = 0;
         nvalid += valid[t];
+        const float fx = u[t].x - d.qx, fy = u[t].y - d.qy;
+        lim[t] = 4.0f * fmaf(fx, fx, fy * fy) * (1.0f + 1e-4f) + 1e-30f;
         if (sizeof(T) == 4) {
-            float xx = u[t].x - d.qx, yy = u[t].y - d.qy;
-            x[t] = xx; y[t] = yy;
-            bu[t] = fmaf(d.k2f, fabsf(xx) + fabsf(yy), d.kf2);
+            x[t] = fx; y[t] = fy;
+            bu[t] = fmaf(d.k2f, fabsf(fx) + fabsf(fy), d.kf2);
         } else {
             double xx = (double)u[t].x - (double)d.qx, yy = (double)u[t].y - (double)d.qy;
             x[t] = (T)xx; y[t] = (T)yy;
@@ -150,23 +161,26 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
             if ((m & 7) == 7) {
                 bool done = true;
 #pragma unroll
-                for (int t = 0; t < UPT; ++t) done &= cnt[t] >= k;
+                for (int t = 0; t < UPT; ++t) done &= cnt[t] >= k || p.w > lim[t];
                 if (__all_sync(FULL, done)) { ++m; break; }
             }
         }
 #pragma unroll
-        for (int t = 0; t < UPT; ++t) und[t] = umin[t] <= 0.0f;
-        evals += (unsigned long long)m * nvalid;
+        for (int t = 0; t < UPT; ++t) und[t] = umin[t] <= 0.0f || lim[t] > rho2;
+        evals += (unsigned)(m * nvalid);
         return;
     }
     for (; m < nb; ++m) {
         T a, b, c;
+        float wm;
         if (sizeof(T) == 4) {
             float4 p = ((const float4*)sp)[m];
             a = (T)p.x; b = (T)p.y; c = (T)p.z;
+            wm = p.w;
         } else {
             const double* p = (const double*)sp + 4 * m;
             a = (T)p[0]; b = (T)p[1]; c = (T)p[2];
+            wm = (float)p[3];       // a float to begin with
         }
 #pragma unroll
         for (int t = 0; t < UPT; ++t) {
@@ -177,11 +191,13 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
         if ((m & 7) == 7) {
             bool done = true;
 #pragma unroll
-            for (int t = 0; t < UPT; ++t) done &= cnt[t] >= k;
+            for (int t = 0; t < UPT; ++t) done &= cnt[t] >= k || wm > lim[t];
             if (__all_sync(FULL, done)) { ++m; break; }
         }
     }
-    evals += (unsigned long long)m * nvalid;
+#pragma unroll
+    for (int t = 0; t < UPT; ++t) und[t] |= lim[t] > rho2;
+    evals += (unsigned)(m * nvalid);
 }
 
 }  // namespace
@@ -192,6 +208,8 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
     extern __shared__ __align__(16) char smem[];
     // every st-th work-item offset, for the item -> slot lookup
     __shared__ int csmp[VERIFY_SAMPLES];
+    pdl_wait();
+    pdl_trigger();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const size_t plane_bytes = (size_t)A.stage_cap * (A.mode == MODE_FP32 ? 16 : 32);
     char* sp = smem + w * (plane_bytes + (size_t)A.seg_stage * sizeof(int2));
@@ -202,7 +220,8 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
     __syncthreads();
     int cur = -1;
     bool seg_staged = false;
-    unsigned long long s_cand = 0, s_evals = 0, s_surv = 0, s_fac = 0, s_rech = 0, s_res = 0;
+    // per-warp statistics (32-bit here, 64-bit in the totals)
+    unsigned s_cand = 0, s_evals = 0, s_surv = 0, s_fac = 0, s_rech = 0, s_res = 0;
     const int total = A.chunk_off[A.nq];
     for (;;) {
         int g = 0;
@@ -248,7 +267,7 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
                     p[0] = -2.0 * dx;
                     p[1] = -2.0 * dy;
                     p[2] = fma(dx, dx, dy * dy);
-                    p[3] = 0.0;
+                    p[3] = (double)A.planes[(size_t)s * A.lc + m].w;
                 }
             }
             // the slot's user segments (nseg ranges and the terminal entry)
@@ -305,23 +324,17 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
         }
         int cnt[UPT], und[UPT];
         const int nbs = min(d.nb, A.stage_cap);
-        if (A.mode == MODE_FP32) filter_users<float, UPT>(d, nbs, sp, pos, u, valid, cnt, und, s_evals);
-        else filter_users<double, UPT>(d, nbs, sp, pos, u, valid, cnt, und, s_evals);
         // A user within rho/2 of q is decided by the half-planes alone: every
         // facility strictly nearer to it than q lies within 2|u-q| <= rho of
         // q, so it is a half-plane.  With no undecided half-plane the
         // certified count is the exact count.  (All half-planes must be
         // staged for this.)
+        const float rho2 = (nbs == d.nb) ? d.rho * d.rho * (1.0f - 1e-5f) : 0.0f;
+        if (A.mode == MODE_FP32) filter_users<float, UPT>(d, nbs, sp, pos, u, valid, cnt, und, s_evals, rho2);
+        else filter_users<double, UPT>(d, nbs, sp, pos, u, valid, cnt, und, s_evals, rho2);
         bool direct[UPT];
-        {
-            const float rho2 = (nbs == d.nb) ? d.rho * d.rho * (1.0f - 1e-5f) : 0.0f;
 #pragma unroll
-            for (int t = 0; t < UPT; ++t) {
-                const float xx = u[t].x - d.qx, yy = u[t].y - d.qy;
-                const float du2 = 4.0f * fmaf(xx, xx, yy * yy) * (1.0f + 1e-5f);
-                direct[t] = valid[t] && cnt[t] < d.k && und[t] == 0 && du2 <= rho2;
-            }
-        }
+        for (int t = 0; t < UPT; ++t) direct[t] = valid[t] && cnt[t] < d.k && und[t] == 0;
 
         // stage 2: survivors go to the list for recount_kernel; when it is
         // full, the warp counts them itself, one user at a time
@@ -360,9 +373,13 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
             while (m) {
                 int l = __ffs(m) - 1;
                 m &= m - 1;
-                float ux = __shfl_sync(FULL, u[t].x, l), uy = __shfl_sync(FULL, u[t].y, l);
-                int c = (A.mode == MODE_FP32) ? exact_count<float>(ux, uy, d, A, s_fac, s_rech)
-                                              : exact_count<double>(ux, uy, d, A, s_fac, s_rech);
+                const float2 ul = A.uxy[VX(__shfl_sync(FULL, pos[t], l), A.nu, 219)];
+                const float ux = ul.x, uy = ul.y;
+                unsigned long long fac = 0, rech = 0;
+                int c = (A.mode == MODE_FP32) ? exact_count<float>(ux, uy, d, A, fac, rech)
+                                              : exact_count<double>(ux, uy, d, A, fac, rech);
+                s_fac += (unsigned)fac;
+                s_rech += (unsigned)rech;
                 if (lane == l) acc[t] = c < d.k;
             }
         }
@@ -396,19 +413,19 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
         s_rech += __shfl_xor_sync(FULL, s_rech, o);
     }
     if (lane == 0 && A.vstats) {
-        atomicAdd(&A.vstats->cand, s_cand);
-        atomicAdd(&A.vstats->plane_evals, s_evals);
-        atomicAdd(&A.vstats->survivors, s_surv);
-        atomicAdd(&A.vstats->fac_checks, s_fac);
-        atomicAdd(&A.vstats->rechecks, s_rech);
-        atomicAdd(&A.vstats->results, s_res);
+        atomicAdd(&A.vstats->cand, (unsigned long long)s_cand);
+        atomicAdd(&A.vstats->plane_evals, (unsigned long long)s_evals);
+        atomicAdd(&A.vstats->survivors, (unsigned long long)s_surv);
+        atomicAdd(&A.vstats->fac_checks, (unsigned long long)s_fac);
+        atomicAdd(&A.vstats->rechecks, (unsigned long long)s_rech);
+        atomicAdd(&A.vstats->results, (unsigned long long)s_res);
     }
 }
 
 // The verification kernel with 2, 4 or 8 users per lane per work item
 // (32 * UPT users per item); blocks of up to 16 warps.
-__global__ void __launch_bounds__(512) verify_kernel(VerifyArgs a) { verify_body<4>(a); }
-__global__ void __launch_bounds__(512) verify_kernel_u2(VerifyArgs a) { verify_body<2>(a); }
+__global__ void __maxnreg__(80) verify_kernel(VerifyArgs a) { verify_body<4>(a); }
+__global__ void __maxnreg__(80) verify_kernel_u2(VerifyArgs a) { verify_body<2>(a); }
 __global__ void __launch_bounds__(512) verify_kernel_u8(VerifyArgs a) { verify_body<8>(a); }
 
 // One warp per listed survivor.  Lane r computes the facility range of
@@ -486,6 +503,8 @@ __device__ __forceinline__ int warp_exact_count(float ux, float uy, const QDesc&
 // appended with one atomic per survivor.
 __global__ void __launch_bounds__(256) recount_kernel(VerifyArgs A)
 {
+    pdl_wait();
+    pdl_trigger();
     const int lane = threadIdx.x & 31;
     const int n = min(*A.surv_count, A.surv_cap);
     unsigned long long s_fac = 0, s_rech = 0, s_res = 0;
@@ -556,6 +575,8 @@ constexpr int SCAN_THREADS = 1024, SCAN_PT = 4, SCAN_TILE = SCAN_THREADS * SCAN_
 __global__ void __launch_bounds__(SCAN_THREADS)
 plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_off, long long pool_cap, int rcap, int chunk)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ int sn[SCAN_TILE];
     __shared__ long long tmp64[32];
     __shared__ int tmp[32];
@@ -610,6 +631,8 @@ plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_off, long long po
 __global__ void __launch_bounds__(SCAN_THREADS)
 scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int* out_off)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ int sn[SCAN_TILE];
     __shared__ int tmp[32];
     const int tid = threadIdx.x;
@@ -749,6 +772,7 @@ __global__ void __launch_bounds__(32 * FIN_WARPS, 1)
 finalize_kernel(int* res_pool, const long long* cand_off, const int* res_count, const int* out_off,
                 int* out, int nq)
 {
+    pdl_wait();
     __shared__ unsigned skeys[FIN_BCAP];
     __shared__ int big[FIN_WARPS];
     __shared__ int nbig;

@@ -410,6 +410,7 @@ __device__ __forceinline__ int inval32(const float4& L, float x, float y, float 
 
 __device__ __forceinline__ void zone_body(const ZoneArgs& A)
 {
+    pdl_trigger();
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
