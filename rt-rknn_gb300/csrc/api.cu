@@ -12,7 +12,6 @@
 //   finalize_kernel  one warp per query (the block for large sets): sort its
 //                    ids into the output
 #include "../../include/rknn_gpu.h"
-#include <utility>
 #include "index.cuh"
 #include "rknn_common.cuh"
 #include "verify.cuh"
@@ -26,6 +25,7 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <utility>
 #include <vector>
 
 using namespace rknn;
@@ -75,7 +75,10 @@ constexpr int MAX_CLASSES = 16;
 
 struct Workspace {
     int nq_cap = 0, lc = 0, seg_cap = 0;
-    int *d_q = nullptr, *d_k = nullptr, *d_order = nullptr;
+    // a batch of nq queries: q at [0, nq), k at [nq, 2 nq), the k order at
+    // [2 nq, 3 nq) of one buffer, on the device and in page-locked staging,
+    // so that one copy moves them
+    int* d_qko = nullptr;
     QDesc* d_qd = nullptr;
     float4* d_planes = nullptr;
     float* d_slice_r = nullptr;    // [slot][32] slice filter bounds
@@ -95,7 +98,7 @@ struct Workspace {
     long long surv_cap = 0;
     char* d_zscratch = nullptr;
     size_t zscratch_bytes = 0;
-    int *h_q = nullptr, *h_k = nullptr, *h_order = nullptr, *h_off = nullptr;
+    int *h_qko = nullptr, *h_off = nullptr;   // h_off: nq+1 offsets, then the run's flags (OFF_TAIL)
     int* h_ids = nullptr;
     long long h_ids_cap = 0;
     std::map<GraphKey, cudaGraphExec_t> graphs;
@@ -130,6 +133,10 @@ struct rknn_index {
     int num_sms = 0;
     int recount_grid = 0;       // one wave of recount_kernel blocks
     bool pdl = true;            // programmatic dependent launch between the batch kernels
+    // occupancy answers by (kernel, threads, dynamic shared memory): a batch's
+    // plan asks the same few questions on every call
+    std::mutex occ_mu;
+    std::map<std::tuple<const void*, int, size_t>, int> occ;
     size_t smem_optin = 0;
     Workspace ws;
     std::mutex mu;
@@ -163,13 +170,13 @@ void free_ws(Workspace& w)
 {
     for (auto& g : w.graphs) cudaGraphExecDestroy(g.second);
     w.graphs.clear();
-    cudaFree(w.d_q); cudaFree(w.d_k); cudaFree(w.d_order);
+    cudaFree(w.d_qko);
     cudaFree(w.d_qd); cudaFree(w.d_planes); cudaFree(w.d_bispos); cudaFree(w.d_segs); cudaFree(w.d_zst);
     cudaFree(w.d_slice_r);
     cudaFree(w.d_cand_off); cudaFree(w.d_chunk_off); cudaFree(w.d_res_count); cudaFree(w.d_out_off);
     cudaFree(w.d_counters); cudaFree(w.d_vstats);
     cudaFree(w.d_pool); cudaFree(w.d_out); cudaFree(w.d_zscratch); cudaFree(w.d_surv);
-    cudaFreeHost(w.h_q); cudaFreeHost(w.h_k); cudaFreeHost(w.h_order); cudaFreeHost(w.h_off);
+    cudaFreeHost(w.h_qko); cudaFreeHost(w.h_off);
     cudaFreeHost(w.h_ids);
     for (int i = 0; i < NAUX; ++i) {
         if (w.aux[i]) cudaStreamDestroy(w.aux[i]);
@@ -193,6 +200,24 @@ struct ZoneLaunch {
     int grid;
 };
 
+// Resident blocks per SM of kernel fn at this block size and dynamic shared
+// memory (at least 1), remembered per index.
+int occupancy(rknn_index* ix, const void* fn, int threads, size_t smem)
+{
+    std::lock_guard<std::mutex> lk(ix->occ_mu);
+    const auto key = std::make_tuple(fn, threads, smem);
+    auto it = ix->occ.find(key);
+    if (it != ix->occ.end()) return it->second;
+    int per = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        per = 1;
+    }
+    per = std::max(per, 1);
+    ix->occ.emplace(key, per);
+    return per;
+}
+
 // The slice filter's kernel for a class whose largest k is kmax.
 using ZoneFn = void (*)(ZoneArgs);
 ZoneFn slice_fn(int kmax)
@@ -205,10 +230,7 @@ ZoneLaunch zone_launch(rknn_index* ix, const ZoneCaps& c, int nq, bool slice = f
     ZoneLaunch L;
     L.slice = slice ? slice_layout(c).bytes : zone_layout(c).bytes;
     L.smem = L.slice * ZONE_WARPS;
-    int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, slice ? slice_fn(kmax) : zone_kernel_smem,
-                                                  32 * ZONE_WARPS, L.smem);
-    if (per_sm < 1) per_sm = 1;
+    const int per_sm = occupancy(ix, (const void*)(slice ? slice_fn(kmax) : zone_kernel_smem), 32 * ZONE_WARPS, L.smem);
     long long want = (nq + ZONE_WARPS - 1) / ZONE_WARPS;
     L.grid = (int)std::max(1LL, std::min<long long>(want, (long long)per_sm * ix->num_sms));
     return L;
@@ -244,7 +266,7 @@ rknn_status ensure_ws(Workspace& w, int nq, const ZoneCaps& caps, long long pool
         w.rcap = rcap;
         w.surv_cap = scap;
         w.nq_cap = nqc; w.lc = lc; w.seg_cap = sc;
-        CK(dalloc(w.d_q, nqc)); CK(dalloc(w.d_k, nqc)); CK(dalloc(w.d_order, nqc));
+        CK(dalloc(w.d_qko, (size_t)3 * nqc));
         CK(dalloc(w.d_qd, nqc));
         CK(dalloc(w.d_planes, (size_t)nqc * lc));
         CK(dalloc(w.d_slice_r, (size_t)nqc * 32));
@@ -252,7 +274,7 @@ rknn_status ensure_ws(Workspace& w, int nq, const ZoneCaps& caps, long long pool
         CK(dalloc(w.d_segs, (size_t)nqc * sc));
         CK(dalloc(w.d_zst, nqc));
         CK(dalloc(w.d_cand_off, nqc + 1)); CK(dalloc(w.d_chunk_off, nqc + 1));
-        CK(dalloc(w.d_res_count, nqc)); CK(dalloc(w.d_out_off, nqc + 1));
+        CK(dalloc(w.d_res_count, nqc)); CK(dalloc(w.d_out_off, nqc + 1 + OFF_TAIL));
         CK(dalloc(w.d_counters, 64));
         CK(cudaMemset(w.d_counters, 0, sizeof(int) * 64));
         for (int i = 0; i < NAUX; ++i) {
@@ -261,10 +283,8 @@ rknn_status ensure_ws(Workspace& w, int nq, const ZoneCaps& caps, long long pool
         }
         CK(cudaEventCreateWithFlags(&w.fork, cudaEventDisableTiming));
         CK(dalloc(w.d_vstats, 1));
-        CK(cudaMallocHost(&w.h_q, sizeof(int) * nqc));
-        CK(cudaMallocHost(&w.h_k, sizeof(int) * nqc));
-        CK(cudaMallocHost(&w.h_order, sizeof(int) * nqc));
-        CK(cudaMallocHost(&w.h_off, sizeof(int) * (nqc + 1)));
+        CK(cudaMallocHost(&w.h_qko, sizeof(int) * 3 * (size_t)nqc));
+        CK(cudaMallocHost(&w.h_off, sizeof(int) * (nqc + 1 + OFF_TAIL)));
         w.pool_cap = 0;
     }
     if (!w.d_surv) {
@@ -373,9 +393,11 @@ BatchPlan plan_batch(rknn_index* ix, int nq, int mode, bool use_order, const int
         b.cls.push_back(ZClass{0, nq, std::max(1, kmax), false, {}, {}});
     }
     b.key = {nq, mode, use_order ? 1 : 0};
-    // half-planes the verification can stage per warp (96 KB per block)
-    const int bpp = mode == MODE_FP32 ? 16 : 32;
-    const int stage_max = std::max(1, (96 << 10) / (ix->vwarps * bpp));
+    // half-planes the verification can stage per warp (128 KB per block;
+    // 32 bytes each in both modes: FP32 stages them pre-duplicated for the
+    // packed FMA)
+    const int bpp = 32;
+    const int stage_max = std::max(1, (128 << 10) / (ix->vwarps * bpp));
     for (auto& c : b.cls) {
         c.slice = use_slice(ix, c.kmax);
         c.caps = c.slice ? slice_caps(c.kmax, std::min(512, stage_max)) : caps_fit(ix, caps_for(c.kmax));
@@ -394,10 +416,8 @@ BatchPlan plan_batch(rknn_index* ix, int nq, int mode, bool use_order, const int
     int rm = 0;
     for (auto& c : b.cls) rm = std::max(rm, c.caps.rm);
     b.seg_stage = std::min(2 * rm + 2, 512);
-    b.vsmem = (size_t)b.vwarps * ((size_t)b.stage_cap * bpp + (size_t)b.seg_stage * sizeof(int2));
-    int vper = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&vper, verify_fn(b.vupt), b.vwarps * 32, b.vsmem);
-    if (vper < 1) vper = 1;
+    b.vsmem = (size_t)b.vwarps * ((size_t)b.stage_cap * bpp + (size_t)b.seg_stage * sizeof(int2) + 32 * sizeof(float));
+    const int vper = occupancy(ix, (const void*)verify_fn(b.vupt), b.vwarps * 32, b.vsmem);
     b.vgrid = vper * ix->num_sms;
     b.key.push_back(b.vupt);
     b.key.push_back(b.vwarps);
@@ -451,7 +471,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     za.gf = ix->gf; za.nf = (int)ix->nf;
     za.ustart = ix->d_ustart; za.gu = ix->gu; za.nu = (int)ix->nu;
     za.sx0 = ix->sx0; za.sy0 = ix->sy0; za.sx1 = ix->sx1; za.sy1 = ix->sy1;
-    za.q_in = w.d_q; za.k_in = w.d_k;
+    za.q_in = w.d_qko; za.k_in = w.d_qko + nq;
     za.skip_coincident = ix->skip_coincident;
     za.seg_cap = w.seg_cap;
     za.qd = w.d_qd; za.planes = w.d_planes; za.bis_pos = w.d_bispos; za.segs = w.d_segs; za.zst = w.d_zst;
@@ -466,7 +486,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     }
     for (int i = 0; i < ncls; ++i) {
         const ZClass& z = b.cls[i];
-        za.order = b.use_order ? w.d_order + z.off : nullptr;
+        za.order = b.use_order ? w.d_qko + 2 * nq + z.off : nullptr;
         za.nq = z.n;
         za.caps = z.caps;
         za.rmax = z.caps.rm;
@@ -511,7 +531,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     mark(4);
 
     CK(launch_k(scan_counts_kernel, 1, 1024, 0, st, pdl, (const int*)w.d_res_count, (const long long*)w.d_cand_off,
-                nq, w.d_out_off));
+                nq, w.d_out_off, (const int*)w.d_counters));
     mark(5);
     CK(launch_k(finalize_kernel, (nq + FIN_WARPS - 1) / FIN_WARPS, 32 * FIN_WARPS, 0, st, pdl, w.d_pool,
                 (const long long*)w.d_cand_off, (const int*)w.d_res_count, (const int*)w.d_out_off, w.d_out, nq));
@@ -581,12 +601,30 @@ rknn_status collect_stats(Ctx& c, int nq, rknn_query_stats* out)
     return RKNN_OK;
 }
 
-// Run a batch whose q/k are already in ws.d_q / ws.d_k.  Grows the result
+// Run a batch whose q/k are already in the workspace (d_qko).  Grows the result
 // pool and reruns when a query's candidate region did not fit.
 // Launch, read the offsets and counters back, and rerun when a region or the
 // pool was too small.  spec (page-locked, spec_n ids) takes a speculative copy
 // of the first spec_n result ids in the same stream round trip: when the batch
 // returned at most spec_n ids the caller needs no second copy.
+// The flags scan_counts_kernel leaves after the nq+1 offsets (OFF_TAIL ints):
+// the sum of the result regions (two halves), whether a slot had more
+// results than its region, and how many survivors were listed.
+struct RunTail {
+    long long region_total;
+    int dropped, survivors;
+};
+
+RunTail run_tail(const int* h_off, int nq)
+{
+    const int* t = h_off + nq + 1;
+    RunTail r;
+    r.region_total = (long long)(((unsigned long long)(unsigned)t[1] << 32) | (unsigned)t[0]);
+    r.dropped = t[2];
+    r.survivors = t[3];
+    return r;
+}
+
 rknn_status run_sync(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = true, int* spec = nullptr,
                      long long spec_n = 0)
 {
@@ -601,18 +639,18 @@ rknn_status run_sync(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = tr
         s = launch(ix, c, b, graph);
         if (s != RKNN_OK) return s;
         CK(cudaEventRecord(c.ev1, c.st));
-        long long region_total = 0;
-        int flags[2] = {0, 0};      // region exceeded, survivors listed
-        CK(cudaMemcpyAsync(&region_total, w.d_cand_off + nq, sizeof(long long), cudaMemcpyDeviceToHost, c.st));
-        CK(cudaMemcpyAsync(flags, w.d_counters + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.st));
-        const int& dropped = flags[0];
-        CK(cudaMemcpyAsync(w.h_off, w.d_out_off, sizeof(int) * (nq + 1), cudaMemcpyDeviceToHost, c.st));
+        // offsets and the run's flags in one copy
+        CK(cudaMemcpyAsync(w.h_off, w.d_out_off, sizeof(int) * (nq + 1 + OFF_TAIL), cudaMemcpyDeviceToHost, c.st));
         const long long sn = std::min(spec_n, w.pool_cap);
         if (spec && sn > 0) CK(cudaMemcpyAsync(spec, w.d_out, sizeof(int) * sn, cudaMemcpyDeviceToHost, c.st));
         CK(cudaStreamSynchronize(c.st));
         float ms = 0;
         cudaEventElapsedTime(&ms, c.ev0, c.ev1);
         *c.device_ms = ms;
+        const RunTail tail = run_tail(w.h_off, nq);
+        const long long region_total = tail.region_total;
+        const int dropped = tail.dropped;
+        const int flags[2] = {tail.dropped, tail.survivors};
         if ((unsigned)flags[1] > (unsigned long long)w.surv_cap) {
             // survivors overflowed the list (they were recounted in-warp):
             // give the next batch room for all of them
@@ -941,14 +979,11 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
     if (s != RKNN_OK) return s;
     Workspace& w = ix->ws;
     Ctx c = main_ctx(ix);
-    std::memcpy(w.h_q, q, sizeof(int) * nq);
-    std::memcpy(w.h_k, k, sizeof(int) * nq);
-    if (!uniform) {
-        std::memcpy(w.h_order, order.data(), sizeof(int) * nq);
-        CK(cudaMemcpyAsync(w.d_order, w.h_order, sizeof(int) * nq, cudaMemcpyHostToDevice, ix->stream));
-    }
-    CK(cudaMemcpyAsync(w.d_q, w.h_q, sizeof(int) * nq, cudaMemcpyHostToDevice, ix->stream));
-    CK(cudaMemcpyAsync(w.d_k, w.h_k, sizeof(int) * nq, cudaMemcpyHostToDevice, ix->stream));
+    std::memcpy(w.h_qko, q, sizeof(int) * nq);
+    std::memcpy(w.h_qko + nq, k, sizeof(int) * nq);
+    if (!uniform) std::memcpy(w.h_qko + 2 * nq, order.data(), sizeof(int) * nq);
+    CK(cudaMemcpyAsync(w.d_qko, w.h_qko, sizeof(int) * (size_t)(uniform ? 2 : 3) * nq, cudaMemcpyHostToDevice,
+                       ix->stream));
     // The ids come back with the offsets when the batch returns no more than
     // the previous one plus a margin: page-locked caller buffers take them
     // directly, pageable ones through the workspace's page-locked staging.
@@ -1047,8 +1082,8 @@ rknn_status rknn_query_batch_device(rknn_index* ix, const int32_t* d_q, const in
     ix->last_lc = b.pstride;
     rknn_status s = ensure_ws(w, nq, plan_caps(b), std::max<long long>(w.pool_cap, (long long)nq * 4096));
     if (s != RKNN_OK) return s;
-    CK(cudaMemcpyAsync(w.d_q, d_q, sizeof(int) * nq, cudaMemcpyDeviceToDevice, ix->stream));
-    CK(cudaMemcpyAsync(w.d_k, d_k, sizeof(int) * nq, cudaMemcpyDeviceToDevice, ix->stream));
+    CK(cudaMemcpyAsync(w.d_qko, d_q, sizeof(int) * nq, cudaMemcpyDeviceToDevice, ix->stream));
+    CK(cudaMemcpyAsync(w.d_qko + nq, d_k, sizeof(int) * nq, cudaMemcpyDeviceToDevice, ix->stream));
     Ctx c = main_ctx(ix);
     s = launch(ix, c, b);
     ix->last_nq = nq;
@@ -1071,11 +1106,11 @@ rknn_status rknn_batch_device_results(rknn_index* ix, const int32_t** d_ids, con
         // and k are still in the workspace) with room for all of them
         Workspace& w = ix->ws;
         const int nq = ix->dev_nq;
-        long long region_total = 0;
-        int dropped = 0;
-        CK(cudaMemcpyAsync(&region_total, w.d_cand_off + nq, sizeof(long long), cudaMemcpyDeviceToHost, ix->stream));
-        CK(cudaMemcpyAsync(&dropped, w.d_counters + 2, sizeof(int), cudaMemcpyDeviceToHost, ix->stream));
+        CK(cudaMemcpyAsync(w.h_off, w.d_out_off, sizeof(int) * (nq + 1 + OFF_TAIL), cudaMemcpyDeviceToHost, ix->stream));
         CK(cudaStreamSynchronize(ix->stream));
+        const RunTail tail = run_tail(w.h_off, nq);
+        const long long region_total = tail.region_total;
+        const int dropped = tail.dropped;
         if (region_total > w.pool_cap || dropped) {
             if (dropped) w.rcap = (int)std::min<long long>((long long)w.rcap * 8, std::max<long long>(ix->nu, 1));
             const BatchPlan b = plan_batch(ix, nq, ix->dev_mode, false, nullptr, ix->dev_kmax);
@@ -1168,7 +1203,7 @@ NoallocLayout noalloc_layout(unsigned char* base, int lc, int seg_cap)
     L.cand_off = (long long*)take(sizeof(long long) * 2);
     L.chunk_off = (int*)take(sizeof(int) * 2);
     L.res_count = (int*)take(sizeof(int));
-    L.out_off = (int*)take(sizeof(int) * 2);
+    L.out_off = (int*)take(sizeof(int) * (2 + OFF_TAIL));
     L.qd = (QDesc*)take(sizeof(QDesc));
     L.zst = (ZStats*)take(sizeof(ZStats));
     L.vstats = (VStats*)take(sizeof(VStats));
@@ -1253,10 +1288,10 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     va.nu = (int)ix->nu; va.nf = (int)ix->nf; va.ncf = ix->gf.gx * ix->gf.gy;
     va.pool_cap = L.pool_cap; va.fault = L.counters + 10; va.dropped = L.counters + 2;
     va.surv = nullptr; va.surv_cap = 0; va.surv_count = L.counters + 3;
-    const size_t vsmem = (size_t)VERIFY_WARPS * caps.lc * (mode == MODE_FP32 ? 16 : 32);
+    const size_t vsmem = (size_t)VERIFY_WARPS * ((size_t)caps.lc * 32 + 32 * sizeof(float));
     verify_kernel<<<2 * ix->num_sms, VERIFY_WARPS * 32, vsmem, st>>>(va);
     CK(cudaGetLastError());
-    scan_counts_kernel<<<1, 1024, 0, st>>>(L.res_count, L.cand_off, 1, L.out_off);
+    scan_counts_kernel<<<1, 1024, 0, st>>>(L.res_count, L.cand_off, 1, L.out_off, L.counters);
     CK(cudaGetLastError());
     finalize_kernel<<<1, 32 * FIN_WARPS, 0, st>>>(L.pool, L.cand_off, L.res_count, L.out_off, L.out, 1);
     CK(cudaGetLastError());
@@ -1318,7 +1353,6 @@ struct Slot {
     Workspace ws;
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, done = nullptr;
-    long long* h_tot = nullptr;      // pinned: [0] region total, [1] region exceeded
     double device_ms = 0;
     std::vector<ReqPtr> reqs;        // the batch in flight
     BatchPlan plan;
@@ -1401,22 +1435,17 @@ rknn_status slot_launch(rknn_server* sv, Slot& sl)
     rknn_status s = ensure_ws(w, nqp, plan_caps(sl.plan), std::max<long long>(w.pool_cap, (long long)nqp * 4096));
     if (s != RKNN_OK) return s;
     for (int i = 0; i < nqp; ++i) {
-        w.h_q[i] = i < nq ? sl.reqs[i]->q : -1;
-        w.h_k[i] = i < nq ? sl.reqs[i]->k : 1;
-        w.h_order[i] = order[i];
+        w.h_qko[i] = i < nq ? sl.reqs[i]->q : -1;
+        w.h_qko[nqp + i] = i < nq ? sl.reqs[i]->k : 1;
+        w.h_qko[2 * nqp + i] = order[i];
     }
-    CK(cudaMemcpyAsync(w.d_q, w.h_q, sizeof(int) * nqp, cudaMemcpyHostToDevice, sl.st));
-    CK(cudaMemcpyAsync(w.d_k, w.h_k, sizeof(int) * nqp, cudaMemcpyHostToDevice, sl.st));
-    CK(cudaMemcpyAsync(w.d_order, w.h_order, sizeof(int) * nqp, cudaMemcpyHostToDevice, sl.st));
+    CK(cudaMemcpyAsync(w.d_qko, w.h_qko, sizeof(int) * 3 * (size_t)nqp, cudaMemcpyHostToDevice, sl.st));
     Ctx c{w, sl.st, sl.ev0, sl.ev1, nullptr, &sl.device_ms};
     CK(cudaEventRecord(sl.ev0, sl.st));
     s = launch(ix, c, sl.plan, false);
     if (s != RKNN_OK) return s;
     CK(cudaEventRecord(sl.ev1, sl.st));
-    sl.h_tot[1] = 0;
-    CK(cudaMemcpyAsync(sl.h_tot, w.d_cand_off + nqp, sizeof(long long), cudaMemcpyDeviceToHost, sl.st));
-    CK(cudaMemcpyAsync(sl.h_tot + 1, w.d_counters + 2, sizeof(int), cudaMemcpyDeviceToHost, sl.st));
-    CK(cudaMemcpyAsync(w.h_off, w.d_out_off, sizeof(int) * (nqp + 1), cudaMemcpyDeviceToHost, sl.st));
+    CK(cudaMemcpyAsync(w.h_off, w.d_out_off, sizeof(int) * (nqp + 1 + OFF_TAIL), cudaMemcpyDeviceToHost, sl.st));
     CK(cudaEventRecord(sl.done, sl.st));
     return RKNN_OK;
 }
@@ -1426,7 +1455,8 @@ rknn_status slot_collect(rknn_server* sv, Slot& sl)
 {
     Workspace& w = sl.ws;
     const int nq = (int)sl.reqs.size();
-    if (sl.h_tot[0] > w.pool_cap || sl.h_tot[1] != 0) {
+    const RunTail tail = run_tail(w.h_off, sl.plan.nq);
+    if (tail.region_total > w.pool_cap || tail.dropped != 0) {
         // a result region did not fit the pool, or held too few ids: rerun
         Ctx c{w, sl.st, sl.ev0, sl.ev1, nullptr, &sl.device_ms};
         rknn_status s = run_sync(sv->ix, c, sl.plan, false);
@@ -1517,7 +1547,6 @@ void destroy_server(rknn_server* sv)
     for (auto& sl : sv->slots) {
         if (sl.st) cudaStreamSynchronize(sl.st);
         free_ws(sl.ws);
-        if (sl.h_tot) cudaFreeHost(sl.h_tot);
         if (sl.ev0) cudaEventDestroy(sl.ev0);
         if (sl.ev1) cudaEventDestroy(sl.ev1);
         if (sl.done) cudaEventDestroy(sl.done);
@@ -1561,7 +1590,6 @@ rknn_status rknn_serve_start(rknn_index* ix, const rknn_serve_opts* opts, rknn_s
         if (e == cudaSuccess) e = cudaEventCreate(&sl.ev0);
         if (e == cudaSuccess) e = cudaEventCreate(&sl.ev1);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_tot, 2 * sizeof(long long));
         if (e != cudaSuccess) {
             destroy_server(sv);
             return fail(RKNN_ERR_CUDA, std::string("server setup: ") + cudaGetErrorString(e));

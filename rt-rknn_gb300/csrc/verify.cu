@@ -132,12 +132,17 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
     int m = 0;
     if constexpr (sizeof(T) == 4) {
         // FP32: users in pairs through the packed FMA (each half rounds as
-        // fmaf).  mv < -bu exactly when fl(mv + bu) is negative, and
-        // |mv| <= bu exactly when fl(|mv| - bu) <= 0: a nonzero exact sum of
-        // two floats never rounds to zero, and bu > 0 rules out -0.
+        // fmaf); half-plane m is staged as (a, a, b, b), (c, c, w, w).  With
+        // r = fl(mv + bu): mv < -bu exactly when r is negative (a nonzero
+        // exact sum of two floats never rounds to zero, and bu > 0 rules out
+        // -0), and |mv| <= bu implies 0 <= r <= 2bu (rounding is monotone):
+        // the smallest non-negative r, taken as the least unsigned bit
+        // pattern (negative floats have the sign bit set), at most 2bu
+        // (rounded up) flags a half-plane too close to call.  That test may
+        // also flag a few decided ones; such users are only recounted.
         constexpr int H2 = UPT / 2;
         float2 X[H2], Y[H2], B[H2];
-        float umin[UPT];
+        unsigned rmin[UPT];
 #pragma unroll
         for (int h = 0; h < H2; ++h) {
             X[h] = make_float2((float)x[2 * h], (float)x[2 * h + 1]);
@@ -145,28 +150,31 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
             B[h] = make_float2((float)bu[2 * h], (float)bu[2 * h + 1]);
         }
 #pragma unroll
-        for (int t = 0; t < UPT; ++t) umin[t] = INFINITY;
+        for (int t = 0; t < UPT; ++t) rmin[t] = 0xffffffffu;
+        const float4* sp4 = (const float4*)sp;
         for (; m < nb; ++m) {
-            const float4 p = ((const float4*)sp)[m];
-            const float2 a2 = make_float2(p.x, p.x), b2 = make_float2(p.y, p.y), c2 = make_float2(p.z, p.z);
+            const float4 ab = sp4[2 * m], cw = sp4[2 * m + 1];
+            const float2 a2 = make_float2(ab.x, ab.y), b2 = make_float2(ab.z, ab.w), c2 = make_float2(cw.x, cw.y);
 #pragma unroll
             for (int h = 0; h < H2; ++h) {
                 const float2 mv = __ffma2_rn(a2, X[h], __ffma2_rn(b2, Y[h], c2));
                 const float2 r = __fadd2_rn(mv, B[h]);
-                cnt[2 * h] += (int)(__float_as_uint(r.x) >> 31);
-                cnt[2 * h + 1] += (int)(__float_as_uint(r.y) >> 31);
-                umin[2 * h] = fminf(umin[2 * h], fabsf(mv.x) - B[h].x);
-                umin[2 * h + 1] = fminf(umin[2 * h + 1], fabsf(mv.y) - B[h].y);
+                const unsigned rx = __float_as_uint(r.x), ry = __float_as_uint(r.y);
+                cnt[2 * h] += (int)(rx >> 31);
+                cnt[2 * h + 1] += (int)(ry >> 31);
+                rmin[2 * h] = min(rmin[2 * h], rx);
+                rmin[2 * h + 1] = min(rmin[2 * h + 1], ry);
             }
             if ((m & 7) == 7) {
                 bool done = true;
 #pragma unroll
-                for (int t = 0; t < UPT; ++t) done &= cnt[t] >= k || p.w > lim[t];
+                for (int t = 0; t < UPT; ++t) done &= cnt[t] >= k || cw.z > lim[t];
                 if (__all_sync(FULL, done)) { ++m; break; }
             }
         }
 #pragma unroll
-        for (int t = 0; t < UPT; ++t) und[t] = umin[t] <= 0.0f || lim[t] > rho2;
+        for (int t = 0; t < UPT; ++t)
+            und[t] = rmin[t] <= __float_as_uint(__fmul_ru((float)bu[t], 2.0f * (1.0f + 0x1p-20f))) || lim[t] > rho2;
         evals += (unsigned)(m * nvalid);
         return;
     }
@@ -211,9 +219,12 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
     pdl_wait();
     pdl_trigger();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const size_t plane_bytes = (size_t)A.stage_cap * (A.mode == MODE_FP32 ? 16 : 32);
-    char* sp = smem + w * (plane_bytes + (size_t)A.seg_stage * sizeof(int2));
+    // per warp: stage_cap half-planes (32 bytes each), seg_stage segments,
+    // the slot's 32 slice bounds
+    const size_t plane_bytes = (size_t)A.stage_cap * 32;
+    char* sp = smem + w * (plane_bytes + (size_t)A.seg_stage * sizeof(int2) + 32 * sizeof(float));
     int2* ssg = (int2*)(sp + plane_bytes);
+    float* sr = (float*)(ssg + A.seg_stage);
     const int st = max(1, (A.nq + VERIFY_SAMPLES) / VERIFY_SAMPLES);     // ceil((nq + 1) / samples)
     const int nsmp = A.nq / st + 1;                                       // samples i * st <= nq
     for (int i = threadIdx.x; i < nsmp; i += blockDim.x) csmp[i] = A.chunk_off[i * st];
@@ -252,13 +263,27 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
                 s = l;
             }
         }
+        if (s != cur && A.mode == MODE_FP32) {
+            // staged before the slot record arrives (the loads do not wait on
+            // it): stage_cap half-planes, seg_stage segments and the slice
+            // bounds, whatever the slot uses of them
+            __syncwarp();
+            const float4* src = A.planes + (size_t)s * A.lc;
+            for (int m = lane; m < A.stage_cap; m += 32) {
+                const float4 p = src[m];
+                ((float4*)sp)[2 * m] = make_float4(p.x, p.x, p.y, p.y);
+                ((float4*)sp)[2 * m + 1] = make_float4(p.z, p.z, p.w, p.w);
+            }
+            const int2* gsg = A.segs + (size_t)s * A.seg_cap;
+            for (int m = lane; m < A.seg_stage; m += 32) ssg[m] = gsg[m];
+            if (A.slice_r) sr[lane] = A.slice_r[(size_t)s * 32 + lane];
+        }
         const QDesc d = A.qd[s];
         if (s != cur) {
-            __syncwarp();
             if (A.mode == MODE_FP32) {
-                const float4* src = A.planes + (size_t)s * A.lc;
-                for (int m = lane; m < min(d.nb, A.stage_cap); m += 32) ((float4*)sp)[m] = src[m];
+                seg_staged = d.nseg + 1 <= A.seg_stage;
             } else {
+                __syncwarp();
                 const int* bp = A.bis_pos + (size_t)s * A.lc;
                 for (int m = lane; m < min(d.nb, A.stage_cap); m += 32) {
                     float2 f = A.fxy[VX(bp[m], A.nf, 204)];
@@ -269,12 +294,13 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
                     p[2] = fma(dx, dx, dy * dy);
                     p[3] = (double)A.planes[(size_t)s * A.lc + m].w;
                 }
-            }
-            // the slot's user segments (nseg ranges and the terminal entry)
-            seg_staged = d.nseg + 1 <= A.seg_stage;
-            if (seg_staged) {
-                const int2* gsg = A.segs + (size_t)s * A.seg_cap;
-                for (int m = lane; m <= d.nseg; m += 32) ssg[m] = gsg[m];
+                // the slot's user segments (nseg ranges and the terminal entry)
+                seg_staged = d.nseg + 1 <= A.seg_stage;
+                if (seg_staged) {
+                    const int2* gsg = A.segs + (size_t)s * A.seg_cap;
+                    for (int m = lane; m <= d.nseg; m += 32) ssg[m] = gsg[m];
+                }
+                if (A.slice_r) sr[lane] = A.slice_r[(size_t)s * 32 + lane];
             }
             cur = s;
             __syncwarp();
@@ -313,7 +339,7 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
         // Slices were widened by 2^-14 rad, far beyond slice_of's 1e-7 rad
         // edge uncertainty, so the computed slice's bound holds for the user.
         if (d.flags & QF_SLICE_R) {
-            const float* Rq = A.slice_r + (size_t)s * 32;
+            const float* Rq = sr;
 #pragma unroll
             for (int t = 0; t < UPT; ++t) {
                 if (!valid[t]) continue;
@@ -336,74 +362,99 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
 #pragma unroll
         for (int t = 0; t < UPT; ++t) direct[t] = valid[t] && cnt[t] < d.k && und[t] == 0;
 
-        // stage 2: survivors go to the list for recount_kernel; when it is
-        // full, the warp counts them itself, one user at a time
-        unsigned sm[UPT];
-        int ns = 0;
+        // stage 2: survivors go to the list for recount_kernel (when it is
+        // full, the warp counts them itself, one user at a time); directly
+        // accepted users are appended to the slot's results.  The accepted
+        // users' ids, the slot's region and both reservations are requested
+        // before any of them is waited for.
+        unsigned sm[UPT], am[UPT];
+        int ns = 0, tot = 0;
+        int idv[UPT];
 #pragma unroll
         for (int t = 0; t < UPT; ++t) {
+            idv[t] = direct[t] ? A.uid[VX(pos[t], A.nu, 207)] : 0;
             sm[t] = __ballot_sync(FULL, valid[t] && cnt[t] < d.k && !direct[t]);
+            am[t] = __ballot_sync(FULL, direct[t]);
             ns += __popc(sm[t]);
+            tot += __popc(am[t]);
         }
+        const long long r0 = A.cand_off[s], region = A.cand_off[s + 1] - r0;
+        const bool try_list = ns && A.surv_cap > 0;
+        int sbase = 0, rbase = 0;
+        if (lane == 0) {
+            if (try_list) sbase = atomicAdd(A.surv_count, ns);
+            if (tot) rbase = atomicAdd(A.res_count + s, tot);
+        }
+        sbase = __shfl_sync(FULL, sbase, 0);
+        rbase = __shfl_sync(FULL, rbase, 0);
         s_surv += (lane == 0) ? ns : 0;
         bool listed = false;
-        if (ns && A.surv_cap > 0) {
-            int base = 0;
-            if (lane == 0) base = atomicAdd(A.surv_count, ns);
-            base = __shfl_sync(FULL, base, 0);
-            if ((long long)base + ns <= A.surv_cap) {
+        if (try_list) {
+            if ((long long)sbase + ns <= A.surv_cap) {
                 int o = 0;
 #pragma unroll
                 for (int t = 0; t < UPT; ++t) {
                     if (sm[t] & (1u << lane))
-                        A.surv[VX((long long)base + o + __popc(sm[t] & ((1u << lane) - 1)), A.surv_cap, 214)] = make_int2(s, pos[t]);
+                        A.surv[VX((long long)sbase + o + __popc(sm[t] & ((1u << lane) - 1)), A.surv_cap, 214)] = make_int2(s, pos[t]);
                     o += __popc(sm[t]);
                 }
                 listed = true;
             } else {
                 // the reservation straddles the end: mark its listed part empty
-                for (int i = base + lane; i < A.surv_cap && i < base + ns; i += 32) A.surv[i] = make_int2(-1, 0);
+                for (int i = sbase + lane; i < A.surv_cap && i < sbase + ns; i += 32) A.surv[i] = make_int2(-1, 0);
             }
         }
-        bool acc[UPT];
-#pragma unroll
-        for (int t = 0; t < UPT; ++t) {
-            acc[t] = direct[t];
-            unsigned m = listed ? 0u : sm[t];
-            while (m) {
-                int l = __ffs(m) - 1;
-                m &= m - 1;
-                const float2 ul = A.uxy[VX(__shfl_sync(FULL, pos[t], l), A.nu, 219)];
-                const float ux = ul.x, uy = ul.y;
-                unsigned long long fac = 0, rech = 0;
-                int c = (A.mode == MODE_FP32) ? exact_count<float>(ux, uy, d, A, fac, rech)
-                                              : exact_count<double>(ux, uy, d, A, fac, rech);
-                s_fac += (unsigned)fac;
-                s_rech += (unsigned)rech;
-                if (lane == l) acc[t] = c < d.k;
-            }
-        }
-        // warp-aggregated append of the accepted users
-        unsigned am[UPT];
-        int tot = 0;
-#pragma unroll
-        for (int t = 0; t < UPT; ++t) { am[t] = __ballot_sync(FULL, acc[t]); tot += __popc(am[t]); }
+        // the slot's region holds min(candidates, rcap) ids; results beyond
+        // it are counted, not stored, and the host reruns
         if (tot) {
-            int base = 0;
-            if (lane == 0) base = atomicAdd(A.res_count + s, tot);
-            base = __shfl_sync(FULL, base, 0);
-            // the slot's region holds min(candidates, rcap) ids; results
-            // beyond it are counted, not stored, and the host reruns
-            const long long r0 = A.cand_off[s], region = A.cand_off[s + 1] - r0;
-            if (lane == 0 && base + tot > region) atomicOr(A.dropped, 1);
+            if (lane == 0 && rbase + tot > region) atomicOr(A.dropped, 1);
             int o = 0;
 #pragma unroll
             for (int t = 0; t < UPT; ++t) {
-                const long long at = (long long)base + o + __popc(am[t] & ((1u << lane) - 1));
-                if (acc[t] && at < region) A.res_pool[VX(r0 + at, A.pool_cap, 206)] = A.uid[VX(pos[t], A.nu, 207)];
+                const long long at = (long long)rbase + o + __popc(am[t] & ((1u << lane) - 1));
+                if (direct[t] && at < region) A.res_pool[VX(r0 + at, A.pool_cap, 206)] = idv[t];
                 o += __popc(am[t]);
             }
             s_res += (lane == 0) ? tot : 0;
+        }
+        if (!listed && ns) {
+            // survivors the list could not take: counted here, appended with
+            // one more reservation
+            bool acc[UPT];
+#pragma unroll
+            for (int t = 0; t < UPT; ++t) {
+                acc[t] = false;
+                unsigned m = sm[t];
+                while (m) {
+                    int l = __ffs(m) - 1;
+                    m &= m - 1;
+                    const float2 ul = A.uxy[VX(__shfl_sync(FULL, pos[t], l), A.nu, 219)];
+                    unsigned long long fac = 0, rech = 0;
+                    int c = (A.mode == MODE_FP32) ? exact_count<float>(ul.x, ul.y, d, A, fac, rech)
+                                                  : exact_count<double>(ul.x, ul.y, d, A, fac, rech);
+                    s_fac += (unsigned)fac;
+                    s_rech += (unsigned)rech;
+                    if (lane == l) acc[t] = c < d.k;
+                }
+            }
+            unsigned bm[UPT];
+            int tot2 = 0;
+#pragma unroll
+            for (int t = 0; t < UPT; ++t) { bm[t] = __ballot_sync(FULL, acc[t]); tot2 += __popc(bm[t]); }
+            if (tot2) {
+                int base = 0;
+                if (lane == 0) base = atomicAdd(A.res_count + s, tot2);
+                base = __shfl_sync(FULL, base, 0);
+                if (lane == 0 && base + tot2 > region) atomicOr(A.dropped, 1);
+                int o = 0;
+#pragma unroll
+                for (int t = 0; t < UPT; ++t) {
+                    const long long at = (long long)base + o + __popc(bm[t] & ((1u << lane) - 1));
+                    if (acc[t] && at < region) A.res_pool[VX(r0 + at, A.pool_cap, 220)] = A.uid[VX(pos[t], A.nu, 221)];
+                    o += __popc(bm[t]);
+                }
+                s_res += (lane == 0) ? tot2 : 0;
+            }
         }
     }
     // statistics: per-lane partials, one atomic per counter per warp
@@ -629,7 +680,7 @@ plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_off, long long po
 
 // Output offsets of the stored results (a slot stores at most its region).
 __global__ void __launch_bounds__(SCAN_THREADS)
-scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int* out_off)
+scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int* out_off, const int* counters)
 {
     pdl_wait();
     pdl_trigger();
@@ -657,7 +708,14 @@ scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int*
         carry += tot;
         __syncthreads();
     }
-    if (tid == 0) out_off[nq] = carry;
+    if (tid == 0) {
+        out_off[nq] = carry;
+        const unsigned long long rt = (unsigned long long)cand_off[nq];
+        out_off[nq + 1] = (int)(unsigned)(rt & 0xffffffffu);
+        out_off[nq + 2] = (int)(unsigned)(rt >> 32);
+        out_off[nq + 3] = counters[2];
+        out_off[nq + 4] = counters[3];
+    }
 }
 
 // ---------------------------------------------------------------- finalize

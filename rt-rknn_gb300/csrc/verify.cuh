@@ -62,7 +62,12 @@ __global__ void plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_o
                             int rcap, int chunk);
 
 // single block: exclusive scan of the stored result counts into out_off
-__global__ void scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int* out_off);
+// out_off: nq+1 offsets, then OFF_TAIL ints: the region total (low and high
+// halves of cand_off[nq]), the dropped flag and the listed survivors
+// (counters[2], counters[3]), so that one copy brings back all of them.
+constexpr int OFF_TAIL = 4;
+__global__ void scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int* out_off,
+                                   const int* counters);
 
 // one block per slot: sort the slot's results into out[out_off[s] ...]
 __global__ void finalize_kernel(int* res_pool, const long long* cand_off, const int* res_count,
