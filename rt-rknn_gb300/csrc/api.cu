@@ -344,7 +344,7 @@ ZoneCaps slice_caps(int kmax, int lc_cap = 512)
 {
     ZoneCaps c;
     c.vc = std::max(1, kmax);
-    c.lc = (int)std::max<long long>(1, std::min<long long>(6LL * c.vc + 40, lc_cap));
+    c.lc = (int)std::max<long long>(1, std::min<long long>(10LL * c.vc + 60, lc_cap));
     c.pc = 0;
     c.rm = 64;
     return c;

@@ -279,7 +279,6 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
 #define SLICE_KTH() (KR > 0 ? RL[(KR > 0 ? KR : 1) - 1] : ((n < k) ? INFINITY : H[lane]))
         int nL = 0;             // half-planes kept (warp-uniform)
         int rho_ring = -1;      // first ring with a streamed facility left out of the half-planes
-        float rho_skip = INFINITY;   // nearest skipped cell
         const int fbudget = max(8192, 128 * k);
         // cell boxes widened for the rounding of the cell function
         const float cmargin = 1e-5f * A.gf.cs + 8.0f * kU32 * (fabsf(A.gf.x0) + fabsf(A.gf.y0) + fabsf(qf.x) + fabsf(qf.y) +
@@ -333,7 +332,8 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
             // Window maxima of the bounds for the ring: a facility helps only
             // slices within 8 of its own, so a cell whose facilities are all
             // farther than twice the largest bound of the slices within 8 of
-            // those the cell spans can enter no heap and is skipped.  (Rs
+            // those the cell spans can enter no heap: its facilities become
+            // half-planes without being loaded or offered (plane-only).  (Rs
             // serves as scratch until the stream ends.)
             {
                 float Rw = Rl;
@@ -350,7 +350,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
             for (int r0 = 0; r0 < nrange; r0 += 32) {
                 const int ri = r0 + lane;
                 int fs = 0, fe = 0;
-                float skipped_at = INFINITY;
+                bool po = false;        // plane-only: the cell's facilities can enter no heap
                 if (ri < nrange) {
                     int cxx, cyy;
                     ring_cell(ring, ri, qcx, qcy, cxx, cyy);
@@ -380,20 +380,10 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                                 const int s1 = (int)floorf((th + al) * (1.0f / SLICE_W));
                                 float Rc = 0.0f;
                                 for (int sl = s0; sl <= s1 && sl <= s0 + NS; ++sl) Rc = fmaxf(Rc, Rs[((sl % NS) + NS) % NS]);
-                                if (0.5f * Lc > Rc * (1.0f + 1e-6f)) {
-                                    skipped_at = Lc;
-                                    fe = fs;
-                                }
+                                if (0.5f * Lc > Rc * (1.0f + 1e-6f)) po = true;
                             }
                         }
                     }
-                }
-                // every facility outside the half-planes stays at least rho from q
-                {
-                    float m = skipped_at;
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(FULL, m, o));
-                    rho_skip = fminf(rho_skip, m);
                 }
                 // the next ring's facility lines, while this ring is streamed
                 if (r0 == 0 && pf_fe > pf_fs) {
@@ -423,18 +413,22 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                     const int rs = __shfl_sync(FULL, fs, lo);
                     const int rincl = __shfl_sync(FULL, incl, lo);
                     const int rlen = __shfl_sync(FULL, len, lo);
+                    const bool rpo = __shfl_sync(FULL, (int)po, lo) != 0;
                     const int fidx = rs + (j - (rincl - rlen));
                     bool ok = j < total && fidx != qpos;
                     float vx = 0.0f, vy = 0.0f;
-                    if (ok) {
+                    if (ok && !rpo) {
                         const float2 f = A.fxy[SX(fidx, A.nf, 314)];
                         vx = f.x - qf.x;
                         vy = f.y - qf.y;
                         // a facility at q's position is never strictly nearer
-                        // (float differences are zero only for equal floats)
+                        // (float differences are zero only for equal floats;
+                        // such a facility lies in q's cell, never plane-only)
                         ok = vx != 0.0f || vy != 0.0f;
                     }
-                    // half-planes: the first LC facilities streamed
+                    // half-planes: the first LC facilities of the rings, in
+                    // ring order, those of plane-only cells included (so that
+                    // rho is limited only by the rings, below)
                     const unsigned pm = __ballot_sync(FULL, ok);
                     if (ok) {
                         const int at = nL + __popc(pm & ((1u << lane) - 1));
@@ -442,14 +436,15 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                     }
                     if (nL + __popc(pm) > LC && rho_ring < 0) rho_ring = ring;
                     nL = min(LC, nL + __popc(pm));
-                    zs.pts += __popc(pm);
+                    const unsigned om = __ballot_sync(FULL, ok && !rpo);      // offered to the bounds
+                    zs.pts += __popc(om);
                     // A facility has finite arcs only for slices within 90 degrees
                     // of its direction (the 8 slices on either side of its own,
                     // counting the widening) and every arc is at least half its
                     // distance: when that exceeds the largest bound R among
                     // them it can enter no heap.  Bounds only shrink, so the
                     // window maxima taken before the batch are conservative.
-                    unsigned m = pm;
+                    unsigned m = om;
                     {
                         const float Rl = SLICE_KTH();
                         float Rw = Rl;
@@ -459,7 +454,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                                                  __shfl_sync(FULL, Rl, (lane - dd) & 31)));
                         const int sj = ok ? slice_of(vx, vy) : 0;
                         const float Rwj = __shfl_sync(FULL, Rw, sj);
-                        const bool useful = ok && !(0.25f * fmaf(vx, vx, vy * vy) * (1.0f - 4.0f * kU32) >= Rwj * Rwj);
+                        const bool useful = ok && !rpo && !(0.25f * fmaf(vx, vx, vy * vy) * (1.0f - 4.0f * kU32) >= Rwj * Rwj);
                         m = __ballot_sync(FULL, useful);
                     }
                     // every lane offers every useful facility to its slice
@@ -515,7 +510,6 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                 const double Lr = (double)(rho_ring - 1) * (double)A.gf.cs - slack;
                 rho = Lr > 0.0 ? __double2float_rd(Lr) : 0.0f;
             }
-            rho = fminf(rho, rho_skip);
         }
         __syncwarp();
         // R(P): k-th smallest arc, rounded up for the user test, and clipped
