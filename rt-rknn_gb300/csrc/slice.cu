@@ -42,7 +42,6 @@ constexpr unsigned FULL = 0xffffffffu;
 constexpr int NS = 32;                                  // slices: one per lane
 constexpr float SLICE_W = 6.28318530717958647692f / NS;
 constexpr float WIDEN = 6.103515625e-05f;               // 2^-14 rad
-constexpr float TWO_PI_F = 6.28318530717958647692f;
 
 #ifdef RKNN_CHECKED
 __device__ int* s_fault;
@@ -101,6 +100,28 @@ __device__ __forceinline__ float exit_dist(float qx, float qy, float ex, float e
     if (ey > 0.0f) t = fminf(t, __fdiv_ru(__fsub_ru(y1, qy), ey));
     else if (ey < 0.0f) t = fminf(t, __fdiv_ru(__fsub_rd(y0, qy), ey));
     return t;
+}
+
+// Largest of Rs over the slices that the box [X0, X1] x [Y0, Y1] (relative to
+// q) meets, or +inf when the box contains q or spans half the circle or
+// more.  A box that does not contain q subtends less than 180 degrees, and
+// the directions it covers lie between those of its corners: taking the
+// corners' slices as offsets from one corner's (mod 32, in [-16, 16)) gives
+// the range.  Near a slice edge slice_of may name the neighbour; the box's
+// points in that direction are then inside the named slice's widened cone,
+// whose bound holds for them.
+__device__ __forceinline__ float box_bound(float X0, float X1, float Y0, float Y1, const float* Rs)
+{
+    if (X0 <= 0.0f && X1 >= 0.0f && Y0 <= 0.0f && Y1 >= 0.0f) return INFINITY;
+    const int c0 = slice_of(X0, Y0);
+    const int d1 = ((slice_of(X1, Y0) - c0 + 48) & 31) - 16;
+    const int d2 = ((slice_of(X0, Y1) - c0 + 48) & 31) - 16;
+    const int d3 = ((slice_of(X1, Y1) - c0 + 48) & 31) - 16;
+    const int lo = min(0, min(d1, min(d2, d3))), hi = max(0, max(d1, max(d2, d3)));
+    if (hi - lo >= 15 || lo == -16) return INFINITY;
+    float r = 0.0f;
+    for (int sl = c0 + lo; sl <= c0 + hi; ++sl) r = fmaxf(r, Rs[sl & 31]);
+    return r;
 }
 
 // Cell ri of the square ring at Chebyshev distance ring around (qcx, qcy):
@@ -368,20 +389,9 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                             const float X0 = A.gf.x0 + (float)cxx * A.gf.cs - cmargin, X1 = A.gf.x0 + (float)(cxx + 1) * A.gf.cs + cmargin;
                             const float Y0 = A.gf.y0 + (float)cyy * A.gf.cs - cmargin, Y1 = A.gf.y0 + (float)(cyy + 1) * A.gf.cs + cmargin;
                             const float ddx = fmaxf(fmaxf(X0 - qf.x, qf.x - X1), 0.0f), ddy = fmaxf(fmaxf(Y0 - qf.y, qf.y - Y1), 0.0f);
-                            const float Lc = sqrtf(fmaf(ddx, ddx, ddy * ddy)) * (1.0f - 1e-6f);
-                            const float cxm = 0.5f * (X0 + X1) - qf.x, cym = 0.5f * (Y0 + Y1) - qf.y;
-                            const float dc = sqrtf(fmaf(cxm, cxm, cym * cym));
-                            const float hd = 0.5f * sqrtf(fmaf(X1 - X0, X1 - X0, (Y1 - Y0) * (Y1 - Y0)));
-                            if (dc > 1.01f * hd) {
-                                float th = atan2f(cym, cxm);
-                                if (th < 0.0f) th += TWO_PI_F;
-                                const float al = asinf(fminf(1.0f, hd / dc)) * 1.001f + WIDEN;
-                                const int s0 = (int)floorf((th - al) * (1.0f / SLICE_W));
-                                const int s1 = (int)floorf((th + al) * (1.0f / SLICE_W));
-                                float Rc = 0.0f;
-                                for (int sl = s0; sl <= s1 && sl <= s0 + NS; ++sl) Rc = fmaxf(Rc, Rs[((sl % NS) + NS) % NS]);
-                                if (0.5f * Lc > Rc * (1.0f + 1e-6f)) po = true;
-                            }
+                            const float Lc2 = fmaf(ddx, ddx, ddy * ddy) * (1.0f - 4e-6f);     // |box - q|^2, rounded down
+                            const float Rc = box_bound(X0 - qf.x, X1 - qf.x, Y0 - qf.y, Y1 - qf.y, Rs);
+                            if (Rc < INFINITY && 0.25f * Lc2 > Rc * Rc * (1.0f + 4e-6f)) po = true;
                         }
                     }
                 }
@@ -607,23 +617,11 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                         const float Y1 = (gu.y0 + (float)(cyy + 1) * gu.cs) - qf.y + delta;
                         if (X0 <= 0.0f && X1 >= 0.0f && Y0 <= 0.0f && Y1 >= 0.0f) keep = true;
                         else {
-                            // nearest point of the cell, and the slices the cell
-                            // spans: its box lies in the disc of the half-diagonal
-                            // hd around its centre, which subtends asin(hd/dc)
+                            // nearest point of the cell against the largest
+                            // bound of the slices the cell spans
                             const float ddx = fmaxf(fmaxf(X0, -X1), 0.0f), ddy = fmaxf(fmaxf(Y0, -Y1), 0.0f);
                             const float dmin2 = fmaf(ddx, ddx, ddy * ddy) * (1.0f - 4.0f * kU32);
-                            const float cxm = 0.5f * (X0 + X1), cym = 0.5f * (Y0 + Y1);
-                            const float dc = sqrtf(fmaf(cxm, cxm, cym * cym));
-                            const float hd = 0.5f * sqrtf(fmaf(X1 - X0, X1 - X0, (Y1 - Y0) * (Y1 - Y0)));
-                            float Rmax = INFINITY;
-                            if (dc > 1.01f * hd) {
-                                const float pc = atan2f(cym, cxm);
-                                const float al = asinf(fminf(1.0f, hd / dc)) * 1.001f + WIDEN;
-                                const int s0 = (int)floorf((pc - al) / SLICE_W);
-                                const int s1 = (int)floorf((pc + al) / SLICE_W);
-                                Rmax = 0.0f;
-                                for (int sl = s0; sl <= s1 && sl <= s0 + NS; ++sl) Rmax = fmaxf(Rmax, Rs[((sl % NS) + NS) % NS]);
-                            }
+                            const float Rmax = box_bound(X0, X1, Y0, Y1, Rs);
                             keep = !(dmin2 > Rmax * Rmax);
                         }
                     }
