@@ -50,8 +50,9 @@ NF, NU, K, NQ = 100_000, 1_000_000, 10, 1000
 
 # DRAM bytes (read + write) per launch of each kernel on this workload, from
 # one ncu capture of the same 1000-query batch
-# (profiles/slice_verify_recount_config2_k10.md)
-TRAFFIC = {"slice_kernel": 1528832, "verify_kernel": 4856064 + 1889280}
+# (profiles/slice_verify_recount_finalize_config2_k10.md); the verification
+# figure is verify_kernel plus recount_kernel
+TRAFFIC = {"slice_kernel": 1533184, "verify_kernel": 6904576 + 386048}
 
 
 def peaks():

@@ -245,7 +245,6 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
         }
         const int qpos = A.fpos[SX(qin, A.nf, 310)];
         const float2 qf = A.fxy[SX(qpos, A.nf, 311)];
-        const double qx = qf.x, qy = qf.y;
         if (k > KC || (KR > 0 && k > KR)) {
             // k beyond the slice bounds' capacity (a device batch whose kmax
             // understates a k): every user is a candidate and the
@@ -534,20 +533,27 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
         tph = clock64();
 
         // ---- half-planes relative to q (as the zone kernel's epilogue) -----
+        // In float: a = -2 fl(fx - qx) and b likewise equal the rounded exact
+        // values (a float difference is correctly rounded); c = |f - q|^2
+        // carries about 5u relative error instead of u.  The verification's
+        // bound 8u (2F'(|x'|+|y'|) + F'^2) exceeds the evaluation error with
+        // it, about 3u|a x'| + 3u|b y'| + 7u|c|, since |a|, |b| <= 2F' and
+        // |c| <= F'^2 (F' from the largest c below, rounded up).
         float4* planes = A.planes + (size_t)s * A.pstride;
-        double cmax = 0.0;
+        float cmax = 0.0f;
         for (int m = lane; m < nL; m += 32) {
             const int pos = lpos[SX(m, LC, 316)];
             const float2 f = A.fxy[SX(pos, A.nf, 317)];
-            const double dx = (double)f.x - qx, dy = (double)f.y - qy;
-            const double c = dx * dx + dy * dy;
-            planes[SX(m, A.pstride, 318)] = make_float4((float)(-2.0 * dx), (float)(-2.0 * dy), (float)c, 0.0f);
+            const float dx = f.x - qf.x, dy = f.y - qf.y;
+            const float c = fmaf(dx, dx, dy * dy);
+            planes[SX(m, A.pstride, 318)] = make_float4(-2.0f * dx, -2.0f * dy, c, 0.0f);
             A.bis_pos[(size_t)s * A.pstride + SX(m, A.pstride, 319)] = pos;
-            cmax = fmax(cmax, c);
-            lpos[SX(m, LC, 316)] = __float_as_int(__double2float_rd(c));    // the slot is free now
+            cmax = fmaxf(cmax, c);
+            // the slot is free now: |f - q|^2 rounded well down
+            lpos[SX(m, LC, 316)] = __float_as_int(__fmul_rd(c, 1.0f - 1e-6f));
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) cmax = fmax(cmax, __shfl_xor_sync(FULL, cmax, o));
+        for (int o = 16; o > 0; o >>= 1) cmax = fmaxf(cmax, __shfl_xor_sync(FULL, cmax, o));
         __syncwarp();
         // Fourth component of half-plane m: the least |f - q|^2 (rounded
         // down) over half-planes m, m+1, ...  Only a facility within 2|u - q|
@@ -568,7 +574,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                 carry = __shfl_sync(FULL, v, 0);
             }
         }
-        const double Fp = sqrt(cmax) * (1.0 + 1e-6) + 1e-30;
+        const double Fp = (double)__fmul_ru(__fsqrt_ru(__fmul_ru(cmax, 1.0f + 1e-5f)), 1.0f + 1e-6f) + 1e-30;
         const float k2f = (float)(8.0 * (double)kU32 * 2.0 * Fp * (1.0 + 1e-6));
         const float kf2 = (float)(8.0 * (double)kU32 * Fp * Fp * (1.0 + 1e-6)) + 1e-30f;
         const double k2f64 = 8.0 * kU64 * 2.0 * Fp * (1.0 + 1e-6);
