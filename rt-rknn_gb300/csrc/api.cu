@@ -222,7 +222,9 @@ int occupancy(rknn_index* ix, const void* fn, int threads, size_t smem)
 using ZoneFn = void (*)(ZoneArgs);
 ZoneFn slice_fn(int kmax)
 {
-    return kmax <= 16 ? slice_kernel_r16 : kmax <= 32 ? slice_kernel_r32 : slice_kernel;
+    return kmax <= 4 ? slice_kernel_r4 : kmax <= 8 ? slice_kernel_r8 : kmax <= 12 ? slice_kernel_r12
+         : kmax <= 16 ? slice_kernel_r16 : kmax <= 24 ? slice_kernel_r24 : kmax <= 32 ? slice_kernel_r32
+         : slice_kernel;
 }
 
 ZoneLaunch zone_launch(rknn_index* ix, const ZoneCaps& c, int nq, bool slice = false, int kmax = 0)
@@ -814,8 +816,9 @@ rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf, 
         ix->recount_grid = std::max(1, per) * ix->num_sms;
     }
     CKB(allow_dynamic_smem((const void*)slice_kernel, optin));
-    CKB(allow_dynamic_smem((const void*)slice_kernel_r16, optin));
-    CKB(allow_dynamic_smem((const void*)slice_kernel_r32, optin));
+    for (const void* f : {(const void*)slice_kernel_r4, (const void*)slice_kernel_r8, (const void*)slice_kernel_r12,
+                          (const void*)slice_kernel_r16, (const void*)slice_kernel_r24, (const void*)slice_kernel_r32})
+        CKB(allow_dynamic_smem(f, optin));
     CKB(allow_dynamic_smem((const void*)verify_kernel, optin));
     CKB(allow_dynamic_smem((const void*)verify_kernel_u2, optin));
     CKB(allow_dynamic_smem((const void*)verify_kernel_u8, optin));

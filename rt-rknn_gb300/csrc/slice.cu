@@ -724,7 +724,11 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
 #undef SLICE_KTH
 
 __global__ void __launch_bounds__(32, 1) slice_kernel(ZoneArgs A) { slice_body<0>(A); }
+__global__ void __launch_bounds__(32, 1) slice_kernel_r4(ZoneArgs A) { slice_body<4>(A); }
+__global__ void __launch_bounds__(32, 1) slice_kernel_r8(ZoneArgs A) { slice_body<8>(A); }
+__global__ void __launch_bounds__(32, 1) slice_kernel_r12(ZoneArgs A) { slice_body<12>(A); }
 __global__ void __launch_bounds__(32, 1) slice_kernel_r16(ZoneArgs A) { slice_body<16>(A); }
+__global__ void __launch_bounds__(32, 1) slice_kernel_r24(ZoneArgs A) { slice_body<24>(A); }
 __global__ void __launch_bounds__(32, 1) slice_kernel_r32(ZoneArgs A) { slice_body<32>(A); }
 
 }  // namespace rknn

@@ -129,9 +129,13 @@ struct ZoneArgs {
 __global__ void zone_kernel_smem(ZoneArgs a);
 
 // angular-slice filter, same arguments and outputs: slice bounds in a
-// shared-memory heap (any k), or in registers for k <= 16 / k <= 32
+// shared-memory heap (any k), or in registers for k <= 4, 8, 12, 16, 24, 32
 __global__ void slice_kernel(ZoneArgs a);
+__global__ void slice_kernel_r4(ZoneArgs a);
+__global__ void slice_kernel_r8(ZoneArgs a);
+__global__ void slice_kernel_r12(ZoneArgs a);
 __global__ void slice_kernel_r16(ZoneArgs a);
+__global__ void slice_kernel_r24(ZoneArgs a);
 __global__ void slice_kernel_r32(ZoneArgs a);
 
 }  // namespace rknn
