@@ -75,18 +75,21 @@ __device__ __forceinline__ float upper_arc(float vx, float vy, float e1x, float 
     return __fdiv_ru(num, den) * (1.0f + 4.0f * kU32);
 }
 
-// upper_arc without branches for the common case: ok is false when the
-// denominator lies outside [2^-126, 2^126] (then call upper_arc).
-__device__ __forceinline__ float upper_arc_fast(float vx, float vy, float e1x, float e1y, float e2x, float e2y, bool& ok)
+// upper_arc without branches: +inf when min((f-q).e1, (f-q).e2), less its
+// rounding allowance, lies outside [2^-100, 2^100] -- an infinite arc only
+// loosens the slice's bound, which stays valid, and there the arc is
+// astronomically large anyway (or |f-q|^2 has overflowed).  Inside, the
+// quotient by __fdividef (within 2 ulp for such divisors) is inflated past
+// its error, as in upper_arc.
+__device__ __forceinline__ float upper_arc_fast(float vx, float vy, float e1x, float e1y, float e2x, float e2y)
 {
     const float d1 = fmaf(vx, e1x, vy * e1y), d2 = fmaf(vx, e2x, vy * e2y);
     const float l1 = fabsf(vx) + fabsf(vy);
     const float dmin = fminf(d1, d2) - 8.0f * kU32 * l1 - 1e-37f;
-    const float num = fmaf(vx, vx, vy * vy) * (1.0f + 8.0f * kU32);
-    const float den = 2.0f * dmin;
-    const bool pos = dmin > 0.0f;
-    ok = !pos || (den > 0x1p-126f && den < 0x1p126f);
-    return pos ? __fdividef(num, den) * (1.0f + 0x1p-20f) : INFINITY;
+    const float num = fmaf(vx, vx, vy * vy);
+    // num (1 + 8u) / (2 dmin), the quotient rounded up by 2^-20
+    constexpr float C = 0.5f * (1.0f + 8.0f * kU32) * (1.0f + 0x1p-20f) * (1.0f + 4.0f * kU32);
+    return (dmin > 0x1p-100f && dmin < 0x1p100f) ? __fdividef(num, dmin) * C : INFINITY;
 }
 
 // Distance from q along unit direction (ex, ey) to the box's boundary,
@@ -479,14 +482,8 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                             m &= m - 1;
                             const float ax = __shfl_sync(FULL, vx, s1), ay = __shfl_sync(FULL, vy, s1);
                             const float bx = __shfl_sync(FULL, vx, s2), by = __shfl_sync(FULL, vy, s2);
-                            bool ok1, ok2;
-                            float u1 = upper_arc_fast(ax, ay, e1x, e1y, e2x, e2y, ok1);
-                            float u2 = upper_arc_fast(bx, by, e1x, e1y, e2x, e2y, ok2);
-                            if (!__all_sync(FULL, ok1 && ok2)) {
-                                if (!ok1) u1 = upper_arc(ax, ay, e1x, e1y, e2x, e2y);
-                                if (!ok2) u2 = upper_arc(bx, by, e1x, e1y, e2x, e2y);
-                            }
-                            if (!two) u2 = INFINITY;
+                            const float u1 = upper_arc_fast(ax, ay, e1x, e1y, e2x, e2y);
+                            const float u2 = two ? upper_arc_fast(bx, by, e1x, e1y, e2x, e2y) : INFINITY;
                             if (__any_sync(FULL, fminf(u1, u2) < RL[(KR > 0 ? KR : 1) - 1])) {
                                 list_insert<KR>(RL, u1);
                                 list_insert<KR>(RL, u2);
