@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -99,6 +100,7 @@ struct Workspace {
     char* d_zscratch = nullptr;
     size_t zscratch_bytes = 0;
     int *h_qko = nullptr, *h_off = nullptr;   // h_off: nq+1 offsets, then the run's flags (OFF_TAIL)
+    int *h_qko_dev = nullptr, *h_off_dev = nullptr;   // the same, as device pointers
     int* h_ids = nullptr;
     long long h_ids_cap = 0;
     std::map<GraphKey, cudaGraphExec_t> graphs;
@@ -143,6 +145,8 @@ struct rknn_index {
     rknn_query_stats last{};
     int last_nq = 0, last_mode = 0, last_lc = 0;
     long long last_total = 0;   // ids the previous host batch returned
+    int32_t* last_out = nullptr;   // the previous host batch's id buffer and capacity
+    long long last_cap = 0;
     int dev_nq = 0, dev_kmax = 0, dev_mode = 0;   // the last device batch (0: none pending a check)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int profiling = 0;
@@ -153,12 +157,26 @@ namespace {
 
 // Where a batch runs: a workspace, a stream, timing events.  The index has
 // one (its own calls); a server owns one per in-flight slot.
+// Where a batch reads its queries and leaves its results.  By default the
+// workspace's device buffers; the host batch call instead lets the kernels
+// read q, k and the order from the page-locked staging buffer and write the
+// offsets (and flags) into page-locked host memory, and -- for a page-locked
+// id buffer the caller passes again -- the sorted ids straight into it (all
+// device-accessible host memory: no copies on the stream).
+struct Io {
+    const int* qko = nullptr;       // q at [0, nq), k at [nq, 2 nq), order at [2 nq, 3 nq)
+    int* off_host = nullptr;        // offsets and flags, mirrored into host memory
+    int* ids = nullptr;             // sorted ids (null: the workspace's d_out)
+    long long ids_cap = 0;          // capacity of ids (slots that would pass it are skipped)
+};
+
 struct Ctx {
     Workspace& w;
     cudaStream_t st;
     cudaEvent_t ev0, ev1;
     cudaEvent_t* kev;          // per-kernel events (profiling), or null
     double* device_ms;         // where run_sync stores the batch's device time
+    Io io{};
 };
 
 Ctx main_ctx(rknn_index* ix)
@@ -287,6 +305,8 @@ rknn_status ensure_ws(Workspace& w, int nq, const ZoneCaps& caps, long long pool
         CK(dalloc(w.d_vstats, 1));
         CK(cudaMallocHost(&w.h_qko, sizeof(int) * 3 * (size_t)nqc));
         CK(cudaMallocHost(&w.h_off, sizeof(int) * (nqc + 1 + OFF_TAIL)));
+        CK(cudaHostGetDevicePointer((void**)&w.h_qko_dev, w.h_qko, 0));
+        CK(cudaHostGetDevicePointer((void**)&w.h_off_dev, w.h_off, 0));
         w.pool_cap = 0;
     }
     if (!w.d_surv) {
@@ -473,7 +493,8 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     za.gf = ix->gf; za.nf = (int)ix->nf;
     za.ustart = ix->d_ustart; za.gu = ix->gu; za.nu = (int)ix->nu;
     za.sx0 = ix->sx0; za.sy0 = ix->sy0; za.sx1 = ix->sx1; za.sy1 = ix->sy1;
-    za.q_in = w.d_qko; za.k_in = w.d_qko + nq;
+    const int* qko = c.io.qko ? c.io.qko : w.d_qko;
+    za.q_in = qko; za.k_in = qko + nq;
     za.skip_coincident = ix->skip_coincident;
     za.seg_cap = w.seg_cap;
     za.qd = w.d_qd; za.planes = w.d_planes; za.bis_pos = w.d_bispos; za.segs = w.d_segs; za.zst = w.d_zst;
@@ -488,7 +509,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     }
     for (int i = 0; i < ncls; ++i) {
         const ZClass& z = b.cls[i];
-        za.order = b.use_order ? w.d_qko + 2 * nq + z.off : nullptr;
+        za.order = b.use_order ? qko + 2 * nq + z.off : nullptr;
         za.nq = z.n;
         za.caps = z.caps;
         za.rmax = z.caps.rm;
@@ -533,10 +554,12 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     mark(4);
 
     CK(launch_k(scan_counts_kernel, 1, 1024, 0, st, pdl, (const int*)w.d_res_count, (const long long*)w.d_cand_off,
-                nq, w.d_out_off, (const int*)w.d_counters));
+                nq, w.d_out_off, (const int*)w.d_counters, c.io.off_host));
     mark(5);
+    int* ids = c.io.ids ? c.io.ids : w.d_out;
+    const long long ids_cap = c.io.ids ? c.io.ids_cap : w.pool_cap;
     CK(launch_k(finalize_kernel, (nq + FIN_WARPS - 1) / FIN_WARPS, 32 * FIN_WARPS, 0, st, pdl, w.d_pool,
-                (const long long*)w.d_cand_off, (const int*)w.d_res_count, (const int*)w.d_out_off, w.d_out, nq));
+                (const long long*)w.d_cand_off, (const int*)w.d_res_count, (const int*)w.d_out_off, ids, nq, ids_cap));
     mark(6);
     return RKNN_OK;
 }
@@ -552,6 +575,10 @@ rknn_status launch(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = true
     key.push_back(w.pool_cap);
     key.push_back(w.rcap);
     key.push_back(w.surv_cap);
+    key.push_back((long long)(uintptr_t)c.io.qko);
+    key.push_back((long long)(uintptr_t)c.io.off_host);
+    key.push_back((long long)(uintptr_t)c.io.ids);
+    key.push_back(c.io.ids_cap);
     auto it = w.graphs.find(key);
     if (it == w.graphs.end()) {
         cudaGraph_t g;
@@ -641,8 +668,10 @@ rknn_status run_sync(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = tr
         s = launch(ix, c, b, graph);
         if (s != RKNN_OK) return s;
         CK(cudaEventRecord(c.ev1, c.st));
-        // offsets and the run's flags in one copy
-        CK(cudaMemcpyAsync(w.h_off, w.d_out_off, sizeof(int) * (nq + 1 + OFF_TAIL), cudaMemcpyDeviceToHost, c.st));
+        // offsets and the run's flags in one copy (none when the scan wrote
+        // them to host memory itself)
+        if (c.io.off_host != w.h_off_dev || !c.io.off_host)
+            CK(cudaMemcpyAsync(w.h_off, w.d_out_off, sizeof(int) * (nq + 1 + OFF_TAIL), cudaMemcpyDeviceToHost, c.st));
         const long long sn = std::min(spec_n, w.pool_cap);
         if (spec && sn > 0) CK(cudaMemcpyAsync(spec, w.d_out, sizeof(int) * sn, cudaMemcpyDeviceToHost, c.st));
         CK(cudaStreamSynchronize(c.st));
@@ -982,23 +1011,39 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
     if (s != RKNN_OK) return s;
     Workspace& w = ix->ws;
     Ctx c = main_ctx(ix);
+    // the kernels read the queries from the page-locked staging buffer and
+    // the offsets scan writes into page-locked host memory: no copies
     std::memcpy(w.h_qko, q, sizeof(int) * nq);
     std::memcpy(w.h_qko + nq, k, sizeof(int) * nq);
     if (!uniform) std::memcpy(w.h_qko + 2 * nq, order.data(), sizeof(int) * nq);
-    CK(cudaMemcpyAsync(w.d_qko, w.h_qko, sizeof(int) * (size_t)(uniform ? 2 : 3) * nq, cudaMemcpyHostToDevice,
-                       ix->stream));
-    // The ids come back with the offsets when the batch returns no more than
-    // the previous one plus a margin: page-locked caller buffers take them
-    // directly, pageable ones through the workspace's page-locked staging.
+    c.io.qko = w.h_qko_dev;
+    c.io.off_host = w.h_off_dev;
     bool locked = false;
+    int* ids_dev = nullptr;
     if (out_ids && cap > 0) {
         cudaPointerAttributes pa;
         locked = cudaPointerGetAttributes(&pa, out_ids) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+        if (locked) ids_dev = (int*)pa.devicePointer;
         cudaGetLastError();
     }
+    // A device-accessible page-locked id buffer that the caller passes again
+    // (same address and capacity as on the previous call) receives the ids
+    // from finalize_kernel itself; the captured graph is kept for it.
+    const bool direct = ids_dev && out_ids == ix->last_out && cap == ix->last_cap;
+    ix->last_out = out_ids;
+    ix->last_cap = cap;
+    if (direct) {
+        c.io.ids = ids_dev;
+        c.io.ids_cap = cap;
+    }
+    // Otherwise the ids come back with the offsets when the batch returns no
+    // more than the previous one plus a margin: page-locked caller buffers
+    // take them directly, pageable ones through the workspace's staging.
     long long guess = ix->last_total + ix->last_total / 4 + 4096;
     int* spec = nullptr;
-    if (locked) {
+    if (direct) {
+        guess = 0;
+    } else if (locked) {
         guess = std::min<long long>(guess, cap);
         spec = out_ids;
     } else if (out_ids && cap > 0) {
@@ -1028,7 +1073,7 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
     if (total > cap || (!out_ids && total > 0))
         return fail(RKNN_ERR_CAPACITY, "output buffer holds " + std::to_string(cap) + " ids, " +
                                            std::to_string(total) + " needed");
-    if (total > 0 && total > std::min(guess, w.pool_cap)) {
+    if (total > 0 && !direct && total > std::min(guess, w.pool_cap)) {
         // more ids than the speculative copy held: fetch them all
         if (!locked && total > w.h_ids_cap) {
             cudaFreeHost(w.h_ids);
@@ -1042,7 +1087,7 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
                            ix->stream));
         CK(cudaStreamSynchronize(ix->stream));
     }
-    if (total > 0 && !locked) std::memcpy(out_ids, w.h_ids, sizeof(int) * total);
+    if (total > 0 && !locked && !direct) std::memcpy(out_ids, w.h_ids, sizeof(int) * total);
     return RKNN_OK;
 }
 
@@ -1294,9 +1339,9 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     const size_t vsmem = (size_t)VERIFY_WARPS * ((size_t)caps.lc * 32 + 32 * sizeof(float));
     verify_kernel<<<2 * ix->num_sms, VERIFY_WARPS * 32, vsmem, st>>>(va);
     CK(cudaGetLastError());
-    scan_counts_kernel<<<1, 1024, 0, st>>>(L.res_count, L.cand_off, 1, L.out_off, L.counters);
+    scan_counts_kernel<<<1, 1024, 0, st>>>(L.res_count, L.cand_off, 1, L.out_off, L.counters, nullptr);
     CK(cudaGetLastError());
-    finalize_kernel<<<1, 32 * FIN_WARPS, 0, st>>>(L.pool, L.cand_off, L.res_count, L.out_off, L.out, 1);
+    finalize_kernel<<<1, 32 * FIN_WARPS, 0, st>>>(L.pool, L.cand_off, L.res_count, L.out_off, L.out, 1, L.pool_cap);
     CK(cudaGetLastError());
 
     QDesc d;

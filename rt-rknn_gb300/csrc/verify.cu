@@ -680,7 +680,8 @@ plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_off, long long po
 
 // Output offsets of the stored results (a slot stores at most its region).
 __global__ void __launch_bounds__(SCAN_THREADS)
-scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int* out_off, const int* counters)
+scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int* out_off, const int* counters,
+                   int* out_off_host)
 {
     pdl_wait();
     pdl_trigger();
@@ -702,19 +703,23 @@ scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int*
 #pragma unroll
         for (int t = 0; t < SCAN_PT; ++t) {
             const int i = base + tid * SCAN_PT + t;
-            if (i < nq) out_off[i] = off;
+            if (i < nq) {
+                out_off[i] = off;
+                if (out_off_host) out_off_host[i] = off;
+            }
             off += v[t];
         }
         carry += tot;
         __syncthreads();
     }
     if (tid == 0) {
-        out_off[nq] = carry;
         const unsigned long long rt = (unsigned long long)cand_off[nq];
-        out_off[nq + 1] = (int)(unsigned)(rt & 0xffffffffu);
-        out_off[nq + 2] = (int)(unsigned)(rt >> 32);
-        out_off[nq + 3] = counters[2];
-        out_off[nq + 4] = counters[3];
+        const int tail[1 + OFF_TAIL] = {carry, (int)(unsigned)(rt & 0xffffffffu), (int)(unsigned)(rt >> 32),
+                                        counters[2], counters[3]};
+        for (int j = 0; j <= OFF_TAIL; ++j) {
+            out_off[nq + j] = tail[j];
+            if (out_off_host) out_off_host[nq + j] = tail[j];
+        }
     }
 }
 
@@ -828,7 +833,7 @@ __device__ __forceinline__ void warp_sort_slot(const unsigned* src, unsigned* ds
 // pool region above that.
 __global__ void __launch_bounds__(32 * FIN_WARPS, 1)
 finalize_kernel(int* res_pool, const long long* cand_off, const int* res_count, const int* out_off,
-                int* out, int nq)
+                int* out, int nq, long long out_cap)
 {
     pdl_wait();
     __shared__ unsigned skeys[FIN_BCAP];
@@ -842,7 +847,9 @@ finalize_kernel(int* res_pool, const long long* cand_off, const int* res_count, 
         const int n = (int)min((long long)res_count[s], cand_off[s + 1] - cand_off[s]);
         const unsigned* src = (const unsigned*)(res_pool + cand_off[s]);
         unsigned* dst = (unsigned*)(out + out_off[s]);
-        if (n <= 32) {
+        if ((long long)out_off[s] + n > out_cap) {
+            // past the output's capacity: left out (the batch fails on the host)
+        } else if (n <= 32) {
             // stable rank: smaller keys, and equal keys in lower lanes
             const unsigned key = lane < n ? okey((int)src[lane]) : 0xffffffffu;
             int rank = 0;

@@ -66,11 +66,16 @@ __global__ void plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_o
 // halves of cand_off[nq]), the dropped flag and the listed survivors
 // (counters[2], counters[3]), so that one copy brings back all of them.
 constexpr int OFF_TAIL = 4;
+// out_off_host (or null): device-accessible host memory that receives a
+// copy of the same nq+1+OFF_TAIL ints.
 __global__ void scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int* out_off,
-                                   const int* counters);
+                                   const int* counters, int* out_off_host);
 
 // one block per slot: sort the slot's results into out[out_off[s] ...]
+// out may be device-accessible host memory of out_cap ids: a slot whose range
+// would pass out_cap is left out (the caller sees the total and fails the
+// batch).
 __global__ void finalize_kernel(int* res_pool, const long long* cand_off, const int* res_count,
-                                const int* out_off, int* out, int nq);
+                                const int* out_off, int* out, int nq, long long out_cap);
 
 }  // namespace rknn

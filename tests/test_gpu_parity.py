@@ -180,6 +180,25 @@ def test_device_batch_with_understated_kmax(engine, filt):
     idx.close()
 
 
+def test_flat_batches_into_page_locked_ids(engine):
+    """query_batch_flat keeps one page-locked id buffer: from its second call
+    the finalize kernel writes the ids into it directly.  Batches that fit,
+    one that outgrows it (capacity error, larger buffer, retry) and smaller
+    ones after give the same ids as the per-query form and the oracle."""
+    ds = datagen.uniform(2000, 100_000, seed=41, nq=50, k=1)
+    o = O.Oracle.of(ds)
+    idx = engine.Index.of(ds)
+    for k in (1, 1, 2, 30, 30, 3, 3):
+        ids, off = idx.query_batch_flat(ds.queries, k, "fp32")
+        ref = idx.query_batch(ds.queries, k, "fp32")
+        assert off[-1] == sum(r.size for r in ref)
+        for i, r in enumerate(ref):
+            assert np.array_equal(ids[off[i]:off[i + 1]], r), (i, k)
+        for i in range(0, len(ds.queries), 10):
+            assert np.array_equal(ref[i], o.query(int(ds.queries[i]), k)), (i, k)
+    idx.close()
+
+
 def test_zone_bisectors_match_port(engine):
     """Same grid, same rules: the zone kernel builds rknn-inf's bisector set
     in the same order as the CPU restatement does."""
