@@ -60,7 +60,7 @@ def sources():
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     stamp = os.path.join(OUT, "stamp")
-    dig = _digest(sources() + [os.path.abspath(__file__)])
+    dig = _digest(sources() + [os.path.abspath(__file__)]) + (" checked" if CHECKED else " plain")
     if (not force and os.path.exists(LIB) and os.path.exists(CLI) and os.path.exists(stamp)
             and open(stamp).read() == dig):
         return LIB

@@ -74,6 +74,9 @@ using GraphKey = std::vector<long long>;
 constexpr int NAUX = 3;            // side streams for concurrent k-class zone launches
 constexpr int MAX_CLASSES = 16;
 
+constexpr int ZB_COUNTERS = 64;     // counter ints at the head of the zeroed block
+constexpr int ZB_VSTATS_INTS = 32;  // room for the statistics after them
+
 struct Workspace {
     int nq_cap = 0, lc = 0, seg_cap = 0;
     // a batch of nq queries: q at [0, nq), k at [nq, 2 nq), the k order at
@@ -89,8 +92,9 @@ struct Workspace {
     long long* d_cand_off = nullptr;   // result region of each slot (64-bit offsets)
     int *d_chunk_off = nullptr, *d_res_count = nullptr, *d_out_off = nullptr;
     int rcap = 1 << 18;            // ids a slot's region holds at most (raised when exceeded)
-    int* d_counters = nullptr;     // [0] zone work, [1] verify work, [2] region exceeded,
-                                   // [4..8] zone fault record,
+    int* d_counters = nullptr;     // ZB_COUNTERS ints, then the statistics and the result counts:
+                                   // [0] zone work, [1] verify work, [2] region exceeded,
+                                   // [3] survivors listed, [4..8] zone fault record,
                                    // [10..14] verify fault record, [16..31] zone work per k class
     VStats* d_vstats = nullptr;
     int *d_pool = nullptr, *d_out = nullptr;
@@ -191,8 +195,8 @@ void free_ws(Workspace& w)
     cudaFree(w.d_qko);
     cudaFree(w.d_qd); cudaFree(w.d_planes); cudaFree(w.d_bispos); cudaFree(w.d_segs); cudaFree(w.d_zst);
     cudaFree(w.d_slice_r);
-    cudaFree(w.d_cand_off); cudaFree(w.d_chunk_off); cudaFree(w.d_res_count); cudaFree(w.d_out_off);
-    cudaFree(w.d_counters); cudaFree(w.d_vstats);
+    cudaFree(w.d_cand_off); cudaFree(w.d_chunk_off); cudaFree(w.d_out_off);
+    cudaFree(w.d_counters);     // with the statistics and result counts
     cudaFree(w.d_pool); cudaFree(w.d_out); cudaFree(w.d_zscratch); cudaFree(w.d_surv);
     cudaFreeHost(w.h_qko); cudaFreeHost(w.h_off);
     cudaFreeHost(w.h_ids);
@@ -294,15 +298,19 @@ rknn_status ensure_ws(Workspace& w, int nq, const ZoneCaps& caps, long long pool
         CK(dalloc(w.d_segs, (size_t)nqc * sc));
         CK(dalloc(w.d_zst, nqc));
         CK(dalloc(w.d_cand_off, nqc + 1)); CK(dalloc(w.d_chunk_off, nqc + 1));
-        CK(dalloc(w.d_res_count, nqc)); CK(dalloc(w.d_out_off, nqc + 1 + OFF_TAIL));
-        CK(dalloc(w.d_counters, 64));
-        CK(cudaMemset(w.d_counters, 0, sizeof(int) * 64));
+        // counters, statistics and per-slot result counts in one block, so
+        // that one memset clears them before each batch
+        static_assert(sizeof(VStats) <= ZB_VSTATS_INTS * sizeof(int), "VStats outgrew its room");
+        CK(dalloc(w.d_counters, (size_t)ZB_COUNTERS + ZB_VSTATS_INTS + nqc));
+        CK(cudaMemset(w.d_counters, 0, sizeof(int) * ((size_t)ZB_COUNTERS + ZB_VSTATS_INTS + nqc)));
+        w.d_vstats = (VStats*)(w.d_counters + ZB_COUNTERS);
+        w.d_res_count = w.d_counters + ZB_COUNTERS + ZB_VSTATS_INTS;
+        CK(dalloc(w.d_out_off, nqc + 1 + OFF_TAIL));
         for (int i = 0; i < NAUX; ++i) {
             CK(cudaStreamCreateWithFlags(&w.aux[i], cudaStreamNonBlocking));
             CK(cudaEventCreateWithFlags(&w.join[i], cudaEventDisableTiming));
         }
         CK(cudaEventCreateWithFlags(&w.fork, cudaEventDisableTiming));
-        CK(dalloc(w.d_vstats, 1));
         CK(cudaMallocHost(&w.h_qko, sizeof(int) * 3 * (size_t)nqc));
         CK(cudaMallocHost(&w.h_off, sizeof(int) * (nqc + 1 + OFF_TAIL)));
         CK(cudaHostGetDevicePointer((void**)&w.h_qko_dev, w.h_qko, 0));
@@ -483,10 +491,8 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     cudaStream_t st = c.st;
     const int nq = b.nq;
     auto mark = [&](int i) { if (events) cudaEventRecord(c.kev[i], st); };
-    CK(cudaMemsetAsync(w.d_counters, 0, sizeof(int) * 4, st));
-    CK(cudaMemsetAsync(w.d_counters + 16, 0, sizeof(int) * MAX_CLASSES, st));
-    CK(cudaMemsetAsync(w.d_res_count, 0, sizeof(int) * nq, st));
-    CK(cudaMemsetAsync(w.d_vstats, 0, sizeof(VStats), st));
+    // counters, statistics and the slots' result counts: one memset
+    CK(cudaMemsetAsync(w.d_counters, 0, sizeof(int) * ((size_t)ZB_COUNTERS + ZB_VSTATS_INTS + nq), st));
 
     ZoneArgs za;
     za.fxy = ix->d_fxy; za.fstart = ix->d_fstart; za.fmbr = ix->d_fmbr; za.fpos = ix->d_fpos;
@@ -682,6 +688,19 @@ rknn_status run_sync(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = tr
         const long long region_total = tail.region_total;
         const int dropped = tail.dropped;
         const int flags[2] = {tail.dropped, tail.survivors};
+#ifdef RKNN_CHECKED
+        {
+            // bounds-checked build: a recorded out-of-range access fails the batch
+            int rec[16];
+            CK(cudaMemcpy(rec, w.d_counters, sizeof(rec), cudaMemcpyDeviceToHost));
+            for (int base : {4, 10})
+                if (rec[base])
+                    return fail(RKNN_ERR_CUDA, "bounds check: array " + std::to_string(rec[base + 1]) + " index " +
+                                                       std::to_string(rec[base + 2]) + " of " +
+                                                       std::to_string(rec[base + 3]) + " at line " +
+                                                       std::to_string(rec[base + 4]));
+        }
+#endif
         if ((unsigned)flags[1] > (unsigned long long)w.surv_cap) {
             // survivors overflowed the list (they were recounted in-warp):
             // give the next batch room for all of them
