@@ -220,6 +220,7 @@ void drop_graphs(Workspace& w)
 struct ZoneLaunch {
     size_t slice, smem;
     int grid;
+    int threads = 32 * ZONE_WARPS;   // 64: the slice filter with two warps per query
 };
 
 // Resident blocks per SM of kernel fn at this block size and dynamic shared
@@ -242,11 +243,20 @@ int occupancy(rknn_index* ix, const void* fn, int threads, size_t smem)
 
 // The slice filter's kernel for a class whose largest k is kmax.
 using ZoneFn = void (*)(ZoneArgs);
-ZoneFn slice_fn(int kmax)
+ZoneFn slice_fn(int kmax, bool two = false)
 {
+    if (two)
+        return kmax <= 4 ? slice_kernel2_r4 : kmax <= 8 ? slice_kernel2_r8 : kmax <= 12 ? slice_kernel2_r12
+             : kmax <= 16 ? slice_kernel2_r16 : kmax <= 24 ? slice_kernel2_r24 : slice_kernel2_r32;
     return kmax <= 4 ? slice_kernel_r4 : kmax <= 8 ? slice_kernel_r8 : kmax <= 12 ? slice_kernel_r12
          : kmax <= 16 ? slice_kernel_r16 : kmax <= 24 ? slice_kernel_r24 : kmax <= 32 ? slice_kernel_r32
          : slice_kernel;
+}
+
+// Register-list width of the slice filter for a class's largest k (0: heap).
+int slice_kr(int kmax)
+{
+    return kmax <= 4 ? 4 : kmax <= 8 ? 8 : kmax <= 12 ? 12 : kmax <= 16 ? 16 : kmax <= 24 ? 24 : kmax <= 32 ? 32 : 0;
 }
 
 ZoneLaunch zone_launch(rknn_index* ix, const ZoneCaps& c, int nq, bool slice = false, int kmax = 0)
@@ -254,6 +264,20 @@ ZoneLaunch zone_launch(rknn_index* ix, const ZoneCaps& c, int nq, bool slice = f
     ZoneLaunch L;
     L.slice = slice ? slice_layout(c).bytes : zone_layout(c).bytes;
     L.smem = L.slice * ZONE_WARPS;
+    const int kr = slice ? slice_kr(kmax) : 0;
+    if (kr > 0) {
+        // two warps per query (shorter chains) when every query of the class
+        // keeps a block resident; one warp each otherwise (more queries in
+        // flight)
+        const size_t smem2 = 2 * L.slice + (size_t)2 * kr * 32 * sizeof(float) + 64;
+        const int per2 = occupancy(ix, (const void*)slice_fn(kmax, true), 64, smem2);
+        if ((long long)nq <= (long long)per2 * ix->num_sms) {
+            L.smem = smem2;
+            L.threads = 64;
+            L.grid = std::max(1, nq);
+            return L;
+        }
+    }
     const int per_sm = occupancy(ix, (const void*)(slice ? slice_fn(kmax) : zone_kernel_smem), 32 * ZONE_WARPS, L.smem);
     long long want = (nq + ZONE_WARPS - 1) / ZONE_WARPS;
     L.grid = (int)std::max(1LL, std::min<long long>(want, (long long)per_sm * ix->num_sms));
@@ -521,7 +545,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
         za.rmax = z.caps.rm;
         za.work_counter = w.d_counters + 16 + i;
         cudaStream_t zs = i == 0 ? st : w.aux[(i - 1) % NAUX];
-        if (z.slice) slice_fn(z.kmax)<<<z.zl.grid, 32, z.zl.smem, zs>>>(za);
+        if (z.slice) slice_fn(z.kmax, z.zl.threads == 64)<<<z.zl.grid, z.zl.threads, z.zl.smem, zs>>>(za);
         else zone_kernel_smem<<<z.zl.grid, 32 * ZONE_WARPS, z.zl.smem, zs>>>(za);
         CK(cudaGetLastError());
     }
@@ -865,7 +889,9 @@ rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf, 
     }
     CKB(allow_dynamic_smem((const void*)slice_kernel, optin));
     for (const void* f : {(const void*)slice_kernel_r4, (const void*)slice_kernel_r8, (const void*)slice_kernel_r12,
-                          (const void*)slice_kernel_r16, (const void*)slice_kernel_r24, (const void*)slice_kernel_r32})
+                          (const void*)slice_kernel_r16, (const void*)slice_kernel_r24, (const void*)slice_kernel_r32,
+                          (const void*)slice_kernel2_r4, (const void*)slice_kernel2_r8, (const void*)slice_kernel2_r12,
+                          (const void*)slice_kernel2_r16, (const void*)slice_kernel2_r24, (const void*)slice_kernel2_r32})
         CKB(allow_dynamic_smem(f, optin));
     CKB(allow_dynamic_smem((const void*)verify_kernel, optin));
     CKB(allow_dynamic_smem((const void*)verify_kernel_u2, optin));

@@ -198,22 +198,38 @@ __device__ __forceinline__ void list_insert(float (&L)[KR], float v)
 
 // KR > 0: the slice bounds live in a register list (k <= KR); KR == 0: in a
 // shared-memory max-heap per lane (any k up to the class's capacity).
-template <int KR>
+// NWQ = 2 (register lists only): two warps per query.  Both walk the same
+// rings (same cell ranges, half-planes and stop decisions); each offers only
+// its half of the useful facilities (alternate bits of the batch's mask) to
+// its own lists.  At every ring top the two warps' lists meet in shared
+// memory: the k-th smallest arc of their union is the slice's bound (the k
+// smallest of all offered facilities are among the two lists' k smallest),
+// computed identically in both warps.  A facility neither warp offers can
+// enter neither warp's k smallest, so the union is unchanged.  At the end
+// warp 0 writes the half-planes while warp 1 scans the user cells.
+template <int KR, int NWQ>
 __device__ __forceinline__ void slice_body(const ZoneArgs& A)
 {
+    static_assert(NWQ == 1 || KR > 0, "two warps per query need register lists");
     pdl_trigger();
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31;
+    const int wq = NWQ == 2 ? (int)(threadIdx.x >> 5) : 0;   // warp within the query's block
 #ifdef RKNN_CHECKED
     if (threadIdx.x == 0 && blockIdx.x == 0) s_fault = A.fault;
     __syncthreads();
     if (!s_fault) s_fault = A.fault;
 #endif
     const SliceLayout LY = slice_layout(A.caps);
-    float* H = (float*)(smem + LY.heap);
-    float* Rs = (float*)(smem + LY.R);
-    int* lpos = (int*)(smem + LY.lpos);
-    uint32_t* bitmap = (uint32_t*)(smem + LY.bitmap);
+    char* wsm = smem + (size_t)wq * LY.bytes;           // this warp's region
+    float* H = (float*)(wsm + LY.heap);
+    float* Rs = (float*)(wsm + LY.R);
+    int* lpos = (int*)(wsm + LY.lpos);
+    uint32_t* bitmap = (uint32_t*)(wsm + LY.bitmap);
+    // NWQ = 2: both warps' lists ([warp][entry][lane]) and a few ints passed
+    // between the warps
+    float* xl = (float*)(smem + (size_t)NWQ * LY.bytes);
+    int* xs = (int*)(xl + (NWQ == 2 ? 2 * KR * 32 : 0));
     const int KC = A.caps.vc, LC = A.caps.lc;
     const long long NCF = (long long)A.gf.gx * A.gf.gy, NCU = (long long)A.gu.gx * A.gu.gy;
     (void)NCF; (void)NCU;
@@ -226,8 +242,15 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
 
     for (;;) {
         int slot = 0;
-        if (lane == 0) slot = atomicAdd(A.work_counter, 1);
-        slot = __shfl_sync(FULL, slot, 0);
+        if constexpr (NWQ == 2) {
+            __syncthreads();            // the previous query is done with the shared ints
+            if (threadIdx.x == 0) xs[0] = atomicAdd(A.work_counter, 1);
+            __syncthreads();
+            slot = xs[0];
+        } else {
+            if (lane == 0) slot = atomicAdd(A.work_counter, 1);
+            slot = __shfl_sync(FULL, slot, 0);
+        }
         if (slot >= A.nq) break;
         const int s = A.order ? A.order[slot] : slot;
         const int qin = A.q_in[s];
@@ -235,7 +258,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
         QDesc* qd = A.qd + s;
         ZStats zs = {};
         if (qin < 0 || qin >= A.nf || k <= 0) {
-            if (lane == 0) {
+            if (threadIdx.x == 0) {
                 QDesc d = {};
                 d.qpos = -1;
                 d.k = k;
@@ -252,7 +275,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
             // k beyond the slice bounds' capacity (a device batch whose kmax
             // understates a k): every user is a candidate and the
             // verification counts exactly
-            if (lane == 0) {
+            if (threadIdx.x == 0) {
                 QDesc d = {};
                 d.qx = qf.x;
                 d.qy = qf.y;
@@ -300,6 +323,29 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
         for (int i = 0; i < (KR > 0 ? KR : 1); ++i) RL[i] = i < KR - k ? -INFINITY : INFINITY;
         // the slice's current bound R: its k-th smallest arc (infinite below k)
 #define SLICE_KTH() (KR > 0 ? RL[(KR > 0 ? KR : 1) - 1] : ((n < k) ? INFINITY : H[lane]))
+        // the slice's bound over both warps' lists (NWQ = 2): the k-th smallest
+        // of their union, min over i of max(a_{i-1}, b_{k-1-i}) for the
+        // ascending real entries a, b (the last k of each list)
+        auto union_kth = [&]() -> float {
+            if constexpr (NWQ == 2) {
+                float* mine = xl + (size_t)wq * KR * 32 + lane;
+#pragma unroll
+                for (int i = 0; i < KR; ++i) mine[i * 32] = RL[(KR > 0 ? i : 0)];
+                __syncthreads();
+                const float* a = xl + lane;
+                const float* b = xl + KR * 32 + lane;
+                float best = INFINITY;
+                for (int i = 0; i <= k; ++i) {
+                    const float x = i > 0 ? a[(KR - k + i - 1) * 32] : -INFINITY;
+                    const float y = i < k ? b[(KR - 1 - i) * 32] : -INFINITY;
+                    best = fminf(best, fmaxf(x, y));
+                }
+                __syncthreads();
+                return best;
+            } else {
+                return SLICE_KTH();
+            }
+        };
         int nL = 0;             // half-planes kept (warp-uniform)
         int rho_ring = -1;      // first ring with a streamed facility left out of the half-planes
         const int fbudget = max(8192, 128 * k);
@@ -338,7 +384,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
             }
             // stop when no facility at or beyond this ring can change a
             // slice's effective bound min(R, C)
-            const float Rl = fminf(SLICE_KTH(), clip);
+            const float Rl = fminf(union_kth(), clip);
             __syncwarp();
             float Rmax = Rl;
 #pragma unroll
@@ -442,7 +488,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                     // ring order, those of plane-only cells included (so that
                     // rho is limited only by the rings, below)
                     const unsigned pm = __ballot_sync(FULL, ok);
-                    if (ok) {
+                    if (ok && wq == 0) {
                         const int at = nL + __popc(pm & ((1u << lane) - 1));
                         if (at < LC) lpos[SX(at, LC, 315)] = fidx;
                     }
@@ -458,16 +504,24 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                     // window maxima taken before the batch are conservative.
                     unsigned m = om;
                     {
-                        const float Rl = SLICE_KTH();
-                        float Rw = Rl;
-#pragma unroll
-                        for (int dd = 1; dd <= 8; ++dd)
-                            Rw = fmaxf(Rw, fmaxf(__shfl_sync(FULL, Rl, (lane + dd) & 31),
-                                                 __shfl_sync(FULL, Rl, (lane - dd) & 31)));
                         const int sj = ok ? slice_of(vx, vy) : 0;
-                        const float Rwj = __shfl_sync(FULL, Rw, sj);
+                        float Rwj;
+                        if constexpr (NWQ == 2) {
+                            // the ring top's window maxima of min(R, C) over both
+                            // warps' lists (arcs beyond C change no effective bound)
+                            Rwj = Rs[sj];
+                        } else {
+                            const float Rl = SLICE_KTH();
+                            float Rw = Rl;
+#pragma unroll
+                            for (int dd = 1; dd <= 8; ++dd)
+                                Rw = fmaxf(Rw, fmaxf(__shfl_sync(FULL, Rl, (lane + dd) & 31),
+                                                     __shfl_sync(FULL, Rl, (lane - dd) & 31)));
+                            Rwj = __shfl_sync(FULL, Rw, sj);
+                        }
                         const bool useful = ok && !rpo && !(0.25f * fmaf(vx, vx, vy * vy) * (1.0f - 4.0f * kU32) >= Rwj * Rwj);
                         m = __ballot_sync(FULL, useful);
+                        if constexpr (NWQ == 2) m &= wq ? 0xaaaaaaaau : 0x55555555u;     // this warp's half
                     }
                     // every lane offers every useful facility to its slice
                     zs.cand += __popc(m);
@@ -521,9 +575,9 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
         // R(P): k-th smallest arc, rounded up for the user test, and clipped
         // to the box (no user lies farther)
         {
-            const float R = SLICE_KTH();
+            const float R = union_kth();
             Rs[lane] = fminf(R < INFINITY ? R * (1.0f + 1e-5f) + 1e-30f : INFINITY, clip);
-            A.slice_r[(size_t)s * 32 + lane] = Rs[lane];
+            if (wq == 0) A.slice_r[(size_t)s * 32 + lane] = Rs[lane];
         }
         __syncwarp();
         zs.cyc[0] += clock64() - tph;
@@ -536,6 +590,9 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
         // bound 8u (2F'(|x'|+|y'|) + F'^2) exceeds the evaluation error with
         // it, about 3u|a x'| + 3u|b y'| + 7u|c|, since |a|, |b| <= 2F' and
         // |c| <= F'^2 (F' from the largest c below, rounded up).
+        float k2f = 0.0f, kf2 = 0.0f;
+        double k2f64 = 0.0, kf264 = 0.0;
+        if (NWQ == 1 || wq == 0) {
         float4* planes = A.planes + (size_t)s * A.pstride;
         float cmax = 0.0f;
         for (int m = lane; m < nL; m += 32) {
@@ -572,14 +629,18 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
             }
         }
         const double Fp = (double)__fmul_ru(__fsqrt_ru(__fmul_ru(cmax, 1.0f + 1e-5f)), 1.0f + 1e-6f) + 1e-30;
-        const float k2f = (float)(8.0 * (double)kU32 * 2.0 * Fp * (1.0 + 1e-6));
-        const float kf2 = (float)(8.0 * (double)kU32 * Fp * Fp * (1.0 + 1e-6)) + 1e-30f;
-        const double k2f64 = 8.0 * kU64 * 2.0 * Fp * (1.0 + 1e-6);
-        const double kf264 = 8.0 * kU64 * Fp * Fp * (1.0 + 1e-6) + 1e-300;
+        k2f = (float)(8.0 * (double)kU32 * 2.0 * Fp * (1.0 + 1e-6));
+        kf2 = (float)(8.0 * (double)kU32 * Fp * Fp * (1.0 + 1e-6)) + 1e-30f;
+        k2f64 = 8.0 * kU64 * 2.0 * Fp * (1.0 + 1e-6);
+        kf264 = 8.0 * kU64 * Fp * Fp * (1.0 + 1e-6) + 1e-300;
+        }   // half-planes
 
         zs.cyc[7] += clock64() - tph;
         tph = clock64();
 
+        int nseg = 0, ncand = 0;
+        int qflags = QF_SLICE_R;
+        if (NWQ == 1 || wq == 1) {
         // ---- ring scan over user cells --------------------------------------
         const Grid gu = A.gu;
         const int ucx = cell_coord(qf.x, gu.x0, gu.inv, gu.gx);
@@ -646,8 +707,6 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
 
         // ---- segments: one user range per row ------------------------------
         int2* seg = A.segs + (size_t)s * A.seg_cap;
-        int nseg = 0, ncand = 0;
-        int qflags = QF_SLICE_R;
         if (all_users) {
             seg[0] = make_int2(0, 0);
             seg[1] = make_int2(0, A.nu);
@@ -693,9 +752,24 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
         } else if (lane == 0) {
             seg[0] = make_int2(0, 0);
         }
+        }   // ring scan and segments
         zs.cyc[7] += clock64() - tph;
         zs.nb = nL;
-        if (lane == 0) {
+        if constexpr (NWQ == 2) {
+            // warp 1's results to warp 0, which writes the descriptor
+            if (threadIdx.x == 32) {
+                xs[1] = nseg; xs[2] = ncand; xs[3] = qflags; xs[4] = zs.rings; xs[5] = zs.cand;
+                ((long long*)(xs + 8))[0] = zs.cyc[2];
+                ((long long*)(xs + 8))[1] = zs.cyc[1];
+            }
+            __syncthreads();
+            if (wq == 0) {
+                nseg = xs[1]; ncand = xs[2]; qflags = xs[3]; zs.rings = xs[4]; zs.cand += xs[5];
+                zs.cyc[2] = ((long long*)(xs + 8))[0];
+                zs.cyc[1] += ((long long*)(xs + 8))[1];
+            }
+        }
+        if (threadIdx.x == 0) {
             QDesc d;
             d.qx = qf.x;
             d.qy = qf.y;
@@ -720,12 +794,18 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
 
 #undef SLICE_KTH
 
-__global__ void __launch_bounds__(32, 1) slice_kernel(ZoneArgs A) { slice_body<0>(A); }
-__global__ void __launch_bounds__(32, 1) slice_kernel_r4(ZoneArgs A) { slice_body<4>(A); }
-__global__ void __launch_bounds__(32, 1) slice_kernel_r8(ZoneArgs A) { slice_body<8>(A); }
-__global__ void __launch_bounds__(32, 1) slice_kernel_r12(ZoneArgs A) { slice_body<12>(A); }
-__global__ void __launch_bounds__(32, 1) slice_kernel_r16(ZoneArgs A) { slice_body<16>(A); }
-__global__ void __launch_bounds__(32, 1) slice_kernel_r24(ZoneArgs A) { slice_body<24>(A); }
-__global__ void __launch_bounds__(32, 1) slice_kernel_r32(ZoneArgs A) { slice_body<32>(A); }
+__global__ void __launch_bounds__(32, 1) slice_kernel(ZoneArgs A) { slice_body<0, 1>(A); }
+__global__ void __launch_bounds__(32, 1) slice_kernel_r4(ZoneArgs A) { slice_body<4, 1>(A); }
+__global__ void __launch_bounds__(32, 1) slice_kernel_r8(ZoneArgs A) { slice_body<8, 1>(A); }
+__global__ void __launch_bounds__(32, 1) slice_kernel_r12(ZoneArgs A) { slice_body<12, 1>(A); }
+__global__ void __launch_bounds__(32, 1) slice_kernel_r16(ZoneArgs A) { slice_body<16, 1>(A); }
+__global__ void __launch_bounds__(32, 1) slice_kernel_r24(ZoneArgs A) { slice_body<24, 1>(A); }
+__global__ void __launch_bounds__(32, 1) slice_kernel_r32(ZoneArgs A) { slice_body<32, 1>(A); }
+__global__ void __launch_bounds__(64, 7) slice_kernel2_r4(ZoneArgs A) { slice_body<4, 2>(A); }
+__global__ void __launch_bounds__(64, 7) slice_kernel2_r8(ZoneArgs A) { slice_body<8, 2>(A); }
+__global__ void __launch_bounds__(64, 7) slice_kernel2_r12(ZoneArgs A) { slice_body<12, 2>(A); }
+__global__ void __launch_bounds__(64, 7) slice_kernel2_r16(ZoneArgs A) { slice_body<16, 2>(A); }
+__global__ void __launch_bounds__(64, 7) slice_kernel2_r24(ZoneArgs A) { slice_body<24, 2>(A); }
+__global__ void __launch_bounds__(64, 7) slice_kernel2_r32(ZoneArgs A) { slice_body<32, 2>(A); }
 
 }  // namespace rknn
