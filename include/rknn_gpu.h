@@ -171,8 +171,9 @@ rknn_status rknn_query_batch(rknn_index* idx, const int32_t* q_index, const int3
 rknn_status rknn_host_alloc(int64_t bytes, void** out);
 rknn_status rknn_host_free(void* p);
 
-/* Device-resident form: q_index/k are device pointers; results stay on the
- * device (see rknn_batch_device_results).  kmax bounds every k[i] (it sizes
+/* Device-resident form: q_index/k are device pointers, read by the kernels
+ * in place (keep them unchanged until rknn_batch_device_results returns);
+ * results stay on the device (see rknn_batch_device_results).  kmax bounds every k[i] (it sizes
  * the zone state; a larger k is still answered exactly, with the zone cut
  * short).  Enqueued on the index's stream; returns without synchronizing.
  * Query indices must be valid (an out-of-range slot yields no results). */
@@ -181,8 +182,8 @@ rknn_status rknn_query_batch_device(rknn_index* idx, const int32_t* d_q_index,
 
 /* Device pointers to the last device batch's results: ids and nq+1 int32
  * offsets.  Synchronizes the index's stream; when a query's results outgrew
- * the room the batch gave them, runs the batch again (from the workspace's
- * copies of q and k) so that the results are complete.  Valid until the next
+ * the room the batch gave them, runs the batch again (from the caller's q
+ * and k) so that the results are complete.  Valid until the next
  * query call on this index. */
 rknn_status rknn_batch_device_results(rknn_index* idx, const int32_t** d_ids,
                                       const int32_t** d_offsets);

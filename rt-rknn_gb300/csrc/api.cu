@@ -74,6 +74,19 @@ using GraphKey = std::vector<long long>;
 constexpr int NAUX = 3;            // side streams for concurrent k-class zone launches
 constexpr int MAX_CLASSES = 16;
 
+// A captured batch: its graph, the executable, and the filter kernels'
+// nodes with their arguments, so that the query arrays can be re-pointed per
+// call (the caller's device arrays, or the page-locked staging) without
+// copies or a new capture.
+struct CachedGraph {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<cudaGraphNode_t> fnodes;
+    std::vector<cudaKernelNodeParams> fparams;
+    std::vector<ZoneArgs> fargs;
+    const int *q = nullptr, *k = nullptr, *order = nullptr;   // what the filter nodes read now
+};
+
 constexpr int ZB_COUNTERS = 64;     // counter ints at the head of the zeroed block
 constexpr int ZB_VSTATS_INTS = 32;  // room for the statistics after them
 
@@ -107,7 +120,7 @@ struct Workspace {
     int *h_qko_dev = nullptr, *h_off_dev = nullptr;   // the same, as device pointers
     int* h_ids = nullptr;
     long long h_ids_cap = 0;
-    std::map<GraphKey, cudaGraphExec_t> graphs;
+    std::map<GraphKey, CachedGraph> graphs;
     cudaStream_t aux[NAUX] = {};
     cudaEvent_t fork = nullptr, join[NAUX] = {};
 };
@@ -152,6 +165,7 @@ struct rknn_index {
     int32_t* last_out = nullptr;   // the previous host batch's id buffer and capacity
     long long last_cap = 0;
     int dev_nq = 0, dev_kmax = 0, dev_mode = 0;   // the last device batch (0: none pending a check)
+    const int32_t *dev_q = nullptr, *dev_k = nullptr;   // its caller's arrays
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int profiling = 0;
     cudaEvent_t kev[7] = {};
@@ -168,7 +182,9 @@ namespace {
 // id buffer the caller passes again -- the sorted ids straight into it (all
 // device-accessible host memory: no copies on the stream).
 struct Io {
-    const int* qko = nullptr;       // q at [0, nq), k at [nq, 2 nq), order at [2 nq, 3 nq)
+    const int* q = nullptr;         // the queries' facility indices (null: the workspace's d_qko)
+    const int* k = nullptr;         // their k
+    const int* order = nullptr;     // slots by descending k (non-uniform batches)
     int* off_host = nullptr;        // offsets and flags, mirrored into host memory
     int* ids = nullptr;             // sorted ids (null: the workspace's d_out)
     long long ids_cap = 0;          // capacity of ids (slots that would pass it are skipped)
@@ -190,7 +206,10 @@ Ctx main_ctx(rknn_index* ix)
 
 void free_ws(Workspace& w)
 {
-    for (auto& g : w.graphs) cudaGraphExecDestroy(g.second);
+    for (auto& g : w.graphs) {
+        cudaGraphExecDestroy(g.second.exec);
+        cudaGraphDestroy(g.second.g);
+    }
     w.graphs.clear();
     cudaFree(w.d_qko);
     cudaFree(w.d_qd); cudaFree(w.d_planes); cudaFree(w.d_bispos); cudaFree(w.d_segs); cudaFree(w.d_zst);
@@ -210,7 +229,10 @@ void free_ws(Workspace& w)
 
 void drop_graphs(Workspace& w)
 {
-    for (auto& g : w.graphs) cudaGraphExecDestroy(g.second);
+    for (auto& g : w.graphs) {
+        cudaGraphExecDestroy(g.second.exec);
+        cudaGraphDestroy(g.second.g);
+    }
     w.graphs.clear();
 }
 
@@ -251,6 +273,19 @@ ZoneFn slice_fn(int kmax, bool two = false)
     return kmax <= 4 ? slice_kernel_r4 : kmax <= 8 ? slice_kernel_r8 : kmax <= 12 ? slice_kernel_r12
          : kmax <= 16 ? slice_kernel_r16 : kmax <= 24 ? slice_kernel_r24 : kmax <= 32 ? slice_kernel_r32
          : slice_kernel;
+}
+
+// Whether a kernel is one of the filter kernels (the readers of the query
+// arrays).
+bool is_filter_kernel(const void* f)
+{
+    for (const void* g : {(const void*)zone_kernel_smem, (const void*)slice_kernel, (const void*)slice_kernel_r4,
+                          (const void*)slice_kernel_r8, (const void*)slice_kernel_r12, (const void*)slice_kernel_r16,
+                          (const void*)slice_kernel_r24, (const void*)slice_kernel_r32, (const void*)slice_kernel2_r4,
+                          (const void*)slice_kernel2_r8, (const void*)slice_kernel2_r12, (const void*)slice_kernel2_r16,
+                          (const void*)slice_kernel2_r24, (const void*)slice_kernel2_r32})
+        if (f == g) return true;
+    return false;
 }
 
 // Register-list width of the slice filter for a class's largest k (0: heap).
@@ -523,8 +558,10 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     za.gf = ix->gf; za.nf = (int)ix->nf;
     za.ustart = ix->d_ustart; za.gu = ix->gu; za.nu = (int)ix->nu;
     za.sx0 = ix->sx0; za.sy0 = ix->sy0; za.sx1 = ix->sx1; za.sy1 = ix->sy1;
-    const int* qko = c.io.qko ? c.io.qko : w.d_qko;
-    za.q_in = qko; za.k_in = qko + nq;
+    const int* qin = c.io.q ? c.io.q : w.d_qko;
+    const int* kin = c.io.q ? c.io.k : w.d_qko + nq;
+    const int* oin = c.io.q ? c.io.order : w.d_qko + 2 * nq;
+    za.q_in = qin; za.k_in = kin;
     za.skip_coincident = ix->skip_coincident;
     za.seg_cap = w.seg_cap;
     za.qd = w.d_qd; za.planes = w.d_planes; za.bis_pos = w.d_bispos; za.segs = w.d_segs; za.zst = w.d_zst;
@@ -539,7 +576,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     }
     for (int i = 0; i < ncls; ++i) {
         const ZClass& z = b.cls[i];
-        za.order = b.use_order ? qko + 2 * nq + z.off : nullptr;
+        za.order = b.use_order ? oin + z.off : nullptr;
         za.nq = z.n;
         za.caps = z.caps;
         za.rmax = z.caps.rm;
@@ -605,25 +642,61 @@ rknn_status launch(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = true
     key.push_back(w.pool_cap);
     key.push_back(w.rcap);
     key.push_back(w.surv_cap);
-    key.push_back((long long)(uintptr_t)c.io.qko);
     key.push_back((long long)(uintptr_t)c.io.off_host);
     key.push_back((long long)(uintptr_t)c.io.ids);
     key.push_back(c.io.ids_cap);
+    const int* q = c.io.q ? c.io.q : w.d_qko;
+    const int* k = c.io.q ? c.io.k : w.d_qko + b.nq;
+    const int* order = c.io.q ? c.io.order : w.d_qko + 2 * b.nq;
     auto it = w.graphs.find(key);
     if (it == w.graphs.end()) {
-        cudaGraph_t g;
+        CachedGraph cg;
         CK(cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal));
         rknn_status s = enqueue(ix, c, b, false, true);
-        cudaError_t e = cudaStreamEndCapture(c.st, &g);
-        if (s != RKNN_OK) { if (e == cudaSuccess) cudaGraphDestroy(g); return s; }
+        cudaError_t e = cudaStreamEndCapture(c.st, &cg.g);
+        if (s != RKNN_OK) { if (e == cudaSuccess) cudaGraphDestroy(cg.g); return s; }
         CK(e);
-        cudaGraphExec_t ge;
-        e = cudaGraphInstantiate(&ge, g, 0);
-        cudaGraphDestroy(g);
-        CK(e);
-        it = w.graphs.emplace(key, ge).first;
+        e = cudaGraphInstantiate(&cg.exec, cg.g, 0);
+        if (e != cudaSuccess) { cudaGraphDestroy(cg.g); CK(e); }
+        // the filter kernels' nodes: the only ones that read the query arrays
+        size_t nn = 0;
+        CK(cudaGraphGetNodes(cg.g, nullptr, &nn));
+        std::vector<cudaGraphNode_t> nodes(nn);
+        CK(cudaGraphGetNodes(cg.g, nodes.data(), &nn));
+        for (cudaGraphNode_t nd : nodes) {
+            cudaGraphNodeType t;
+            CK(cudaGraphNodeGetType(nd, &t));
+            if (t != cudaGraphNodeTypeKernel) continue;
+            cudaKernelNodeParams kp;
+            CK(cudaGraphKernelNodeGetParams(nd, &kp));
+            if (!is_filter_kernel(kp.func)) continue;
+            cg.fnodes.push_back(nd);
+            cg.fparams.push_back(kp);
+            cg.fargs.push_back(*(const ZoneArgs*)kp.kernelParams[0]);
+        }
+        cg.q = q;
+        cg.k = k;
+        cg.order = order;
+        it = w.graphs.emplace(key, std::move(cg)).first;
     }
-    CK(cudaGraphLaunch(it->second, c.st));
+    CachedGraph& cg = it->second;
+    if (cg.q != q || cg.k != k || cg.order != order) {
+        for (size_t i = 0; i < cg.fnodes.size(); ++i) {
+            ZoneArgs& a = cg.fargs[i];
+            a.q_in = q;
+            a.k_in = k;
+            if (a.order) a.order = order + (a.order - cg.order);
+            void* args[1] = {&a};
+            cudaKernelNodeParams kp = cg.fparams[i];
+            kp.kernelParams = args;
+            kp.extra = nullptr;
+            CK(cudaGraphExecKernelNodeSetParams(cg.exec, cg.fnodes[i], &kp));
+        }
+        cg.q = q;
+        cg.k = k;
+        cg.order = order;
+    }
+    CK(cudaGraphLaunch(cg.exec, c.st));
     return RKNN_OK;
 }
 
@@ -1061,7 +1134,9 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
     std::memcpy(w.h_qko, q, sizeof(int) * nq);
     std::memcpy(w.h_qko + nq, k, sizeof(int) * nq);
     if (!uniform) std::memcpy(w.h_qko + 2 * nq, order.data(), sizeof(int) * nq);
-    c.io.qko = w.h_qko_dev;
+    c.io.q = w.h_qko_dev;
+    c.io.k = w.h_qko_dev + nq;
+    c.io.order = w.h_qko_dev + 2 * nq;
     c.io.off_host = w.h_off_dev;
     bool locked = false;
     int* ids_dev = nullptr;
@@ -1175,9 +1250,13 @@ rknn_status rknn_query_batch_device(rknn_index* ix, const int32_t* d_q, const in
     ix->last_lc = b.pstride;
     rknn_status s = ensure_ws(w, nq, plan_caps(b), std::max<long long>(w.pool_cap, (long long)nq * 4096));
     if (s != RKNN_OK) return s;
-    CK(cudaMemcpyAsync(w.d_qko, d_q, sizeof(int) * nq, cudaMemcpyDeviceToDevice, ix->stream));
-    CK(cudaMemcpyAsync(w.d_qko + nq, d_k, sizeof(int) * nq, cudaMemcpyDeviceToDevice, ix->stream));
+    // the filter kernels read the caller's arrays (kept for a rerun by
+    // rknn_batch_device_results)
     Ctx c = main_ctx(ix);
+    c.io.q = d_q;
+    c.io.k = d_k;
+    ix->dev_q = d_q;
+    ix->dev_k = d_k;
     s = launch(ix, c, b);
     ix->last_nq = nq;
     ix->last_mode = mode;
@@ -1195,8 +1274,8 @@ rknn_status rknn_batch_device_results(rknn_index* ix, const int32_t** d_ids, con
     CK(cudaSetDevice(ix->device));
     if (ix->dev_nq > 0) {
         // a slot whose results outgrew its region, or regions that outgrew
-        // the pool, left the device batch incomplete: run it again (its q
-        // and k are still in the workspace) with room for all of them
+        // the pool, left the device batch incomplete: run it again (from the
+        // caller's q and k) with room for all of them
         Workspace& w = ix->ws;
         const int nq = ix->dev_nq;
         CK(cudaMemcpyAsync(w.h_off, w.d_out_off, sizeof(int) * (nq + 1 + OFF_TAIL), cudaMemcpyDeviceToHost, ix->stream));
@@ -1208,6 +1287,8 @@ rknn_status rknn_batch_device_results(rknn_index* ix, const int32_t** d_ids, con
             if (dropped) w.rcap = (int)std::min<long long>((long long)w.rcap * 8, std::max<long long>(ix->nu, 1));
             const BatchPlan b = plan_batch(ix, nq, ix->dev_mode, false, nullptr, ix->dev_kmax);
             Ctx c = main_ctx(ix);
+            c.io.q = ix->dev_q;
+            c.io.k = ix->dev_k;
             rknn_status s = run_sync(ix, c, b);
             if (s != RKNN_OK) return s;
         }
