@@ -1140,6 +1140,8 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
     c.io.off_host = w.h_off_dev;
     bool locked = false;
     int* ids_dev = nullptr;
+    // asked on every call: a freed page-locked buffer's address may come back
+    // as ordinary memory
     if (out_ids && cap > 0) {
         cudaPointerAttributes pa;
         locked = cudaPointerGetAttributes(&pa, out_ids) == cudaSuccess && pa.type == cudaMemoryTypeHost;

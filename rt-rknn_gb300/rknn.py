@@ -303,20 +303,33 @@ class Index:
         output buffers are reused between calls)."""
         L = load()
         qs = np.ascontiguousarray(qs, dtype=np.int32)
-        ks = np.ascontiguousarray(np.broadcast_to(np.asarray(ks, np.int32), qs.shape), dtype=np.int32)
         nq = qs.shape[0]
-        off = getattr(self, "_flat_off", None)
-        if off is None or off.shape[0] < nq + 1:
-            off = self._flat_off = np.zeros(nq + 1, np.int64)
-        buf = getattr(self, "_flat_out", None)
-        if buf is None:
-            buf = self._flat_out = pinned_ids(1 << 16)
+        if np.ndim(ks) == 0:
+            # a scalar k: one cached array of it per batch size
+            kc = getattr(self, "_flat_k", None)
+            if kc is None or kc[0] != (nq, int(ks)):
+                kc = self._flat_k = ((nq, int(ks)), np.full(nq, int(ks), np.int32))
+            ks = kc[1]
+        else:
+            ks = np.ascontiguousarray(np.broadcast_to(np.asarray(ks, np.int32), qs.shape), dtype=np.int32)
+        # the offsets and the page-locked id buffer persist, their addresses
+        # with them
+        fo = getattr(self, "_flat_off", None)
+        if fo is None or fo[0].shape[0] < nq + 1:
+            a = np.zeros(max(nq + 1, 1024), np.int64)
+            fo = self._flat_off = (a, a.ctypes.data)
+        off, off_p = fo
+        fb = getattr(self, "_flat_out", None)
+        if fb is None:
+            b = pinned_ids(1 << 16)
+            fb = self._flat_out = (b, b.ctypes.data, b.shape[0])
         while True:
-            out = buf
-            rc = L.rknn_query_batch(self.h, _ptr(qs), _ptr(ks), nq, _MODES[mode], out.ctypes.data,
-                                    out.shape[0], off.ctypes.data, None)
-            if rc == 5 and off[nq] > out.shape[0]:
-                buf = self._flat_out = pinned_ids(int(off[nq] * 5 // 4))
+            out, out_p, cap = fb
+            rc = L.rknn_query_batch(self.h, qs.ctypes.data, ks.ctypes.data, nq, _MODES[mode], out_p, cap, off_p,
+                                    None)
+            if rc == 5 and off[nq] > cap:
+                b = pinned_ids(int(off[nq] * 5 // 4))
+                fb = self._flat_out = (b, b.ctypes.data, b.shape[0])
                 continue
             _check(rc)
             return out[: off[nq]], off[: nq + 1]
