@@ -18,7 +18,10 @@ exact fallback; result sets are bit-exact.  Prints one JSON line (rank 0).
              before every step
   roofline   the dominant kernel (of the filter and the verification),
              timed live per launch with CUDA events in profiling mode;
-             roofline_other: the same for the other one
+             roofline_other: the same for the other one;
+             roofline_saturated: both kernels on the same workload as one
+             batch of 16384 queries (GPU full), against peak instruction
+             issue (their bound there), HBM and FP32
   fp64_single_query  the plain form: one query per launch, FP64 predicates,
              rknn-inf's influence zone (the drop-in); p50/p99 latency
   serving    open-loop Poisson arrivals through the continuous batcher
@@ -53,6 +56,12 @@ NF, NU, K, NQ = 100_000, 1_000_000, 10, 1000
 # (profiles/slice_verify_recount_finalize_config2_k10.md); the verification
 # figure is verify_kernel plus recount_kernel
 TRAFFIC = {"slice_kernel": 1533184, "verify_kernel": 6904576 + 386048}
+# warp instructions per unit of work of the two kernels in a batch of SAT_NQ
+# queries of this workload, from one ncu capture (smsp__inst_executed.sum of
+# the launch over its queries or its half-plane evaluations;
+# profiles/slice_verify_config2_16k_queries.md)
+SAT_NQ = 16384
+INSTR = {"slice_kernel_per_query": 164.45e6 / 16384, "verify_kernel_per_eval": 108.18e6 / 175826300}
 
 
 def peaks():
@@ -365,6 +374,42 @@ def run_ours(args):
     roof, other = (froof, vroof) if zms >= vms else (vroof, froof)
     roof = dict(roof, kernel_ms=kavg, share={n: v / sum(kavg.values()) for n, v in kavg.items()})
 
+    # ---- the same workload with the GPU full: one batch of SAT_NQ queries.
+    # Both kernels are bound by instruction issue there; their issue roofline
+    # is the warp instructions the work needs (per query for the filter, per
+    # half-plane evaluation for the verification, from one ncu capture of this
+    # batch) at the SMs' peak issue rate (4 warp instructions per cycle per
+    # SM at the sampled clock).
+    sat = None
+    if not args.no_saturation and NQ < SAT_NQ:
+        qsat = np.random.default_rng(99 + rank).choice(ds.nf, size=SAT_NQ, replace=False).astype(np.int32)
+        idx.query_batch_flat(qsat, K, "fp32")
+        idx.set_profiling(True)
+        with torch.cuda.stream(stream):
+            flush.fill_(7.0)
+        stream.synchronize()
+        idx.query_batch_flat(qsat, K, "fp32")
+        ksat = idx.kernel_ms()
+        sst = idx.last_stats()
+        idx.set_profiling(False)
+        clk_ghz = (clk.summary().get("sm_mhz") or 2070.0) / 1e3
+        issue_peak = 4 * props.multi_processor_count * clk_ghz * 1e9          # warp instructions / s
+        sz = ksat["zone"] / 1e3
+        sv = ksat["verify"] / 1e3
+        zi = INSTR["slice_kernel_per_query"] * SAT_NQ
+        vi = INSTR["verify_kernel_per_eval"] * sst["plane_evals"]
+        sat = {"queries": SAT_NQ, "queries_per_s_device": SAT_NQ / (sum(ksat.values()) / 1e3),
+               "issue_peak_warp_instr_per_s": issue_peak,
+               "slice_kernel": {"launch_ms": ksat["zone"], "warp_instr": zi, "frac_issue": zi / sz / issue_peak,
+                                "hbm_frac": (8 * sst["zone_points"] + 8 * sst["zone_cells"] + 20 * sst["bisectors"]
+                                             + 64 * SAT_NQ) / sz / (hbm_peak * 1e9)},
+               "verify_kernel": {"launch_ms": ksat["verify"], "warp_instr": vi, "frac_issue": vi / sv / issue_peak,
+                                 "tflops": 4 * sst["plane_evals"] / sv / 1e12,
+                                 "fp32_frac": 4 * sst["plane_evals"] / sv / 1e12 / fp32_peak,
+                                 "hbm_frac": (8 * sst["candidates"] + 16 * sst["bisectors"] + 4 * sst["results"])
+                                             / sv / (hbm_peak * 1e9)},
+               "note": "warp instructions per unit from ncu (profiles/slice_verify_config2_16k_queries.md)"}
+
     # ---- CPU baseline (rank 0, N=1 only) ---------------------------------
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -395,6 +440,7 @@ def run_ours(args):
         "speedup_fp32_batched_vs_fp64_single": value / ws / fp64_single_qps,
         "roofline": roof,
         "roofline_other": other,
+        "roofline_saturated": sat,
         "stats": {k2: st[k2] for k2 in ("bisectors", "zone_vertices_max", "zone_candidates", "zone_fp64",
                                         "zone_points", "zone_cells",
                                         "candidates", "plane_evals", "survivors", "fac_checks",
@@ -422,6 +468,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=400000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-saturation", action="store_true", help="skip the 16384-query saturation batch")
     ap.add_argument("--queries", type=int, default=NQ,
                     help="queries per step (default 1000, the headline workload; larger batches for profiling)")
     args = ap.parse_args()

@@ -237,8 +237,12 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
     float e1x, e1y, e2x, e2y;
     sincosf((float)lane * SLICE_W - WIDEN, &e1y, &e1x);
     sincosf((float)(lane + 1) * SLICE_W + WIDEN, &e2y, &e2x);
-    const double slack = 1e-5 * ((double)A.gf.cs + fmax(fmax(fabs(A.sx0), fabs(A.sx1)), fmax(fabs(A.sy0), fabs(A.sy1))));
-    const float slack_f = __double2float_ru(slack);
+    // the data box, rounded outward
+    const float bx0 = __double2float_rd(A.sx0), by0 = __double2float_rd(A.sy0);
+    const float bx1 = __double2float_ru(A.sx1), by1 = __double2float_ru(A.sy1);
+    // rounding slack of the ring distances: 1e-5 (cs + max |box|), rounded up
+    const float slack_f = __fmul_ru(1.0001e-5f, __fadd_ru(A.gf.cs,
+        fmaxf(fmaxf(fabsf(bx0), fabsf(bx1)), fmaxf(fabsf(by0), fabsf(by1)))));
 
     for (;;) {
         int slot = 0;
@@ -301,8 +305,6 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
         // inside the cone), rounded up
         float clip;
         {
-            const float bx0 = __double2float_rd(A.sx0), by0 = __double2float_rd(A.sy0);
-            const float bx1 = __double2float_ru(A.sx1), by1 = __double2float_ru(A.sy1);
             clip = fmaxf(exit_dist(qf.x, qf.y, e1x, e1y, bx0, by0, bx1, by1),
                          exit_dist(qf.x, qf.y, e2x, e2y, bx0, by0, bx1, by1));
 #pragma unroll
@@ -567,8 +569,8 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
             if (rho_ring < 0) rho_ring = ring;          // every streamed facility is a half-plane
             if (rho_ring > rmaxf) rho = INFINITY;
             else {
-                const double Lr = (double)(rho_ring - 1) * (double)A.gf.cs - slack;
-                rho = Lr > 0.0 ? __double2float_rd(Lr) : 0.0f;
+                const float Lr = __fsub_rd(__fmul_rd((float)(rho_ring - 1), A.gf.cs), slack_f);
+                rho = Lr > 0.0f ? Lr : 0.0f;
             }
         }
         __syncwarp();
@@ -628,11 +630,14 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                 carry = __shfl_sync(FULL, v, 0);
             }
         }
-        const double Fp = (double)__fmul_ru(__fsqrt_ru(__fmul_ru(cmax, 1.0f + 1e-5f)), 1.0f + 1e-6f) + 1e-30;
-        k2f = (float)(8.0 * (double)kU32 * 2.0 * Fp * (1.0 + 1e-6));
-        kf2 = (float)(8.0 * (double)kU32 * Fp * Fp * (1.0 + 1e-6)) + 1e-30f;
-        k2f64 = 8.0 * kU64 * 2.0 * Fp * (1.0 + 1e-6);
-        kf264 = 8.0 * kU64 * Fp * Fp * (1.0 + 1e-6) + 1e-300;
+        // in float, rounded up (the constants carry a 2e-6 margin over their
+        // own rounding); an overflow to +inf only makes every test undecided
+        const float Fp = __fadd_ru(__fmul_ru(__fsqrt_ru(__fmul_ru(cmax, 1.0f + 1e-5f)), 1.0f + 1e-6f), 1e-30f);
+        const float Fp2 = __fmul_ru(Fp, Fp);
+        k2f = __fmul_ru(Fp, 16.0f * kU32 * (1.0f + 2e-6f));
+        kf2 = __fadd_ru(__fmul_ru(Fp2, 8.0f * kU32 * (1.0f + 2e-6f)), 1e-30f);
+        k2f64 = (double)__fmul_ru(Fp, 16.0f * (float)kU64 * (1.0f + 2e-6f));
+        kf264 = (double)__fmul_ru(Fp2, 8.0f * (float)kU64 * (1.0f + 2e-6f)) + 1e-300;
         }   // half-planes
 
         zs.cyc[7] += clock64() - tph;
