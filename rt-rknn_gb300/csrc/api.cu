@@ -88,7 +88,14 @@ struct CachedGraph {
 };
 
 constexpr int ZB_COUNTERS = 64;     // counter ints at the head of the zeroed block
+// most candidates the fused slice filter verifies itself (more go to the
+// verification kernel, which spreads a slot over the whole GPU)
+constexpr int FUSE_CAND = 4096;
 constexpr int ZB_VSTATS_INTS = 32;  // room for the statistics after them
+// counter ints: 1 verification work, 2 dropped, 3 listed survivors, 4-8 and
+// 10-14 bounds-check records, 16-31 slice filter work per k class, 36
+// slots the fused filter left over, 37 its blocks done, 40-41 the 64-bit
+// result-region total
 
 struct Workspace {
     int nq_cap = 0, lc = 0, seg_cap = 0;
@@ -103,6 +110,8 @@ struct Workspace {
     int2* d_segs = nullptr;
     ZStats* d_zst = nullptr;
     long long* d_cand_off = nullptr;   // result region of each slot (64-bit offsets)
+    int* d_reg_len = nullptr;          // and its length
+    int* d_deflist = nullptr;          // slots the fused filter leaves to the verification kernel
     int *d_chunk_off = nullptr, *d_res_count = nullptr, *d_out_off = nullptr;
     int rcap = 1 << 18;            // ids a slot's region holds at most (raised when exceeded)
     int* d_counters = nullptr;     // ZB_COUNTERS ints, then the statistics and the result counts:
@@ -152,6 +161,8 @@ struct rknn_index {
     int num_sms = 0;
     int recount_grid = 0;       // one wave of recount_kernel blocks
     bool pdl = true;            // programmatic dependent launch between the batch kernels
+    bool fuse = true;           // FP32 slice batches: the filter verifies its own slots
+                                // (RKNN_FUSE=0 in the environment turns it off)
     // occupancy answers by (kernel, threads, dynamic shared memory): a batch's
     // plan asks the same few questions on every call
     std::mutex occ_mu;
@@ -214,7 +225,8 @@ void free_ws(Workspace& w)
     cudaFree(w.d_qko);
     cudaFree(w.d_qd); cudaFree(w.d_planes); cudaFree(w.d_bispos); cudaFree(w.d_segs); cudaFree(w.d_zst);
     cudaFree(w.d_slice_r);
-    cudaFree(w.d_cand_off); cudaFree(w.d_chunk_off); cudaFree(w.d_out_off);
+    cudaFree(w.d_cand_off); cudaFree(w.d_reg_len); cudaFree(w.d_deflist); cudaFree(w.d_chunk_off);
+    cudaFree(w.d_out_off);
     cudaFree(w.d_counters);     // with the statistics and result counts
     cudaFree(w.d_pool); cudaFree(w.d_out); cudaFree(w.d_zscratch); cudaFree(w.d_surv);
     cudaFreeHost(w.h_qko); cudaFreeHost(w.h_off);
@@ -294,17 +306,23 @@ int slice_kr(int kmax)
     return kmax <= 4 ? 4 : kmax <= 8 ? 8 : kmax <= 12 ? 12 : kmax <= 16 ? 16 : kmax <= 24 ? 24 : kmax <= 32 ? 32 : 0;
 }
 
-ZoneLaunch zone_launch(rknn_index* ix, const ZoneCaps& c, int nq, bool slice = false, int kmax = 0)
+// fuse_sc, fuse_ss > 0: the slice filter keeps that many half-planes and
+// segments in shared memory for the fused verification.
+ZoneLaunch zone_launch(rknn_index* ix, const ZoneCaps& c, int nq, bool slice = false, int kmax = 0,
+                       int fuse_sc = 0, int fuse_ss = 0)
 {
     ZoneLaunch L;
     L.slice = slice ? slice_layout(c).bytes : zone_layout(c).bytes;
     L.smem = L.slice * ZONE_WARPS;
+    const bool fuse = slice && fuse_sc > 0;
+    if (fuse) L.smem = fuse_layout(slice_own_bytes(L.slice, 1, 0), fuse_sc, fuse_ss).bytes;
     const int kr = slice ? slice_kr(kmax) : 0;
     if (kr > 0) {
         // two warps per query (shorter chains) when every query of the class
         // keeps a block resident; one warp each otherwise (more queries in
         // flight)
-        const size_t smem2 = 2 * L.slice + (size_t)2 * kr * 32 * sizeof(float) + 64;
+        size_t smem2 = slice_own_bytes(L.slice, 2, kr);
+        if (fuse) smem2 = fuse_layout(smem2, fuse_sc, fuse_ss).bytes;
         const int per2 = occupancy(ix, (const void*)slice_fn(kmax, true), 64, smem2);
         if ((long long)nq <= (long long)per2 * ix->num_sms) {
             L.smem = smem2;
@@ -356,7 +374,8 @@ rknn_status ensure_ws(Workspace& w, int nq, const ZoneCaps& caps, long long pool
         CK(dalloc(w.d_bispos, (size_t)nqc * lc));
         CK(dalloc(w.d_segs, (size_t)nqc * sc));
         CK(dalloc(w.d_zst, nqc));
-        CK(dalloc(w.d_cand_off, nqc + 1)); CK(dalloc(w.d_chunk_off, nqc + 1));
+        CK(dalloc(w.d_cand_off, nqc + 1)); CK(dalloc(w.d_reg_len, nqc + 1)); CK(dalloc(w.d_chunk_off, nqc + 1));
+        CK(dalloc(w.d_deflist, nqc));
         // counters, statistics and per-slot result counts in one block, so
         // that one memset clears them before each batch
         static_assert(sizeof(VStats) <= ZB_VSTATS_INTS * sizeof(int), "VStats outgrew its room");
@@ -457,6 +476,7 @@ struct BatchPlan {
     int stage_cap = 0;          // half-planes the verification stages per warp
     int seg_stage = 0;          // user segments it stages per warp
     int vupt = VERIFY_UPT, vwarps = VERIFY_WARPS;
+    bool fuse = false;          // the slice filter verifies its own slots (FP32, every class a slice class)
     size_t vsmem = 0;
     int vgrid = 0;
     GraphKey key;
@@ -490,7 +510,6 @@ BatchPlan plan_batch(rknn_index* ix, int nq, int mode, bool use_order, const int
     for (auto& c : b.cls) {
         c.slice = use_slice(ix, c.kmax);
         c.caps = c.slice ? slice_caps(c.kmax, std::min(512, stage_max)) : caps_fit(ix, caps_for(c.kmax));
-        c.zl = zone_launch(ix, c.caps, c.n, c.slice, c.kmax);
         b.pstride = std::max(b.pstride, c.caps.lc);
         b.key.push_back(c.n);
         b.key.push_back(c.kmax);
@@ -505,6 +524,21 @@ BatchPlan plan_batch(rknn_index* ix, int nq, int mode, bool use_order, const int
     int rm = 0;
     for (auto& c : b.cls) rm = std::max(rm, c.caps.rm);
     b.seg_stage = std::min(2 * rm + 2, 512);
+    // Fused verification for FP32 batches whose every class runs the slice
+    // filter two warps a query (batches that fit resident): there it takes
+    // the verification kernel's latency off each query's path.  Larger
+    // batches keep the separate verification, whose wider blocks hide the
+    // half-plane loop's latency better than one-warp filter blocks.
+    b.fuse = ix->fuse && mode == MODE_FP32;
+    for (auto& c : b.cls) b.fuse = b.fuse && c.slice;
+    if (b.fuse)
+        for (auto& c : b.cls) {
+            c.zl = zone_launch(ix, c.caps, c.n, c.slice, c.kmax, b.stage_cap, b.seg_stage);
+            b.fuse = b.fuse && c.zl.threads == 64;
+        }
+    if (!b.fuse)
+        for (auto& c : b.cls) c.zl = zone_launch(ix, c.caps, c.n, c.slice, c.kmax);
+    b.key.push_back(b.fuse ? 1 : 0);
     b.vsmem = (size_t)b.vwarps * ((size_t)b.stage_cap * bpp + (size_t)b.seg_stage * sizeof(int2) + 32 * sizeof(float));
     const int vper = occupancy(ix, (const void*)verify_fn(b.vupt), b.vwarps * 32, b.vsmem);
     b.vgrid = vper * ix->num_sms;
@@ -544,6 +578,9 @@ cudaError_t launch_k(void (*k)(Exp...), dim3 grid, dim3 block, size_t smem, cuda
 // Enqueue the batch's kernels (no synchronization, no non-stream CUDA calls:
 // this runs under stream capture).  k classes after the first run on side
 // streams, forked from and joined back to the context's stream.
+// the 64-bit total of the batch's result regions (zeroed with the counters)
+inline long long* region_top(Workspace& w) { return (long long*)(w.d_counters + 40); }
+
 rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = false, bool chain = false)
 {
     Workspace& w = c.w;
@@ -556,7 +593,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     ZoneArgs za;
     za.fxy = ix->d_fxy; za.fstart = ix->d_fstart; za.fmbr = ix->d_fmbr; za.fpos = ix->d_fpos;
     za.gf = ix->gf; za.nf = (int)ix->nf;
-    za.ustart = ix->d_ustart; za.gu = ix->gu; za.nu = (int)ix->nu;
+    za.ustart = ix->d_ustart; za.uxy = ix->d_uxy; za.uid = ix->d_uid; za.gu = ix->gu; za.nu = (int)ix->nu;
     za.sx0 = ix->sx0; za.sy0 = ix->sy0; za.sx1 = ix->sx1; za.sy1 = ix->sy1;
     const int* qin = c.io.q ? c.io.q : w.d_qko;
     const int* kin = c.io.q ? c.io.k : w.d_qko + nq;
@@ -567,7 +604,42 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     za.qd = w.d_qd; za.planes = w.d_planes; za.bis_pos = w.d_bispos; za.segs = w.d_segs; za.zst = w.d_zst;
     za.slice_r = w.d_slice_r;
     za.pstride = b.pstride;
+    VerifyArgs va;
+    va.qd = w.d_qd; va.planes = w.d_planes; va.bis_pos = w.d_bispos; va.lc = b.pstride;
+    va.slice_r = w.d_slice_r;
+    va.stage_cap = b.stage_cap;
+    va.segs = w.d_segs; va.seg_cap = w.seg_cap; va.seg_stage = b.seg_stage;
+    va.chunk_off = w.d_chunk_off; va.cand_off = w.d_cand_off; va.reg_len = w.d_reg_len; va.nq = nq;
+    va.uxy = ix->d_uxy; va.uid = ix->d_uid; va.fxy = ix->d_fxy; va.fstart = ix->d_fstart; va.gf = ix->gf;
+    va.res_count = w.d_res_count; va.res_pool = w.d_pool; va.work_counter = w.d_counters + 1;
+    va.vstats = w.d_vstats; va.mode = b.mode;
+    va.nu = (int)ix->nu; va.nf = (int)ix->nf; va.ncf = ix->gf.gx * ix->gf.gy;
+    va.pool_cap = w.pool_cap; va.fault = w.d_counters + 10; va.dropped = w.d_counters + 2;
+    va.surv = w.d_surv; va.surv_cap = (int)std::min<long long>(w.surv_cap, INT32_MAX); va.surv_count = w.d_counters + 3;
+    va.region_top = region_top(w);
+    if (b.fuse) {
+        // the verification takes only the slots the filter left over
+        va.deflist = w.d_deflist;
+        va.ndef = w.d_counters + 36;
+    }
     za.fault = w.d_counters + 4;
+    if (b.fuse) {
+        za.fuse = 1;
+        za.fuse_cand = FUSE_CAND;
+        za.fuse_sc = b.stage_cap;
+        za.fuse_ss = b.seg_stage;
+        za.rcap = w.rcap;
+        za.cand_off_w = w.d_cand_off;
+        za.reg_len_w = w.d_reg_len;
+        za.deflist = w.d_deflist;
+        za.ndef = w.d_counters + 36;
+        za.chunk_off_w = w.d_chunk_off;
+        za.vchunk = 32 * b.vupt;
+        za.done_total = 0;
+        for (const ZClass& z : b.cls) za.done_total += z.zl.grid;
+        za.v = va;
+        za.v.done = w.d_counters + 37;
+    }
     mark(0);
     const int ncls = (int)b.cls.size();
     if (ncls > 1) {
@@ -599,34 +671,24 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     // cross-stream join, nor in serving, where blocks waiting early would
     // hold resources that other slots' kernels need)
     const bool pdl = chain && !events && ix->pdl;
-    CK(launch_k(plan_kernel, 1, 1024, 0, st, pdl && ncls == 1, w.d_qd, nq, w.d_cand_off, w.d_chunk_off, w.pool_cap,
-                w.rcap, 32 * b.vupt));
+    // fused batches: the filter's last block planned the left-over slots,
+    // and the verification takes only those
+    if (!b.fuse)
+        CK(launch_k(plan_kernel, 1, 1024, 0, st, pdl && ncls == 1, w.d_qd, nq, w.d_cand_off, w.d_reg_len,
+                    region_top(w), w.d_chunk_off, w.pool_cap, w.rcap, 32 * b.vupt));
     mark(2);
-
-    VerifyArgs va;
-    va.qd = w.d_qd; va.planes = w.d_planes; va.bis_pos = w.d_bispos; va.lc = b.pstride;
-    va.slice_r = w.d_slice_r;
-    va.stage_cap = b.stage_cap;
-    va.segs = w.d_segs; va.seg_cap = w.seg_cap; va.seg_stage = b.seg_stage;
-    va.chunk_off = w.d_chunk_off; va.cand_off = w.d_cand_off; va.nq = nq;
-    va.uxy = ix->d_uxy; va.uid = ix->d_uid; va.fxy = ix->d_fxy; va.fstart = ix->d_fstart; va.gf = ix->gf;
-    va.res_count = w.d_res_count; va.res_pool = w.d_pool; va.work_counter = w.d_counters + 1;
-    va.vstats = w.d_vstats; va.mode = b.mode;
-    va.nu = (int)ix->nu; va.nf = (int)ix->nf; va.ncf = ix->gf.gx * ix->gf.gy;
-    va.pool_cap = w.pool_cap; va.fault = w.d_counters + 10; va.dropped = w.d_counters + 2;
-    va.surv = w.d_surv; va.surv_cap = (int)std::min<long long>(w.surv_cap, INT32_MAX); va.surv_count = w.d_counters + 3;
-    CK(launch_k(verify_fn(b.vupt), b.vgrid, b.vwarps * 32, b.vsmem, st, pdl, va));
+    CK(launch_k(verify_fn(b.vupt), b.vgrid, b.vwarps * 32, b.vsmem, st, pdl && (ncls == 1 || !b.fuse), va));
     mark(3);
     CK(launch_k(recount_kernel, ix->recount_grid, 256, 0, st, pdl, va));
     mark(4);
-
-    CK(launch_k(scan_counts_kernel, 1, 1024, 0, st, pdl, (const int*)w.d_res_count, (const long long*)w.d_cand_off,
-                nq, w.d_out_off, (const int*)w.d_counters, c.io.off_host));
+    CK(launch_k(scan_counts_kernel, 1, 1024, 0, st, pdl, (const int*)w.d_res_count, (const int*)w.d_reg_len,
+                (const long long*)region_top(w), nq, w.d_out_off, (const int*)w.d_counters, c.io.off_host));
     mark(5);
     int* ids = c.io.ids ? c.io.ids : w.d_out;
     const long long ids_cap = c.io.ids ? c.io.ids_cap : w.pool_cap;
     CK(launch_k(finalize_kernel, (nq + FIN_WARPS - 1) / FIN_WARPS, 32 * FIN_WARPS, 0, st, pdl, w.d_pool,
-                (const long long*)w.d_cand_off, (const int*)w.d_res_count, (const int*)w.d_out_off, ids, nq, ids_cap));
+                (const long long*)w.d_cand_off, (const int*)w.d_reg_len, (const int*)w.d_res_count,
+                (const int*)w.d_out_off, ids, nq, ids_cap));
     mark(6);
     return RKNN_OK;
 }
@@ -927,6 +989,7 @@ rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf, 
     if (o.filter < RKNN_FILTER_AUTO || o.filter > RKNN_FILTER_SLICE) return bail(fail(RKNN_ERR_ARG, "bad filter"));
     ix->filter = o.filter;
     ix->slice_min_k = o.slice_min_k > 0 ? o.slice_min_k : 1;
+    if (const char* f = std::getenv("RKNN_FUSE")) ix->fuse = std::strcmp(f, "0") != 0;
     ix->nf = nf;
     ix->nu = nu;
     ix->sx0 = x0; ix->sy0 = y0; ix->sx1 = x1; ix->sy1 = y1;
@@ -1356,8 +1419,8 @@ std::mutex g_noalloc_mu;
 unsigned char* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
 
 struct NoallocLayout {
-    int *counters, *q, *k, *chunk_off, *res_count, *out_off, *bispos, *pool, *out;
-    long long* cand_off;
+    int *counters, *q, *k, *chunk_off, *res_count, *out_off, *bispos, *pool, *out, *reg_len;
+    long long *cand_off, *region_top;
     QDesc* qd;
     ZStats* zst;
     float4* planes;
@@ -1377,6 +1440,8 @@ NoallocLayout noalloc_layout(unsigned char* base, int lc, int seg_cap)
     L.q = (int*)take(sizeof(int));
     L.k = (int*)take(sizeof(int));
     L.cand_off = (long long*)take(sizeof(long long) * 2);
+    L.region_top = (long long*)take(sizeof(long long));
+    L.reg_len = (int*)take(sizeof(int));
     L.chunk_off = (int*)take(sizeof(int) * 2);
     L.res_count = (int*)take(sizeof(int));
     L.out_off = (int*)take(sizeof(int) * (2 + OFF_TAIL));
@@ -1433,7 +1498,7 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     ZoneArgs za;
     za.fxy = ix->d_fxy; za.fstart = ix->d_fstart; za.fmbr = ix->d_fmbr; za.fpos = ix->d_fpos;
     za.gf = ix->gf; za.nf = (int)ix->nf;
-    za.ustart = ix->d_ustart; za.gu = ix->gu; za.nu = (int)ix->nu;
+    za.ustart = ix->d_ustart; za.uxy = ix->d_uxy; za.uid = ix->d_uid; za.gu = ix->gu; za.nu = (int)ix->nu;
     za.sx0 = ix->sx0; za.sy0 = ix->sy0; za.sx1 = ix->sx1; za.sy1 = ix->sy1;
     za.q_in = L.q; za.k_in = L.k; za.order = nullptr; za.nq = 1;
     za.work_counter = L.counters + 0;
@@ -1448,7 +1513,7 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     const size_t zsmem = zone_layout(caps).bytes * ZONE_WARPS;
     zone_kernel_smem<<<1, 32 * ZONE_WARPS, zsmem, st>>>(za);
     CK(cudaGetLastError());
-    plan_kernel<<<1, 1024, 0, st>>>(L.qd, 1, L.cand_off, L.chunk_off, L.pool_cap,
+    plan_kernel<<<1, 1024, 0, st>>>(L.qd, 1, L.cand_off, L.reg_len, L.region_top, L.chunk_off, L.pool_cap,
                                     (int)std::min<long long>(L.pool_cap, INT32_MAX), VERIFY_CHUNK);
     CK(cudaGetLastError());
 
@@ -1457,7 +1522,7 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     va.slice_r = nullptr;
     va.stage_cap = caps.lc;
     va.segs = L.segs; va.seg_cap = seg_cap;
-    va.chunk_off = L.chunk_off; va.cand_off = L.cand_off; va.nq = 1;
+    va.chunk_off = L.chunk_off; va.cand_off = L.cand_off; va.reg_len = L.reg_len; va.nq = 1;
     va.uxy = ix->d_uxy; va.uid = ix->d_uid; va.fxy = ix->d_fxy; va.fstart = ix->d_fstart; va.gf = ix->gf;
     va.res_count = L.res_count; va.res_pool = L.pool; va.work_counter = L.counters + 1;
     va.vstats = L.vstats; va.mode = mode;
@@ -1467,9 +1532,10 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     const size_t vsmem = (size_t)VERIFY_WARPS * ((size_t)caps.lc * 32 + 32 * sizeof(float));
     verify_kernel<<<2 * ix->num_sms, VERIFY_WARPS * 32, vsmem, st>>>(va);
     CK(cudaGetLastError());
-    scan_counts_kernel<<<1, 1024, 0, st>>>(L.res_count, L.cand_off, 1, L.out_off, L.counters, nullptr);
+    scan_counts_kernel<<<1, 1024, 0, st>>>(L.res_count, L.reg_len, L.region_top, 1, L.out_off, L.counters, nullptr);
     CK(cudaGetLastError());
-    finalize_kernel<<<1, 32 * FIN_WARPS, 0, st>>>(L.pool, L.cand_off, L.res_count, L.out_off, L.out, 1, L.pool_cap);
+    finalize_kernel<<<1, 32 * FIN_WARPS, 0, st>>>(L.pool, L.cand_off, L.reg_len, L.res_count, L.out_off, L.out, 1,
+                                                  L.pool_cap);
     CK(cudaGetLastError());
 
     QDesc d;

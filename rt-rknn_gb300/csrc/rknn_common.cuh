@@ -19,6 +19,26 @@ struct Grid {
     int gx, gy;        // cells per axis
 };
 
+// Bring the line holding p into this SM's L1 (no register, no wait).
+__device__ __forceinline__ void prefetch_l1(const void* p)
+{
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
+// Hint: bring bytes [off, off + bytes) of the array at base (base_bytes
+// long) into L2, one bulk prefetch.  The span is widened to 16-byte
+// boundaries and clipped to the array's 16-byte-aligned interior, as the
+// instruction requires; it does not wait and writes nothing.
+__device__ __forceinline__ void prefetch_l2_span(const void* base, size_t base_bytes, size_t off, size_t bytes)
+{
+    const unsigned long long b = (unsigned long long)base;
+    const unsigned long long lo = (b + 15) & ~15ull, hi = (b + base_bytes) & ~15ull;
+    const unsigned long long a0 = max((b + off) & ~15ull, lo);
+    const unsigned long long a1 = min((b + off + bytes + 15) & ~15ull, hi);
+    if (a1 > a0)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a0), "r"((unsigned)(a1 - a0)) : "memory");
+}
+
 // Programmatic dependent launch.  A kernel launched with programmatic stream
 // serialization may start while its predecessor in the stream still runs:
 // pdl_wait() blocks until that grid has completed and its memory operations

@@ -32,6 +32,7 @@
 // of pruned cells closes it).
 #include "rknn_common.cuh"
 #include "zone.cuh"
+#include "verify_item.cuh"
 #include <cfloat>
 
 namespace rknn {
@@ -142,11 +143,6 @@ __device__ __forceinline__ void ring_cell(int ring, int ri, int qcx, int qcy, in
     }
 }
 
-__device__ __forceinline__ void prefetch_l1(const void* p)
-{
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-
 // Max-heap of one slice, interleaved across lanes: entry i of lane l at
 // H[i * 32 + l] (all lanes touching the same level hit distinct banks).
 __device__ __forceinline__ void heap_insert(float* H, int lane, int& n, int cap, float v)
@@ -194,6 +190,51 @@ __device__ __forceinline__ void list_insert(float (&L)[KR], float v)
     L[0] = fminf(L[0], v);
 }
 
+constexpr int FUSE_UPT = 4;     // users per lane per item of the fused verification
+
+// Fused verification, thread 0: claim slot s's result region (min(ncand,
+// rcap) ids at the pool's running top) and decide where the slot is
+// verified: by this block (here), or by the verification kernel (listed).
+// A region past the pool's end is flagged and not verified; the host grows
+// the pool and runs the batch again.  The record and the region go to
+// shared memory for the block.
+__device__ __forceinline__ void fuse_claim(const ZoneArgs& A, int s, QDesc& d, char* smem, const FuseLayout& FL,
+                                           bool may_here)
+{
+    const int rl = min(d.ncand, A.rcap);
+    const long long r0 = (long long)atomicAdd((unsigned long long*)A.v.region_top, (unsigned long long)rl);
+    const bool fits = r0 + rl <= A.v.pool_cap;
+    A.cand_off_w[s] = r0;
+    A.reg_len_w[s] = rl;
+    if (!fits) d.flags |= QF_RESULT_OVERFLOW;
+    const bool verify = fits && d.ncand > 0 && !(d.flags & QF_BAD_QUERY);
+    const bool here = verify && may_here && d.ncand <= A.fuse_cand;
+    if (verify && !here) A.deflist[atomicAdd(A.ndef, 1)] = s;
+    *(QDesc*)(smem + FL.d) = d;
+    *(long long*)(smem + FL.r0) = r0;
+    *(int*)(smem + FL.rlen) = rl;
+    *(int*)(smem + FL.here) = here ? 1 : 0;
+}
+
+// Fused verification, every warp of the block: the slot's candidates in
+// items of 32 * FUSE_UPT users, the block's warps taking alternate items,
+// against the half-planes and segments the filter left in shared memory.
+template <int NWQ>
+__device__ __forceinline__ void fuse_verify(const ZoneArgs& A, int s, const char* smem, const FuseLayout& FL,
+                                            const float* Rs, vitem::VCount& vc)
+{
+    if (!*(const int*)(smem + FL.here)) return;
+    const QDesc d = *(const QDesc*)(smem + FL.d);
+    const long long r0 = *(const long long*)(smem + FL.r0);
+    const int rl = *(const int*)(smem + FL.rlen);
+    const int2* sg = d.nseg + 1 <= A.fuse_ss ? (const int2*)(smem + FL.segs) : A.segs + (size_t)s * A.seg_cap;
+    const int nbs = min(d.nb, A.fuse_sc);
+    const int wq = NWQ == 2 ? (int)(threadIdx.x >> 5) : 0;
+    constexpr int CH = 32 * FUSE_UPT;
+    for (int v0 = wq * CH; v0 < d.ncand; v0 += NWQ * CH)
+        vitem::verify_item<FUSE_UPT>(A.v, d, s, v0, smem + FL.planes, sg, Rs, nbs, r0, rl, vc);
+}
+
 }  // namespace
 
 // KR > 0: the slice bounds live in a register list (k <= KR); KR == 0: in a
@@ -230,6 +271,15 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
     // between the warps
     float* xl = (float*)(smem + (size_t)NWQ * LY.bytes);
     int* xs = (int*)(xl + (NWQ == 2 ? 2 * KR * 32 : 0));
+    // fused verification: the slot's record, region, half-planes and
+    // segments after the filter's own shared memory
+    const FuseLayout FL = fuse_layout(slice_own_bytes(LY.bytes, NWQ, KR), A.fuse_sc, A.fuse_ss);
+    float4* fzp = (float4*)(smem + FL.planes);
+    int2* fzs = (int2*)(smem + FL.segs);
+    vitem::VCount vc = {};
+    // the host fuses only batches that run two warps a query; the one-warp
+    // variants keep their registers for more queries in flight
+    const bool FUSED = NWQ == 2 && A.fuse;
     const int KC = A.caps.vc, LC = A.caps.lc;
     const long long NCF = (long long)A.gf.gx * A.gf.gy, NCU = (long long)A.gu.gx * A.gu.gy;
     (void)NCF; (void)NCU;
@@ -267,6 +317,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                 d.qpos = -1;
                 d.k = k;
                 d.flags = QF_BAD_QUERY;
+                if (FUSED) fuse_claim(A, s, d, smem, FL, false);
                 *qd = d;
                 A.zst[s] = zs;
                 A.segs[(size_t)s * A.seg_cap] = make_int2(0, 0);
@@ -290,6 +341,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                 d.kf264 = 1e-300;
                 d.ncand = A.nu;
                 d.flags = QF_ALL_USERS;
+                if (FUSED) fuse_claim(A, s, d, smem, FL, false);
                 *qd = d;
                 A.zst[s] = zs;
                 int2* seg = A.segs + (size_t)s * A.seg_cap;
@@ -603,6 +655,10 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
             const float dx = f.x - qf.x, dy = f.y - qf.y;
             const float c = fmaf(dx, dx, dy * dy);
             planes[SX(m, A.pstride, 318)] = make_float4(-2.0f * dx, -2.0f * dy, c, 0.0f);
+            if (FUSED && m < A.fuse_sc) {
+                fzp[2 * m] = make_float4(-2.0f * dx, -2.0f * dx, -2.0f * dy, -2.0f * dy);
+                fzp[2 * m + 1] = make_float4(c, c, 0.0f, 0.0f);
+            }
             A.bis_pos[(size_t)s * A.pstride + SX(m, A.pstride, 319)] = pos;
             cmax = fmaxf(cmax, c);
             // the slot is free now: |f - q|^2 rounded well down
@@ -627,6 +683,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                 }
                 v = fminf(v, carry);
                 if (m < nL) planes[SX(m, A.pstride, 318)].w = v;
+                if (FUSED && m < nL && m < A.fuse_sc) ((float2*)(fzp + 2 * m + 1))[1] = make_float2(v, v);
                 carry = __shfl_sync(FULL, v, 0);
             }
         }
@@ -712,9 +769,14 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
 
         // ---- segments: one user range per row ------------------------------
         int2* seg = A.segs + (size_t)s * A.seg_cap;
+        // segment i, also kept in shared memory for the fused verification
+        auto put_seg = [&](int i, int2 v) {
+            seg[i] = v;
+            if (FUSED && i < A.fuse_ss) fzs[i] = v;
+        };
         if (all_users) {
-            seg[0] = make_int2(0, 0);
-            seg[1] = make_int2(0, A.nu);
+            put_seg(0, make_int2(0, 0));
+            put_seg(1, make_int2(0, A.nu));
             nseg = 1;
             ncand = A.nu;
             qflags |= QF_ALL_USERS;
@@ -749,13 +811,20 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                     if (lane >= o) incl += v;
                 }
                 const int excl = incl - (has ? len : 0);
-                if (has) seg[SX(nseg + pre, A.seg_cap, 325)] = make_int2(st, ncand + excl);
+                if (has) {
+                    put_seg(SX(nseg + pre, A.seg_cap, 325), make_int2(st, ncand + excl));
+                    // the verification reads these users next: start their
+                    // coordinates and ids on the way to L2 (at most 64 KB a row)
+                    const size_t n = (size_t)min(len, 8192);
+                    prefetch_l2_span(A.uxy, sizeof(float2) * (size_t)A.nu, sizeof(float2) * (size_t)st, sizeof(float2) * n);
+                    prefetch_l2_span(A.uid, sizeof(int) * (size_t)A.nu, sizeof(int) * (size_t)st, sizeof(int) * n);
+                }
                 nseg += __popc(m);
                 ncand += __shfl_sync(FULL, incl, 31);
             }
-            if (lane == 0) seg[SX(nseg, A.seg_cap, 326)] = make_int2(0, ncand);
+            if (lane == 0) put_seg(SX(nseg, A.seg_cap, 326), make_int2(0, ncand));
         } else if (lane == 0) {
-            seg[0] = make_int2(0, 0);
+            put_seg(0, make_int2(0, 0));
         }
         }   // ring scan and segments
         zs.cyc[7] += clock64() - tph;
@@ -790,10 +859,24 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
             d.flags = qflags;
             d.rho = rho;
             d.pad = 0;
+            if (FUSED) fuse_claim(A, s, d, smem, FL, true);
             *qd = d;
             A.zst[s] = zs;
         }
+        if (FUSED) {
+            if constexpr (NWQ == 2) __syncthreads(); else __syncwarp();
+            fuse_verify<NWQ>(A, s, smem, FL, Rs, vc);
+        }
         __syncwarp();
+    }
+    if (FUSED) {
+        vc.flush(A.v.vstats);
+        // the batch's last filter block: the work items of the slots left
+        // over (the lists' room and a shared int serve as scratch)
+        if (vitem::last_block(A.v.done, A.done_total, xs + 15)) {
+            const int n = __ldcg(A.ndef);
+            if (n > 0) vitem::plan_deferred_block(A.v, n, A.vchunk, A.chunk_off_w, (int*)xl);
+        }
     }
 }
 

@@ -26,7 +26,8 @@ struct VerifyArgs {
     int seg_stage = 0;       // user segments staged per warp beside the half-planes
                              // (a slot with more reads them from global memory)
     const int* chunk_off;    // [nq+1]
-    const long long* cand_off;   // [nq+1] result region of each slot
+    const long long* cand_off;   // [nq] start of each slot's result region in res_pool
+    const int* reg_len;          // [nq] its length (ids the slot stores at most)
     int nq;
     const float2* uxy;       // cell-sorted users
     const int* uid;          // their ids
@@ -46,6 +47,12 @@ struct VerifyArgs {
     int surv_cap;            // 0: no list (the verification kernel recounts in-warp)
     int* surv_count;
     int* fault;              // checked builds: {flag, array id, index, size, line}
+    // slots to verify: chunk_off indexes deflist[0 .. *ndef) when deflist is
+    // set (the fused slice filter verified the others), else slots 0 .. nq
+    const int* deflist = nullptr;
+    const int* ndef = nullptr;
+    long long* region_top = nullptr;   // total of the result regions (fused claims)
+    int* done = nullptr;               // fused filter: its blocks finished
 };
 
 __global__ void verify_kernel(VerifyArgs a);        // 4 users per lane per work item
@@ -55,27 +62,27 @@ __global__ void verify_kernel_u8(VerifyArgs a);     // 8
 // exact recount of the listed survivors, one thread each
 __global__ void recount_kernel(VerifyArgs a);
 
-// single block: result regions (min(candidates, rcap) ids, 64-bit offsets)
-// and work-item offsets from QDesc.ncand; flags slots whose region does not
-// fit the pool
-__global__ void plan_kernel(QDesc* qd, int nq, long long* cand_off, int* chunk_off, long long pool_cap,
-                            int rcap, int chunk);
+// single block: result regions (min(candidates, rcap) ids at 64-bit offsets,
+// their lengths and *region_top = their total) and work-item offsets from
+// QDesc.ncand; flags slots whose region does not fit the pool
+__global__ void plan_kernel(QDesc* qd, int nq, long long* cand_off, int* reg_len, long long* region_top,
+                            int* chunk_off, long long pool_cap, int rcap, int chunk);
 
 // single block: exclusive scan of the stored result counts into out_off
 // out_off: nq+1 offsets, then OFF_TAIL ints: the region total (low and high
-// halves of cand_off[nq]), the dropped flag and the listed survivors
+// halves of *region_top), the dropped flag and the listed survivors
 // (counters[2], counters[3]), so that one copy brings back all of them.
 constexpr int OFF_TAIL = 4;
 // out_off_host (or null): device-accessible host memory that receives a
 // copy of the same nq+1+OFF_TAIL ints.
-__global__ void scan_counts_kernel(const int* res_count, const long long* cand_off, int nq, int* out_off,
-                                   const int* counters, int* out_off_host);
+__global__ void scan_counts_kernel(const int* res_count, const int* reg_len, const long long* region_top, int nq,
+                                   int* out_off, const int* counters, int* out_off_host);
 
 // one block per slot: sort the slot's results into out[out_off[s] ...]
 // out may be device-accessible host memory of out_cap ids: a slot whose range
 // would pass out_cap is left out (the caller sees the total and fails the
 // batch).
-__global__ void finalize_kernel(int* res_pool, const long long* cand_off, const int* res_count,
+__global__ void finalize_kernel(int* res_pool, const long long* cand_off, const int* reg_len, const int* res_count,
                                 const int* out_off, int* out, int nq, long long out_cap);
 
 }  // namespace rknn

@@ -1,6 +1,7 @@
 // Influence-zone kernel interface: capacities, per-warp state layout, args.
 #pragma once
 #include "rknn_common.cuh"
+#include "verify.cuh"
 
 namespace rknn {
 
@@ -101,6 +102,8 @@ struct ZoneArgs {
     int nf;
     // user index
     const int* ustart;       // user cell starts (gu.gx*gu.gy+1)
+    const float2* uxy;       // cell-sorted user coordinates and ids (the slice
+    const int* uid;          // filter prefetches each candidate range into L2)
     Grid gu;
     int nu;
     double sx0, sy0, sx1, sy1;   // bounding box of all points (the zone's space)
@@ -123,7 +126,53 @@ struct ZoneArgs {
     int2* segs;              // [slot][seg_cap]: (user start, candidate offset)
     ZStats* zst;
     int* fault;              // checked builds: {flag, array id, index, capacity, line}
+    // Fused verification (slice filter, FP32 batches): the block claims each
+    // slot's result region itself and verifies the slot's users when there
+    // are at most fuse_cand of them; larger slots are listed for the
+    // verification kernel.
+    int fuse = 0;
+    int fuse_cand = 0;       // most candidates a block verifies itself
+    int fuse_sc = 0;         // half-planes kept in shared memory
+    int fuse_ss = 0;         // segments kept in shared memory
+    int rcap = 0;            // most ids a slot's region holds
+    long long* cand_off_w = nullptr;   // [slot] region start (written here)
+    int* reg_len_w = nullptr;          // [slot] region length
+    int* deflist = nullptr;            // slots left to the verification kernel
+    int* ndef = nullptr;               // their count
+    int* chunk_off_w = nullptr;        // their work-item offsets (items of vchunk users)
+    int vchunk = 0;
+    int done_total = 0;                // blocks of all the batch's filter launches (v.done counts them)
+    VerifyArgs v;            // the verification's arguments
 };
+
+// Fused verification state after the slice filter's own shared memory:
+// the slot's descriptor, region, verify-here flag, then fuse_sc half-planes
+// of 32 bytes ((a, a, b, b), (c, c, w, w)) and fuse_ss segments.
+struct FuseLayout {
+    size_t d, r0, rlen, here, planes, segs, bytes;
+};
+
+__host__ __device__ inline FuseLayout fuse_layout(size_t base, int sc, int ss)
+{
+    FuseLayout L;
+    size_t o = zl_align(base);
+    L.d = o;      o += sizeof(QDesc);
+    L.r0 = o;     o += 8;
+    L.rlen = o;   o += 4;
+    L.here = o;   o += 4;
+    o = zl_align(o);
+    L.planes = o; o += 32 * (size_t)sc;
+    L.segs = o;   o += 8 * (size_t)ss;
+    L.bytes = zl_align(o);
+    return L;
+}
+
+// Start of the slice kernel's shared memory after its own state: NWQ warps'
+// regions, then (two warps) both warps' lists and 64 bytes of shared ints.
+__host__ __device__ inline size_t slice_own_bytes(size_t warp_bytes, int nwq, int kr)
+{
+    return (size_t)nwq * warp_bytes + (nwq == 2 ? (size_t)2 * kr * 32 * sizeof(float) + 64 : 0);
+}
 
 // zone state in shared memory, one warp (one query at a time) per block
 __global__ void zone_kernel_smem(ZoneArgs a);
