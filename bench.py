@@ -5,9 +5,11 @@
 Workload (the reference's headline configuration): 100,000 facilities and
 1,000,000 users, float32 uniform in [0,1000]^2 (seeded synthetic data), k=10.
 One step = one batch of 1,000 random facility queries through the engine:
-candidate filter (angular slices, the default) -> plan -> verification ->
-result offsets -> finalize (one CUDA graph), FP32-filtered predicates with
-exact fallback; result sets are bit-exact.  Prints one JSON line (rank 0).
+angular-slice filter, which at this batch size also verifies each query's
+users itself (fused) -> verification of left-over queries -> exact recount
+of the survivors -> result offsets -> finalize (one CUDA graph),
+FP32-filtered predicates with exact fallback; result sets are bit-exact.
+Prints one JSON line (rank 0).
 
   value      queries/s with the facility/user index and the query batch
              resident in HBM, device time from CUDA events on the engine's
@@ -16,9 +18,10 @@ exact fallback; result sets are bit-exact.  Prints one JSON line (rank 0).
              buffers; ids land in a page-locked buffer): query ids H2D,
              result offsets and ids D2H, per step, L2 flushed (untimed)
              before every step
-  roofline   the dominant kernel (of the filter and the verification),
-             timed live per launch with CUDA events in profiling mode;
-             roofline_other: the same for the other one;
+  roofline   the dominant kernel (the filter with its fused verification),
+             timed live per launch with CUDA events in profiling mode,
+             against HBM and against peak instruction issue;
+             roofline_other: the verification and recount kernels;
              roofline_saturated: both kernels on the same workload as one
              batch of 16384 queries (GPU full), against peak instruction
              issue (their bound there), HBM and FP32
@@ -52,10 +55,15 @@ METRIC = "RkNN queries/s (1M users,100k fac,k=10) FP32-filtered vs FP64; p99 ms"
 NF, NU, K, NQ = 100_000, 1_000_000, 10, 1000
 
 # DRAM bytes (read + write) per launch of each kernel on this workload, from
-# one ncu capture of the same 1000-query batch
-# (profiles/slice_verify_recount_finalize_config2_k10.md); the verification
-# figure is verify_kernel plus recount_kernel
-TRAFFIC = {"slice_kernel": 1533184, "verify_kernel": 6904576 + 386048}
+# one ncu capture of the same 1000-query batch: the slice filter with the
+# fused verification (profiles/fused_slice_verify_config2_1k_queries.md), and
+# the separate filter and verification kernels (verify_kernel plus
+# recount_kernel) as larger batches run them
+# (profiles/slice_verify_recount_finalize_config2_k10.md)
+TRAFFIC = {"fused_slice_kernel": 4842240, "slice_kernel": 1533184, "verify_kernel": 6904576 + 386048}
+# warp instructions per query of the fused filter + verification kernel
+# (two warps a query) on this workload, same capture
+FUSED_INSTR_PER_QUERY = 22.05e6 / 1000
 # warp instructions per unit of work of the two kernels in a batch of SAT_NQ
 # queries of this workload, from one ncu capture (smsp__inst_executed.sum of
 # the launch over its queries or its half-plane evaluations;
@@ -348,31 +356,54 @@ def run_ours(args):
     # filter kernel (angular slices for this workload): bytes it must move
     # per launch = facilities streamed (8 B), facility cell-range starts read
     # (8 B per ring range), half-planes and their positions written (20 B),
-    # one 64 B query descriptor and its user segments (8 B per row) per query
+    # one 64 B query descriptor and its user segments (8 B per row) per query.
+    # At this batch size it also verifies its own queries (fused): users read
+    # (8 B) and result ids written (4 B) on top.
+    fused = st.get("fused_slots", 0) > 0
     zms = kavg["zone"]
     zbytes = 8 * st["zone_points"] + 8 * st["zone_cells"] + 20 * st["bisectors"] + 64 * NQ
+    if fused:
+        zbytes += 8 * st["candidates"] + 4 * st["results"]
     zgbs = zbytes / (zms / 1e3) / 1e9
+    clk_ghz = (clk.summary().get("sm_mhz") or 2070.0) / 1e3
+    issue_peak = 4 * props.multi_processor_count * clk_ghz * 1e9          # warp instructions / s
     froof = {"bound": "hbm", "achieved": zgbs, "peak": hbm_peak, "unit": "GB/s",
-             "frac": zgbs / hbm_peak, "peak_kind": kind, "kernel": "slice_kernel", "launch_ms": zms,
-             "alg_bytes": zbytes, "traffic": TRAFFIC.get("slice_kernel"),
-             "note": "latency-bound: one warp per query streams facilities ring by ring"}
-    # verification kernel: users read (8 B), half-planes staged (16 B each
+             "frac": zgbs / hbm_peak, "peak_kind": kind,
+             "kernel": "slice_kernel2 (filter + fused verification)" if fused else "slice_kernel",
+             "launch_ms": zms, "alg_bytes": zbytes,
+             "traffic": TRAFFIC.get("fused_slice_kernel" if fused else "slice_kernel"),
+             "note": ("latency-bound: two warps a query walk the facility rings, then verify the query's "
+                      "users against the half-planes in shared memory" if fused else
+                      "latency-bound: one warp per query streams facilities ring by ring")}
+    if fused:
+        zi = FUSED_INSTR_PER_QUERY * NQ
+        froof["issue"] = {"warp_instr": zi, "achieved_warp_instr_per_s": zi / (zms / 1e3),
+                          "peak_warp_instr_per_s": issue_peak, "frac": zi / (zms / 1e3) / issue_peak,
+                          "note": "instructions per query from ncu; peak = 4 per SM per cycle at the sampled clock"}
+    # verification kernels: users read (8 B), half-planes staged (16 B each
     # per query), result ids written (4 B), facilities read by the exact
-    # recount (8 B); FLOP = 4 per (user, half-plane) evaluation executed
+    # recount (8 B); FLOP = 4 per (user, half-plane) evaluation executed.
+    # Fused batches leave them only the left-over queries and the listed
+    # survivors' exact recount.
     vms = kavg["verify"] + kavg["recount"]
-    vbytes = 8 * st["candidates"] + 16 * st["bisectors"] + 4 * st["results"] + 8 * st["fac_checks"]
-    vflops = 4 * st["plane_evals"]
+    if fused:
+        vbytes = 8 * st["survivors"] + 4 * st["survivors"] + 8 * st["fac_checks"]
+        vflops = 0
+    else:
+        vbytes = 8 * st["candidates"] + 16 * st["bisectors"] + 4 * st["results"] + 8 * st["fac_checks"]
+        vflops = 4 * st["plane_evals"]
     vgbs = vbytes / (vms / 1e3) / 1e9
     vtfs = vflops / (vms / 1e3) / 1e12
     vroof = {"bound": "hbm", "achieved": vgbs, "peak": hbm_peak, "unit": "GB/s", "frac": vgbs / hbm_peak,
              "peak_kind": kind, "kernel": "verify_kernel", "kernels": "verify_kernel + recount_kernel",
              "launch_ms": vms,
-             "alg_bytes": vbytes, "alg_flop": vflops, "traffic": TRAFFIC.get("verify_kernel"),
+             "alg_bytes": vbytes, "alg_flop": vflops, "traffic": None if fused else TRAFFIC.get("verify_kernel"),
              "fp32": {"achieved_tflops": vtfs, "frac": vtfs / fp32_peak, "peak": fp32_peak,
                       "peak_kind": "nominal (SMs x 128 FMA x 2.07 GHz)"}}
     # the dominant kernel's roofline leads; the other rides beside it
     roof, other = (froof, vroof) if zms >= vms else (vroof, froof)
-    roof = dict(roof, kernel_ms=kavg, share={n: v / sum(kavg.values()) for n, v in kavg.items()})
+    roof = dict(roof, kernel_ms=kavg, share={n: v / sum(kavg.values()) for n, v in kavg.items()},
+                fused_queries=int(st.get("fused_slots", 0)))
 
     # ---- the same workload with the GPU full: one batch of SAT_NQ queries.
     # Both kernels are bound by instruction issue there; their issue roofline
@@ -392,8 +423,6 @@ def run_ours(args):
         ksat = idx.kernel_ms()
         sst = idx.last_stats()
         idx.set_profiling(False)
-        clk_ghz = (clk.summary().get("sm_mhz") or 2070.0) / 1e3
-        issue_peak = 4 * props.multi_processor_count * clk_ghz * 1e9          # warp instructions / s
         sz = ksat["zone"] / 1e3
         sv = ksat["verify"] / 1e3
         zi = INSTR["slice_kernel_per_query"] * SAT_NQ

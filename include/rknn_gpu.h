@@ -102,9 +102,13 @@ typedef struct {
                                The slice filter fills 0 facility stream, and within it 1
                                slice-bound offers, 3 ring stop tests, 4 cell ranges, 5 facility
                                items (with 1); 2 user-cell ring scan, 7 half-planes and
-                               segments */
+                               segments, 6 the verification of the query's users when
+                               the filter does it (warp 0's share) */
     int64_t zone_points;    /* facilities taken from the zone search's queue */
     int64_t zone_cells;     /* facility grid cells taken from the queue */
+    int64_t fused_slots;    /* queries the slice filter verified itself (FP32 batches
+                               small enough for two warps a query); the rest went
+                               through the verification kernel */
 } rknn_query_stats;
 
 void rknn_index_opts_default(rknn_index_opts* opts);

@@ -98,6 +98,7 @@ constexpr int ZB_VSTATS_INTS = 32;  // room for the statistics after them
 // result-region total
 
 struct Workspace {
+    bool last_fuse = false;        // the last batch ran the fused verification
     int nq_cap = 0, lc = 0, seg_cap = 0;
     // a batch of nq queries: q at [0, nq), k at [nq, 2 nq), the k order at
     // [2 nq, 3 nq) of one buffer, on the device and in page-locked staging,
@@ -698,6 +699,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
 rknn_status launch(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = true)
 {
     Workspace& w = c.w;
+    w.last_fuse = b.fuse;
     if (c.kev) return enqueue(ix, c, b, true);
     if (!graph) return enqueue(ix, c, b);
     GraphKey key = b.key;
@@ -771,6 +773,8 @@ rknn_status collect_stats(Ctx& c, int nq, rknn_query_stats* out)
     CK(cudaMemcpyAsync(z.data(), w.d_zst, sizeof(ZStats) * nq, cudaMemcpyDeviceToHost, c.st));
     CK(cudaMemcpyAsync(qd.data(), w.d_qd, sizeof(QDesc) * nq, cudaMemcpyDeviceToHost, c.st));
     CK(cudaMemcpyAsync(&v, w.d_vstats, sizeof(VStats), cudaMemcpyDeviceToHost, c.st));
+    int ndef = 0;
+    CK(cudaMemcpyAsync(&ndef, w.d_counters + 36, sizeof(int), cudaMemcpyDeviceToHost, c.st));
     CK(cudaStreamSynchronize(c.st));
     rknn_query_stats s{};
     s.queries = nq;
@@ -790,6 +794,7 @@ rknn_status collect_stats(Ctx& c, int nq, rknn_query_stats* out)
     s.survivors = (int64_t)v.survivors;
     s.fac_checks = (int64_t)v.fac_checks;
     s.rechecks = (int64_t)v.rechecks;
+    s.fused_slots = w.last_fuse ? nq - ndef : 0;
     s.device_ms = *c.device_ms;
     *out = s;
     return RKNN_OK;

@@ -239,15 +239,16 @@ __device__ __forceinline__ void fuse_verify(const ZoneArgs& A, int s, const char
 
 // KR > 0: the slice bounds live in a register list (k <= KR); KR == 0: in a
 // shared-memory max-heap per lane (any k up to the class's capacity).
-// NWQ = 2 (register lists only): two warps per query.  Both walk the same
-// rings (same cell ranges, half-planes and stop decisions); each offers only
-// its half of the useful facilities (alternate bits of the batch's mask) to
-// its own lists.  At every ring top the two warps' lists meet in shared
-// memory: the k-th smallest arc of their union is the slice's bound (the k
-// smallest of all offered facilities are among the two lists' k smallest),
-// computed identically in both warps.  A facility neither warp offers can
-// enter neither warp's k smallest, so the union is unchanged.  At the end
-// warp 0 writes the half-planes while warp 1 scans the user cells.
+// NWQ = 2 (register lists only): two warps per query.  Both step through the
+// same rings with the same stop decisions; each takes alternate cells of a
+// ring (loads, tests and offers their facilities to its own lists) and
+// appends their half-planes to one list through a shared count.  At every
+// ring top the two warps' lists meet in shared memory: the k-th smallest arc
+// of their union is the slice's bound (the k smallest of all offered
+// facilities are among the two lists' k smallest), computed identically in
+// both warps, and the stream's budget is read from a shared count between
+// the same barriers.  At the end warp 0 writes the half-planes while warp 1
+// scans the user cells.
 template <int KR, int NWQ>
 __device__ __forceinline__ void slice_body(const ZoneArgs& A)
 {
@@ -298,7 +299,11 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
         int slot = 0;
         if constexpr (NWQ == 2) {
             __syncthreads();            // the previous query is done with the shared ints
-            if (threadIdx.x == 0) xs[0] = atomicAdd(A.work_counter, 1);
+            if (threadIdx.x == 0) {
+                xs[0] = atomicAdd(A.work_counter, 1);
+                xs[6] = 0;              // half-planes taken (both warps)
+                xs[7] = 0;              // facilities offered (both warps)
+            }
             __syncthreads();
             slot = xs[0];
         } else {
@@ -380,12 +385,17 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
         // the slice's bound over both warps' lists (NWQ = 2): the k-th smallest
         // of their union, min over i of max(a_{i-1}, b_{k-1-i}) for the
         // ascending real entries a, b (the last k of each list)
+        // (NWQ = 2: between its barriers it also reads the facilities both
+        // warps offered so far, for the budget test: a count both warps see
+        // alike)
+        int pts_all = 0;
         auto union_kth = [&]() -> float {
             if constexpr (NWQ == 2) {
                 float* mine = xl + (size_t)wq * KR * 32 + lane;
 #pragma unroll
                 for (int i = 0; i < KR; ++i) mine[i * 32] = RL[(KR > 0 ? i : 0)];
                 __syncthreads();
+                pts_all = xs[7];
                 const float* a = xl + lane;
                 const float* b = xl + KR * 32 + lane;
                 float best = INFINITY;
@@ -410,6 +420,10 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
         const int qcy = cell_coord(qf.y, A.gf.y0, A.gf.inv, A.gf.gy);
         const int rmaxf = max(max(qcx, A.gf.gx - 1 - qcx), max(qcy, A.gf.gy - 1 - qcy));
         const int gx = A.gf.gx, gy = A.gf.gy;
+        // NWQ = 2: the warps take alternate cells of each ring (warp 0 ring
+        // 0's), and append their half-planes to warp 0's list through a
+        // shared count
+        int* lpos0 = (int*)(smem + LY.lpos);
         // Rings of up to 32 cells have their cell ranges loaded one ring
         // ahead (lane = range index), so that the load latency overlaps the
         // previous ring's work; ring 0's before the loop.
@@ -451,7 +465,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
             // Every heap top is an upper bound at any time, so the stream may
             // stop early; past a budget the remaining (sparse-direction)
             // slices keep their bounds and the kept region grows instead.
-            if (zs.pts >= fbudget) break;
+            if ((NWQ == 2 ? pts_all : zs.pts) >= fbudget) break;
             // Window maxima of the bounds for the ring: a facility helps only
             // slices within 8 of its own, so a cell whose facilities are all
             // farther than twice the largest bound of the slices within 8 of
@@ -474,7 +488,7 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                 const int ri = r0 + lane;
                 int fs = 0, fe = 0;
                 bool po = false;        // plane-only: the cell's facilities can enter no heap
-                if (ri < nrange) {
+                if (ri < nrange && (NWQ == 1 || (ri & 1) == wq)) {
                     int cxx, cyy;
                     ring_cell(ring, ri, qcx, qcy, cxx, cyy);
                     if (cxx >= 0 && cxx < gx && cyy >= 0 && cyy < gy) {
@@ -542,14 +556,22 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                     // ring order, those of plane-only cells included (so that
                     // rho is limited only by the rings, below)
                     const unsigned pm = __ballot_sync(FULL, ok);
-                    if (ok && wq == 0) {
-                        const int at = nL + __popc(pm & ((1u << lane) - 1));
-                        if (at < LC) lpos[SX(at, LC, 315)] = fidx;
+                    int at0 = nL;       // this batch's first half-plane slot
+                    if constexpr (NWQ == 2) {
+                        int a = 0;
+                        if (lane == 0 && pm) a = atomicAdd(xs + 6, __popc(pm));
+                        at0 = __shfl_sync(FULL, a, 0);
                     }
-                    if (nL + __popc(pm) > LC && rho_ring < 0) rho_ring = ring;
-                    nL = min(LC, nL + __popc(pm));
+                    if (ok) {
+                        const int at = at0 + __popc(pm & ((1u << lane) - 1));
+                        if (at < LC) lpos0[SX(at, LC, 315)] = fidx;
+                    }
+                    if (at0 + __popc(pm) > LC && rho_ring < 0) rho_ring = ring;
+                    if constexpr (NWQ == 1) nL = min(LC, nL + __popc(pm));
                     const unsigned om = __ballot_sync(FULL, ok && !rpo);      // offered to the bounds
                     zs.pts += __popc(om);
+                    if constexpr (NWQ == 2)
+                        if (lane == 0 && om) atomicAdd(xs + 7, __popc(om));
                     // A facility has finite arcs only for slices within 90 degrees
                     // of its direction (the 8 slices on either side of its own,
                     // counting the widening) and every arc is at least half its
@@ -575,7 +597,6 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                         }
                         const bool useful = ok && !rpo && !(0.25f * fmaf(vx, vx, vy * vy) * (1.0f - 4.0f * kU32) >= Rwj * Rwj);
                         m = __ballot_sync(FULL, useful);
-                        if constexpr (NWQ == 2) m &= wq ? 0xaaaaaaaau : 0x55555555u;     // this warp's half
                     }
                     // every lane offers every useful facility to its slice
                     zs.cand += __popc(m);
@@ -614,6 +635,25 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
             zs.cells += nrange;
         }
         zs.rings = ring;
+        // NWQ = 2: each warp's first ring with a facility left out of the
+        // half-planes, read by both after the barriers of the bound below
+        if constexpr (NWQ == 2)
+            if (lane == 0) xs[12 + wq] = rho_ring < 0 ? INT_MAX : rho_ring;
+        __syncwarp();
+        // R(P): k-th smallest arc, rounded up for the user test, and clipped
+        // to the box (no user lies farther)
+        {
+            const float R = union_kth();
+            Rs[lane] = fminf(R < INFINITY ? R * (1.0f + 1e-5f) + 1e-30f : INFINITY, clip);
+            if (wq == 0) A.slice_r[(size_t)s * 32 + lane] = Rs[lane];
+        }
+        __syncwarp();
+        if constexpr (NWQ == 2) {
+            const int rr = min(xs[12], xs[13]);
+            rho_ring = rr == INT_MAX ? -1 : rr;
+            nL = min(LC, xs[6]);
+            zs.pts = xs[7];
+        }
         // rho: every facility outside the half-planes lies in ring rho_ring or
         // beyond, at least (rho_ring - 1) cs from q (less the rounding slack)
         float rho;
@@ -625,15 +665,6 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
                 rho = Lr > 0.0f ? Lr : 0.0f;
             }
         }
-        __syncwarp();
-        // R(P): k-th smallest arc, rounded up for the user test, and clipped
-        // to the box (no user lies farther)
-        {
-            const float R = union_kth();
-            Rs[lane] = fminf(R < INFINITY ? R * (1.0f + 1e-5f) + 1e-30f : INFINITY, clip);
-            if (wq == 0) A.slice_r[(size_t)s * 32 + lane] = Rs[lane];
-        }
-        __syncwarp();
         zs.cyc[0] += clock64() - tph;
         tph = clock64();
 
@@ -861,11 +892,14 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
             d.pad = 0;
             if (FUSED) fuse_claim(A, s, d, smem, FL, true);
             *qd = d;
-            A.zst[s] = zs;
+            if (!FUSED) A.zst[s] = zs;
         }
         if (FUSED) {
             if constexpr (NWQ == 2) __syncthreads(); else __syncwarp();
+            tph = clock64();
             fuse_verify<NWQ>(A, s, smem, FL, Rs, vc);
+            zs.cyc[6] += clock64() - tph;
+            if (threadIdx.x == 0) A.zst[s] = zs;
         }
         __syncwarp();
     }

@@ -120,7 +120,8 @@ class Stats(C.Structure):
                 ("zone_fp64", C.c_int64), ("candidates", C.c_int64), ("plane_evals", C.c_int64),
                 ("survivors", C.c_int64), ("fac_checks", C.c_int64), ("rechecks", C.c_int64),
                 ("overflow", C.c_int64), ("device_ms", C.c_double),
-                ("zone_cycles", C.c_int64 * 8), ("zone_points", C.c_int64), ("zone_cells", C.c_int64)]
+                ("zone_cycles", C.c_int64 * 8), ("zone_points", C.c_int64), ("zone_cells", C.c_int64),
+                ("fused_slots", C.c_int64)]
 
     def as_dict(self):
         d = {n: getattr(self, n) for n, _ in self._fields_}
