@@ -54,22 +54,18 @@ sys.path.insert(0, os.path.join(REPO, "rt-rknn_gb300"))
 METRIC = "RkNN queries/s (1M users,100k fac,k=10) FP32-filtered vs FP64; p99 ms"
 NF, NU, K, NQ = 100_000, 1_000_000, 10, 1000
 
-# DRAM bytes (read + write) per launch of each kernel on this workload, from
-# one ncu capture of the same 1000-query batch: the slice filter with the
-# fused verification (profiles/fused_slice_verify_config2_1k_queries.md), and
-# the separate filter and verification kernels (verify_kernel plus
-# recount_kernel) as larger batches run them
-# (profiles/slice_verify_recount_finalize_config2_k10.md)
-TRAFFIC = {"fused_slice_kernel": 4842240, "slice_kernel": 1533184, "verify_kernel": 6904576 + 386048}
-# warp instructions per query of the fused filter + verification kernel
-# (two warps a query) on this workload, same capture
-FUSED_INSTR_PER_QUERY = 22.05e6 / 1000
+# DRAM bytes (read + write) per launch of the slice filter with the fused
+# verification on this workload's 1000-query batch, from one ncu capture
+# (profiles/fused_slice_verify_config2_1k_queries.md)
+TRAFFIC = {"fused_slice_kernel": 4844032}
+# warp instructions per query of that kernel (two warps a query), same capture
+FUSED_INSTR_PER_QUERY = 21.87e6 / 1000
 # warp instructions per unit of work of the two kernels in a batch of SAT_NQ
 # queries of this workload, from one ncu capture (smsp__inst_executed.sum of
 # the launch over its queries or its half-plane evaluations;
 # profiles/slice_verify_config2_16k_queries.md)
 SAT_NQ = 16384
-INSTR = {"slice_kernel_per_query": 164.45e6 / 16384, "verify_kernel_per_eval": 108.18e6 / 175826300}
+INSTR = {"slice_kernel_per_query": 164.89e6 / 16384, "verify_kernel_per_eval": 100.98e6 / 175826300}
 
 
 def peaks():
@@ -371,7 +367,7 @@ def run_ours(args):
              "frac": zgbs / hbm_peak, "peak_kind": kind,
              "kernel": "slice_kernel2 (filter + fused verification)" if fused else "slice_kernel",
              "launch_ms": zms, "alg_bytes": zbytes,
-             "traffic": TRAFFIC.get("fused_slice_kernel" if fused else "slice_kernel"),
+             "traffic": TRAFFIC.get("fused_slice_kernel") if fused else None,
              "note": ("latency-bound: two warps a query walk the facility rings, then verify the query's "
                       "users against the half-planes in shared memory" if fused else
                       "latency-bound: one warp per query streams facilities ring by ring")}
@@ -397,7 +393,7 @@ def run_ours(args):
     vroof = {"bound": "hbm", "achieved": vgbs, "peak": hbm_peak, "unit": "GB/s", "frac": vgbs / hbm_peak,
              "peak_kind": kind, "kernel": "verify_kernel", "kernels": "verify_kernel + recount_kernel",
              "launch_ms": vms,
-             "alg_bytes": vbytes, "alg_flop": vflops, "traffic": None if fused else TRAFFIC.get("verify_kernel"),
+             "alg_bytes": vbytes, "alg_flop": vflops, "traffic": None,
              "fp32": {"achieved_tflops": vtfs, "frac": vtfs / fp32_peak, "peak": fp32_peak,
                       "peak_kind": "nominal (SMs x 128 FMA x 2.07 GHz)"}}
     # the dominant kernel's roofline leads; the other rides beside it
