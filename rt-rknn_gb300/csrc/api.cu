@@ -119,6 +119,12 @@ struct Workspace {
                                    // [0] zone work, [1] verify work, [2] region exceeded,
                                    // [3] survivors listed, [4..8] zone fault record,
                                    // [10..14] verify fault record, [16..31] zone work per k class
+                                   // (the block of the last batch launched: one of d_zb)
+    int* d_zb[2] = {nullptr, nullptr};   // two such blocks, used by alternate batches: each
+                                         // batch's finalize clears the other for the next one,
+                                         // so no batch starts with a memset
+    int zb_next = 0;               // the block the next batch uses
+    long long zb_ints = 0;         // ints in each block
     VStats* d_vstats = nullptr;
     int *d_pool = nullptr, *d_out = nullptr;
     long long pool_cap = 0;
@@ -228,7 +234,9 @@ void free_ws(Workspace& w)
     cudaFree(w.d_slice_r);
     cudaFree(w.d_cand_off); cudaFree(w.d_reg_len); cudaFree(w.d_deflist); cudaFree(w.d_chunk_off);
     cudaFree(w.d_out_off);
-    cudaFree(w.d_counters);     // with the statistics and result counts
+    cudaFree(w.d_zb[0]);        // the counters, statistics and result counts
+    cudaFree(w.d_zb[1]);
+    w.d_zb[0] = w.d_zb[1] = w.d_counters = nullptr;
     cudaFree(w.d_pool); cudaFree(w.d_out); cudaFree(w.d_zscratch); cudaFree(w.d_surv);
     cudaFreeHost(w.h_qko); cudaFreeHost(w.h_off);
     cudaFreeHost(w.h_ids);
@@ -353,6 +361,15 @@ ZoneCaps caps_fit(rknn_index* ix, ZoneCaps c)
     return c;
 }
 
+// Point the workspace's counters, statistics and result counts at zeroed
+// block i.
+void use_block(Workspace& w, int i)
+{
+    w.d_counters = w.d_zb[i];
+    w.d_vstats = (VStats*)(w.d_counters + ZB_COUNTERS);
+    w.d_res_count = w.d_counters + ZB_COUNTERS + ZB_VSTATS_INTS;
+}
+
 rknn_status ensure_ws(Workspace& w, int nq, const ZoneCaps& caps, long long pool_need)
 {
     const int seg_cap = 2 * caps.rm + 2;
@@ -377,13 +394,16 @@ rknn_status ensure_ws(Workspace& w, int nq, const ZoneCaps& caps, long long pool
         CK(dalloc(w.d_zst, nqc));
         CK(dalloc(w.d_cand_off, nqc + 1)); CK(dalloc(w.d_reg_len, nqc + 1)); CK(dalloc(w.d_chunk_off, nqc + 1));
         CK(dalloc(w.d_deflist, nqc));
-        // counters, statistics and per-slot result counts in one block, so
-        // that one memset clears them before each batch
+        // counters, statistics and per-slot result counts in one block, two
+        // of them for alternate batches, both zero to begin with
         static_assert(sizeof(VStats) <= ZB_VSTATS_INTS * sizeof(int), "VStats outgrew its room");
-        CK(dalloc(w.d_counters, (size_t)ZB_COUNTERS + ZB_VSTATS_INTS + nqc));
-        CK(cudaMemset(w.d_counters, 0, sizeof(int) * ((size_t)ZB_COUNTERS + ZB_VSTATS_INTS + nqc)));
-        w.d_vstats = (VStats*)(w.d_counters + ZB_COUNTERS);
-        w.d_res_count = w.d_counters + ZB_COUNTERS + ZB_VSTATS_INTS;
+        w.zb_ints = (long long)ZB_COUNTERS + ZB_VSTATS_INTS + nqc;
+        for (int z = 0; z < 2; ++z) {
+            CK(dalloc(w.d_zb[z], (size_t)w.zb_ints));
+            CK(cudaMemset(w.d_zb[z], 0, sizeof(int) * (size_t)w.zb_ints));
+        }
+        w.zb_next = 0;
+        use_block(w, 0);
         CK(dalloc(w.d_out_off, nqc + 1 + OFF_TAIL));
         for (int i = 0; i < NAUX; ++i) {
             CK(cudaStreamCreateWithFlags(&w.aux[i], cudaStreamNonBlocking));
@@ -588,8 +608,8 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     cudaStream_t st = c.st;
     const int nq = b.nq;
     auto mark = [&](int i) { if (events) cudaEventRecord(c.kev[i], st); };
-    // counters, statistics and the slots' result counts: one memset
-    CK(cudaMemsetAsync(w.d_counters, 0, sizeof(int) * ((size_t)ZB_COUNTERS + ZB_VSTATS_INTS + nq), st));
+    // the counters, statistics and result counts start zero: the previous
+    // batch's finalize cleared this block (or it is new)
 
     ZoneArgs za;
     za.fxy = ix->d_fxy; za.fstart = ix->d_fstart; za.fmbr = ix->d_fmbr; za.fpos = ix->d_fpos;
@@ -689,7 +709,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     const long long ids_cap = c.io.ids ? c.io.ids_cap : w.pool_cap;
     CK(launch_k(finalize_kernel, (nq + FIN_WARPS - 1) / FIN_WARPS, 32 * FIN_WARPS, 0, st, pdl, w.d_pool,
                 (const long long*)w.d_cand_off, (const int*)w.d_reg_len, (const int*)w.d_res_count,
-                (const int*)w.d_out_off, ids, nq, ids_cap));
+                (const int*)w.d_out_off, ids, nq, ids_cap, w.d_zb[w.zb_next], w.zb_ints));
     mark(6);
     return RKNN_OK;
 }
@@ -700,9 +720,14 @@ rknn_status launch(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = true
 {
     Workspace& w = c.w;
     w.last_fuse = b.fuse;
+    // this batch's zeroed block; its finalize clears the other one
+    const int zb = w.zb_next;
+    w.zb_next ^= 1;
+    use_block(w, zb);
     if (c.kev) return enqueue(ix, c, b, true);
     if (!graph) return enqueue(ix, c, b);
     GraphKey key = b.key;
+    key.push_back(zb);
     key.push_back(w.pool_cap);
     key.push_back(w.rcap);
     key.push_back(w.surv_cap);
@@ -1540,7 +1565,7 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     scan_counts_kernel<<<1, 1024, 0, st>>>(L.res_count, L.reg_len, L.region_top, 1, L.out_off, L.counters, nullptr);
     CK(cudaGetLastError());
     finalize_kernel<<<1, 32 * FIN_WARPS, 0, st>>>(L.pool, L.cand_off, L.reg_len, L.res_count, L.out_off, L.out, 1,
-                                                  L.pool_cap);
+                                                  L.pool_cap, nullptr, 0);
     CK(cudaGetLastError());
 
     QDesc d;

@@ -189,8 +189,22 @@ __global__ void __launch_bounds__(512) verify_kernel_u8(VerifyArgs a) { verify_b
 // disc row r (trimmed to the chord), a warp prefix sum flattens the rows,
 // and each round tests 32 facilities (__ballot_sync/__popc), stopping at k:
 // the survivor costs a couple of load latencies, not one per facility.
-__device__ __forceinline__ int warp_exact_count(float ux, float uy, const QDesc& d, const VerifyArgs& A,
-                                                unsigned long long& fac, unsigned long long& rech)
+__device__ __forceinline__ void group_barrier(int id, int nthreads)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// Exact count of the facilities strictly nearer to u than q, stopping at k,
+// by a group of G warps (G = 1, 2, 4, 8; gi this warp's index in it): lane r
+// computes the facility range of disc row r (trimmed to the disc's chord), a
+// warp prefix sum flattens the rows, and the group's warps take alternate
+// rounds of 32 facilities (__ballot_sync/__popc), adding their counts to the
+// group's shared counter *sc and stopping once it reaches k.  The count is
+// exact below k and at least k otherwise, whatever G.  Groups of more than
+// one warp synchronise on named barrier bar (G * 32 threads).
+__device__ __forceinline__ int group_exact_count(float ux, float uy, const QDesc& d, const VerifyArgs& A, int G,
+                                                 int gi, int bar, int* sc, unsigned long long& fac,
+                                                 unsigned long long& rech)
 {
     const int lane = threadIdx.x & 31;
     const float qx = d.qx, qy = d.qy;
@@ -208,11 +222,16 @@ __device__ __forceinline__ int warp_exact_count(float ux, float uy, const QDesc&
         Dq64 = fma(dx, dx, dy * dy);
         r = (float)sqrt(Dq64) * (1.0f + 4e-6f) + slack;
     }
+    if (G > 1) {
+        if (gi == 0 && lane == 0) *sc = 0;
+        group_barrier(bar, G * 32);
+    }
     const Grid& g = A.gf;
     const float ym = 1e-5f * g.cs + 8.0f * kU32 * (fabsf(g.y0) + fabsf(uy) + g.cs * (float)g.gy);
     const int cy0 = cell_coord(uy - r, g.y0, g.inv, g.gy), cy1 = cell_coord(uy + r, g.y0, g.inv, g.gy);
     int cnt = 0;
-    for (int rb = cy0; rb <= cy1; rb += 32) {
+    bool stop = false;
+    for (int rb = cy0; rb <= cy1 && !stop; rb += 32) {
         const int cy = rb + lane;
         int f0 = 0, len = 0;
         if (cy <= cy1) {
@@ -230,7 +249,7 @@ __device__ __forceinline__ int warp_exact_count(float ux, float uy, const QDesc&
             if (lane >= o) incl += v;
         }
         const int total = __shfl_sync(FULL, incl, 31);
-        for (int t0 = 0; t0 < total; t0 += 32) {
+        for (int t0 = gi * 32; t0 < total; t0 += G * 32) {
             const int j = t0 + lane;
             int lo = 0;
 #pragma unroll
@@ -248,31 +267,57 @@ __device__ __forceinline__ int warp_exact_count(float ux, float uy, const QDesc&
                 c = f32 ? closer_f32(ux, uy, f.x, f.y, qx, qy, Dq32, &rech)
                         : closer_f64(ux, uy, f.x, f.y, qx, qy, Dq64, &rech);
             }
-            cnt += __popc(__ballot_sync(FULL, c));
+            const int pc = __popc(__ballot_sync(FULL, c));
             fac += (unsigned long long)min(32, total - t0);
-            if (cnt >= d.k) return cnt;
+            if (G == 1) {
+                cnt += pc;
+            } else {
+                int now = 0;
+                if (lane == 0) now = atomicAdd(sc, pc) + pc;
+                cnt = __shfl_sync(FULL, now, 0);
+            }
+            if (cnt >= d.k) { stop = true; break; }
         }
+    }
+    if (G > 1) {
+        group_barrier(bar, G * 32);
+        cnt = *(volatile int*)sc;
+        group_barrier(bar, G * 32);      // the counter is read before the next survivor resets it
     }
     return cnt;
 }
 
-// Exact recount of the listed survivors, one warp each; accepted users are
-// appended with one atomic per survivor.
-// The listed survivors, one warp each over the grid's warps.
-__device__ __forceinline__ void recount_listed(const VerifyArgs& A, VCount& vc)
+// One warp's exact count (a group of one).
+__device__ __forceinline__ int warp_exact_count(float ux, float uy, const QDesc& d, const VerifyArgs& A,
+                                                unsigned long long& fac, unsigned long long& rech)
+{
+    return group_exact_count(ux, uy, d, A, 1, 0, 0, nullptr, fac, rech);
+}
+
+// Exact recount of the listed survivors; accepted users are appended with
+// one atomic per survivor.  A survivor gets a group of G warps of one block
+// (G a power of two up to the block's warps, as large as the grid's warps
+// allow for all survivors at once), which split its rounds of facilities:
+// the count's latency, not its work, bounds a small batch.  sc: one shared
+// counter per group.
+__device__ __forceinline__ void recount_listed(const VerifyArgs& A, VCount& vc, int* sc)
 {
     const int lane = threadIdx.x & 31;
     const int n = min(*A.surv_count, A.surv_cap);
     unsigned long long s_fac = 0, s_rech = 0, s_res = 0;
-    const int nw = gridDim.x * (blockDim.x >> 5);
-    for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nw) {
+    const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5;
+    const int nw = gridDim.x * wpb;
+    int G = 1;
+    while (2 * G <= wpb && (long long)n * 2 * G <= nw) G *= 2;
+    const int gi = w % G, gid = w / G, gpb = wpb / G;
+    for (int i = blockIdx.x * gpb + gid; i < n; i += gridDim.x * gpb) {
         const int2 e = A.surv[VX(i, A.surv_cap, 215)];
-        if (e.x < 0) continue;
+        if (e.x < 0) continue;           // the group's warps skip it alike
         const int slot = e.x, pos = e.y;
         const QDesc d = A.qd[slot];
         const float2 u = A.uxy[VX(pos, A.nu, 216)];
-        const int c = warp_exact_count(u.x, u.y, d, A, s_fac, s_rech);
-        if (c < d.k && lane == 0) {
+        const int c = group_exact_count(u.x, u.y, d, A, G, gi, 1 + gid, sc + gid, s_fac, s_rech);
+        if (c < d.k && gi == 0 && lane == 0) {
             const int at = atomicAdd(A.res_count + slot, 1);
             const long long r0 = A.cand_off[slot], region = A.reg_len[slot];
             if (at < region) A.res_pool[VX(r0 + at, A.pool_cap, 217)] = A.uid[VX(pos, A.nu, 218)];
@@ -289,15 +334,13 @@ __global__ void __launch_bounds__(256) recount_kernel(VerifyArgs A)
 {
     pdl_wait();
     pdl_trigger();
+    __shared__ int sc[8];
     VCount vc = {};
-    recount_listed(A, vc);
+    recount_listed(A, vc, sc);
     vc.flush(A.vstats);
 }
 
 // ---------------------------------------------------------------- scans
-namespace {
-}  // namespace
-
 // Scans over the batch's slots run in one block of SCAN_THREADS threads, a
 // tile of SCAN_TILE slots per round: values are read coalesced into shared
 // memory, each thread scans SCAN_PT consecutive slots of the tile, and a
@@ -520,8 +563,13 @@ __device__ __forceinline__ void warp_sort_slot(const unsigned* src, unsigned* ds
 // pool region above that.
 __global__ void __launch_bounds__(32 * FIN_WARPS, 1)
 finalize_kernel(int* res_pool, const long long* cand_off, const int* reg_len, const int* res_count,
-                const int* out_off, int* out, int nq, long long out_cap)
+                const int* out_off, int* out, int nq, long long out_cap, int* zero, long long zero_n)
 {
+    // the next batch's counters (no kernel of this batch uses them), while
+    // the predecessor drains
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < zero_n;
+         i += (long long)gridDim.x * blockDim.x)
+        zero[i] = 0;
     pdl_wait();
     __shared__ unsigned skeys[FIN_BCAP];
     __shared__ int big[FIN_WARPS];

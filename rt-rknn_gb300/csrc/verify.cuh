@@ -81,8 +81,10 @@ __global__ void scan_counts_kernel(const int* res_count, const int* reg_len, con
 // one block per slot: sort the slot's results into out[out_off[s] ...]
 // out may be device-accessible host memory of out_cap ids: a slot whose range
 // would pass out_cap is left out (the caller sees the total and fails the
-// batch).
+// batch).  zero[0 .. zero_n) (another batch's counters, unused by this one)
+// is cleared for the next batch.
 __global__ void finalize_kernel(int* res_pool, const long long* cand_off, const int* reg_len, const int* res_count,
-                                const int* out_off, int* out, int nq, long long out_cap);
+                                const int* out_off, int* out, int nq, long long out_cap, int* zero,
+                                long long zero_n);
 
 }  // namespace rknn

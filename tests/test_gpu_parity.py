@@ -180,6 +180,40 @@ def test_device_batch_with_understated_kmax(engine, filt):
     idx.close()
 
 
+def test_fused_and_separate_verification_agree(engine, monkeypatch):
+    """Batches that fit two warps a query are verified inside the slice
+    filter (fused); RKNN_FUSE=0 at index creation keeps the separate
+    verification kernel.  Both give the oracle's ids, including queries with
+    more than 4096 candidates (left over to the verification kernel in the
+    fused batch), mixed k (several filter launches counted by one last-block
+    counter) and a device batch whose kmax understates some k."""
+    import torch
+    ds = datagen.uniform(300, 60_000, seed=51, nq=80, k=1)
+    o = O.Oracle.of(ds)
+    rng = np.random.default_rng(8)
+    ks = rng.integers(1, 30, ds.queries.shape[0]).astype(np.int32)
+    want = [o.query(int(q), int(k)) for q, k in zip(ds.queries, ks)]
+    got = {}
+    for fuse in ("1", "0"):
+        monkeypatch.setenv("RKNN_FUSE", fuse)
+        idx = engine.Index.of(ds)
+        res, st = idx.query_batch(ds.queries, ks, "fp32", stats=True)
+        assert (st["fused_slots"] > 0) == (fuse == "1"), st["fused_slots"]
+        if fuse == "1":
+            assert st["fused_slots"] < len(ks)        # some queries were left over
+            assert st["candidates"] > 4096
+        got[fuse] = res
+        for q, k, r, w in zip(ds.queries, ks, res, want):
+            assert np.array_equal(r, w), (int(q), int(k), fuse)
+        d_q = torch.from_numpy(ds.queries.astype(np.int32)).cuda()
+        d_k = torch.from_numpy(ks).cuda()
+        idx.query_batch_device(d_q.data_ptr(), d_k.data_ptr(), len(ks), 4, "fp32")
+        for q, k, r, w in zip(ds.queries, ks, _device_results(idx, len(ks)), want):
+            assert np.array_equal(r, w), (int(q), int(k), fuse, "device")
+        idx.close()
+    assert all(np.array_equal(a, b) for a, b in zip(got["1"], got["0"]))
+
+
 def test_flat_batches_into_page_locked_ids(engine):
     """query_batch_flat keeps one page-locked id buffer: from its second call
     the finalize kernel writes the ids into it directly.  Batches that fit,
