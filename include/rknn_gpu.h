@@ -124,6 +124,27 @@ rknn_status rknn_index_destroy(rknn_index* idx);
 /* Number of facilities / users in the index. */
 rknn_status rknn_index_size(const rknn_index* idx, int64_t* nf, int64_t* nu);
 
+/* Binary snapshot of an index's input points: a file that loads in
+ * milliseconds where the reference parses text (rknn-inf/inf.cpp:129-161)
+ * and builds an R*-tree per process.  Little-endian layout:
+ *   "RKNNSNP1", uint32 version (1), uint32 0, int64 nf, int64 nu,
+ *   float fxy[2 nf], int32 fid[nf], float uxy[2 nu], int32 uid[nu],
+ *   uint64 hash: FNV-1a (64-bit) over the preceding bytes taken as
+ *   little-endian 64-bit words, the last one zero-padded.
+ * The snapshot functions are host code: they need no GPU. */
+rknn_status rknn_snapshot_write(const char* path, const float* fxy, const int32_t* fid, int64_t nf,
+                                const float* uxy, const int32_t* uid, int64_t nu);
+/* Reads a snapshot into arrays the library allocates (release each with
+ * rknn_snapshot_free).  RKNN_ERR_ARG: not a snapshot, truncated, or the
+ * hash does not match. */
+rknn_status rknn_snapshot_read(const char* path, float** fxy, int32_t** fid, int64_t* nf,
+                               float** uxy, int32_t** uid, int64_t* nu);
+void rknn_snapshot_free(void* p);
+/* rknn_index_create over a snapshot's points. */
+rknn_status rknn_index_open(const char* path, const rknn_index_opts* opts, rknn_index** out);
+/* Writes the index's input points (facility ids included) as a snapshot. */
+rknn_status rknn_index_save(const rknn_index* idx, const char* path);
+
 typedef struct {
     int64_t nf, nu;
     double x0, y0, x1, y1;          /* bounding box of all points: the zone's space */

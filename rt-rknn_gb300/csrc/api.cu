@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -155,6 +156,7 @@ struct rknn_index {
     float2* d_uxy = nullptr;
     int *d_uid = nullptr, *d_ustart = nullptr;
     std::vector<int> h_fidx;       // cell-sorted position -> facility input index
+    std::vector<int32_t> h_fid;    // facility ids as given (for snapshots)
     // the input points, kept on the device so the grids can be rebuilt
     // with other cell sizes (rknn_index_tune)
     float2 *d_fin = nullptr, *d_uin = nullptr;
@@ -1022,6 +1024,11 @@ rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf, 
     if (const char* f = std::getenv("RKNN_FUSE")) ix->fuse = std::strcmp(f, "0") != 0;
     ix->nf = nf;
     ix->nu = nu;
+    if (fid) ix->h_fid.assign(fid, fid + nf);
+    else {
+        ix->h_fid.resize(nf);
+        for (int64_t i = 0; i < nf; ++i) ix->h_fid[i] = (int32_t)i;
+    }
     ix->sx0 = x0; ix->sy0 = y0; ix->sx1 = x1; ix->sy1 = y1;
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -1102,6 +1109,153 @@ rknn_status rknn_index_destroy(rknn_index* ix)
     if (ix->own_stream) cudaStreamDestroy(ix->own_stream);
     delete ix;
     return RKNN_OK;
+}
+
+// ---------------------------------------------------------------- snapshots
+namespace {
+constexpr char SNAP_MAGIC[8] = {'R', 'K', 'N', 'N', 'S', 'N', 'P', '1'};
+
+// FNV-1a over 64-bit little-endian words (the tail zero-padded), streamed.
+struct SnapHash {
+    uint64_t h = 1469598103934665603ull;
+    unsigned char pend[8];
+    int npend = 0;
+    void word(uint64_t w)
+    {
+        h ^= w;
+        h *= 1099511628211ull;
+    }
+    static uint64_t le64(const unsigned char* p)
+    {
+        uint64_t w = 0;
+        for (int i = 7; i >= 0; --i) w = (w << 8) | p[i];
+        return w;
+    }
+    void add(const void* data, size_t n)
+    {
+        const unsigned char* p = (const unsigned char*)data;
+        while (n && npend) {
+            pend[npend++] = *p++;
+            --n;
+            if (npend == 8) { word(le64(pend)); npend = 0; }
+        }
+        for (; n >= 8; n -= 8, p += 8) word(le64(p));
+        while (n--) pend[npend++] = *p++;
+    }
+    uint64_t done()
+    {
+        if (npend) {
+            while (npend < 8) pend[npend++] = 0;
+            word(le64(pend));
+            npend = 0;
+        }
+        return h;
+    }
+};
+
+// Writes n bytes and adds them to the hash.
+bool snap_put(FILE* f, SnapHash& hs, const void* p, size_t n)
+{
+    hs.add(p, n);
+    return n == 0 || std::fwrite(p, 1, n, f) == n;
+}
+
+bool snap_get(FILE* f, SnapHash& hs, void* p, size_t n)
+{
+    if (n && std::fread(p, 1, n, f) != n) return false;
+    hs.add(p, n);
+    return true;
+}
+}  // namespace
+
+rknn_status rknn_snapshot_write(const char* path, const float* fxy, const int32_t* fid, int64_t nf,
+                                const float* uxy, const int32_t* uid, int64_t nu)
+{
+    g_err.clear();
+    if (!path || !fxy || !fid || nf < 1 || nu < 0 || (nu > 0 && (!uxy || !uid)))
+        return fail(RKNN_ERR_ARG, "bad snapshot arguments");
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(RKNN_ERR_ARG, std::string("cannot write ") + path);
+    SnapHash hs;
+    const uint32_t ver[2] = {1, 0};
+    const int64_t n[2] = {nf, nu};
+    bool ok = snap_put(f, hs, SNAP_MAGIC, 8) && snap_put(f, hs, ver, sizeof(ver)) && snap_put(f, hs, n, sizeof(n)) &&
+              snap_put(f, hs, fxy, sizeof(float) * 2 * (size_t)nf) && snap_put(f, hs, fid, sizeof(int32_t) * (size_t)nf) &&
+              snap_put(f, hs, uxy, sizeof(float) * 2 * (size_t)nu) && snap_put(f, hs, uid, sizeof(int32_t) * (size_t)nu);
+    const uint64_t h = hs.done();
+    ok = ok && std::fwrite(&h, 1, sizeof(h), f) == sizeof(h);
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) return fail(RKNN_ERR_ARG, std::string("write failed: ") + path);
+    return RKNN_OK;
+}
+
+rknn_status rknn_snapshot_read(const char* path, float** fxy, int32_t** fid, int64_t* nf, float** uxy,
+                               int32_t** uid, int64_t* nu)
+{
+    g_err.clear();
+    if (!path || !fxy || !fid || !nf || !uxy || !uid || !nu) return fail(RKNN_ERR_ARG, "null argument");
+    *fxy = *uxy = nullptr;
+    *fid = *uid = nullptr;
+    *nf = *nu = 0;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(RKNN_ERR_ARG, std::string("cannot open ") + path);
+    SnapHash hs;
+    char magic[8];
+    uint32_t ver[2];
+    int64_t n[2];
+    if (!snap_get(f, hs, magic, 8) || std::memcmp(magic, SNAP_MAGIC, 8) != 0 || !snap_get(f, hs, ver, sizeof(ver)) ||
+        ver[0] != 1 || !snap_get(f, hs, n, sizeof(n)) || n[0] < 1 || n[1] < 0 || n[0] >= INT32_MAX / 2 ||
+        n[1] >= INT32_MAX / 2) {
+        std::fclose(f);
+        return fail(RKNN_ERR_ARG, std::string("not an index snapshot: ") + path);
+    }
+    float* a = (float*)std::malloc(sizeof(float) * 2 * (size_t)n[0]);
+    int32_t* b = (int32_t*)std::malloc(sizeof(int32_t) * (size_t)n[0]);
+    float* c = (float*)std::malloc(sizeof(float) * 2 * (size_t)std::max<int64_t>(n[1], 1));
+    int32_t* d = (int32_t*)std::malloc(sizeof(int32_t) * (size_t)std::max<int64_t>(n[1], 1));
+    uint64_t h = 0;
+    bool ok = a && b && c && d && snap_get(f, hs, a, sizeof(float) * 2 * (size_t)n[0]) &&
+              snap_get(f, hs, b, sizeof(int32_t) * (size_t)n[0]) && snap_get(f, hs, c, sizeof(float) * 2 * (size_t)n[1]) &&
+              snap_get(f, hs, d, sizeof(int32_t) * (size_t)n[1]);
+    const uint64_t want = hs.done();
+    ok = ok && std::fread(&h, 1, sizeof(h), f) == sizeof(h) && h == want;
+    std::fclose(f);
+    if (!ok) {
+        std::free(a); std::free(b); std::free(c); std::free(d);
+        return fail(RKNN_ERR_ARG, std::string("truncated or corrupt index snapshot: ") + path);
+    }
+    *fxy = a; *fid = b; *uxy = c; *uid = d;
+    *nf = n[0]; *nu = n[1];
+    return RKNN_OK;
+}
+
+void rknn_snapshot_free(void* p) { std::free(p); }
+
+rknn_status rknn_index_open(const char* path, const rknn_index_opts* opts, rknn_index** out)
+{
+    float *fxy = nullptr, *uxy = nullptr;
+    int32_t *fid = nullptr, *uid = nullptr;
+    int64_t nf = 0, nu = 0;
+    rknn_status s = rknn_snapshot_read(path, &fxy, &fid, &nf, &uxy, &uid, &nu);
+    if (s != RKNN_OK) return s;
+    s = rknn_index_create(fxy, fid, nf, uxy, uid, nu, opts, out);
+    std::free(fxy); std::free(fid); std::free(uxy); std::free(uid);
+    return s;
+}
+
+rknn_status rknn_index_save(const rknn_index* ix, const char* path)
+{
+    g_err.clear();
+    if (!ix || !path) return fail(RKNN_ERR_ARG, "null argument");
+    std::vector<float> fxy(2 * (size_t)ix->nf), uxy(2 * (size_t)ix->nu);
+    std::vector<int32_t> uid((size_t)ix->nu);
+    CK(cudaSetDevice(ix->device));
+    CK(cudaMemcpy(fxy.data(), ix->d_fin, sizeof(float) * fxy.size(), cudaMemcpyDeviceToHost));
+    if (ix->nu > 0) {
+        CK(cudaMemcpy(uxy.data(), ix->d_uin, sizeof(float) * uxy.size(), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(uid.data(), ix->d_uidin, sizeof(int32_t) * uid.size(), cudaMemcpyDeviceToHost));
+    }
+    return rknn_snapshot_write(path, fxy.data(), ix->h_fid.data(), ix->nf, uxy.data(), uid.data(), ix->nu);
 }
 
 rknn_status rknn_index_size(const rknn_index* ix, int64_t* nf, int64_t* nu)

@@ -1,8 +1,11 @@
 // rknn-gb300: command-line drop-in for the reference's query binaries.
 //
 //   rknn-gb300 -if <file> -k <k> -q <index> [-al <name>] [--mode fp64|fp32]
-//              [--queries i,j,...] [--log <dir>] [--no-log]
+//              [--queries i,j,...] [--log <dir>] [--no-log] [--save <snapshot>]
 //
+// The input file may also be a binary index snapshot (rknn_snapshot_write's
+// format, recognised by its magic), which loads without parsing; --save
+// writes one of the loaded points.
 // Same options and defaults as rknn-inf (rknn-inf/inf.cpp:38-119: -if/--infile,
 // -k (default 4), -q (default 0, an index into the facility list), -al parsed
 // and ignored), same input format (inf.cpp:129-161), and the reference's
@@ -15,6 +18,7 @@
 #include <sys/stat.h>
 #include <sys/time.h>
 
+#include <charconv>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -46,6 +50,8 @@ double wall()
                  "         --queries i,j,...           several query indices in one batch\n"
                  "         --log <dir>                 result directory (default log)\n"
                  "         --no-log                    do not write result files\n"
+                 "         --save <file>               also write the points as a binary snapshot\n"
+                 "                                     (a later -if loads it without parsing)\n"
                  "         --help | -h                 print this message\n",
                  argv0);
     std::exit(1);
@@ -54,16 +60,49 @@ double wall()
 struct Parser {
     const char* p;
     const char* end;
-    bool next(std::string& tok)
+    // the next whitespace-separated token as [b, e)
+    bool span(const char*& b, const char*& e)
     {
         while (p < end && (*p == ' ' || *p == '\n' || *p == '\t' || *p == '\r')) ++p;
         if (p >= end) return false;
-        const char* b = p;
+        b = p;
         while (p < end && !(*p == ' ' || *p == '\n' || *p == '\t' || *p == '\r')) ++p;
-        tok.assign(b, p - b);
+        e = p;
+        return true;
+    }
+    bool next(std::string& tok)
+    {
+        const char *b, *e;
+        if (!span(b, e)) return false;
+        tok.assign(b, e - b);
         return true;
     }
 };
+
+// A token as an integer / a double: std::from_chars on the buffer (no
+// copies, no locale), strtoll / strtod for the forms it does not take (a
+// leading '+', hexadecimal floats, inf / nan); both give the correctly
+// rounded double, as the reference's stream extraction does.
+bool parse_int(const char* b, const char* e, long long& v)
+{
+    const auto r = std::from_chars(b, e, v);
+    if (r.ec == std::errc() && r.ptr == e) return true;
+    std::string t(b, e);
+    char* x;
+    errno = 0;
+    v = std::strtoll(t.c_str(), &x, 10);
+    return !*x && !errno && !t.empty();
+}
+
+bool parse_double(const char* b, const char* e, double& v)
+{
+    const auto r = std::from_chars(b, e, v);
+    if (r.ec == std::errc() && r.ptr == e) return true;
+    std::string t(b, e);
+    char* x;
+    v = std::strtod(t.c_str(), &x);
+    return !*x && !t.empty();
+}
 
 bool read_file(const std::string& path, std::string& data)
 {
@@ -83,18 +122,14 @@ bool parse_points(Parser& ps, long long n, std::vector<float>& xy, std::vector<i
 {
     xy.resize(2 * n);
     id.resize(n);
-    std::string t;
+    const char *b, *e;
     for (long long i = 0; i < n; ++i) {
-        if (!ps.next(t)) return false;
-        char* e;
-        errno = 0;
-        long long v = std::strtoll(t.c_str(), &e, 10);
-        if (*e || errno) return false;
+        long long v;
+        if (!ps.span(b, e) || !parse_int(b, e, v)) return false;
         id[i] = (int32_t)v;
         for (int c = 0; c < 2; ++c) {
-            if (!ps.next(t)) return false;
-            double d = std::strtod(t.c_str(), &e);
-            if (*e) return false;
+            double d;
+            if (!ps.span(b, e) || !parse_double(b, e, d)) return false;
             float f = (float)d;
             if ((double)f != d) ++inexact;
             xy[2 * i + c] = f;
@@ -107,7 +142,7 @@ bool parse_points(Parser& ps, long long n, std::vector<float>& xy, std::vector<i
 
 int main(int argc, char** argv)
 {
-    std::string infile, logdir = "log", mode_s = "fp64", filter_s = "inf";
+    std::string infile, logdir = "log", mode_s = "fp64", filter_s = "inf", save_path;
     long long k = 4, q = 0;
     std::vector<long long> queries;
     bool write_log = true;
@@ -145,6 +180,7 @@ int main(int argc, char** argv)
             }
         } else if (a == "--log") logdir = val();
         else if (a == "--no-log") write_log = false;
+        else if (a == "--save") save_path = val();
         else {
             std::fprintf(stderr, "Unknown option '%s'\n", a.c_str());
             usage(argv[0]);
@@ -170,14 +206,37 @@ int main(int argc, char** argv)
         std::fprintf(stderr, "Error opening file: %s\n", infile.c_str());
         return 1;
     }
-    Parser ps{data.data(), data.data() + data.size()};
-    std::string t;
     std::vector<float> fxy, uxy;
     std::vector<int32_t> fid, uid;
     long long inexact = 0, nf = 0, nu = 0;
-    if (!ps.next(t) || (nf = std::atoll(t.c_str())) < 1 || !parse_points(ps, nf, fxy, fid, inexact) ||
-        !ps.next(t) || (nu = std::atoll(t.c_str())) < 0 || !parse_points(ps, nu, uxy, uid, inexact)) {
-        std::fprintf(stderr, "Error parsing file: %s\n", infile.c_str());
+    if (data.size() >= 8 && std::memcmp(data.data(), "RKNNSNP1", 8) == 0) {
+        // a binary snapshot: read by the library (checked against its hash)
+        data.clear();
+        data.shrink_to_fit();
+        float *a = nullptr, *c = nullptr;
+        int32_t *b = nullptr, *d = nullptr;
+        int64_t n1 = 0, n2 = 0;
+        if (rknn_snapshot_read(infile.c_str(), &a, &b, &n1, &c, &d, &n2) != RKNN_OK) {
+            std::fprintf(stderr, "Error reading snapshot: %s\n", rknn_last_error());
+            return 1;
+        }
+        nf = n1;
+        nu = n2;
+        fxy.assign(a, a + 2 * n1); fid.assign(b, b + n1);
+        uxy.assign(c, c + 2 * n2); uid.assign(d, d + n2);
+        rknn_snapshot_free(a); rknn_snapshot_free(b); rknn_snapshot_free(c); rknn_snapshot_free(d);
+    } else {
+        Parser ps{data.data(), data.data() + data.size()};
+        std::string t;
+        if (!ps.next(t) || (nf = std::atoll(t.c_str())) < 1 || !parse_points(ps, nf, fxy, fid, inexact) ||
+            !ps.next(t) || (nu = std::atoll(t.c_str())) < 0 || !parse_points(ps, nu, uxy, uid, inexact)) {
+            std::fprintf(stderr, "Error parsing file: %s\n", infile.c_str());
+            return 1;
+        }
+    }
+    if (!save_path.empty() &&
+        rknn_snapshot_write(save_path.c_str(), fxy.data(), fid.data(), nf, uxy.data(), uid.data(), nu) != RKNN_OK) {
+        std::fprintf(stderr, "Error writing snapshot: %s\n", rknn_last_error());
         return 1;
     }
     std::printf("Loaded %lld facilities and %lld users.\n", nf, nu);

@@ -38,7 +38,8 @@ EXPORTS = ["rknn_index_opts_default", "rknn_index_create", "rknn_index_destroy",
            "rknn_last_zone", "rknn_set_profiling", "rknn_last_kernel_ms",
            "rknn_serve_opts_default", "rknn_serve_start", "rknn_serve_submit", "rknn_serve_wait",
            "rknn_serve_replay", "rknn_serve_stats_get", "rknn_serve_stop", "rknn_index_tune",
-           "rknn_host_alloc", "rknn_host_free", "rknn_last_error", "rknn_version"]
+           "rknn_host_alloc", "rknn_host_free", "rknn_snapshot_write", "rknn_snapshot_read",
+           "rknn_snapshot_free", "rknn_index_open", "rknn_index_save", "rknn_last_error", "rknn_version"]
 
 
 class ServeOpts(C.Structure):
@@ -169,12 +170,19 @@ def load(path: str = LIB_PATH):
     L.rknn_serve_stats_get.argtypes = [vp, i32, C.POINTER(ServeStats)]
     L.rknn_serve_stop.argtypes = [vp]
     L.rknn_index_tune.argtypes = [vp, vp, vp, i32, i32, C.POINTER(TuneResult)]
+    L.rknn_snapshot_write.argtypes = [C.c_char_p, vp, vp, i64, vp, vp, i64]
+    L.rknn_snapshot_read.argtypes = [C.c_char_p, C.POINTER(vp), C.POINTER(vp), C.POINTER(i64), C.POINTER(vp),
+                                     C.POINTER(vp), C.POINTER(i64)]
+    L.rknn_snapshot_free.argtypes = [vp]
+    L.rknn_snapshot_free.restype = None
+    L.rknn_index_open.argtypes = [C.c_char_p, C.POINTER(Opts), C.POINTER(vp)]
+    L.rknn_index_save.argtypes = [vp, C.c_char_p]
     L.rknn_last_error.restype = C.c_char_p
     L.rknn_version.restype = C.c_char_p
     for name in EXPORTS:
         fn = getattr(L, name)
         if name not in ("rknn_last_error", "rknn_version", "rknn_index_opts_default",
-                        "rknn_serve_opts_default"):
+                        "rknn_serve_opts_default", "rknn_snapshot_free"):
             fn.restype = C.c_int
     _lib = L
     return L
@@ -187,6 +195,36 @@ def _check(rc: int):
 
 def _ptr(a: np.ndarray):
     return a.ctypes.data if a is not None and a.size else None
+
+
+def snapshot_write(path: str, fxy, fid, uxy, uid):
+    """Write points as a binary index snapshot (rknn_snapshot_write)."""
+    fxy = np.ascontiguousarray(fxy, dtype=np.float32).reshape(-1, 2)
+    uxy = np.ascontiguousarray(uxy, dtype=np.float32).reshape(-1, 2)
+    fid = np.ascontiguousarray(fid, dtype=np.int32)
+    uid = np.ascontiguousarray(uid, dtype=np.int32)
+    _check(load().rknn_snapshot_write(os.fsencode(path), _ptr(fxy), _ptr(fid), fxy.shape[0], _ptr(uxy),
+                                      _ptr(uid), uxy.shape[0]))
+
+
+def snapshot_read(path: str):
+    """(fxy, fid, uxy, uid) of a binary index snapshot (rknn_snapshot_read)."""
+    L = load()
+    p = [C.c_void_p() for _ in range(4)]
+    nf, nu = C.c_int64(), C.c_int64()
+    _check(L.rknn_snapshot_read(os.fsencode(path), C.byref(p[0]), C.byref(p[1]), C.byref(nf), C.byref(p[2]),
+                                C.byref(p[3]), C.byref(nu)))
+    try:
+        def arr(ptr, n, ct):
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ct)), shape=(n,)).copy() if n else np.zeros(0, np.dtype(ct))
+        fxy = arr(p[0], 2 * nf.value, C.c_float).reshape(-1, 2)
+        fid = arr(p[1], nf.value, C.c_int32)
+        uxy = arr(p[2], 2 * nu.value, C.c_float).reshape(-1, 2)
+        uid = arr(p[3], nu.value, C.c_int32)
+    finally:
+        for x in p:
+            L.rknn_snapshot_free(x)
+    return fxy, fid, uxy, uid
 
 
 class Index:
@@ -225,6 +263,17 @@ class Index:
     @classmethod
     def of(cls, ds, **kw):
         return cls(ds.fxy, ds.uxy, ds.fid, ds.uid, **kw)
+
+    @classmethod
+    def open(cls, path: str, **kw):
+        """Index over a binary snapshot's points (the same index
+        rknn_index_open builds)."""
+        fxy, fid, uxy, uid = snapshot_read(path)
+        return cls(fxy, uxy, fid, uid, **kw)
+
+    def save(self, path: str):
+        """Write the index's points as a binary snapshot (rknn_index_save)."""
+        _check(load().rknn_index_save(self.h, os.fsencode(path)))
 
     def close(self):
         if getattr(self, "h", None):

@@ -214,6 +214,35 @@ def test_fused_and_separate_verification_agree(engine, monkeypatch):
     assert all(np.array_equal(a, b) for a, b in zip(got["1"], got["0"]))
 
 
+def test_snapshot_index_gives_the_same_ids(engine, tmp_path):
+    """An index saved as a snapshot and reopened (rknn_index_save /
+    rknn_index_open, through the command line as well) answers as the
+    original."""
+    import subprocess
+    ds = datagen.uniform(2000, 30_000, seed=61, nq=12, k=4)
+    o = O.Oracle.of(ds)
+    idx = engine.Index.of(ds)
+    p = str(tmp_path / "idx.rkx")
+    idx.save(p)
+    fxy, fid, uxy, uid = engine.snapshot_read(p)
+    assert np.array_equal(fxy, ds.fxy) and np.array_equal(fid, ds.fid)
+    assert np.array_equal(uxy, ds.uxy) and np.array_equal(uid, ds.uid)
+    idx2 = engine.Index.open(p)
+    a = idx.query_batch(ds.queries, 4, "fp32")
+    b = idx2.query_batch(ds.queries, 4, "fp32")
+    for q, x, y in zip(ds.queries, a, b):
+        assert np.array_equal(x, y) and np.array_equal(x, o.query(int(q), 4)), int(q)
+    cli = os.path.join(os.path.dirname(engine.__file__), "rknn-gb300")
+    q = int(ds.queries[0])
+    r = subprocess.run([cli, "-if", p, "-k", "4", "-q", str(q), "--log", str(tmp_path / "log")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = np.loadtxt(tmp_path / "log" / f"fp64_k4_q{q}.txt", dtype=np.int64, ndmin=1)
+    assert np.array_equal(got, o.query(q, 4))
+    idx.close()
+    idx2.close()
+
+
 def test_flat_batches_into_page_locked_ids(engine):
     """query_batch_flat keeps one page-locked id buffer: from its second call
     the finalize kernel writes the ids into it directly.  Batches that fit,

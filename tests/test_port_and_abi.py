@@ -63,3 +63,37 @@ def test_cli_rejects_bad_arguments(engine, tmp_path):
     p.write_text("2\n0 1 1\n1 2\n")
     r = subprocess.run([cli, "-if", str(p)], capture_output=True, text=True)
     assert r.returncode == 1 and "Error parsing" in r.stderr
+
+
+def test_snapshot_round_trip_and_checks(engine, tmp_path):
+    """The binary snapshot (host code, no GPU): points written and read back
+    bit for bit; a flipped byte or a cut file is refused; the command line's
+    --save writes the same bytes as the library from the parsed text, and a
+    snapshot given as -if loads the same points."""
+    ds = datagen.uniform(300, 5000, seed=17)
+    p = str(tmp_path / "pts.rkx")
+    engine.snapshot_write(p, ds.fxy, ds.fid, ds.uxy, ds.uid)
+    fxy, fid, uxy, uid = engine.snapshot_read(p)
+    assert np.array_equal(fxy, ds.fxy) and np.array_equal(uxy, ds.uxy)
+    assert np.array_equal(fid, ds.fid) and np.array_equal(uid, ds.uid)
+    raw = bytearray(open(p, "rb").read())
+    assert raw[:8] == b"RKNNSNP1" and len(raw) == 8 + 8 + 16 + 12 * ds.nf + 12 * ds.nu + 8
+    bad = bytearray(raw)
+    bad[40] ^= 1
+    (tmp_path / "bad.rkx").write_bytes(bytes(bad))
+    with pytest.raises(engine.RkNNError):
+        engine.snapshot_read(str(tmp_path / "bad.rkx"))
+    (tmp_path / "cut.rkx").write_bytes(bytes(raw[:-20]))
+    with pytest.raises(engine.RkNNError):
+        engine.snapshot_read(str(tmp_path / "cut.rkx"))
+    # the command line: text in, --save out (it stops at the index build
+    # when there is no GPU, after loading and saving)
+    cli = os.path.join(REPO, "rt-rknn_gb300", "rknn-gb300")
+    txt = tmp_path / "pts.txt"
+    datagen.write_text(txt, ds)
+    r = subprocess.run([cli, "-if", str(txt), "-k", "3", "--no-log", "--save", str(tmp_path / "cli.rkx")],
+                       capture_output=True, text=True)
+    assert f"Loaded {ds.nf} facilities and {ds.nu} users." in r.stdout
+    assert open(tmp_path / "cli.rkx", "rb").read() == bytes(raw)
+    r = subprocess.run([cli, "-if", p, "-k", "3", "--no-log"], capture_output=True, text=True)
+    assert f"Loaded {ds.nf} facilities and {ds.nu} users." in r.stdout
