@@ -15,17 +15,17 @@
 // has k certified violations for all its users (__all_sync).
 //
 // Stage 2 (exact count).  Users that survive stage 1 go to a survivor list,
-// and recount_kernel counts each one exactly, one thread per survivor (many
-// independent chains of facility loads in flight): the facility cells
-// covering the disc of radius d(u,q) around u, row by row (one contiguous
-// range of the cell-sorted facility array per row, trimmed to the disc's
-// chord), counting d2(u,f) < d2(u,q) and stopping at k.  Each comparison is
-// decided in float (or double) with its error bound, and the undecided ones
-// by the exact expansion predicate.  Accepted users are appended with
-// warp-aggregated atomics (lanes grouped by query with __match_any_sync).
-// When the survivor list is full, the warp recounts its own survivors, the
-// whole warp scanning one survivor's rows at a time with
-// __ballot_sync/__popc.
+// and recount_kernel counts each one exactly, a warp (or a group of up to
+// eight warps, when warps outnumber survivors) per survivor: the facility
+// cells covering the disc of radius d(u,q) around u, row by row (one
+// contiguous range of the cell-sorted facility array per row, trimmed to the
+// disc's chord), 32 facilities a round, counting d2(u,f) < d2(u,q) and
+// stopping at k.  Each comparison is decided in float (or double) with its
+// error bound, and the undecided ones by the exact expansion predicate.
+// Accepted users are appended to their query's result region.  When the
+// survivor list is full, the warp counts its own survivors, one lane per
+// facility.  The item code itself lives in verify_item.cuh, shared with the
+// slice filter's fused verification.
 #include "verify_item.cuh"
 #include <climits>
 
@@ -285,13 +285,6 @@ __device__ __forceinline__ int group_exact_count(float ux, float uy, const QDesc
         group_barrier(bar, G * 32);      // the counter is read before the next survivor resets it
     }
     return cnt;
-}
-
-// One warp's exact count (a group of one).
-__device__ __forceinline__ int warp_exact_count(float ux, float uy, const QDesc& d, const VerifyArgs& A,
-                                                unsigned long long& fac, unsigned long long& rech)
-{
-    return group_exact_count(ux, uy, d, A, 1, 0, 0, nullptr, fac, rech);
 }
 
 // Exact recount of the listed survivors; accepted users are appended with
