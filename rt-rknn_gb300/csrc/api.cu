@@ -704,14 +704,24 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     mark(3);
     CK(launch_k(recount_kernel, ix->recount_grid, 256, 0, st, pdl, va));
     mark(4);
-    CK(launch_k(scan_counts_kernel, 1, 1024, 0, st, pdl, (const int*)w.d_res_count, (const int*)w.d_reg_len,
-                (const long long*)region_top(w), nq, w.d_out_off, (const int*)w.d_counters, c.io.off_host));
+    // the output offsets: in finalize itself for batches of up to
+    // FIN_SCAN_MAX slots, else by the scan kernel
+    FinScan fs;
+    if (nq <= FIN_SCAN_MAX) {
+        fs.on = 1;
+        fs.out_off_host = c.io.off_host;
+        fs.region_top = region_top(w);
+        fs.counters = w.d_counters;
+    } else {
+        CK(launch_k(scan_counts_kernel, 1, 1024, 0, st, pdl, (const int*)w.d_res_count, (const int*)w.d_reg_len,
+                    (const long long*)region_top(w), nq, w.d_out_off, (const int*)w.d_counters, c.io.off_host));
+    }
     mark(5);
     int* ids = c.io.ids ? c.io.ids : w.d_out;
     const long long ids_cap = c.io.ids ? c.io.ids_cap : w.pool_cap;
     CK(launch_k(finalize_kernel, (nq + FIN_WARPS - 1) / FIN_WARPS, 32 * FIN_WARPS, 0, st, pdl, w.d_pool,
                 (const long long*)w.d_cand_off, (const int*)w.d_reg_len, (const int*)w.d_res_count,
-                (const int*)w.d_out_off, ids, nq, ids_cap, w.d_zb[w.zb_next], w.zb_ints));
+                w.d_out_off, ids, nq, ids_cap, w.d_zb[w.zb_next], w.zb_ints, fs));
     mark(6);
     return RKNN_OK;
 }
@@ -1719,7 +1729,7 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     scan_counts_kernel<<<1, 1024, 0, st>>>(L.res_count, L.reg_len, L.region_top, 1, L.out_off, L.counters, nullptr);
     CK(cudaGetLastError());
     finalize_kernel<<<1, 32 * FIN_WARPS, 0, st>>>(L.pool, L.cand_off, L.reg_len, L.res_count, L.out_off, L.out, 1,
-                                                  L.pool_cap, nullptr, 0);
+                                                  L.pool_cap, nullptr, 0, FinScan{});
     CK(cudaGetLastError());
 
     QDesc d;

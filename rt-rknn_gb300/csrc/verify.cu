@@ -556,7 +556,7 @@ __device__ __forceinline__ void warp_sort_slot(const unsigned* src, unsigned* ds
 // pool region above that.
 __global__ void __launch_bounds__(32 * FIN_WARPS, 1)
 finalize_kernel(int* res_pool, const long long* cand_off, const int* reg_len, const int* res_count,
-                const int* out_off, int* out, int nq, long long out_cap, int* zero, long long zero_n)
+                int* out_off, int* out, int nq, long long out_cap, int* zero, long long zero_n, FinScan S)
 {
     // the next batch's counters (no kernel of this batch uses them), while
     // the predecessor drains
@@ -567,15 +567,62 @@ finalize_kernel(int* res_pool, const long long* cand_off, const int* reg_len, co
     __shared__ unsigned skeys[FIN_BCAP];
     __shared__ int big[FIN_WARPS];
     __shared__ int nbig;
+    __shared__ int s_part[FIN_WARPS];
+    __shared__ int s_off[FIN_WARPS];      // this block's slots' output offsets
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int first = blockIdx.x * FIN_WARPS;
     if (tid == 0) nbig = 0;
+    if (S.on) {
+        // stored ids of the slots before this block's (four loads in flight
+        // per thread)
+        int part = 0;
+        for (int i0 = tid; i0 < first; i0 += 4 * (int)blockDim.x) {
+            int v[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int i = i0 + j * (int)blockDim.x;
+                v[j] = i < first ? min(res_count[i], reg_len[i]) : 0;
+            }
+            part += v[0] + v[1] + v[2] + v[3];
+        }
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
+        if (lane == 0) s_part[w] = part;
+        __syncthreads();
+        if (w == 0) {
+            int base = lane < FIN_WARPS ? s_part[lane] : 0;
+            for (int o = 16; o > 0; o >>= 1) base += __shfl_xor_sync(FULL, base, o);
+            const int sj = first + lane;
+            const int nj = (lane < FIN_WARPS && sj < nq) ? min(res_count[sj], reg_len[sj]) : 0;
+            int incl = nj;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const int excl = base + incl - nj;
+            if (lane < FIN_WARPS) s_off[lane] = excl;
+            if (lane < FIN_WARPS && sj < nq) {
+                out_off[sj] = excl;
+                if (S.out_off_host) S.out_off_host[sj] = excl;
+            }
+            const int total = base + __shfl_sync(FULL, incl, 31);
+            if (blockIdx.x == gridDim.x - 1 && lane <= OFF_TAIL) {
+                // the total and the run's flags (as scan_counts_kernel)
+                const unsigned long long rt = (unsigned long long)*S.region_top;
+                const int tail[1 + OFF_TAIL] = {total, (int)(unsigned)(rt & 0xffffffffu), (int)(unsigned)(rt >> 32),
+                                                S.counters[2], S.counters[3]};
+                out_off[nq + lane] = tail[lane];
+                if (S.out_off_host) S.out_off_host[nq + lane] = tail[lane];
+            }
+        }
+    }
     __syncthreads();
-    const int s = blockIdx.x * FIN_WARPS + w;
+    const int s = first + w;
     if (s < nq) {
         const int n = min(res_count[s], reg_len[s]);
+        const int os = S.on ? s_off[w] : out_off[s];
         const unsigned* src = (const unsigned*)(res_pool + cand_off[s]);
-        unsigned* dst = (unsigned*)(out + out_off[s]);
-        if ((long long)out_off[s] + n > out_cap) {
+        unsigned* dst = (unsigned*)(out + os);
+        if ((long long)os + n > out_cap) {
             // past the output's capacity: left out (the batch fails on the host)
         } else if (n <= 32) {
             // stable rank: smaller keys, and equal keys in lower lanes
@@ -606,7 +653,7 @@ finalize_kernel(int* res_pool, const long long* cand_off, const int* reg_len, co
         const int t = big[bi];
         const int n = min(res_count[t], reg_len[t]);
         unsigned* src = (unsigned*)(res_pool + cand_off[t]);
-        unsigned* dst = (unsigned*)(out + out_off[t]);
+        unsigned* dst = (unsigned*)(out + (S.on ? s_off[t - first] : out_off[t]));
         if (n <= FIN_BCAP) {
             int P = 1;
             while (P < n) P <<= 1;

@@ -78,13 +78,26 @@ constexpr int OFF_TAIL = 4;
 __global__ void scan_counts_kernel(const int* res_count, const int* reg_len, const long long* region_top, int nq,
                                    int* out_off, const int* counters, int* out_off_host);
 
+// Output offsets computed by finalize_kernel itself (batches of up to
+// FIN_SCAN_MAX slots, which then need no scan_counts_kernel): each block sums
+// the stored ids of the slots before its own, writes its slots' offsets to
+// out_off (and out_off_host) and the last block the total and the run's
+// flags, as scan_counts_kernel does.
+constexpr int FIN_SCAN_MAX = 4096;
+struct FinScan {
+    int on = 0;
+    int* out_off_host = nullptr;
+    const long long* region_top = nullptr;
+    const int* counters = nullptr;
+};
+
 // one block per slot: sort the slot's results into out[out_off[s] ...]
 // out may be device-accessible host memory of out_cap ids: a slot whose range
 // would pass out_cap is left out (the caller sees the total and fails the
 // batch).  zero[0 .. zero_n) (another batch's counters, unused by this one)
 // is cleared for the next batch.
 __global__ void finalize_kernel(int* res_pool, const long long* cand_off, const int* reg_len, const int* res_count,
-                                const int* out_off, int* out, int nq, long long out_cap, int* zero,
-                                long long zero_n);
+                                int* out_off, int* out, int nq, long long out_cap, int* zero,
+                                long long zero_n, FinScan S);
 
 }  // namespace rknn
