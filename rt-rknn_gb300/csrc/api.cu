@@ -24,6 +24,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <tuple>
@@ -144,6 +145,10 @@ struct Workspace {
 
 }  // namespace
 
+namespace {
+struct BatchPlan;
+}
+
 struct rknn_index {
     int device = 0;
     cudaStream_t own_stream = nullptr, stream = nullptr;
@@ -170,6 +175,11 @@ struct rknn_index {
     int num_sms = 0;
     int recount_grid = 0;       // one wave of recount_kernel blocks
     bool pdl = true;            // programmatic dependent launch between the batch kernels
+    // the last uniform-k host batch's plan, reused by the next batch of the
+    // same size, mode and k (dropped when the grids or the verification's
+    // shape change)
+    std::unique_ptr<BatchPlan> plan_cache;
+    int plan_nq = 0, plan_mode = -1, plan_k = 0;
     bool fuse = true;           // FP32 slice batches: the filter verifies its own slots
                                 // (RKNN_FUSE=0 in the environment turns it off)
     // occupancy answers by (kernel, threads, dynamic shared memory): a batch's
@@ -928,9 +938,25 @@ rknn_status run_sync(rknn_index* ix, Ctx& c, const BatchPlan& b, bool graph = tr
     return fail(RKNN_ERR_CAPACITY, "result pool could not be sized");
 }
 
-rknn_status check_queries(rknn_index* ix, const int32_t* q, const int32_t* k, int nq, int* kmax)
+rknn_status check_queries(rknn_index* ix, const int32_t* q, const int32_t* k, int nq, int* kmax,
+                          bool* uniform = nullptr)
 {
+    // one pass of minima and maxima; the error message comes from the
+    // second loop only when a query is bad
+    int32_t qlo = INT32_MAX, qhi = INT32_MIN, klo = INT32_MAX, khi = INT32_MIN;
+    for (int i = 0; i < nq; ++i) {
+        qlo = std::min(qlo, q[i]);
+        qhi = std::max(qhi, q[i]);
+        klo = std::min(klo, k[i]);
+        khi = std::max(khi, k[i]);
+    }
+    if (nq > 0 && qlo >= 0 && (int64_t)qhi < ix->nf && klo > 0) {
+        *kmax = std::max(1, (int)khi);
+        if (uniform) *uniform = klo == khi;
+        return RKNN_OK;
+    }
     *kmax = 1;
+    if (uniform) *uniform = true;
     for (int i = 0; i < nq; ++i) {
         if (q[i] < 0 || q[i] >= ix->nf)
             return fail(RKNN_ERR_ARG, "query index " + std::to_string(q[i]) + " out of range [0, " +
@@ -945,6 +971,7 @@ rknn_status check_queries(rknn_index* ix, const int32_t* q, const int32_t* k, in
 // points: cell ids, stable radix sort, cell starts, per-cell facility boxes.
 rknn_status build_grids(rknn_index* ix, float fac_per_cell, float usr_per_cell)
 {
+    ix->plan_cache.reset();
     cudaStream_t st = ix->stream;
     CK(cudaStreamSynchronize(st));
     cudaFree(ix->d_fxy); cudaFree(ix->d_fidx); cudaFree(ix->d_fpos); cudaFree(ix->d_fstart);
@@ -1364,15 +1391,14 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
     if (mode != RKNN_MODE_FP32 && mode != RKNN_MODE_FP64) return fail(RKNN_ERR_ARG, "bad mode");
     if (nq == 0) { offsets[0] = 0; return RKNN_OK; }
     int kmax = 1;
-    rknn_status s = check_queries(ix, q, k, nq, &kmax);
+    bool uniform = true;
+    rknn_status s = check_queries(ix, q, k, nq, &kmax, &uniform);
     if (s != RKNN_OK) return s;
     std::lock_guard<std::mutex> lk(ix->mu);
     CK(cudaSetDevice(ix->device));
     ix->dev_nq = 0;     // the workspace now holds this batch
     // descending k: the longest zones start first, and each k class gets its
     // own zone launch
-    bool uniform = true;
-    for (int i = 1; i < nq && uniform; ++i) uniform = k[i] == k[0];
     std::vector<int> order, ksorted;
     if (!uniform) {
         order.resize(nq);
@@ -1381,7 +1407,22 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
         ksorted.resize(nq);
         for (int i = 0; i < nq; ++i) ksorted[i] = k[order[i]];
     }
-    const BatchPlan b = plan_batch(ix, nq, mode, !uniform, uniform ? nullptr : ksorted.data(), kmax);
+    BatchPlan fresh;
+    const BatchPlan* bp = nullptr;
+    if (uniform && ix->plan_cache && ix->plan_nq == nq && ix->plan_mode == mode && ix->plan_k == kmax) {
+        bp = ix->plan_cache.get();
+    } else {
+        fresh = plan_batch(ix, nq, mode, !uniform, uniform ? nullptr : ksorted.data(), kmax);
+        bp = &fresh;
+        if (uniform) {
+            ix->plan_cache = std::make_unique<BatchPlan>(fresh);
+            ix->plan_nq = nq;
+            ix->plan_mode = mode;
+            ix->plan_k = kmax;
+            bp = ix->plan_cache.get();
+        }
+    }
+    const BatchPlan& b = *bp;
     s = ensure_ws(ix->ws, nq, plan_caps(b), ix->ws.pool_cap);
     if (s != RKNN_OK) return s;
     Workspace& w = ix->ws;
@@ -2233,6 +2274,7 @@ extern "C" rknn_status rknn_index_tune(rknn_index* ix, const int32_t* q, const i
         for (int vw : vws) {
             ix->vupt = upt;
             ix->vwarps = vw;
+            ix->plan_cache.reset();
             double ms = 0;
             s = time_batch(ms);
             if (s != RKNN_OK) return s;
@@ -2250,6 +2292,7 @@ extern "C" rknn_status rknn_index_tune(rknn_index* ix, const int32_t* q, const i
     if (s != RKNN_OK) return s;
     ix->vupt = r.users_per_thread;
     ix->vwarps = r.verify_warps;
+    ix->plan_cache.reset();
     *result = r;
     return RKNN_OK;
 }
