@@ -97,3 +97,33 @@ def test_snapshot_round_trip_and_checks(engine, tmp_path):
     assert open(tmp_path / "cli.rkx", "rb").read() == bytes(raw)
     r = subprocess.run([cli, "-if", p, "-k", "3", "--no-log"], capture_output=True, text=True)
     assert f"Loaded {ds.nf} facilities and {ds.nu} users." in r.stdout
+
+
+def test_python_structs_match_the_header(engine, tmp_path):
+    """Every public struct of include/rknn_gpu.h has the size and field
+    offsets of its ctypes mirror in rknn.py (a C program built against the
+    header prints them)."""
+    import ctypes as C
+    mirrors = {"rknn_index_opts": engine.Opts, "rknn_query_stats": engine.Stats, "rknn_index_info": engine.Info,
+               "rknn_serve_opts": engine.ServeOpts, "rknn_serve_stats": engine.ServeStats,
+               "rknn_tune_result": engine.TuneResult}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "rknn_gpu.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c99", f"-I{os.path.join(REPO, 'include')}", str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        a, b, v = line.split()
+        got[(a, b)] = int(v)
+    for cname, py in mirrors.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
