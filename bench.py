@@ -7,7 +7,8 @@ Workload (the reference's headline configuration): 100,000 facilities and
 One step = one batch of 1,000 random facility queries through the engine:
 angular-slice filter, which at this batch size also verifies each query's
 users itself (fused) -> verification of left-over queries -> exact recount
-of the survivors -> result offsets -> finalize (one CUDA graph),
+of the survivors -> finalize, which also writes the result offsets (one
+CUDA graph),
 FP32-filtered predicates with exact fallback; result sets are bit-exact.
 Prints one JSON line (rank 0).
 
