@@ -127,3 +127,30 @@ def test_python_structs_match_the_header(engine, tmp_path):
         assert got[(cname, "size")] == C.sizeof(py), cname
         for fname, _ in py._fields_:
             assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def test_cli_parser_number_forms(engine, tmp_path):
+    """The command line's text parser (from_chars, with strtoll/strtod for
+    the forms from_chars does not take) reads ids and coordinates as the
+    reference's stream extraction does: signs, exponents, a leading '+',
+    hexadecimal floats, tabs and CR line ends; the points it saves as a
+    snapshot equal Python's parse rounded to float32."""
+    rows_f = [("0", "1.5", "2.25"), ("+1", "+3e2", "-4.5E-1"), ("2", "0x1.8p1", "7"), ("3", "1e-3", ".5")]
+    rows_u = [("10", "0.1", "0.2"), ("11", "-0", "1e+1"), ("+12", "123456.789", "3.")]
+    text = f"{len(rows_f)}\r\n" + "".join("\t".join(r) + "\r\n" for r in rows_f)
+    text += f"{len(rows_u)}\n" + "".join(" ".join(r) + "\n" for r in rows_u)
+    src = tmp_path / "forms.txt"
+    src.write_text(text)
+    cli = os.path.join(REPO, "rt-rknn_gb300", "rknn-gb300")
+    snap = tmp_path / "forms.rkx"
+    r = subprocess.run([cli, "-if", str(src), "-k", "1", "--no-log", "--save", str(snap)],
+                       capture_output=True, text=True)
+    assert "Loaded 4 facilities and 3 users." in r.stdout, r.stdout + r.stderr
+    fxy, fid, uxy, uid = engine.snapshot_read(str(snap))
+
+    def num(t):
+        return float.fromhex(t) if "0x" in t else float(t)
+
+    assert fid.tolist() == [int(r[0]) for r in rows_f] and uid.tolist() == [int(r[0]) for r in rows_u]
+    assert np.array_equal(fxy, np.array([[num(r[1]), num(r[2])] for r in rows_f], np.float32))
+    assert np.array_equal(uxy, np.array([[num(r[1]), num(r[2])] for r in rows_u], np.float32))
