@@ -234,7 +234,11 @@ rknn_status rknn_set_profiling(rknn_index* idx, int32_t on);
 
 /* Device time of each kernel of the last profiled call, in milliseconds:
  * ms[0] zone (or slice filter), ms[1] plan, ms[2] verify, ms[3] exact
- * recount of the survivors, ms[4] result offsets, ms[5] finalize. */
+ * recount of the survivors, ms[4] result offsets, ms[5] finalize.  A stage
+ * that the batch does not launch reads about 0: the plan when the slice
+ * filter verifies its own queries (FP32 batches of up to about 1200
+ * queries; ms[0] then includes that verification), the offsets for
+ * batches of up to 4096 queries (finalize computes them, in ms[5]). */
 rknn_status rknn_last_kernel_ms(rknn_index* idx, double* ms);
 
 /* ---- Serving: continuous batching over a resident index ----------------
