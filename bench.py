@@ -8,8 +8,10 @@ One step = one batch of 1,000 random facility queries through the engine:
 angular-slice filter, which at this batch size also verifies each query's
 users itself (fused) -> verification of left-over queries -> exact recount
 of the survivors -> finalize, which also writes the result offsets (one
-CUDA graph),
-FP32-filtered predicates with exact fallback; result sets are bit-exact.
+CUDA graph), FP32-filtered predicates with exact fallback.  Step i answers
+query set i mod 32 of a seeded pool; every step's results (device-timed and
+end-to-end) are checked against the exact oracle's fixture of that pool
+(tests/golden/oracle_config2.npz) outside the timed intervals.
 Prints one JSON line (rank 0).
 
   value      queries/s with the facility/user index and the query batch
@@ -19,6 +21,8 @@ Prints one JSON line (rank 0).
              buffers; ids land in a page-locked buffer): query ids H2D,
              result offsets and ids D2H, per step, L2 flushed (untimed)
              before every step
+  mismatches_vs_oracle  queries of the timed and end-to-end steps whose ids
+             differ from the oracle's
   roofline   the dominant kernel (the filter with its fused verification),
              timed live per launch with CUDA events in profiling mode,
              against HBM and against peak instruction issue;
@@ -28,22 +32,33 @@ Prints one JSON line (rank 0).
              issue (their bound there), HBM and FP32
   fp64_single_query  the plain form: one query per launch, FP64 predicates,
              rknn-inf's influence zone (the drop-in); p50/p99 latency
-  serving    open-loop Poisson arrivals through the continuous batcher
-  cpu_baseline  the C restatement of rknn-inf's query path (R-tree,
-             influence-zone filter + verification) on the host's cores,
-             over a bounded sample of the same workload
+  serving    open-loop Poisson arrivals through the continuous batcher, on
+             this workload and on the resident 1M-facility / 10M-user index
+             (k log-uniform in [1,64], 1k-100k requests/s)
+  cpu_baseline  the reference's own rknn-inf binary (built from its sources
+             into oracle/_ref) on the host's cores, one query per process as
+             the binary answers them, over a bounded sample of the same
+             workload; without the binary, the C restatement of its query
+             path (oracle/inf_port.c)
 
---impl reference times that CPU restatement alone (all host threads) on the
-same workload and prints the same JSON line with "impl": "reference".
+--impl reference times the reference's own CPU implementation alone (the
+rknn-inf binary, one process per host core, each answering one query of the
+step; the C restatement where the binary was not built) on the same workload
+and prints the same JSON line with "impl": "reference", beside the
+reference's other binaries on this host: rknn-naive at 1k/10k, and its two
+CUDA binaries, rknn-inf-gpu at this workload and rknn-naive-gpu at 1k/10k.
 """
 from __future__ import annotations
 
 import argparse
 import json
 import os
+import re
+import shutil
 import statistics
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -51,20 +66,21 @@ import numpy as np
 
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(REPO, "rt-rknn_gb300"))
+sys.path.insert(0, os.path.join(REPO, "tests", "golden"))
 
 METRIC = "RkNN queries/s (1M users,100k fac,k=10) FP32-filtered vs FP64; p99 ms"
 NF, NU, K, NQ = 100_000, 1_000_000, 10, 1000
+WORKLOAD = "uniform 100k facilities / 1M users, k=10, 1000 queries per step"
 
 # DRAM bytes (read + write) per launch of the slice filter with the fused
-# verification on this workload's 1000-query batch, from one ncu capture
-# (profiles/fused_slice_verify_config2_1k_queries.md)
+# verification on this workload's 1000-query batch, from one ncu capture of
+# that launch (the capture's commit is recorded with its summary)
 TRAFFIC = {"fused_slice_kernel": 4844032}
 # warp instructions per query of that kernel (two warps a query), same capture
 FUSED_INSTR_PER_QUERY = 21.87e6 / 1000
 # warp instructions per unit of work of the two kernels in a batch of SAT_NQ
 # queries of this workload, from one ncu capture (smsp__inst_executed.sum of
-# the launch over its queries or its half-plane evaluations;
-# profiles/slice_verify_config2_16k_queries.md)
+# the launch over its queries or its half-plane evaluations)
 SAT_NQ = 16384
 INSTR = {"slice_kernel_per_query": 164.89e6 / 16384, "verify_kernel_per_eval": 100.98e6 / 175826300}
 
@@ -130,7 +146,116 @@ class Clocks:
 
 def dataset():
     import datagen
-    return datagen.uniform(NF, NU, seed=2, nq=NQ, k=K)
+    return datagen.config(2)
+
+
+def query_pool(ds, nq):
+    """Step i answers pool[i % len(pool)]; the 1000-query pool is the one the
+    oracle fixture covers."""
+    import config_fixtures as CF
+    if nq == CF.BENCH_NQ:
+        return CF.bench_query_sets(ds), True
+    rng = np.random.default_rng(17)
+    return [rng.choice(ds.nf, size=nq, replace=nq > ds.nf).astype(np.int32) for _ in range(8)], False
+
+
+class OracleCheck:
+    """Counts queries whose ids differ from the oracle fixture's (per query
+    size and digest of the sorted ids)."""
+
+    def __init__(self, ds):
+        import config_fixtures as CF
+        self.CF = CF
+        fx = CF.load("config2")
+        self.ok = CF.data_sha256(ds) == fx["data_sha256"]
+        self.fx = fx
+        self.checked = 0
+        self.mismatches = 0
+
+    def add(self, set_index, ids, offsets):
+        if not self.ok:
+            return
+        rows = self.CF.bench_set_rows(set_index % self.CF.BENCH_SETS)
+        cnt, dig = self.CF.digests(ids, offsets)
+        bad = (cnt != self.fx["count"][rows]) | (dig != self.fx["digest"][rows])
+        self.checked += int(cnt.shape[0])
+        self.mismatches += int(bad.sum())
+
+    def add_one(self, set_index, slot, ids):
+        if not self.ok:
+            return
+        row = self.CF.bench_set_rows(set_index % self.CF.BENCH_SETS).start + slot
+        self.checked += 1
+        self.mismatches += int(ids.shape[0] != self.fx["count"][row]
+                               or self.CF.ids_digest(ids) != int(self.fx["digest"][row]))
+
+
+class _CudaArray:
+    """A device int32 array as __cuda_array_interface__ (read by torch)."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (int(n),), "typestr": "<i4", "data": (int(ptr), True),
+                                         "version": 3, "strides": None}
+
+
+def device_results_to_host(idx, nq, device):
+    """The last device batch's (ids, offsets), copied to the host."""
+    import torch
+    ids_p, off_p = idx.device_results()          # synchronizes the index's stream
+    off = torch.as_tensor(_CudaArray(off_p, nq + 1), device=device).cpu().numpy().astype(np.int64)
+    n = int(off[-1])
+    ids = torch.as_tensor(_CudaArray(ids_p, max(n, 1)), device=device)[:n].cpu().numpy()
+    return ids, off
+
+
+# ---------------------------------------------------------------- reference
+REF_DIR = os.path.join(REPO, "oracle", "_ref")
+_NUM = r"([-+0-9.eE]+)"
+
+
+def ref_binary(name):
+    """Path of a reference binary built for this host, or None."""
+    p = os.path.join(REF_DIR, name)
+    if not (os.path.isfile(p) and os.access(p, os.X_OK)):
+        return None
+    try:
+        subprocess.run([p, "-h"], capture_output=True, timeout=20)
+    except (OSError, subprocess.TimeoutExpired):
+        return None                               # not runnable here (other architecture)
+    return p
+
+
+def parse_ref(out: str) -> dict:
+    r = {}
+    for key, pat in (("total_s", r"Total time: " + _NUM), ("build_s", r"R\*-tree is built in " + _NUM),
+                     ("search_s", r"completed in " + _NUM), ("filter_s", r"Filtering time: " + _NUM),
+                     ("verify_s", r"Verification time(?: \(\w+\))?: " + _NUM), ("found", r"Found (\d+) RkNN")):
+        m = re.search(pat, out)
+        if m:
+            r[key] = float(m.group(1))
+    return r
+
+
+def run_ref_procs(binary, path, qs, k, parallel, extra=()):
+    """Runs binary once per query (qs), at most `parallel` processes at a
+    time; returns the parsed outputs with each process's wall time."""
+    out, pending = [], list(qs)
+    running = []
+    while pending or running:
+        while pending and len(running) < parallel:
+            q = pending.pop(0)
+            p = subprocess.Popen([binary, "-if", path, "-k", str(k), "-q", str(int(q)), *extra],
+                                 stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True,
+                                 errors="replace")
+            running.append((q, p, time.perf_counter()))
+        q, p, t0 = running.pop(0)
+        so, se = p.communicate()
+        r = parse_ref(so)
+        r.update(q=int(q), rc=p.returncode, wall_s=time.perf_counter() - t0)
+        if p.returncode != 0 or "total_s" not in r and "search_s" not in r:
+            r["error"] = (se or so)[-300:]
+        out.append(r)
+    return out
 
 
 def cpu_port_run(ds, nq_sample, nthreads, seed=5):
@@ -145,6 +270,25 @@ def cpu_port_run(ds, nq_sample, nthreads, seed=5):
     cnt = port.query_many(qs, K, nthreads=nthreads)
     dt = time.perf_counter() - t0
     return nq_sample / dt, dt, int(cnt.sum())
+
+
+def write_workload_text(ds, tmp, name="config2.txt", integer=False):
+    import datagen
+    p = os.path.join(tmp, name)
+    datagen.write_text(p, ds, integer=integer)
+    return p
+
+
+def ref_inf_sample(ds, path, nproc, seed):
+    """One bounded sample of the reference's rknn-inf: nproc processes at
+    once, one random query each.  Returns the processes' results."""
+    rng = np.random.default_rng(seed)
+    qs = rng.choice(ds.nf, size=nproc, replace=False)
+    res = run_ref_procs(ref_binary("rknn-inf"), path, qs, K, nproc)
+    bad = [r for r in res if "error" in r]
+    if bad:
+        raise RuntimeError(f"rknn-inf failed: {bad[0]['error']}")
+    return res
 
 
 def dist_env():
@@ -167,36 +311,149 @@ def replicas_throughput(dev_s: float, ws: int, units: int, device: str = "cpu") 
     return ws * units / dev_s
 
 
+def reference_suite(ds, tmp, path2, nproc):
+    """The reference's other binaries on this host, beside the timed arm:
+    rknn-naive at 1k/10k (integer twin: it reads integer coordinates), and
+    its CUDA binaries rknn-inf-gpu (this workload) and rknn-naive-gpu
+    (1k/10k integer twin; its |U|x|F| matrix does not fit at this workload)."""
+    import datagen
+    out = {}
+    c1 = datagen.uniform(1000, 10000, seed=1, nq=10, k=5, integer=True)
+    p1 = write_workload_text(c1, tmp, "config1_int.txt", integer=True)
+    nb = ref_binary("rknn-naive")
+    if nb:
+        res = run_ref_procs(nb, p1, c1.queries, 5, nproc)
+        ok = [r["search_s"] for r in res if "search_s" in r]
+        out["rknn_naive_1k10k_int_k5"] = {"queries": len(ok), "mean_s_per_query": statistics.mean(ok),
+                                         "queries_per_s_1core": 1.0 / statistics.mean(ok),
+                                         "processes_at_once": nproc}
+    g = ref_binary("rknn-naive-gpu")
+    if g:
+        res = run_ref_procs(g, p1, c1.queries[:5], 5, 1, extra=("--gpu",))
+        ok = [r["search_s"] for r in res if "search_s" in r]
+        out["rknn_naive_gpu_1k10k_int_k5"] = {"queries": len(ok), "errors": len(res) - len(ok),
+                                             "mean_s_per_query": statistics.mean(ok) if ok else None,
+                                             "queries_per_s": 1.0 / statistics.mean(ok) if ok else None}
+    g = ref_binary("rknn-inf-gpu")
+    if g:
+        rng = np.random.default_rng(77)
+        res = run_ref_procs(g, path2, rng.choice(ds.nf, 4, replace=False), K, 2)
+        ok = [r for r in res if "total_s" in r]
+        out["rknn_inf_gpu_100k1M_k10"] = {
+            "queries": len(ok), "errors": len(res) - len(ok),
+            "mean_total_s": statistics.mean(r["total_s"] for r in ok) if ok else None,
+            "mean_verify_s": statistics.mean(r.get("verify_s", 0.0) for r in ok) if ok else None,
+            "queries_per_s": 1.0 / statistics.mean(r["total_s"] for r in ok) if ok else None,
+            "note": "filter on the CPU, verification of all users on the GPU per query (cudaMalloc, "
+                    "copies, one thread per user); Total time as the binary prints it"}
+    return out
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
     ds = dataset()
     nthreads = os.cpu_count() or 1
-    per_step = NQ
-    for _ in range(args.warmup):
-        cpu_port_run(ds, per_step, nthreads, seed=99)
-    times = []
-    for s in range(args.steps):
-        qps, dt, _ = cpu_port_run(ds, per_step, nthreads, seed=1000 + s)
-        times.append(dt)
-    tot = sum(times)
-    value = per_step * args.steps / tot
+    tmp = tempfile.mkdtemp(prefix="rknn_ref_")
+    try:
+        binary = ref_binary("rknn-inf")
+        extra = {}
+        if binary:
+            path = write_workload_text(ds, tmp)
+            # warm-up steps (untimed); the first runs one process alone: the
+            # uncontended single-core query time and the R*-tree build
+            alone = ref_inf_sample(ds, path, 1, seed=99)[0]
+            for w in range(1, args.warmup):
+                ref_inf_sample(ds, path, nthreads, seed=99 + w)
+            per_q, builds, walls = [], [], []
+            for s in range(args.steps):
+                res = ref_inf_sample(ds, path, nthreads, seed=1000 + s)
+                per_q.append([r["total_s"] for r in res])
+                builds += [r["build_s"] for r in res]
+                walls += [r["wall_s"] for r in res]
+            qn = sum(len(x) for x in per_q)
+            busy = sum(sum(x) for x in per_q)
+            value = nthreads * qn / busy
+            ms_step = 1e3 * busy / nthreads / args.steps
+            kind = "reference"
+            sample = (f"{nthreads} rknn-inf processes per step, one random query each (k=10); value = "
+                      f"{nthreads} cores / mean per-query Total time (filter + verification, the "
+                      f"binary's own timer; load and R*-tree build excluded, as the binary reports it)")
+            extra = {"reference_binary": "rknn-inf (reference sources, g++ -O2)",
+                     "single_core_alone": {"total_ms": 1e3 * alone["total_s"],
+                                           "queries_per_s": 1.0 / alone["total_s"],
+                                           "rtree_build_s": alone.get("build_s"),
+                                           "load_s": alone["wall_s"] - alone.get("build_s", 0) - alone["total_s"]},
+                     "all_cores": {"processes": nthreads, "mean_total_ms": 1e3 * busy / qn,
+                                   "queries_per_s": value,
+                                   "rtree_build_s_mean": statistics.mean(builds),
+                                   "process_wall_s_mean": statistics.mean(walls)}}
+            if not args.no_ref_suite:
+                extra["reference_other_binaries"] = reference_suite(ds, tmp, path, nthreads)
+        else:
+            for _ in range(args.warmup):
+                cpu_port_run(ds, NQ, nthreads, seed=99)
+            times = []
+            for s in range(args.steps):
+                _, dt, _ = cpu_port_run(ds, NQ, nthreads, seed=1000 + s)
+                times.append(dt)
+            busy = sum(times)
+            value = NQ * args.steps / busy
+            ms_step = 1e3 * busy / args.steps
+            kind = "port"
+            sample = (f"{NQ} queries per step, C restatement of rknn-inf (R-tree, influence zone + "
+                      f"verification) on {nthreads} threads (the reference binary was not built here)")
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
     line = {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded uniform float32, the reference's text format values)",
         "impl": "reference",
-        "config": {"workload": "uniform 100k facilities / 1M users, k=10, 1000 queries per step",
-                   "nf": NF, "nu": NU, "k": K, "queries_per_step": per_step},
-        "cpu_baseline": {"value": value, "unit": "queries/s", "cores": nthreads, "kind": "port",
-                         "sample": f"{per_step} queries per step, rknn-inf restatement (R-tree, "
-                                   f"influence zone + verification) on {nthreads} threads"},
+        "config": {"workload": WORKLOAD, "nf": NF, "nu": NU, "k": K, "queries_per_step": NQ},
+        "cpu_baseline": {"value": value, "unit": "queries/s", "cores": nthreads, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    line.update(extra)
     print(json.dumps(line), flush=True)
     return 0
+
+
+def serving_config5(rknn, device, modes=("fp32", "fp64")):
+    """The serving workload: resident 1M facilities / 10M users, open-loop
+    Poisson arrivals at 1k-100k requests/s, k log-uniform in [1,64] (the
+    oracle fixture's 2000 requests, cycled); result sizes are checked
+    against the fixture."""
+    import datagen
+    import config_fixtures as CF
+    ds5 = datagen.config(5)
+    qs, ks = CF.config5_requests(ds5)
+    fx = CF.load("config5")
+    check = CF.data_sha256(ds5) == fx["data_sha256"]
+    out = {"workload": "1M facilities / 10M users resident, Poisson arrivals, k log-uniform in [1,64]"}
+    size_mismatches = 0
+    with rknn.Index.of(ds5, device=device) as idx5:
+        with rknn.Server(idx5, slots=3, max_batch=2048) as srv:
+            srv.replay(qs[:500], ks[:500], modes[0], np.linspace(0, 0.01, 500))     # warm
+            srv.stats(reset=True)
+            for rate, n in ((1e3, 1000), (1e4, 4000), (5e4, 8000), (1e5, 10000)):
+                rng = np.random.default_rng(int(rate))
+                arrival = np.cumsum(rng.exponential(1.0 / rate, n))
+                sel = np.arange(n) % qs.shape[0]
+                for mode in modes:
+                    _, nr = srv.replay(qs[sel], ks[sel], mode, arrival)
+                    st = srv.stats(reset=True)
+                    if check:
+                        size_mismatches += int((nr != fx["count"][sel]).sum())
+                    out[f"{mode}@{int(rate)}"] = {"offered_qps": rate, "requests": n,
+                                                  "throughput_qps": st["throughput_qps"],
+                                                  "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                                                  "mean_batch": st["mean_batch"],
+                                                  "max_inflight": st["max_inflight"]}
+    out["result_size_mismatches_vs_oracle"] = size_mismatches if check else None
+    return out
 
 
 def run_ours(args):
@@ -208,6 +465,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
     build.build()
     ds = dataset()
     # the chosen form: batched, FP32-filtered predicates, default candidate
@@ -217,31 +475,30 @@ def run_ours(args):
     stream = torch.cuda.Stream(device=local)
     idx.set_stream(stream.cuda_stream)
     idx_inf.set_stream(stream.cuda_stream)
-    rng = np.random.default_rng(17 + rank)
     nsteps = args.steps
-    qsets = [rng.choice(ds.nf, size=NQ, replace=False).astype(np.int32)
-             for _ in range(nsteps + args.warmup)]
+    pool, checkable = query_pool(ds, NQ)
+    qsets = [pool[i % len(pool)] for i in range(nsteps + args.warmup)]
     ks = np.full(NQ, K, np.int32)
+    orc = OracleCheck(ds) if checkable else None
 
-    # correctness of the timed configuration (host path, sizes the pools):
-    # FP32 and FP64 predicates, both filters, give the same id sets
+    # FP32 and FP64 predicates, both filters, give the same id sets (extra
+    # information beside the oracle check; also sizes the pools)
     res = idx.query_batch(qsets[0], ks, "fp32")
     res64 = idx.query_batch(qsets[0], ks, "fp64")
     res64_inf = idx_inf.query_batch(qsets[0][:100], ks[:100], "fp64")
-    mismatches = sum(not np.array_equal(a, b) for a, b in zip(res, res64))
-    mismatches += sum(not np.array_equal(a, b) for a, b in zip(res[:100], res64_inf))
-    assert mismatches == 0
+    mism_modes = sum(not np.array_equal(a, b) for a, b in zip(res, res64))
+    mism_modes += sum(not np.array_equal(a, b) for a, b in zip(res[:100], res64_inf))
 
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
-    d_qs = [torch.from_numpy(q).to(f"cuda:{local}") for q in qsets]
-    d_k = torch.from_numpy(ks).to(f"cuda:{local}")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    d_qs = [torch.from_numpy(q).to(dev) for q in pool]
+    d_k = torch.from_numpy(ks).to(dev)
 
     def step(i, ev=None):
         with torch.cuda.stream(stream):
             flush.fill_(float(i))
             if ev:
                 ev[0].record(stream)
-            idx.query_batch_device(d_qs[i].data_ptr(), d_k.data_ptr(), NQ, K, "fp32")
+            idx.query_batch_device(d_qs[i % len(pool)].data_ptr(), d_k.data_ptr(), NQ, K, "fp32")
             if ev:
                 ev[1].record(stream)
 
@@ -253,24 +510,31 @@ def run_ours(args):
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    got = []
     with Clocks(local) as clk:
         t0 = time.perf_counter()
         for i in range(nsteps):
             step(args.warmup + i, evs[i])
+            if orc:
+                # after the step's closing event: outside its timed interval
+                got.append((args.warmup + i, device_results_to_host(idx, NQ, dev)))
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     if ws > 1:
         torch.distributed.barrier()
     step_ms = [a.elapsed_time(b) for a, b in evs]
-    value = replicas_throughput(sum(step_ms) / 1e3, ws, NQ * nsteps, f"cuda:{local}")
+    value = replicas_throughput(sum(step_ms) / 1e3, ws, NQ * nsteps, dev)
     dev_s = ws * NQ * nsteps / value
+    for si, (ids, off) in got:
+        orc.add(si % len(pool), ids, off)
 
     # ---- end to end through the C ABI with host buffers ------------------
     e2e_times, h2d, d2h = [], 0, 0
     idx.query_batch_flat(qsets[0], ks, "fp32")                      # sizes the output buffers
     idx.query_batch_flat(qsets[1], ks, "fp32")                      # warm: ids written in place from now on
     for i in range(nsteps):
-        q = qsets[args.warmup + i]
+        si = (args.warmup + i) % len(pool)
+        q = pool[si]
         with torch.cuda.stream(stream):
             flush.fill_(float(-i))                                  # L2 flushed between steps, untimed
         stream.synchronize()
@@ -279,17 +543,21 @@ def run_ours(args):
         e2e_times.append(time.perf_counter() - t1)
         h2d = q.nbytes + ks.nbytes
         d2h = 4 * (NQ + 1) + 4 * int(ids.shape[0])
+        if orc:
+            orc.add(si, ids, offs)
     e2e = NQ / statistics.mean(e2e_times) * ws
 
     # ---- plain FP64 single-query form (one query per launch, influence zone)
-    single = qsets[0][:200]
+    single = pool[0][:200]
     lat = []
     for q in single[:10]:
         idx_inf.query(int(q), K, "fp64")
-    for q in single:
+    for j, q in enumerate(single):
         t1 = time.perf_counter()
-        idx_inf.query(int(q), K, "fp64")
+        r1 = idx_inf.query(int(q), K, "fp64")
         lat.append(1e3 * (time.perf_counter() - t1))
+        if orc:
+            orc.add_one(0, j, r1)
     fp64_single_qps = 1e3 / statistics.mean(lat)
     lat.sort()
     p50 = lat[len(lat) // 2]
@@ -304,6 +572,7 @@ def run_ours(args):
         e1.record(stream)
     torch.cuda.synchronize()
     fp64_batch_qps = NQ / (e0.elapsed_time(e1) / 1e3)
+
     # the influence-zone filter batched in FP32 (same device timing)
     def dev_qps(ix, mode, reps=3):
         ms = []
@@ -329,11 +598,12 @@ def run_ours(args):
         for mode in ("fp32", "fp64"):
             srv.replay(sq[:2000], K, mode, arrival[:2000])            # warm the slots
             srv.stats(reset=True)
-            lat_s, _ = srv.replay(sq, K, mode, arrival)
+            srv.replay(sq, K, mode, arrival)
             st_s = srv.stats(reset=True)
             serving[mode] = {"offered_qps": srv_rate, "throughput_qps": st_s["throughput_qps"],
                              "p50_ms": st_s["p50_ms"], "p99_ms": st_s["p99_ms"],
                              "mean_batch": st_s["mean_batch"], "max_inflight": st_s["max_inflight"]}
+    serving5 = None if args.no_serving5 else serving_config5(rknn, local)
 
     # ---- rooflines (live, profiling mode: per-kernel CUDA events) ----------
     idx.set_profiling(True)
@@ -434,35 +704,61 @@ def run_ours(args):
                                  "fp32_frac": 4 * sst["plane_evals"] / sv / 1e12 / fp32_peak,
                                  "hbm_frac": (8 * sst["candidates"] + 16 * sst["bisectors"] + 4 * sst["results"])
                                              / sv / (hbm_peak * 1e9)},
-               "note": "warp instructions per unit from ncu (profiles/slice_verify_config2_16k_queries.md)"}
+               "note": "warp instructions per unit of work from one ncu capture of this batch"}
 
     # ---- CPU baseline (rank 0, N=1 only) ---------------------------------
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         nthreads = os.cpu_count() or 1
+        if ref_binary("rknn-inf"):
+            tmp = tempfile.mkdtemp(prefix="rknn_ref_")
+            try:
+                path = write_workload_text(ds, tmp)
+                t0 = time.perf_counter()
+                res = []
+                while time.perf_counter() - t0 < args.cpu_seconds:
+                    res += ref_inf_sample(ds, path, nthreads, seed=5000 + len(res))
+            finally:
+                shutil.rmtree(tmp, ignore_errors=True)
+            tot = [r["total_s"] for r in res]
+            cpu = {"value": nthreads / statistics.mean(tot), "unit": "queries/s", "cores": nthreads,
+                   "kind": "reference",
+                   "sample": f"{len(res)} random facility queries at k=10, rknn-inf binary, {nthreads} "
+                             f"processes at once, one query each; value = {nthreads} / mean per-query Total "
+                             f"time ({1e3 * statistics.mean(tot):.3f} ms; R*-tree build "
+                             f"{statistics.mean(r['build_s'] for r in res):.1f} s per process, excluded)"}
         sample = args.cpu_sample
         qps, dt, _ = cpu_port_run(ds, sample, nthreads)
-        cpu = {"value": qps, "unit": "queries/s", "cores": nthreads, "kind": "port",
-               "sample": f"{sample} random facility queries at k=10 ({dt:.1f} s on {nthreads} threads), "
-                         "rknn-inf restatement: R-tree, influence-zone filter, verification"}
+        port = {"value": qps, "unit": "queries/s", "cores": nthreads, "kind": "port",
+                "sample": f"{sample} random facility queries at k=10 ({dt:.1f} s on {nthreads} threads), "
+                          "rknn-inf restatement: R-tree, influence-zone filter, verification"}
+        if cpu:
+            cpu["port"] = port
+        else:
+            cpu = port
 
     line = {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws,
         "steps": nsteps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / nsteps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded uniform float32 in [0,1000]^2)",
-        "config": {"workload": "uniform 100k facilities / 1M users, k=10, 1000 queries per step",
+        "config": {"workload": WORKLOAD,
                    "nf": NF, "nu": NU, "k": K, "queries_per_step": NQ, "mode": "fp32 batched",
                    "filter": "angular slices (rknn-slice rule, 32 slices); plain form: influence zone",
                    "l2": "256 MB flush before each timed step", "parallelism": f"replicas x{ws}"},
         "wall_s": wall,
         "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": 5 * nsteps,
+        "mismatches_vs_oracle": orc.mismatches if orc and orc.ok else None,
+        "checked_vs_oracle": (f"{orc.checked} query results (every timed device step, every end-to-end "
+                              f"step, the plain form's queries) against the exact oracle's fixture"
+                              if orc and orc.ok else "not checked (no fixture for this batch size)"),
         "fp64_single_query": {"qps": fp64_single_qps, "p50_ms": p50, "p99_ms": p99,
                               "filter": "influence zone (rknn-inf rules)"},
         "fp64_batched_qps": fp64_batch_qps,
         "inf_zone_fp32_batched_qps": inf_batch_qps,
         "serving": dict(serving, workload=f"{srv_n} Poisson requests at {srv_rate:.0f}/s, k={K}"),
+        "serving_config5": serving5,
         "speedup_fp32_batched_vs_fp64_single": value / ws / fp64_single_qps,
         "roofline": roof,
         "roofline_other": other,
@@ -472,8 +768,8 @@ def run_ours(args):
                                         "candidates", "plane_evals", "survivors", "fac_checks",
                                         "rechecks", "results", "overflow")},
         "recheck_fraction": st["rechecks"] / max(1, st["fac_checks"]),
-        "mismatches_fp32_vs_fp64": mismatches,
-        "mismatches_checked": f"{NQ} queries FP32 vs FP64 (default filter) + 100 vs FP64 influence zone",
+        "mismatches_fp32_vs_fp64": mism_modes,
+        "mismatches_fp32_vs_fp64_checked": f"{NQ} queries FP32 vs FP64 (default filter) + 100 vs FP64 influence zone",
         "clocks": clk.summary(),
     }
     if cpu:
@@ -492,8 +788,13 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-sample", type=int, default=400000)
+    ap.add_argument("--cpu-sample", type=int, default=400000, help="queries of the C restatement's timing")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="seconds of reference-binary rounds in the CPU baseline")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ref-suite", action="store_true",
+                    help="reference arm: skip the reference's other binaries")
+    ap.add_argument("--no-serving5", action="store_true", help="skip the 1M/10M serving workload")
     ap.add_argument("--no-saturation", action="store_true", help="skip the 16384-query saturation batch")
     ap.add_argument("--queries", type=int, default=NQ,
                     help="queries per step (default 1000, the headline workload; larger batches for profiling)")

@@ -174,9 +174,12 @@ rknn_status rknn_query(rknn_index* idx, int32_t q_index, int32_t k, int32_t mode
  * at most about 2 million candidate users for the query (otherwise
  * RKNN_ERR_CAPACITY; use rknn_query).  The first call on a device looks up
  * the array's device address; make that first call before any stream
- * capture.  All calls share the array: they are serialized by a process-wide
- * lock and finish before returning (calls that overlapped on the GPU would
- * race on it).  The index is built beforehand by rknn_index_create. */
+ * capture.  Creating an index on a device drops that cached address (after
+ * a cudaDeviceReset every index must be created again anyway), so the next
+ * call looks it up once more.  All calls share the array: they are
+ * serialized by a process-wide lock and leave the GPU idle before
+ * returning, on failure too (calls that overlapped on the GPU would race on
+ * it).  The index is built beforehand by rknn_index_create. */
 rknn_status rknn_query_noalloc(rknn_index* idx, int32_t q_index, int32_t k, int32_t mode,
                                int32_t* out_ids, int64_t cap, int64_t* n_out);
 

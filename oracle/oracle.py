@@ -47,6 +47,13 @@ def lib():
         L.orc_query_brute.restype = C.c_int
         L.orc_query_brute.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
                                       C.c_int64, C.c_int32, C.c_void_p]
+        L.orc_query_many.restype = C.c_void_p
+        L.orc_query_many.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int32]
+        L.orc_many_pairs.restype = C.c_int64
+        L.orc_many_pairs.argtypes = [C.c_void_p]
+        L.orc_many_fetch.restype = C.c_int
+        L.orc_many_fetch.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_many_free.argtypes = [C.c_void_p]
         for name in ("orc_sign_d2diff", "orc_sign_d2diff_expansion"):
             fn = getattr(L, name)
             fn.restype = C.c_int
@@ -100,6 +107,31 @@ class Oracle:
         """Sorted user ids of RkNN_k(q)."""
         f = self.flags(q, k, tie)
         return np.sort(self.uid[np.nonzero(f)[0]])
+
+    def query_many(self, qs, ks):
+        """All queries (qs[s], ks[s]) at once, evaluated user by user
+        (orc_query_many): (offsets[nq+1], ids) with the sorted result ids of
+        slot s in ids[offsets[s]:offsets[s+1]]."""
+        qs = np.ascontiguousarray(qs, dtype=np.int64)
+        ks = np.ascontiguousarray(np.broadcast_to(np.asarray(ks, np.int32), qs.shape), dtype=np.int32)
+        L = lib()
+        r = L.orc_query_many(self.h, qs.ctypes.data, ks.ctypes.data, qs.shape[0], self.nthreads)
+        if not r:
+            raise ValueError("oracle batch rejected (bad query or out of memory)")
+        try:
+            n = int(L.orc_many_pairs(r))
+            off = np.zeros(qs.shape[0] + 1, np.int64)
+            users = np.zeros(max(n, 1), np.int32)
+            if L.orc_many_fetch(r, off.ctypes.data, users.ctypes.data) != 0:
+                raise ValueError("oracle batch fetch failed")
+        finally:
+            L.orc_many_free(r)
+        ids = self.uid[users[:n]]
+        if not np.all(np.diff(self.uid) > 0):
+            # users come out in input order: sort each slot's ids
+            slot = np.repeat(np.arange(qs.shape[0]), np.diff(off))
+            ids = ids[np.lexsort((ids, slot))]
+        return off, ids
 
     def count_closer(self, u: int, q: int, cap: int = 1 << 30) -> int:
         return int(lib().orc_count_closer(self.h, int(u), int(q), int(cap)))

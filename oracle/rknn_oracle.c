@@ -357,3 +357,281 @@ int orc_query_brute(const float *fxy, int64_t nf, const float *uxy, int64_t nu,
     }
     return ORC_OK;
 }
+
+/* ------------------------------------------------- many queries, user-major
+ *
+ * The same predicate evaluated user by user, for a whole query list at once
+ * (the fixture generator's form: tens of thousands of queries over millions
+ * of users, where the query-major loop above costs O(|U|) per query).
+ *
+ * For a user u and a facility f let c_f(u) = #{ g : d2(u,g) < d2(u,f) }
+ * (g = f never counts, so this equals the count over g != f).  Then
+ *
+ *     u in RkNN_k(q)  <=>  c_q(u) < k
+ *
+ * which is rknn-naive's test (rknn-naive/rknn.cpp:169-198, q among the
+ * first k) under the strict-< rule.  Every facility with c_f(u) < K lies
+ * within u's K-th smallest facility distance d_K(u) (K facilities at
+ * distance <= d_K are all strictly nearer than anything farther), so for
+ * K = the largest k of the list it is enough to collect, by grid rings
+ * around u, every facility up to d_K(u), rank them exactly, and add u to
+ * every query slot s whose facility has c < k_s.  The counts are exact for
+ * every collected facility within d_K(u); a collected facility beyond it
+ * has a computed count >= K, as its true count, so it is never reported.
+ * Ranks are taken in double precision where they are clear and by the exact
+ * predicate above (sign_d2diff) inside a band around each distance. */
+
+typedef struct {
+    double d2;
+    int32_t f;
+} orc_cand;
+
+static int cand_cmp(const void *a, const void *b)
+{
+    double x = ((const orc_cand *)a)->d2, y = ((const orc_cand *)b)->d2;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+typedef struct {
+    int32_t *slot, *user;
+    int64_t n, cap;
+} orc_pairs;
+
+static int pairs_push(orc_pairs *p, int32_t s, int32_t u)
+{
+    if (p->n == p->cap) {
+        int64_t nc = p->cap ? 2 * p->cap : 4096;
+        int32_t *ns = (int32_t *)realloc(p->slot, sizeof(int32_t) * nc);
+        if (!ns) return 0;
+        p->slot = ns;
+        int32_t *nu = (int32_t *)realloc(p->user, sizeof(int32_t) * nc);
+        if (!nu) return 0;
+        p->user = nu;
+        p->cap = nc;
+    }
+    p->slot[p->n] = s;
+    p->user[p->n] = u;
+    p->n++;
+    return 1;
+}
+
+typedef struct {
+    const orc_index *h;
+    const int32_t *ks;
+    const int64_t *first;   /* [nf] first slot of each facility, -1: none */
+    const int64_t *next;    /* [nq] next slot with the same facility, -1: none */
+    int kmax;
+    int64_t u0, u1;
+    orc_pairs out;
+    int failed;
+} orc_many_job;
+
+static void *run_many(void *p)
+{
+    orc_many_job *j = (orc_many_job *)p;
+    const orc_index *h = j->h;
+    const int K = j->kmax;
+    int64_t cap = 1024;
+    orc_cand *c = (orc_cand *)malloc(sizeof(orc_cand) * cap);
+    if (!c) { j->failed = 1; return NULL; }
+    const int rmax = h->gx > h->gy ? h->gx : h->gy;
+    for (int64_t u = j->u0; u < j->u1 && !j->failed; ++u) {
+        const double ux = h->uxy[2 * u], uy = h->uxy[2 * u + 1];
+        const int cx = cell_of(h, ux, h->x0, h->gx), cy = cell_of(h, uy, h->y0, h->gy);
+        int64_t m = 0;
+        for (int r = 0; r <= rmax; ++r) {
+            if (r >= 1 && m >= K) {
+                /* K-th smallest collected distance (an upper bound of d_K) */
+                double kth = c[0].d2;
+                /* partial selection: the K-th smallest of the collected */
+                {
+                    /* copy-free: sort the collected prefix (m is small) */
+                    qsort(c, (size_t)m, sizeof(orc_cand), cand_cmp);
+                    kth = c[K - 1].d2;
+                }
+                const double reach = sqrt(kth) * (1.0 + 1e-9) + h->cs * 1e-6;
+                if ((double)(r - 1) * h->cs > reach) break;
+            }
+            const int y0 = cy - r, y1 = cy + r, x0 = cx - r, x1 = cx + r;
+            for (int yy = y0; yy <= y1; ++yy) {
+                if (yy < 0 || yy >= h->gy) continue;
+                const int ring_row = (yy == y0 || yy == y1);
+                for (int xx = x0; xx <= x1; ++xx) {
+                    if (xx < 0 || xx >= h->gx) continue;
+                    if (!ring_row && xx != x0 && xx != x1) continue;
+                    const int64_t cc = (int64_t)yy * h->gx + xx;
+                    for (int64_t p2 = h->cstart[cc]; p2 < h->cstart[cc + 1]; ++p2) {
+                        const int32_t f = h->fcell[p2];
+                        if (m == cap) {
+                            orc_cand *nc2 = (orc_cand *)realloc(c, sizeof(orc_cand) * cap * 2);
+                            if (!nc2) { j->failed = 1; break; }
+                            c = nc2;
+                            cap *= 2;
+                        }
+                        const double dx = ux - h->fxy[2 * f], dy = uy - h->fxy[2 * f + 1];
+                        c[m].d2 = dx * dx + dy * dy;
+                        c[m].f = f;
+                        ++m;
+                    }
+                }
+            }
+        }
+        if (j->failed) break;
+        qsort(c, (size_t)m, sizeof(orc_cand), cand_cmp);
+        /* exact rank of each collected facility: everything clearly below
+         * its distance counts, the band around it is decided exactly.  The
+         * band half-width 32u*d2 exceeds the sum of both distances' errors
+         * (each <= 4.0001u of itself) for every distance inside it. */
+        int64_t lo = 0;
+        for (int64_t i = 0; i < m; ++i) {
+            const double d = c[i].d2, tol = 3.552713678800501e-15 * d + 1e-300; /* 32 * 2^-53 */
+            while (lo < i && c[lo].d2 < d - tol) ++lo;
+            if (lo >= K) break;   /* lo facilities strictly nearer: c_f >= K from here on */
+            const int64_t first = j->first[c[i].f];
+            if (first < 0) continue;
+            int64_t cnt = lo;
+            const float fx = h->fxy[2 * c[i].f], fy = h->fxy[2 * c[i].f + 1];
+            for (int64_t t = lo; t < m && c[t].d2 <= d + tol; ++t) {
+                if (t == i) continue;
+                if (sign_d2diff(ux, uy, h->fxy[2 * c[t].f], h->fxy[2 * c[t].f + 1], fx, fy) < 0) ++cnt;
+            }
+            if (cnt >= K) continue;
+            for (int64_t s = first; s >= 0; s = j->next[s])
+                if (cnt < j->ks[s] && !pairs_push(&j->out, (int32_t)s, (int32_t)u)) { j->failed = 1; break; }
+        }
+    }
+    free(c);
+    return NULL;
+}
+
+typedef struct {
+    int64_t nq, npairs;
+    int64_t *off;     /* [nq+1] */
+    int32_t *users;   /* [npairs], ascending within each slot */
+} orc_many_result;
+
+/* Answers nq queries (facility index qs[s], k = ks[s]) over every user.
+ * Returns a result handle (null on a bad argument or allocation failure);
+ * read it with orc_many_sizes / orc_many_fetch, release it with
+ * orc_many_free. */
+void *orc_query_many(void *p, const int64_t *qs, const int32_t *ks, int64_t nq, int32_t nthreads)
+{
+    orc_index *h = (orc_index *)p;
+    if (!h || nq < 0 || (nq > 0 && (!qs || !ks))) return NULL;
+    int kmax = 0;
+    for (int64_t s = 0; s < nq; ++s) {
+        if (qs[s] < 0 || qs[s] >= h->nf || ks[s] <= 0) return NULL;
+        if (ks[s] > kmax) kmax = ks[s];
+    }
+    orc_many_result *R = (orc_many_result *)calloc(1, sizeof(orc_many_result));
+    if (!R) return NULL;
+    R->nq = nq;
+    R->off = (int64_t *)calloc((size_t)nq + 1, sizeof(int64_t));
+    int64_t *first = (int64_t *)malloc(sizeof(int64_t) * (size_t)h->nf);
+    int64_t *next = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nq > 0 ? nq : 1));
+    if (!R->off || !first || !next) goto fail;
+    for (int64_t f = 0; f < h->nf; ++f) first[f] = -1;
+    for (int64_t s = nq - 1; s >= 0; --s) {
+        next[s] = first[qs[s]];
+        first[qs[s]] = s;
+    }
+    if (nq == 0 || h->nu == 0) {
+        free(first);
+        free(next);
+        R->users = (int32_t *)malloc(sizeof(int32_t));
+        if (!R->users) { free(R->off); free(R); return NULL; }
+        return R;
+    }
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    if (h->nu < 4096) nthreads = 1;
+    orc_many_job *jobs = (orc_many_job *)calloc((size_t)nthreads, sizeof(orc_many_job));
+    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+    char *started = (char *)calloc((size_t)nthreads, 1);
+    if (!jobs || !th || !started) { free(jobs); free(th); free(started); goto fail; }
+    const int64_t per = (h->nu + nthreads - 1) / nthreads;
+    for (int t = 0; t < nthreads; ++t) {
+        jobs[t].h = h;
+        jobs[t].ks = ks;
+        jobs[t].first = first;
+        jobs[t].next = next;
+        jobs[t].kmax = kmax;
+        jobs[t].u0 = t * per < h->nu ? t * per : h->nu;
+        jobs[t].u1 = (t + 1) * per < h->nu ? (t + 1) * per : h->nu;
+    }
+    for (int t = 1; t < nthreads; ++t) started[t] = pthread_create(&th[t], NULL, run_many, &jobs[t]) == 0;
+    for (int t = 0; t < nthreads; ++t)
+        if (!started[t]) run_many(&jobs[t]);
+    for (int t = 1; t < nthreads; ++t)
+        if (started[t]) pthread_join(th[t], NULL);
+    int bad = 0;
+    int64_t tot = 0;
+    for (int t = 0; t < nthreads; ++t) {
+        bad |= jobs[t].failed;
+        tot += jobs[t].out.n;
+        for (int64_t i = 0; i < jobs[t].out.n; ++i) R->off[jobs[t].out.slot[i] + 1]++;
+    }
+    if (!bad) {
+        for (int64_t s = 0; s < nq; ++s) R->off[s + 1] += R->off[s];
+        R->npairs = tot;
+        R->users = (int32_t *)malloc(sizeof(int32_t) * (size_t)(tot > 0 ? tot : 1));
+        int64_t *fill = (int64_t *)malloc(sizeof(int64_t) * (size_t)nq);
+        if (R->users && fill) {
+            memcpy(fill, R->off, sizeof(int64_t) * (size_t)nq);
+            /* threads cover increasing user ranges: each slot's users come
+             * out ascending */
+            for (int t = 0; t < nthreads; ++t)
+                for (int64_t i = 0; i < jobs[t].out.n; ++i)
+                    R->users[fill[jobs[t].out.slot[i]]++] = jobs[t].out.user[i];
+        } else {
+            bad = 1;
+        }
+        free(fill);
+    }
+    for (int t = 0; t < nthreads; ++t) {
+        free(jobs[t].out.slot);
+        free(jobs[t].out.user);
+    }
+    free(jobs);
+    free(th);
+    free(started);
+    free(first);
+    free(next);
+    if (bad) {
+        free(R->users);
+        free(R->off);
+        free(R);
+        return NULL;
+    }
+    return R;
+fail:
+    free(first);
+    free(next);
+    free(R->off);
+    free(R);
+    return NULL;
+}
+
+int64_t orc_many_pairs(const void *r)
+{
+    return r ? ((const orc_many_result *)r)->npairs : -1;
+}
+
+/* off: nq+1 offsets; users: npairs user positions (input order) */
+int orc_many_fetch(const void *r, int64_t *off, int32_t *users)
+{
+    const orc_many_result *R = (const orc_many_result *)r;
+    if (!R || !off || !users) return ORC_ERR_ARG;
+    memcpy(off, R->off, sizeof(int64_t) * (size_t)(R->nq + 1));
+    if (R->npairs > 0) memcpy(users, R->users, sizeof(int32_t) * (size_t)R->npairs);
+    return ORC_OK;
+}
+
+void orc_many_free(void *r)
+{
+    orc_many_result *R = (orc_many_result *)r;
+    if (!R) return;
+    free(R->off);
+    free(R->users);
+    free(R);
+}

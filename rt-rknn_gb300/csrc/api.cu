@@ -51,6 +51,10 @@ rknn_status fail(rknn_status s, const std::string& msg)
                         std::string(#call) + ": " + cudaGetErrorString(e_));          \
     } while (0)
 
+// Drops the cached device address of the no-alloc scratch array on one
+// device (defined with that entry point below).
+void noalloc_forget(int device);
+
 template <typename T>
 cudaError_t dalloc(T*& p, size_t n)
 {
@@ -1072,6 +1076,7 @@ rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf, 
     if (e != cudaSuccess || ndev == 0)
         return bail(fail(RKNN_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e)));
     if (o.device < 0 || o.device >= ndev) return bail(fail(RKNN_ERR_ARG, "bad device ordinal"));
+    noalloc_forget(o.device);
 #define CKB(call)                                                                            \
     do {                                                                                     \
         cudaError_t e_ = (call);                                                             \
@@ -1695,6 +1700,15 @@ NoallocLayout noalloc_layout(unsigned char* base, int lc, int seg_cap)
 
 }  // namespace
 
+namespace {
+void noalloc_forget(int device)
+{
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES) return;
+    std::lock_guard<std::mutex> glk(g_noalloc_mu);
+    g_noalloc_ptr[device] = nullptr;
+}
+}  // namespace
+
 extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, int32_t mode,
                                           int32_t* out_ids, int64_t cap, int64_t* n_out)
 {
@@ -1712,6 +1726,9 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     std::lock_guard<std::mutex> lk(ix->mu);
     CK(cudaSetDevice(ix->device));
     // once per device, with that device current: the array's device address
+    // (host code must not pass the symbol itself).  rknn_index_create drops
+    // the cached address of its device, so an index built after a
+    // cudaDeviceReset looks it up again in the new context.
     if (!g_noalloc_ptr[ix->device]) {
         void* p = nullptr;
         CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
@@ -1721,6 +1738,15 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     const int seg_cap = 2 * caps.rm + 2;
     NoallocLayout L = noalloc_layout(g_noalloc_ptr[ix->device], caps_for(NOALLOC_KMAX).lc, seg_cap);
     cudaStream_t st = ix->stream;
+    // Every return after the first enqueued operation, failures included,
+    // leaves the stream idle: the next call (once the lock is released)
+    // clears and reuses the same array, which kernels still running from
+    // this call would otherwise share.  Declared after the locks, so it runs
+    // before they are released.
+    struct DrainStream {
+        cudaStream_t s;
+        ~DrainStream() { (void)cudaStreamSynchronize(s); }
+    } drain{st};
 
     // inputs and zeroed counters (the array keeps the previous call's contents)
     int qk[2] = {q, k};
@@ -1755,7 +1781,6 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     VerifyArgs va;
     va.qd = L.qd; va.planes = L.planes; va.bis_pos = L.bispos; va.lc = caps.lc;
     va.slice_r = nullptr;
-    va.stage_cap = caps.lc;
     va.segs = L.segs; va.seg_cap = seg_cap;
     va.chunk_off = L.chunk_off; va.cand_off = L.cand_off; va.reg_len = L.reg_len; va.nq = 1;
     va.uxy = ix->d_uxy; va.uid = ix->d_uid; va.fxy = ix->d_fxy; va.fstart = ix->d_fstart; va.gf = ix->gf;
@@ -1764,7 +1789,11 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     va.nu = (int)ix->nu; va.nf = (int)ix->nf; va.ncf = ix->gf.gx * ix->gf.gy;
     va.pool_cap = L.pool_cap; va.fault = L.counters + 10; va.dropped = L.counters + 2;
     va.surv = nullptr; va.surv_cap = 0; va.surv_count = L.counters + 3;
-    const size_t vsmem = (size_t)VERIFY_WARPS * ((size_t)caps.lc * 32 + 32 * sizeof(float));
+    // at most 512 half-planes staged per warp, as in batches (128 KB of
+    // staging per block); fewer staged planes only send more users to the
+    // exact count
+    va.stage_cap = std::max(1, std::min(caps.lc, (128 << 10) / (VERIFY_WARPS * 32)));
+    const size_t vsmem = (size_t)VERIFY_WARPS * ((size_t)va.stage_cap * 32 + 32 * sizeof(float));
     verify_kernel<<<2 * ix->num_sms, VERIFY_WARPS * 32, vsmem, st>>>(va);
     CK(cudaGetLastError());
     scan_counts_kernel<<<1, 1024, 0, st>>>(L.res_count, L.reg_len, L.region_top, 1, L.out_off, L.counters, nullptr);
@@ -1779,7 +1808,20 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     CK(cudaMemcpyAsync(&d, L.qd, sizeof(QDesc), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(off, L.out_off, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&dropped, L.counters + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+#ifdef RKNN_CHECKED
+    int rec[16];
+    CK(cudaMemcpyAsync(rec, L.counters, sizeof(rec), cudaMemcpyDeviceToHost, st));
+#endif
     CK(cudaStreamSynchronize(st));
+#ifdef RKNN_CHECKED
+    // bounds-checked build: a recorded out-of-range access fails the call
+    // (zone record at counters[4..9), verification record at [10..15))
+    for (int base : {4, 10})
+        if (rec[base])
+            return fail(RKNN_ERR_CUDA, "bounds check: array " + std::to_string(rec[base + 1]) + " index " +
+                                           std::to_string(rec[base + 2]) + " of " + std::to_string(rec[base + 3]) +
+                                           " at line " + std::to_string(rec[base + 4]));
+#endif
     if ((d.flags & QF_RESULT_OVERFLOW) || dropped)
         return fail(RKNN_ERR_CAPACITY, "rknn_query_noalloc: the query's results exceed the fixed "
                                        "scratch (about 2M ids); use rknn_query");

@@ -134,3 +134,51 @@ def test_street_layout():
     assert ds.fxy.shape == (500, 2) and ds.uxy.shape == (20000, 2)
     assert ds.ks.min() >= 1 and ds.ks.max() <= 100
     assert (ds.uxy >= 0).all() and (ds.uxy <= 1000).all()
+
+
+def test_user_major_oracle_matches_query_major():
+    """orc_query_many (user by user, every query at once; the fixture
+    generator's form) gives the same sets as the query-by-query oracle that
+    the golden vectors pin, on uniform, integer-lattice (many exact ties),
+    Gaussian-mixture (forced bisector ties, duplicates) and street data, k
+    from 1 to beyond |F|."""
+    rng = np.random.default_rng(12)
+    sets = [datagen.uniform(800, 8000, seed=31, nq=30, k=5),
+            datagen.uniform(300, 5000, seed=32, nq=30, k=5, integer=True),
+            datagen.gaussmix(1500, 30000, seed=3, nq=40, k=10),
+            datagen.street(nu=30000, nf=1500, seed=4, nq=60)]
+    for ds in sets:
+        o = O.Oracle.of(ds)
+        qs = np.concatenate([ds.queries, ds.queries[:3]])          # repeated facilities
+        ks = rng.integers(1, 40, qs.shape[0]).astype(np.int32)
+        ks[0], ks[1] = ds.nf, ds.nf + 7                            # k >= |F|: every user
+        off, ids = o.query_many(qs, ks)
+        for s in range(qs.shape[0]):
+            assert np.array_equal(ids[off[s]:off[s + 1]], o.query(int(qs[s]), int(ks[s]))), (ds.name, s)
+    for c in json.load(open(os.path.join(os.path.dirname(__file__), "golden", "handmade.json"))):
+        o = O.Oracle(np.array(c["fxy"], np.float32), np.array(c["uxy"], np.float32), c["fid"], c["uid"])
+        keys = list(c["expect"])
+        off, ids = o.query_many([int(k.split(",")[0]) for k in keys], [int(k.split(",")[1]) for k in keys])
+        for s, key in enumerate(keys):
+            assert ids[off[s]:off[s + 1]].tolist() == c["expect"][key], (c["name"], key)
+
+
+@pytest.mark.parametrize("name,picks", [("config1", 10), ("config2", 16), ("config3", 3),
+                                        ("config4", 8), ("config5", 3)])
+def test_config_fixtures_are_the_oracle(name, picks):
+    """The committed per-query fixtures of the full-size workloads come from
+    the oracle: the input points regenerate to the recorded digest, and
+    queries spread over each list (every k class) match the query-by-query
+    oracle's answers."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import config_fixtures as CF
+    ds, qs, ks = CF.spec(name)
+    fx = CF.load(name)
+    assert CF.data_sha256(ds) == fx["data_sha256"]
+    assert np.array_equal(fx["qs"], qs) and np.array_equal(fx["ks"], ks)
+    o = O.Oracle.of(ds)
+    order = np.argsort(ks, kind="stable")
+    for i in order[np.linspace(0, len(order) - 1, picks).astype(int)]:
+        ids = o.query(int(qs[i]), int(ks[i]))
+        assert ids.shape[0] == fx["count"][i] and CF.ids_digest(ids) == int(fx["digest"][i]), (name, int(i))
