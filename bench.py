@@ -194,7 +194,7 @@ class _CudaArray:
     """A device int32 array as __cuda_array_interface__ (read by torch)."""
 
     def __init__(self, ptr, n):
-        self.__cuda_array_interface__ = {"shape": (int(n),), "typestr": "<i4", "data": (int(ptr), True),
+        self.__cuda_array_interface__ = {"shape": (int(n),), "typestr": "<i4", "data": (int(ptr), False),
                                          "version": 3, "strides": None}
 
 

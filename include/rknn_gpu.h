@@ -278,7 +278,11 @@ void rknn_serve_opts_default(rknn_serve_opts* opts);
 /* Start a server over idx (which must outlive it). */
 rknn_status rknn_serve_start(rknn_index* idx, const rknn_serve_opts* opts, rknn_server** out);
 
-/* Queue one request; *ticket identifies it in rknn_serve_wait.  Thread-safe. */
+/* Queue one request; *ticket identifies it in rknn_serve_wait.  Thread-safe.
+ * Admission rule: a request whose scratch estimate on its own (a batch of
+ * one, padded as batches are) exceeds the server's scratch_bytes is refused
+ * with RKNN_ERR_CAPACITY, so no batch passes the budget; other requests are
+ * combined first come first served while the batch's estimate fits. */
 rknn_status rknn_serve_submit(rknn_server* srv, int32_t q_index, int32_t k, int32_t mode,
                               uint64_t* ticket);
 
@@ -299,6 +303,14 @@ rknn_status rknn_serve_replay(rknn_server* srv, int64_t n, const int32_t* q_inde
 /* Counters and latency percentiles of requests completed since the start
  * (or since the last call with reset != 0). */
 rknn_status rknn_serve_stats_get(rknn_server* srv, int32_t reset, rknn_serve_stats* stats);
+
+/* Failure test hook (no counterpart in the reference): the next `count`
+ * batches the worker launches fail on the host, with no GPU fault involved.
+ * kind 1: the batch's workspace allocation fails as a cudaMalloc would
+ * (after its old arrays were released), its requests end with RKNN_ERR_OOM;
+ * kind 2: the launch fails after the batch's input copy, its requests end
+ * with RKNN_ERR_CUDA.  Later batches allocate afresh and run normally. */
+rknn_status rknn_serve_inject_fault(rknn_server* srv, int32_t kind, int32_t count);
 
 /* Finish queued and running requests, stop the worker, free the server. */
 rknn_status rknn_serve_stop(rknn_server* srv);

@@ -145,6 +145,7 @@ struct Workspace {
     std::map<GraphKey, CachedGraph> graphs;
     cudaStream_t aux[NAUX] = {};
     cudaEvent_t fork = nullptr, join[NAUX] = {};
+    bool inject_oom = false;       // failure test hook: the next ensure_ws fails (host only)
 };
 
 }  // namespace
@@ -386,14 +387,67 @@ void use_block(Workspace& w, int i)
     w.d_res_count = w.d_counters + ZB_COUNTERS + ZB_VSTATS_INTS;
 }
 
+rknn_status grow_ws(Workspace& w, int nqc, int lc, int sc);
+
+// Sizes a workspace for a batch.  Every failure leaves the workspace either
+// as it was or released entirely (all capacities zero), never half grown: a
+// failed allocation in the middle of a growth frees everything, so the next
+// call allocates afresh instead of finding null arrays behind nonzero
+// capacities.
 rknn_status ensure_ws(Workspace& w, int nq, const ZoneCaps& caps, long long pool_need)
 {
     const int seg_cap = 2 * caps.rm + 2;
+    if (w.inject_oom) {
+        // failure test hook (rknn_serve_inject_fault): this growth fails as
+        // a cudaMalloc would, after the old arrays were released
+        w.inject_oom = false;
+        free_ws(w);
+        return fail(RKNN_ERR_OOM, "workspace growth failed (injected for a failure test)");
+    }
     if (nq > w.nq_cap || caps.lc > w.lc || seg_cap > w.seg_cap) {
-        int nqc = std::max(nq, w.nq_cap);
-        int lc = std::max(caps.lc, w.lc);
-        int sc = std::max(seg_cap, w.seg_cap);
-        long long pool = w.pool_cap;
+        const rknn_status s = grow_ws(w, std::max(nq, w.nq_cap), std::max(caps.lc, w.lc), std::max(seg_cap, w.seg_cap));
+        if (s != RKNN_OK) {
+            free_ws(w);
+            return s;
+        }
+    }
+    if (!w.d_surv) {
+        const long long cap = std::max<long long>(w.surv_cap, 1 << 22);
+        const cudaError_t e = dalloc(w.d_surv, (size_t)cap);
+        if (e != cudaSuccess) {
+            w.d_surv = nullptr;
+            return fail(e == cudaErrorMemoryAllocation ? RKNN_ERR_OOM : RKNN_ERR_CUDA,
+                        std::string("survivor list: ") + cudaGetErrorString(e));
+        }
+        w.surv_cap = cap;
+    }
+    if (pool_need > w.pool_cap) {
+        drop_graphs(w);
+        cudaFree(w.d_pool);
+        cudaFree(w.d_out);
+        w.d_pool = w.d_out = nullptr;
+        w.pool_cap = 0;
+        long long cap = std::max<long long>(pool_need, 1 << 20);
+        cudaError_t e = dalloc(w.d_pool, (size_t)cap);
+        if (e == cudaSuccess) e = dalloc(w.d_out, (size_t)cap);
+        if (e != cudaSuccess) {
+            cudaFree(w.d_pool);
+            cudaFree(w.d_out);
+            w.d_pool = w.d_out = nullptr;
+            return fail(e == cudaErrorMemoryAllocation ? RKNN_ERR_OOM : RKNN_ERR_CUDA,
+                        std::string("result pool: ") + cudaGetErrorString(e));
+        }
+        w.pool_cap = cap;
+    }
+    return RKNN_OK;
+}
+
+// Reallocates the per-slot arrays for nqc slots (the result pool and the
+// survivor list are kept out: the caller sizes them).
+rknn_status grow_ws(Workspace& w, int nqc, int lc, int sc)
+{
+    {
+        const long long pool = w.pool_cap;
         const int rcap = w.rcap;
         const long long scap = w.surv_cap;
         free_ws(w);
@@ -431,21 +485,6 @@ rknn_status ensure_ws(Workspace& w, int nq, const ZoneCaps& caps, long long pool
         CK(cudaHostGetDevicePointer((void**)&w.h_qko_dev, w.h_qko, 0));
         CK(cudaHostGetDevicePointer((void**)&w.h_off_dev, w.h_off, 0));
         w.pool_cap = 0;
-    }
-    if (!w.d_surv) {
-        const long long cap = std::max<long long>(w.surv_cap, 1 << 22);
-        CK(dalloc(w.d_surv, (size_t)cap));
-        w.surv_cap = cap;
-    }
-    if (pool_need > w.pool_cap) {
-        drop_graphs(w);
-        cudaFree(w.d_pool);
-        cudaFree(w.d_out);
-        w.d_pool = w.d_out = nullptr;
-        long long cap = std::max<long long>(pool_need, 1 << 20);
-        CK(dalloc(w.d_pool, (size_t)cap));
-        CK(dalloc(w.d_out, (size_t)cap));
-        w.pool_cap = cap;
     }
     return RKNN_OK;
 }
@@ -1908,6 +1947,8 @@ struct rknn_server {
     uint64_t next_ticket = 1;
     bool stopping = false;
     std::thread th;
+    // failure test hooks (under mu): the next batches that fail on purpose
+    int inject_oom = 0, inject_launch = 0;
     // statistics (under mu)
     int64_t submitted = 0, completed = 0, failed = 0, batches = 0, batched = 0;
     int inflight = 0, max_inflight = 0;
@@ -1933,8 +1974,12 @@ void finish(rknn_server* sv, const ReqPtr& r, rknn_status st, const std::string&
     }
 }
 
+// Failure test hooks (rknn_serve_inject_fault): made on the host, no GPU
+// fault is involved.
+enum { INJECT_NONE = 0, INJECT_OOM = 1, INJECT_LAUNCH = 2 };
+
 // Launch a batch on a free slot (worker thread, mu not held).
-rknn_status slot_launch(rknn_server* sv, Slot& sl)
+rknn_status slot_launch(rknn_server* sv, Slot& sl, int inject)
 {
     rknn_index* ix = sv->ix;
     const int nq = (int)sl.reqs.size();
@@ -1951,6 +1996,7 @@ rknn_status slot_launch(rknn_server* sv, Slot& sl)
     }
     sl.plan = plan_batch(ix, nqp, sl.reqs[0]->mode, true, ksorted.data(), kmax);
     Workspace& w = sl.ws;
+    if (inject == INJECT_OOM) w.inject_oom = true;
     rknn_status s = ensure_ws(w, nqp, plan_caps(sl.plan), std::max<long long>(w.pool_cap, (long long)nqp * 4096));
     if (s != RKNN_OK) return s;
     for (int i = 0; i < nqp; ++i) {
@@ -1959,6 +2005,8 @@ rknn_status slot_launch(rknn_server* sv, Slot& sl)
         w.h_qko[2 * nqp + i] = order[i];
     }
     CK(cudaMemcpyAsync(w.d_qko, w.h_qko, sizeof(int) * 3 * (size_t)nqp, cudaMemcpyHostToDevice, sl.st));
+    if (inject == INJECT_LAUNCH)
+        return fail(RKNN_ERR_CUDA, "batch launch failed after its input copy (injected for a failure test)");
     Ctx c{w, sl.st, sl.ev0, sl.ev1, nullptr, &sl.device_ms};
     CK(cudaEventRecord(sl.ev0, sl.st));
     s = launch(ix, c, sl.plan, false);
@@ -2028,19 +2076,32 @@ void serve_loop(rknn_server* sv)
                 ReqPtr r = *it;
                 if (r->mode != mode) { ++it; continue; }
                 const int km = std::max(kmax, (int)r->k);
+                // a request's own estimate never exceeds the budget (submit
+                // refuses such requests), so the first one always fits
                 const long long need = (long long)pad_pow2((int)sl.reqs.size() + 1) * scratch_per_query(sv->ix, km);
                 if (!sl.reqs.empty() && need > budget) break;
                 sl.reqs.push_back(r);
                 kmax = km;
                 it = sv->pending.erase(it);
             }
+            int inject = INJECT_NONE;
+            if (sv->inject_oom > 0) {
+                sv->inject_oom--;
+                inject = INJECT_OOM;
+            } else if (sv->inject_launch > 0) {
+                sv->inject_launch--;
+                inject = INJECT_LAUNCH;
+            }
             lk.unlock();
-            rknn_status s = slot_launch(sv, sl);
+            rknn_status s = slot_launch(sv, sl, inject);
             std::string err = s == RKNN_OK ? "" : g_err;
             lk.lock();
             sv->batches++;
             sv->batched += (int64_t)sl.reqs.size();
             if (s != RKNN_OK) {
+                // the batch's requests fail with the launch's status; the
+                // slot stays free and takes the next batch (its workspace,
+                // released by a failed growth, is allocated afresh)
                 cudaStreamSynchronize(sl.st);
                 for (auto& r : sl.reqs) finish(sv, r, s, err);
                 sl.reqs.clear();
@@ -2127,6 +2188,14 @@ rknn_status rknn_serve_submit(rknn_server* sv, int32_t q, int32_t k, int32_t mod
                                       std::to_string(sv->ix->nf) + ")");
     if (k <= 0) return fail(RKNN_ERR_ARG, "k must be a positive integer");
     if (mode != RKNN_MODE_FP32 && mode != RKNN_MODE_FP64) return fail(RKNN_ERR_ARG, "bad mode");
+    // admission: a request whose scratch estimate alone (as a batch of its
+    // own) exceeds the server's budget is refused, so that no batch passes
+    // the budget
+    const long long need1 = (long long)pad_pow2(1) * scratch_per_query(sv->ix, k);
+    if (need1 > sv->o.scratch_bytes)
+        return fail(RKNN_ERR_CAPACITY, "request needs about " + std::to_string(need1) +
+                                           " bytes of scratch, more than the server's scratch_bytes (" +
+                                           std::to_string(sv->o.scratch_bytes) + ")");
     auto r = std::make_shared<ServeReq>();
     r->q = q;
     r->k = k;
@@ -2236,6 +2305,15 @@ rknn_status rknn_serve_stats_get(rknn_server* sv, int32_t reset, rknn_serve_stat
         sv->max_inflight = sv->inflight;
         sv->have_first = false;
     }
+    return RKNN_OK;
+}
+
+rknn_status rknn_serve_inject_fault(rknn_server* sv, int32_t kind, int32_t count)
+{
+    if (!sv || count < 0) return fail(RKNN_ERR_ARG, "bad argument");
+    if (kind != INJECT_OOM && kind != INJECT_LAUNCH) return fail(RKNN_ERR_ARG, "unknown fault kind");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    (kind == INJECT_OOM ? sv->inject_oom : sv->inject_launch) = count;
     return RKNN_OK;
 }
 

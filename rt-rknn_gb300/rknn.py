@@ -37,7 +37,8 @@ EXPORTS = ["rknn_index_opts_default", "rknn_index_create", "rknn_index_destroy",
            "rknn_batch_device_results", "rknn_sync", "rknn_set_stream", "rknn_last_stats",
            "rknn_last_zone", "rknn_set_profiling", "rknn_last_kernel_ms",
            "rknn_serve_opts_default", "rknn_serve_start", "rknn_serve_submit", "rknn_serve_wait",
-           "rknn_serve_replay", "rknn_serve_stats_get", "rknn_serve_stop", "rknn_index_tune",
+           "rknn_serve_replay", "rknn_serve_stats_get", "rknn_serve_inject_fault", "rknn_serve_stop",
+           "rknn_index_tune",
            "rknn_host_alloc", "rknn_host_free", "rknn_snapshot_write", "rknn_snapshot_read",
            "rknn_snapshot_free", "rknn_index_open", "rknn_index_save", "rknn_last_error", "rknn_version"]
 
@@ -168,6 +169,7 @@ def load(path: str = LIB_PATH):
     L.rknn_serve_wait.argtypes = [vp, C.c_uint64, i32, vp, i64, C.POINTER(i64), C.POINTER(C.c_double)]
     L.rknn_serve_replay.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp]
     L.rknn_serve_stats_get.argtypes = [vp, i32, C.POINTER(ServeStats)]
+    L.rknn_serve_inject_fault.argtypes = [vp, i32, i32]
     L.rknn_serve_stop.argtypes = [vp]
     L.rknn_index_tune.argtypes = [vp, vp, vp, i32, i32, C.POINTER(TuneResult)]
     L.rknn_snapshot_write.argtypes = [C.c_char_p, vp, vp, i64, vp, vp, i64]
@@ -480,6 +482,12 @@ class Server:
         _check(load().rknn_serve_replay(self.h, n, q.ctypes.data, k.ctypes.data, m.ctypes.data,
                                         t.ctypes.data, lat.ctypes.data, nr.ctypes.data))
         return lat, nr
+
+    def inject_fault(self, kind: str, count: int = 1):
+        """Failure test hook: the next `count` batches fail on the host
+        ("oom": workspace allocation, RKNN_ERR_OOM; "launch": after the
+        input copy, RKNN_ERR_CUDA)."""
+        _check(load().rknn_serve_inject_fault(self.h, {"oom": 1, "launch": 2}[kind], int(count)))
 
     def stats(self, reset: bool = False) -> dict:
         st = ServeStats()

@@ -87,3 +87,52 @@ def test_rejects_bad_requests(engine, served):
 
 def orc_ids(served, q, k):
     return served[2].query(q, k).tolist()
+
+
+@pytest.mark.parametrize("kind,status", [("oom", 2), ("launch", 3)])
+def test_failed_batches_and_recovery(engine, served, kind, status):
+    """A batch whose workspace allocation fails (kind "oom") or whose launch
+    fails after its input copy ("launch"), made to fail on the host through
+    the server's failure hook (no GPU fault): its requests end with
+    RKNN_ERR_OOM / RKNN_ERR_CUDA, every other request of the stream gets the
+    oracle's ids, and requests after the failure complete normally."""
+    ds, idx, orc = served
+    rng = np.random.default_rng(11 if kind == "oom" else 12)
+    qs = rng.integers(0, ds.nf, 64)
+    ks = rng.integers(1, 20, 64)
+    with engine.Server(idx, slots=2, max_batch=16) as srv:
+        srv.inject_fault(kind, 1)
+        tickets = [srv.submit(int(q), int(k), "fp32" if i % 2 else "fp64") for i, (q, k) in enumerate(zip(qs, ks))]
+        failed = 0
+        for t, q, k in zip(tickets, qs, ks):
+            try:
+                got = srv.wait(t)
+            except engine.RkNNError as e:
+                assert e.status == status, (e.status, str(e))
+                failed += 1
+                continue
+            assert np.array_equal(got, orc.query(int(q), int(k))), (int(q), int(k))
+        assert 1 <= failed <= 16
+        st = srv.stats()
+        assert st["failed"] == failed and st["completed"] == 64 - failed
+        # after the failure: the slot allocates afresh and every request completes
+        more = [srv.submit(int(q), int(k), "fp32") for q, k in zip(qs[:32], ks[:32])]
+        for t, q, k in zip(more, qs[:32], ks[:32]):
+            assert np.array_equal(srv.wait(t), orc.query(int(q), int(k)))
+
+
+def test_request_beyond_the_scratch_budget_is_refused(engine, served):
+    """Admission: a request whose own scratch estimate exceeds the server's
+    scratch_bytes is refused at submit with RKNN_ERR_CAPACITY (never run over
+    budget); requests that fit are served."""
+    ds, idx, orc = served
+    q = int(ds.queries[0])
+    # a batch of one is padded to 32 slots, each with a 32 KB share of the
+    # result pool: one request alone needs more than 1 MiB
+    with engine.Server(idx, slots=1, max_batch=8, scratch_bytes=1 << 20) as srv:
+        with pytest.raises(engine.RkNNError) as e:
+            srv.submit(q, 5, "fp32")
+        assert e.value.status == 5
+    with engine.Server(idx, slots=1, max_batch=8, scratch_bytes=8 << 20) as srv:
+        t = srv.submit(q, 5, "fp32")
+        assert np.array_equal(srv.wait(t), orc.query(q, 5))
