@@ -436,7 +436,12 @@ def serving_config5(rknn, device, modes=("fp32", "fp64")):
     size_mismatches = 0
     with rknn.Index.of(ds5, device=device) as idx5:
         with rknn.Server(idx5, slots=3, max_batch=2048) as srv:
-            srv.replay(qs[:500], ks[:500], modes[0], np.linspace(0, 0.01, 500))     # warm
+            # warm every slot in both modes at a low and a high rate (workspace
+            # sizes and the k-class shapes the open-loop runs will meet)
+            for mode in modes:
+                for rate in (2e3, 1e5):
+                    arrival = np.cumsum(np.random.default_rng(1).exponential(1.0 / rate, 600))
+                    srv.replay(qs[:600], ks[:600], mode, arrival)
             srv.stats(reset=True)
             for rate, n in ((1e3, 1000), (1e4, 4000), (5e4, 8000), (1e5, 10000)):
                 rng = np.random.default_rng(int(rate))

@@ -31,6 +31,7 @@ NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 UNITS = {
     "index.cu": [],
     "zone.cu": ["-fmad=false"],
+    "zone_cta.cu": ["-fmad=false"],
     "verify.cu": [],
     "slice.cu": [],
     "api.cu": [],

@@ -166,6 +166,10 @@ struct rknn_index {
     float2* d_uxy = nullptr;
     int *d_uid = nullptr, *d_ustart = nullptr;
     std::vector<int> h_fidx;       // cell-sorted position -> facility input index
+    std::vector<float> h_fxy;      // facility coordinates in input order
+    std::vector<int> h_fstart, h_ustart;   // cell starts of both grids (host copies)
+    bool order_est = false;        // host batches: order each k class by candidate estimate
+                                   // (RKNN_ORDER=est), else by k alone
     std::vector<int32_t> h_fid;    // facility ids as given (for snapshots)
     // the input points, kept on the device so the grids can be rebuilt
     // with other cell sizes (rknn_index_tune)
@@ -186,6 +190,9 @@ struct rknn_index {
     std::unique_ptr<BatchPlan> plan_cache;
     int plan_nq = 0, plan_mode = -1, plan_k = 0;
     bool fuse = true;           // FP32 slice batches: the filter verifies its own slots
+    int zone_cta = ZCTA_THREADS;  // influence-zone batches small enough for a block per query run
+                                  // the one-block kernel with this many threads (RKNN_ZONE_CTA:
+                                  // 0 = the one-warp kernel, 128 or 256)
                                 // (RKNN_FUSE=0 in the environment turns it off)
     // occupancy answers by (kernel, threads, dynamic shared memory): a batch's
     // plan asks the same few questions on every call
@@ -281,6 +288,7 @@ struct ZoneLaunch {
     size_t slice, smem;
     int grid;
     int threads = 32 * ZONE_WARPS;   // 64: the slice filter with two warps per query
+    bool cta = false;                // zone_kernel_cta, one block of ZCTA_THREADS per query
 };
 
 // Resident blocks per SM of kernel fn at this block size and dynamic shared
@@ -317,7 +325,9 @@ ZoneFn slice_fn(int kmax, bool two = false)
 // arrays).
 bool is_filter_kernel(const void* f)
 {
-    for (const void* g : {(const void*)zone_kernel_smem, (const void*)slice_kernel, (const void*)slice_kernel_r4,
+    for (const void* g : {(const void*)zone_kernel_smem, (const void*)zone_kernel_cta, (const void*)zone_kernel_cta_half,
+                          (const void*)slice_kernel,
+                          (const void*)slice_kernel_r4,
                           (const void*)slice_kernel_r8, (const void*)slice_kernel_r12, (const void*)slice_kernel_r16,
                           (const void*)slice_kernel_r24, (const void*)slice_kernel_r32, (const void*)slice_kernel2_r4,
                           (const void*)slice_kernel2_r8, (const void*)slice_kernel2_r12, (const void*)slice_kernel2_r16,
@@ -353,6 +363,21 @@ ZoneLaunch zone_launch(rknn_index* ix, const ZoneCaps& c, int nq, bool slice = f
         if ((long long)nq <= (long long)per2 * ix->num_sms) {
             L.smem = smem2;
             L.threads = 64;
+            L.grid = std::max(1, nq);
+            return L;
+        }
+    }
+    if (!slice && ix->zone_cta && c.pc <= ZCTA_PQ_MAX) {
+        // the influence zone with a block per query when every query of the
+        // class gets one at once: the same search, its steps spread over the
+        // block (lower latency per query)
+        const int nt = ix->zone_cta;
+        const void* fn = nt == ZCTA_THREADS ? (const void*)zone_kernel_cta : (const void*)zone_kernel_cta_half;
+        const int per = occupancy(ix, fn, nt, L.slice);
+        if ((long long)nq <= (long long)per * ix->num_sms) {
+            L.smem = L.slice;
+            L.threads = nt;
+            L.cta = true;
             L.grid = std::max(1, nq);
             return L;
         }
@@ -571,7 +596,9 @@ BatchPlan plan_batch(rknn_index* ix, int nq, int mode, bool use_order, const int
             const int c = k_class(k_sorted[i]);
             int j = i + 1;
             while (j < nq && k_class(k_sorted[j]) == c) ++j;
-            b.cls.push_back(ZClass{i, j - i, std::max(1, k_sorted[i]), false, {}, {}});
+            int km = 1;
+            for (int t = i; t < j; ++t) km = std::max(km, k_sorted[t]);   // the class's largest k
+            b.cls.push_back(ZClass{i, j - i, km, false, {}, {}});
             i = j;
         }
     } else {
@@ -596,6 +623,10 @@ BatchPlan plan_batch(rknn_index* ix, int nq, int mode, bool use_order, const int
     // exact recount still decides)
     b.vupt = ix->vupt;
     b.vwarps = ix->vwarps;
+    // a handful of queries: smaller work items spread each query's users over
+    // more warps (a lone FP64 query's evaluations are bound by one warp's
+    // FP64 issue rate)
+    if (nq <= 16 && b.vupt > 2) b.vupt = 2;
     b.stage_cap = std::max(1, std::min(b.pstride, stage_max));
     int rm = 0;
     for (auto& c : b.cls) rm = std::max(rm, c.caps.rm);
@@ -731,6 +762,8 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
         za.work_counter = w.d_counters + 16 + i;
         cudaStream_t zs = i == 0 ? st : w.aux[(i - 1) % NAUX];
         if (z.slice) slice_fn(z.kmax, z.zl.threads == 64)<<<z.zl.grid, z.zl.threads, z.zl.smem, zs>>>(za);
+        else if (z.zl.cta && z.zl.threads == ZCTA_THREADS) zone_kernel_cta<<<z.zl.grid, ZCTA_THREADS, z.zl.smem, zs>>>(za);
+        else if (z.zl.cta) zone_kernel_cta_half<<<z.zl.grid, ZCTA_THREADS / 2, z.zl.smem, zs>>>(za);
         else zone_kernel_smem<<<z.zl.grid, 32 * ZONE_WARPS, z.zl.smem, zs>>>(za);
         CK(cudaGetLastError());
     }
@@ -1041,8 +1074,37 @@ rknn_status build_grids(rknn_index* ix, float fac_per_cell, float usr_per_cell)
     CK(grid_sort(ix->d_uin, ix->d_uidin, (int)nu, ix->gu, ix->d_uxy, ix->d_uid, nullptr, nullptr, ix->d_ustart, st));
     ix->h_fidx.resize(nf);
     CK(cudaMemcpyAsync(ix->h_fidx.data(), ix->d_fidx, sizeof(int) * nf, cudaMemcpyDeviceToHost, st));
+    ix->h_fstart.resize(ncf + 1);
+    ix->h_ustart.resize(ncu + 1);
+    CK(cudaMemcpyAsync(ix->h_fstart.data(), ix->d_fstart, sizeof(int) * (ncf + 1), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(ix->h_ustart.data(), ix->d_ustart, sizeof(int) * (ncu + 1), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     return RKNN_OK;
+}
+
+// Cheap estimate of a query's candidate users: k times the users per
+// facility around q -- the facilities of the 5 x 5 facility cells centred
+// on q's cell and the users of the user cells covering the same box, from
+// the host copies of both grids' cell starts.  Used only to order work.
+double cand_estimate(const rknn_index* ix, int q, int k)
+{
+    const Grid& g = ix->gf;
+    const Grid& u = ix->gu;
+    const float x = ix->h_fxy[2 * (size_t)q], y = ix->h_fxy[2 * (size_t)q + 1];
+    const int cx = cell_coord(x, g.x0, g.inv, g.gx), cy = cell_coord(y, g.y0, g.inv, g.gy);
+    const int x0 = std::max(0, cx - 2), x1 = std::min(g.gx - 1, cx + 2);
+    const int y0 = std::max(0, cy - 2), y1 = std::min(g.gy - 1, cy + 2);
+    long long nfac = 0;
+    for (int r = y0; r <= y1; ++r)
+        nfac += ix->h_fstart[(size_t)r * g.gx + x1 + 1] - ix->h_fstart[(size_t)r * g.gx + x0];
+    const int ux0 = cell_coord(g.x0 + (float)x0 * g.cs, u.x0, u.inv, u.gx);
+    const int ux1 = cell_coord(g.x0 + (float)(x1 + 1) * g.cs, u.x0, u.inv, u.gx);
+    const int uy0 = cell_coord(g.y0 + (float)y0 * g.cs, u.y0, u.inv, u.gy);
+    const int uy1 = cell_coord(g.y0 + (float)(y1 + 1) * g.cs, u.y0, u.inv, u.gy);
+    long long nusr = 0;
+    for (int r = uy0; r <= uy1; ++r)
+        nusr += ix->h_ustart[(size_t)r * u.gx + ux1 + 1] - ix->h_ustart[(size_t)r * u.gx + ux0];
+    return (double)k * (double)nusr / (double)std::max(nfac, 1LL);
 }
 
 }  // namespace
@@ -1102,8 +1164,14 @@ rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf, 
     ix->filter = o.filter;
     ix->slice_min_k = o.slice_min_k > 0 ? o.slice_min_k : 1;
     if (const char* f = std::getenv("RKNN_FUSE")) ix->fuse = std::strcmp(f, "0") != 0;
+    if (const char* f = std::getenv("RKNN_ZONE_CTA")) {
+        const int v = std::atoi(f);
+        ix->zone_cta = v == 0 ? 0 : v == ZCTA_THREADS / 2 ? ZCTA_THREADS / 2 : ZCTA_THREADS;
+    }
     ix->nf = nf;
     ix->nu = nu;
+    ix->h_fxy.assign(fxy, fxy + 2 * nf);
+    if (const char* f = std::getenv("RKNN_ORDER")) ix->order_est = std::strcmp(f, "est") == 0;
     if (fid) ix->h_fid.assign(fid, fid + nf);
     else {
         ix->h_fid.resize(nf);
@@ -1136,6 +1204,8 @@ rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf, 
     // maximum less the kernel's static shared memory, set once (each launch
     // asks for what its plan needs)
     CKB(allow_dynamic_smem((const void*)zone_kernel_smem, optin));
+    CKB(allow_dynamic_smem((const void*)zone_kernel_cta, optin));
+    CKB(allow_dynamic_smem((const void*)zone_kernel_cta_half, optin));
     {
         int per = 1;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, recount_kernel, 256, 0);
@@ -1444,21 +1514,32 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
     // descending k: the longest zones start first, and each k class gets its
     // own zone launch
     std::vector<int> order, ksorted;
-    if (!uniform) {
+    const bool use_order = !uniform || ix->order_est;
+    if (use_order) {
         order.resize(nq);
         for (int i = 0; i < nq; ++i) order[i] = i;
-        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return k[a] > k[b]; });
+        if (ix->order_est) {
+            // each k class in descending candidate estimate (longest first)
+            std::vector<double> est(nq);
+            for (int i = 0; i < nq; ++i) est[i] = cand_estimate(ix, q[i], k[i]);
+            std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+                const int ca = k_class(k[a]), cb = k_class(k[b]);
+                return ca != cb ? ca > cb : est[a] > est[b];
+            });
+        } else {
+            std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return k[a] > k[b]; });
+        }
         ksorted.resize(nq);
         for (int i = 0; i < nq; ++i) ksorted[i] = k[order[i]];
     }
     BatchPlan fresh;
     const BatchPlan* bp = nullptr;
-    if (uniform && ix->plan_cache && ix->plan_nq == nq && ix->plan_mode == mode && ix->plan_k == kmax) {
+    if (!use_order && ix->plan_cache && ix->plan_nq == nq && ix->plan_mode == mode && ix->plan_k == kmax) {
         bp = ix->plan_cache.get();
     } else {
-        fresh = plan_batch(ix, nq, mode, !uniform, uniform ? nullptr : ksorted.data(), kmax);
+        fresh = plan_batch(ix, nq, mode, use_order, use_order ? ksorted.data() : nullptr, kmax);
         bp = &fresh;
-        if (uniform) {
+        if (!use_order) {
             ix->plan_cache = std::make_unique<BatchPlan>(fresh);
             ix->plan_nq = nq;
             ix->plan_mode = mode;
@@ -1475,7 +1556,7 @@ rknn_status rknn_query_batch(rknn_index* ix, const int32_t* q, const int32_t* k,
     // the offsets scan writes into page-locked host memory: no copies
     std::memcpy(w.h_qko, q, sizeof(int) * nq);
     std::memcpy(w.h_qko + nq, k, sizeof(int) * nq);
-    if (!uniform) std::memcpy(w.h_qko + 2 * nq, order.data(), sizeof(int) * nq);
+    if (use_order) std::memcpy(w.h_qko + 2 * nq, order.data(), sizeof(int) * nq);
     c.io.q = w.h_qko_dev;
     c.io.k = w.h_qko_dev + nq;
     c.io.order = w.h_qko_dev + 2 * nq;

@@ -6,6 +6,10 @@
 namespace rknn {
 
 constexpr int ZONE_WARPS = 1;          // warps (queries in flight) per block
+// zone_kernel_cta: one block of ZCTA_THREADS threads per query; its queue
+// holds at most ZCTA_PQ_MAX entries (a multiple of ZCTA_THREADS)
+constexpr int ZCTA_THREADS = 256;
+constexpr int ZCTA_PQ_MAX = 2048;
 
 // Per-query capacities of the zone state.  Measured on uniform data
 // (100k facilities): about 4.6k bisectors and at most ~4k^2 live vertices
@@ -176,6 +180,10 @@ __host__ __device__ inline size_t slice_own_bytes(size_t warp_bytes, int nwq, in
 
 // zone state in shared memory, one warp (one query at a time) per block
 __global__ void zone_kernel_smem(ZoneArgs a);
+// the same search, one block of ZCTA_THREADS per query (small batches), and
+// with blocks of ZCTA_THREADS / 2
+__global__ void zone_kernel_cta(ZoneArgs a);
+__global__ void zone_kernel_cta_half(ZoneArgs a);
 
 // angular-slice filter, same arguments and outputs: slice bounds in a
 // shared-memory heap (any k), or in registers for k <= 4, 8, 12, 16, 24, 32

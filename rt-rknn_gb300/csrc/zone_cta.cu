@@ -1,0 +1,1102 @@
+// Influence-zone kernel, one block per query.
+//
+// The same search as the one-warp kernel (zone.cu): rknn-inf's influence-zone
+// filter (rknn-inf/inf.cpp:201-585) over the uniform facility grid, with the
+// same entries taken in the same order, the same three pruning rules, the
+// same bisectors, vertices and counts, and every decision on the FP64 values
+// the reference computes (this file is built with -fmad=false).  What
+// changes is how each step runs:
+//   * the priority queue is a sorted array in shared memory: a batch of new
+//     entries (one ring's cells, one cell's facilities) is merged into it by
+//     every thread at once (each entry's new place is its rank among the old
+//     entries plus its rank within the batch), and the queue's head is read
+//     by every thread, so a pop needs no broadcast.  Entries are ordered by
+//     (squared distance, code) as in the heap of zone.cu; codes are unique,
+//     so the pop sequence is the heap's;
+//   * the loops over vertices and candidates run over the block's threads
+//     (ordered compactions keep the reference's vertex order);
+//   * a candidate intersection's certified pre-discard and its count over the
+//     earlier bisectors are split over a group of ZG threads, each taking
+//     every ZG-th bisector, and summed within the group.
+// It serves batches in which every query can have a block of its own (the
+// plain single-query form first of all); larger batches run the one-warp
+// kernel, which keeps more queries in flight per SM.
+#include "zone_geom.cuh"
+
+namespace rknn {
+
+namespace {
+
+constexpr int ZMAXT = ZCTA_THREADS;      // the largest block size (shared arrays)
+constexpr int ZMAXW = ZMAXT / 32;
+
+struct ZcShared {
+    uint64_t tk[ZMAXT];   // a batch of new queue entries: keys
+    uint32_t tc[ZMAXT];   //   and codes
+    int wc[2][ZMAXW];     // per-warp counts (ordered compactions, scans)
+    double rd[ZMAXW];     // per-warp partials of reductions
+    long long rl[ZMAXW];
+    float rf[ZMAXW];
+    int ri[2][ZMAXW];
+    long long ek[ZMAXW][8];   // extreme boundary points: per-warp best keys
+    int ei[ZMAXW][8];         //   and list positions
+    double bd[4];         // values one thread computed for all
+    int bi[12];
+};
+
+// Ordered ranks of two predicates over the block (thread order is item
+// order): the number of threads before this one with each predicate set,
+// and the totals.  Two barriers; the shared counts are free again on return.
+template <int ZW>
+__device__ __forceinline__ void block_rank2(bool p, bool q, ZcShared& sh, int& rp, int& rq, int& tp, int& tq)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned mp = __ballot_sync(FULL, p), mq = __ballot_sync(FULL, q);
+    if (lane == 0) {
+        sh.wc[0][w] = __popc(mp);
+        sh.wc[1][w] = __popc(mq);
+    }
+    __syncthreads();
+    int bp = 0, bq = 0;
+    tp = 0;
+    tq = 0;
+#pragma unroll
+    for (int j = 0; j < ZW; ++j) {
+        const int cp = sh.wc[0][j], cq = sh.wc[1][j];
+        if (j < w) { bp += cp; bq += cq; }
+        tp += cp;
+        tq += cq;
+    }
+    __syncthreads();
+    const unsigned below = (1u << lane) - 1;
+    rp = bp + __popc(mp & below);
+    rq = bq + __popc(mq & below);
+}
+
+template <int ZW>
+__device__ __forceinline__ int block_rank(bool p, ZcShared& sh, int& tot)
+{
+    int rp, rq, tq;
+    block_rank2<ZW>(p, false, sh, rp, rq, tot, tq);
+    return rp;
+}
+
+// Exclusive ordered sums of two ints over the block, with totals.
+template <int ZW>
+__device__ __forceinline__ void block_scan2(int a, int b, ZcShared& sh, int& ea, int& eb, int& ta, int& tb)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int xa = a, xb = b;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int ya = __shfl_up_sync(FULL, xa, o), yb = __shfl_up_sync(FULL, xb, o);
+        if (lane >= o) { xa += ya; xb += yb; }
+    }
+    if (lane == 31) {
+        sh.ri[0][w] = xa;
+        sh.ri[1][w] = xb;
+    }
+    __syncthreads();
+    int ba = 0, bb = 0;
+    ta = 0;
+    tb = 0;
+#pragma unroll
+    for (int j = 0; j < ZW; ++j) {
+        const int ca = sh.ri[0][j], cb = sh.ri[1][j];
+        if (j < w) { ba += ca; bb += cb; }
+        ta += ca;
+        tb += cb;
+    }
+    __syncthreads();
+    ea = ba + xa - a;
+    eb = bb + xb - b;
+}
+
+template <int ZW>
+__device__ __forceinline__ double block_max_d(double v, ZcShared& sh)
+{
+    v = warp_max(v);
+    if ((threadIdx.x & 31) == 0) sh.rd[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double r = sh.rd[0];
+#pragma unroll
+    for (int j = 1; j < ZW; ++j) r = fmax(r, sh.rd[j]);
+    __syncthreads();
+    return r;
+}
+
+template <int ZW>
+__device__ __forceinline__ float block_max_f(float v, ZcShared& sh)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(FULL, v, o));
+    if ((threadIdx.x & 31) == 0) sh.rf[threadIdx.x >> 5] = v;
+    __syncthreads();
+    float r = sh.rf[0];
+#pragma unroll
+    for (int j = 1; j < ZW; ++j) r = fmaxf(r, sh.rf[j]);
+    __syncthreads();
+    return r;
+}
+
+template <int ZW>
+__device__ __forceinline__ long long block_max_ll(long long v, ZcShared& sh)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, (long long)__shfl_xor_sync(FULL, v, o));
+    if ((threadIdx.x & 31) == 0) sh.rl[threadIdx.x >> 5] = v;
+    __syncthreads();
+    long long r = sh.rl[0];
+#pragma unroll
+    for (int j = 1; j < ZW; ++j) r = max(r, sh.rl[j]);
+    __syncthreads();
+    return r;
+}
+
+template <int ZW>
+__device__ __forceinline__ int block_sum_i(int v, ZcShared& sh)
+{
+    v = warp_sum(v);
+    if ((threadIdx.x & 31) == 0) sh.ri[0][threadIdx.x >> 5] = v;
+    __syncthreads();
+    int r = 0;
+#pragma unroll
+    for (int j = 0; j < ZW; ++j) r += sh.ri[0][j];
+    __syncthreads();
+    return r;
+}
+
+// Sum over the ZG threads of a candidate group (aligned within the warp).
+template <int ZG>
+__device__ __forceinline__ int group_sum(int v)
+{
+#pragma unroll
+    for (int o = ZG / 2; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o, ZG);
+    return v;
+}
+
+// Merges the batch sh.tk/tc[0 .. m) into the sorted queue [h, h + n) of
+// (K, C); the merged queue starts at 0 afterwards (h = 0).  Entries beyond
+// cap are not taken (the batch's later ones first; *over is set).  Every
+// thread calls it; it begins and ends at a barrier.
+template <int ZT>
+__device__ __forceinline__ void pq_merge(uint64_t* K, uint32_t* C, int& h, int& n, int m, int cap, bool& over,
+                                         const ZcShared& sh)
+{
+    constexpr int PQ_PT = ZCTA_PQ_MAX / ZT;   // queue entries a thread holds while merging
+    const int tid = threadIdx.x;
+    if (n + m > cap) {
+        over = true;
+        m = cap - n;
+    }
+    if (m <= 0) return;
+    __syncthreads();                       // the batch is complete
+    // old entries: read, and moved past the new entries smaller than them
+    uint64_t ok[PQ_PT];
+    uint32_t oc[PQ_PT];
+    int opos[PQ_PT];
+#pragma unroll
+    for (int t = 0; t < PQ_PT; ++t) {
+        const int j = tid + t * ZT;
+        opos[t] = -1;
+        if (j < n) {
+            ok[t] = K[h + j];
+            oc[t] = C[h + j];
+            int r = 0;
+            for (int e = 0; e < m; ++e) r += pq_less(sh.tk[e], sh.tc[e], ok[t], oc[t]);
+            opos[t] = j + r;
+        }
+    }
+    // new entries: rank among the old ones (bisection) plus among the batch
+    uint64_t nk = 0;
+    uint32_t nc = 0;
+    int npos = -1;
+    if (tid < m) {
+        nk = sh.tk[tid];
+        nc = sh.tc[tid];
+        int lo = 0, len = n;                  // first old entry not less than the new one
+        while (len > 0) {
+            const int half = len >> 1;
+            if (pq_less(K[h + lo + half], C[h + lo + half], nk, nc)) { lo += half + 1; len -= half + 1; }
+            else len = half;
+        }
+        int r = 0;
+        for (int e = 0; e < m; ++e) r += pq_less(sh.tk[e], sh.tc[e], nk, nc);
+        npos = lo + r;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < PQ_PT; ++t)
+        if (opos[t] >= 0) { K[opos[t]] = ok[t]; C[opos[t]] = oc[t]; }
+    if (npos >= 0) { K[npos] = nk; C[npos] = nc; }
+    h = 0;
+    n += m;
+    __syncthreads();
+}
+
+}  // namespace
+
+// Extreme boundary points (inf.cpp:283-321): over the boundary list in
+// vertex order, extreme j (left min/max y, right min/max y, bottom min/max x,
+// top min/max x) is the first strict minimum / maximum among the entries on
+// its edge -- the smallest key (largest for a maximum), the earliest entry
+// among equal keys.  Each thread keeps its best of the entries it reads, then
+// a block reduction by (key, position).  ext[j] = vertex index or -1.
+template <int ZT>
+__device__ __forceinline__ void extreme_points(const Slice& S, int nB, ZcShared& sh, int (&ext)[8])
+{
+    constexpr int ZW = ZT / 32;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    long long bk[8];
+    int bp[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) { bk[j] = 0; bp[j] = INT_MAX; }
+    for (int t = tid; t < nB; t += ZT) {
+        const int vi = IX(S.blist, t);
+        const uint32_t fl = vfl_of(IX(S.v4, vi).w);
+        const double2 p = IX(S.vd, vi);
+        const long long kx = order_key(p.x), ky = order_key(p.y);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const uint32_t ebit = j < 2 ? VB_EL : j < 4 ? VB_ER : j < 6 ? VB_EB : VB_ET;
+            if (!(fl & ebit)) continue;
+            const long long kk = j < 4 ? ky : kx;
+            // entries come in increasing t: a later one wins only if strictly better
+            if (bp[j] == INT_MAX || ((j & 1) == 0 ? kk < bk[j] : kk > bk[j])) { bk[j] = kk; bp[j] = t; }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const long long ok = __shfl_xor_sync(FULL, bk[j], o);
+            const int op = __shfl_xor_sync(FULL, bp[j], o);
+            const bool better = op != INT_MAX &&
+                                (bp[j] == INT_MAX || ((j & 1) == 0 ? ok < bk[j] : ok > bk[j]) || (ok == bk[j] && op < bp[j]));
+            if (better) { bk[j] = ok; bp[j] = op; }
+        }
+        if (lane == 0) { sh.ek[w][j] = bk[j]; sh.ei[w][j] = bp[j]; }
+    }
+    __syncthreads();
+    if (tid < 8) {
+        const int j = tid;
+        long long k0 = sh.ek[0][j];
+        int p0 = sh.ei[0][j];
+#pragma unroll
+        for (int u = 1; u < ZW; ++u) {
+            const long long ok = sh.ek[u][j];
+            const int op = sh.ei[u][j];
+            if (op != INT_MAX && (p0 == INT_MAX || ((j & 1) == 0 ? ok < k0 : ok > k0) || (ok == k0 && op < p0))) {
+                k0 = ok;
+                p0 = op;
+            }
+        }
+        sh.bi[4 + j] = p0 == INT_MAX ? -1 : (int)IX(S.blist, p0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 8; ++j) ext[j] = sh.bi[4 + j];
+}
+
+template <int ZT>
+__device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
+{
+    constexpr int ZW = ZT / 32;          // warps
+    constexpr int ZG = ZT / 32;          // threads per candidate in the candidate passes
+    constexpr int ZGN = ZT / ZG;         // candidates per pass (32)
+    pdl_trigger();
+    extern __shared__ __align__(16) char smem[];
+    __shared__ ZcShared sh;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int gi = tid / ZG, gl = tid % ZG;
+#ifdef RKNN_CHECKED
+    if (tid == 0 && blockIdx.x == 0) g_fault = A.fault;
+    __syncthreads();
+    if (!g_fault) g_fault = A.fault;
+#endif
+    Slice S = carve(smem, A.caps);
+    const int VC = A.caps.vc, LC = A.caps.lc, PC = min(A.caps.pc, ZCTA_PQ_MAX);
+    const long long NCF = (long long)A.gf.gx * A.gf.gy, NCU = (long long)A.gu.gx * A.gu.gy;
+    (void)NCF; (void)NCU;
+    const double sx0 = A.sx0, sy0 = A.sy0, sx1 = A.sx1, sy1 = A.sy1;
+    const float E = kU32 * (float)fmax(fmax(fabs(sx0), fabs(sx1)), fmax(fabs(sy0), fabs(sy1))) * 1.01f + 1e-37f;
+    const float fsx0 = __double2float_rd(sx0), fsy0 = __double2float_rd(sy0);
+    const float fsx1 = __double2float_ru(sx1), fsy1 = __double2float_ru(sy1);
+    const double slack = 1e-5 * ((double)A.gf.cs + fmax(fmax(fabs(sx0), fabs(sx1)), fmax(fabs(sy0), fabs(sy1))));
+    const float tolE = (1e-9f + 2.0f * E) * (1.0f + 0x1p-20f);
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) sh.bi[0] = atomicAdd(A.work_counter, 1);
+        __syncthreads();
+        const int slot = sh.bi[0];
+        if (slot >= A.nq) break;
+        const int s = A.order ? A.order[slot] : slot;
+        const int qin = A.q_in[s];
+        const int k = A.k_in[s];
+        QDesc* qd = A.qd + s;
+        ZStats zs = {};
+        int qflags = 0;
+        if (qin < 0 || qin >= A.nf || k <= 0) {
+            if (tid == 0) {
+                QDesc d = {};
+                d.qpos = -1;
+                d.k = k;
+                d.flags = QF_BAD_QUERY;
+                *qd = d;
+                A.zst[s] = zs;
+                A.segs[(size_t)s * A.seg_cap] = make_int2(0, 0);
+            }
+            continue;
+        }
+        const int qpos = A.fpos[GX(qin, A.nf, 105)];
+        const float2 qf = A.fxy[GX(qpos, A.nf, 101)];
+        const double qx = qf.x, qy = qf.y;
+        const uint32_t ku = (uint32_t)k;
+        // block-uniform state (identical in every thread)
+        int nV = 4, nL = 0, nP = 0, hP = 0, nCons = -1, flags = 0;
+        double far_ = 0.0, nearb = DBL_MAX;
+        int cand_local = 0, cand64_local = 0;   // per-thread statistics
+
+        // ---- init: four space corners (inf.cpp:211-226) -------------------
+        double d2c = 0.0;
+        if (tid < 4) {
+            const double x = (tid & 1) ? sx1 : sx0;
+            const double y = (tid & 2) ? sy1 : sy0;
+            d2c = d2_64(x, y, qx, qy);
+            IX(S.vd, tid) = make_double2(x, y);
+            IX(S.v4, tid) = make_float4((float)x, (float)y, (float)d2c,
+                                        vpack(0, VB_BND | edge_bits(x, y, sx0, sy0, sx1, sy1)));
+        }
+        far_ = __dsqrt_rn(block_max_d<ZW>(d2c, sh));
+        Cut K1 = sqrt_cut(2.0 * far_, false);
+        Cut K2 = sqrt_cut(2.0 * DBL_MAX, true);
+
+        long long tph = clock64();
+#define PHASE(i) do { long long t_ = clock64(); zs.cyc[i] += t_ - tph; tph = t_; } while (0)
+        const int qcx = cell_coord(qf.x, A.gf.x0, A.gf.inv, A.gf.gx);
+        const int qcy = cell_coord(qf.y, A.gf.y0, A.gf.inv, A.gf.gy);
+        const int rmaxf = max(max(qcx, A.gf.gx - 1 - qcx), max(qcy, A.gf.gy - 1 - qcy));
+        int ring = 0;
+        bool ring_open;
+        uint64_t ring_key;
+        ring_gate(ring, rmaxf, (double)A.gf.cs, slack, far_, ring_open, ring_key);
+
+        // ---- best-first search --------------------------------------------
+        for (;;) {
+            // make the top poppable: expand rings whose cells could precede it
+            for (;;) {
+                if (!ring_open) break;
+                if (nP > 0 && IX(S.pqk, hP) < ring_key) break;
+                const int ncell = ring == 0 ? 1 : 8 * ring;
+                for (int t0 = 0; t0 < ncell; t0 += ZT) {
+                    const int t = t0 + tid;
+                    int cxx = 0, cyy = 0;
+                    bool ok = t < ncell;
+                    if (ok) {
+                        if (ring == 0) { cxx = qcx; cyy = qcy; }
+                        else {
+                            const int side = 2 * ring + 1;
+                            if (t < side) { cxx = qcx - ring + t; cyy = qcy - ring; }
+                            else if (t < 2 * side) { cxx = qcx - ring + (t - side); cyy = qcy + ring; }
+                            else if (t < 2 * side + (2 * ring - 1)) { cxx = qcx - ring; cyy = qcy - ring + 1 + (t - 2 * side); }
+                            else { cxx = qcx + ring; cyy = qcy - ring + 1 + (t - 2 * side - (2 * ring - 1)); }
+                        }
+                        ok = cxx >= 0 && cxx < A.gf.gx && cyy >= 0 && cyy < A.gf.gy;
+                    }
+                    int cid = 0;
+                    if (ok) {
+                        cid = cyy * A.gf.gx + cxx;
+                        ok = A.fstart[GX(cid + 1, NCF + 1, 102)] > A.fstart[GX(cid, NCF + 1, 102)];
+                    }
+                    const double key = ok ? rect_d2_64(qx, qy, A.fmbr[GX(cid, NCF, 103)]) : 0.0;
+                    int m;
+                    const int r = block_rank<ZW>(ok, sh, m);
+                    if (ok) { sh.tk[r] = (uint64_t)__double_as_longlong(key); sh.tc[r] = (uint32_t)cid; }
+                    bool over = false;
+                    pq_merge<ZT>(S.pqk.p, S.pqc.p, hP, nP, m, PC, over, sh);
+                    if (over) { flags |= QF_ZONE_PQ_OVERFLOW; break; }
+                }
+                ring++;
+                ring_gate(ring, rmaxf, (double)A.gf.cs, slack, far_, ring_open, ring_key);
+                if (flags) break;
+            }
+            PHASE(0);
+            if (flags || nP == 0) break;
+            // pop: every thread reads the head (nothing writes the queue
+            // until the next merge, which starts at a barrier)
+            const uint64_t keybits = IX(S.pqk, hP);
+            const uint32_t code = IX(S.pqc, hP);
+            hP++;
+            nP--;
+            const double key = __longlong_as_double((long long)keybits);
+
+            const bool is_point = (code & KIND_POINT) != 0;
+            const int id = (int)(code & ~KIND_POINT);
+            double px = 0, py = 0;
+            float4 mbr = make_float4(0, 0, 0, 0);
+            if (is_point) {
+                if (id == qpos) continue;
+                const float2 pf = A.fxy[GX(id, A.nf, 101)];
+                px = pf.x; py = pf.y;
+                if (A.skip_coincident && pf.x == qf.x && pf.y == qf.y) continue;
+                zs.pts++;
+            } else {
+                mbr = A.fmbr[GX(id, NCF, 103)];
+                zs.cells++;
+            }
+            bool prune;
+            PHASE(1);
+            // rule 1: prunes this entry and every later one (the zone is final)
+            bool r1;
+            if (keybits >= K1.hi) r1 = true;
+            else if (keybits <= K1.lo) r1 = false;
+            else r1 = __dsqrt_rn(key) > 2.0 * far_;
+            if (r1) break;
+            // rule 2: keep when nearer than twice the nearest bisector
+            bool r2;
+            if (keybits >= K2.hi) r2 = false;
+            else if (keybits <= K2.lo) r2 = true;
+            else r2 = __dsqrt_rn(key) < 2.0 * nearb;
+            if (r2) prune = false;
+            else {
+                // ---- vertex test (inf.cpp:268-353, 466-551) -------------
+                if (nCons < 0) {
+                    int nC = 0, nB = 0;
+                    for (int i0 = 0; i0 < nV; i0 += ZT) {
+                        const int i = i0 + tid;
+                        uint32_t cnt = 0, fl = 0;
+                        const bool in = i < nV;
+                        if (in) {
+                            const float w = IX(S.v4, i).w;
+                            cnt = vcnt_of(w);
+                            fl = vfl_of(w);
+                        }
+                        const bool c = in && cnt == ku - 1;
+                        const bool b = in && (fl & VB_BND) && cnt < ku;
+                        int rc, rb, tc, tb;
+                        block_rank2<ZW>(c, b, sh, rc, rb, tc, tb);
+                        if (c) IX(S.cons, nC + rc) = (uint16_t)i;
+                        if (b) IX(S.blist, nB + rb) = (uint16_t)i;
+                        nC += tc;
+                        nB += tb;
+                    }
+                    __syncthreads();
+                    int ext[8];
+                    extreme_points<ZT>(S, nB, sh, ext);
+                    float ex[8], ey[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        ex[j] = 0.0f; ey[j] = 0.0f;
+                        if (ext[j] >= 0) {
+                            const float4 e = IX(S.v4, ext[j]);
+                            ex[j] = e.x; ey[j] = e.y;
+                        }
+                    }
+                    // boundary vertices (count < k, not already considered)
+                    // within EPS of an extreme point (inf.cpp:326-346)
+                    for (int t0 = 0; t0 < nB; t0 += ZT) {
+                        const int t = t0 + tid;
+                        bool c = false;
+                        int vi = 0;
+                        if (t < nB) {
+                            vi = IX(S.blist, t);
+                            const float4 v = IX(S.v4, vi);
+                            if (vcnt_of(v.w) != ku - 1) {
+#pragma unroll
+                                for (int j = 0; j < 8; ++j) {
+                                    if (c || ext[j] < 0 || fabsf(v.x - ex[j]) > tolE || fabsf(v.y - ey[j]) > tolE) continue;
+                                    const double2 a = IX(S.vd, vi), b = IX(S.vd, ext[j]);
+                                    if (fabs(__dsub_rn(a.x, b.x)) < EPS && fabs(__dsub_rn(a.y, b.y)) < EPS) c = true;
+                                }
+                            }
+                        }
+                        int tot;
+                        const int r = block_rank<ZW>(c, sh, tot);
+                        if (c) IX(S.cons, nC + r) = (uint16_t)vi;
+                        nC += tot;
+                    }
+                    nCons = nC;
+                    __syncthreads();
+                }
+                const int nC = nCons;
+                bool hit = false;
+                const float px32 = (float)px, py32 = (float)py;
+                for (int t = tid; t < nC && !hit; t += ZT) {
+                    const int i = IX(S.cons, t);
+                    const float4 v = IX(S.v4, i);
+                    int r;
+                    if (is_point) r = closer32(px32 - v.x, py32 - v.y, E, v.z);
+                    else r = closer32(rect_dx32(v.x, mbr.x, mbr.z), rect_dx32(v.y, mbr.y, mbr.w), E, v.z);
+                    if (r < 0) {
+                        const double2 p = IX(S.vd, i);
+                        double dx64 = 0, dy64 = 0;
+                        if (is_point) {
+                            dx64 = __dsub_rn(px, p.x);
+                            dy64 = __dsub_rn(py, p.y);
+                        } else {
+                            if (p.x < (double)mbr.x) dx64 = __dsub_rn((double)mbr.x, p.x);
+                            else if (p.x > (double)mbr.z) dx64 = __dsub_rn(p.x, (double)mbr.z);
+                            if (p.y < (double)mbr.y) dy64 = __dsub_rn((double)mbr.y, p.y);
+                            else if (p.y > (double)mbr.w) dy64 = __dsub_rn(p.y, (double)mbr.w);
+                        }
+                        r = closer64(dx64, dy64, p.x, p.y, qx, qy);
+                    }
+                    hit = r != 0;
+                }
+                prune = !__syncthreads_or(hit);
+                PHASE(2);
+            }
+            if (prune) continue;
+
+            if (!is_point) {
+                // push the cell's facilities (inf.cpp:556-565)
+                const int p0 = A.fstart[GX(id, NCF + 1, 102)], p1 = A.fstart[GX(id + 1, NCF + 1, 102)];
+                for (int t0 = p0; t0 < p1; t0 += ZT) {
+                    const int t = t0 + tid;
+                    if (t < p1) {
+                        const float2 pf = A.fxy[GX(t, A.nf, 101)];
+                        sh.tk[tid] = (uint64_t)__double_as_longlong(d2_64(qx, qy, (double)pf.x, (double)pf.y));
+                        sh.tc[tid] = KIND_POINT | (uint32_t)t;
+                    }
+                    bool over = false;
+                    pq_merge<ZT>(S.pqk.p, S.pqc.p, hP, nP, min(ZT, p1 - t0), PC, over, sh);
+                    if (over) { flags |= QF_ZONE_PQ_OVERFLOW; break; }
+                }
+                if (flags) break;
+                continue;
+            }
+
+            // ================= accept facility `id`: add its bisector ======
+            if (nL >= LC) { flags |= QF_ZONE_L_OVERFLOW; break; }
+            if (tid < 32) {
+                Line64 l = {0.0, 0.0, 0, 0};
+                if (lane == 0) {
+                    l = make_bisector(qx, qy, px, py);
+                    sh.bd[0] = l.a;
+                    sh.bd[1] = l.b;
+                    sh.bi[1] = l.vert;
+                    sh.bi[2] = l.valid;
+                }
+            }
+            __syncthreads();
+            Line64 nb;
+            nb.a = sh.bd[0];
+            nb.b = sh.bd[1];
+            nb.vert = sh.bi[1];
+            nb.valid = sh.bi[2];
+            const float na32 = (float)nb.a, nb32 = (float)nb.b;
+            const float nab = fabsf(na32);
+            zs.nb++;
+            // The nearest bisector distance (inf.cpp:430-434) and the new
+            // line's records, by thread 32 while the count pass runs (the
+            // FP64 square root and division leave the critical path): nothing
+            // reads them before step (6), and nothing before it reads line nL.
+            if (tid == 32) {
+                double dl = nearb;
+                bool need = true;
+                if (nearb < DBL_MAX) {
+                    float est, err;
+                    if (nb.vert) {
+                        est = fabsf(qf.x - nb32);
+                        err = 4.0f * kU32 * (fabsf(qf.x) + fabsf(nb32)) + 1e-30f;
+                    } else {
+                        const float den = sqrtf(fmaf(na32, na32, 1.0f));
+                        est = fabsf(fmaf(na32, qf.x, nb32 - qf.y)) / den;
+                        err = 8.0f * kU32 * ((fabsf(na32 * qf.x) + fabsf(qf.y) + fabsf(nb32)) / den + est) + 1e-30f;
+                    }
+                    if ((double)__fsub_rd(est, err) > nearb) need = false;   // NaN keeps need
+                }
+                if (need) {
+                    const double d = line_dist64(qx, qy, nb.a, nb.b, nb.vert);
+                    if (d < nearb) dl = d;
+                }
+                sh.bd[2] = dl;
+                const uint32_t lf = (nb.vert ? LB_VERT : 0) | (nb.valid ? LB_VALID : 0);
+                IX(S.ld, nL) = make_double2(nb.a, nb.b);
+                IX(S.l4, nL) = make_float4(na32, nb32, 3.01f * kU32 * fabsf(nb32) + 1e-37f, __uint_as_float(lf));
+                IX(S.lpos, nL) = id;
+            }
+
+            // (1) count pass over the existing vertices (inf.cpp:359-364)
+            const int nV0 = nV;
+            for (int i = tid; i < nV0; i += ZT) {
+                const float4 v = IX(S.v4, i);
+                float r32, err;
+                if (nb.vert) {
+                    r32 = v.x - nb32;
+                    err = 3.0f * kU32 * (fabsf(v.x) + fabsf(nb32)) + 1e-37f;
+                } else {
+                    const float t = nab * fabsf(v.x);
+                    r32 = v.y - fmaf(na32, v.x, nb32);
+                    err = 5.0f * kU32 * (fabsf(v.y) + t + fabsf(nb32)) + 1e-37f;
+                }
+                bool valid;
+                if (r32 > err) valid = nb.valid == 1;
+                else if (r32 < -err) valid = nb.valid == 0;
+                else {
+                    const double2 p = IX(S.vd, i);
+                    valid = valid64(nb.a, nb.b, nb.vert, nb.valid, p.x, p.y);
+                }
+                const float tol = (1.0f + nab) * 1.2e-9f + err;
+                uint32_t fl = vfl_of(v.w) & ~VB_ON;
+                if (fabsf(r32) <= tol || !(fabsf(r32) < FLT_MAX)) fl |= VB_ON;
+                IX(S.v4, i).w = vpack(vcnt_of(v.w) + (valid ? 0u : 1u), fl);
+            }
+            __syncthreads();
+
+            PHASE(3);
+            // (2) candidate intersections: boundary edges (bottom, top, left,
+            //     right; inf.h:340-374) then every earlier bisector in order;
+            //     a group of ZG threads per candidate
+            const int C = 4 + nL;
+            const float a1l = __double2float_rd(nb.a), a1h = __double2float_ru(nb.a);
+            const float b1l = __double2float_rd(nb.b), b1h = __double2float_ru(nb.b);
+            // (every lane of a warp runs each pass, so that the group sums
+            // see the whole warp; a group past C computes nothing)
+            for (int c0 = 0; c0 < C; c0 += ZGN) {
+                const int c = c0 + gi;
+                const bool active = c < C;
+                double x = 0, y = 0;
+                bool ok = false;
+                uint8_t cf = 0;
+                bool need64 = true;           // bisector candidates: intersect in FP64
+                bool do_cert = false;         // the group counts certified violations
+                float xc = 0, yc = 0, KX = 0, KY = 0;
+                const int j = c - 4;
+                int ev = 0;
+                if (active && c >= 4) {
+                    const float4 e4 = IX(S.l4, j);
+                    ev = (__float_as_uint(e4.w) & LB_VERT) ? 1 : 0;
+                    if (!nb.vert && !ev) {
+                        // float interval of the intersection (directed rounding)
+                        const float a2l = lo32(e4.x), a2h = hi32(e4.x);
+                        const float b2l = lo32(e4.y), b2h = hi32(e4.y);
+                        const float dl = __fsub_rd(a1l, a2h), dh = __fsub_ru(a1h, a2l);
+                        const float nl = __fsub_rd(b2l, b1h), nh = __fsub_ru(b2h, b1l);
+                        if ((dl > 4e-9f || dh < -4e-9f) && fabsf(nl) < FLT_MAX && fabsf(nh) < FLT_MAX &&
+                            fabsf(dl) < FLT_MAX && fabsf(dh) < FLT_MAX) {
+                            float xl, xh;
+                            if (dl > 0.0f) {
+                                xl = __fdiv_rd(nl, nl >= 0.0f ? dh : dl);
+                                xh = __fdiv_ru(nh, nh >= 0.0f ? dl : dh);
+                            } else {
+                                const float pl = -dh, ph = -dl;
+                                xl = -__fdiv_ru(nh, nh >= 0.0f ? pl : ph);
+                                xh = -__fdiv_rd(nl, nl >= 0.0f ? ph : pl);
+                            }
+                            const float m1 = __fmul_rd(a1l, xl), m2 = __fmul_rd(a1l, xh), m3 = __fmul_rd(a1h, xl), m4 = __fmul_rd(a1h, xh);
+                            const float n1 = __fmul_ru(a1l, xl), n2 = __fmul_ru(a1l, xh), n3 = __fmul_ru(a1h, xl), n4 = __fmul_ru(a1h, xh);
+                            float yl = __fadd_rd(fminf(fminf(m1, m2), fminf(m3, m4)), b1l);
+                            float yh = __fadd_ru(fmaxf(fmaxf(n1, n2), fmaxf(n3, n4)), b1h);
+                            // pad for the FP64 rounding of the reference's evaluation
+                            const float px_ = 1e-12f * fmaxf(fabsf(xl), fabsf(xh)) + 1e-37f;
+                            const float py_ = 1e-12f * (fmaxf(fabsf(yl), fabsf(yh)) + fabsf(a1h) * fmaxf(fabsf(xl), fabsf(xh)) + fabsf(b1h)) + 1e-37f;
+                            xl = __fsub_rd(xl, px_); xh = __fadd_ru(xh, px_);
+                            yl = __fsub_rd(yl, py_); yh = __fadd_ru(yh, py_);
+                            if (xl <= xh && yl <= yh && fabsf(xl) < FLT_MAX && fabsf(xh) < FLT_MAX &&
+                                fabsf(yl) < FLT_MAX && fabsf(yh) < FLT_MAX) {
+                                if (xh < fsx0 || xl > fsx1 || yh < fsy0 || yl > fsy1) need64 = false;  // outside
+                                else {
+                                    xc = 0.5f * xl + 0.5f * xh;
+                                    yc = 0.5f * yl + 0.5f * yh;
+                                    const float rx = (0.5f * xh - 0.5f * xl) * (1.0f + 4.0f * kU32) + fabsf(xc) * 2.0f * kU32 + 1e-37f;
+                                    const float ry = (0.5f * yh - 0.5f * yl) * (1.0f + 4.0f * kU32) + fabsf(yc) * 2.0f * kU32 + 1e-37f;
+                                    KX = rx * (1.0f + kU32) + 3.01f * kU32 * fabsf(xc);
+                                    KY = ry + 3.01f * kU32 * fabsf(yc) + 1e-37f;
+                                    do_cert = true;
+                                }
+                            }
+                        }
+                    }
+                }
+                // certified violations of earlier bisectors, the group's
+                // threads taking every ZG-th one
+                int cert = 0;
+                if (do_cert)
+                    for (int m = gl; m < nL; m += ZG) cert += inval32(IX(S.l4, m), xc, yc, KX, KY);
+                cert = group_sum<ZG>(cert);
+                if (do_cert && cert >= k) need64 = false;
+                if (active && gl == 0) {
+                    if (c < 4) {
+                        const double ea = 0, eb = (c == 0) ? sy0 : (c == 1) ? sy1 : (c == 2) ? sx0 : sx1;
+                        const int bev = c >= 2;
+                        if (intersect64(nb.a, nb.b, nb.vert, ea, eb, bev, x, y))
+                            ok = (c < 2) ? (x >= sx0 && x <= sx1) : (y >= sy0 && y <= sy1);
+                        cf = VB_BND;
+                        cand_local += ok;
+                    } else {
+                        if (need64) {
+                            cand64_local++;
+                            const double2 e = IX(S.ld, j);
+                            if (intersect64(nb.a, nb.b, nb.vert, e.x, e.y, ev, x, y))
+                                ok = x >= sx0 && x <= sx1 && y >= sy0 && y <= sy1;
+                        }
+                        cand_local++;
+                    }
+                    IX(S.cd, c) = make_double2(x, y);
+                    IX(S.c2, c) = make_float2((float)x, (float)y);
+                    IX(S.cfl, c) = ok ? (uint8_t)(cf | 0x80) : (uint8_t)0;
+                }
+            }
+            __syncthreads();
+
+            PHASE(4);
+            // (3) deduplicate (|dx| < 1e-9 and |dy| < 1e-9) against existing
+            //     vertices near the new line
+            {
+                int nOn = 0;
+                for (int i0 = 0; i0 < nV0; i0 += ZT) {
+                    const int i = i0 + tid;
+                    const bool on = i < nV0 && (vfl_of(IX(S.v4, i).w) & VB_ON);
+                    int tot;
+                    const int r = block_rank<ZW>(on, sh, tot);
+                    if (on) IX(S.cons, nOn + r) = (uint16_t)i;   // cons reused as scratch
+                    nOn += tot;
+                }
+                __syncthreads();
+                nCons = -1;   // considered list must be rebuilt
+                if (nOn > 0) {
+                    for (int c = tid; c < C; c += ZT) {
+                        if (!(IX(S.cfl, c) & 0x80)) continue;
+                        const float2 c32 = IX(S.c2, c);
+                        bool dup = false;
+                        for (int t = 0; t < nOn && !dup; ++t) {
+                            const int i = IX(S.cons, t);
+                            const float4 v = IX(S.v4, i);
+                            if (fabsf(v.x - c32.x) > tolE || fabsf(v.y - c32.y) > tolE) continue;
+                            const double2 p = IX(S.vd, i), q = IX(S.cd, c);
+                            if (fabs(__dsub_rn(p.x, q.x)) < EPS && fabs(__dsub_rn(p.y, q.y)) < EPS) dup = true;
+                        }
+                        if (dup) IX(S.cfl, c) &= 0x7f;
+                    }
+                }
+                __syncthreads();
+            }
+
+            PHASE(5);
+            // (4) counts of the surviving candidates over earlier bisectors,
+            //     a group per candidate: certain violations in float, the
+            //     undecided ones in FP64
+            for (int c0 = 0; c0 < C; c0 += ZGN) {
+                const int c = c0 + gi;
+                const bool live = c < C && (IX(S.cfl, c) & 0x80) != 0;
+                int cnt = 0, undec = 0;
+                double2 p = make_double2(0, 0);
+                float2 c32 = make_float2(0, 0);
+                float KX = 0, KY = 0;
+                const int gen = c - 4;
+                if (live) {
+                    p = IX(S.cd, c);
+                    c32 = IX(S.c2, c);
+                    KX = kU32 * fabsf(c32.x) * (1.0f + kU32) + 3.01f * kU32 * fabsf(c32.x);
+                    KY = kU32 * fabsf(c32.y) + 3.01f * kU32 * fabsf(c32.y) + 1e-37f;
+                    // the generating bisector passes through the candidate: FP64
+                    if (gen >= 0 && gl == 0) {
+                        const double2 g = IX(S.ld, gen);
+                        const uint32_t lf = __float_as_uint(IX(S.l4, gen).w);
+                        cnt += !valid64(g.x, g.y, lf & LB_VERT, (lf & LB_VALID) ? 1 : 0, p.x, p.y);
+                    }
+                    for (int m = gl; m < nL; m += ZG) {
+                        const int sm = (m == gen) ? -1 : side32(IX(S.l4, m), c32.x, c32.y, KX, KY);
+                        cnt += sm > 0;
+                        undec += sm == 0;
+                    }
+                }
+                cnt = group_sum<ZG>(cnt);
+                undec = group_sum<ZG>(undec);
+                // the bisectors the float test left undecided, in FP64
+                int extra = 0;
+                if (live && cnt < k && undec > 0) {
+                    for (int m = gl; m < nL; m += ZG) {
+                        if (m == gen) continue;
+                        const float4 q = IX(S.l4, m);
+                        if (side32(q, c32.x, c32.y, KX, KY) != 0) continue;
+                        const double2 g = IX(S.ld, m);
+                        const uint32_t lf = __float_as_uint(q.w);
+                        extra += !valid64(g.x, g.y, lf & LB_VERT, (lf & LB_VALID) ? 1 : 0, p.x, p.y);
+                    }
+                }
+                cnt += group_sum<ZG>(extra);
+                if (c < C && gl == 0) IX(S.ccnt, c) = live ? cnt : k;
+            }
+            __syncthreads();
+            // (4b) a candidate closer than 1e-9 to an earlier one is not added
+            // (the reference keeps the first): float prefilter, then the exact
+            // sequential resolution when anything is close
+            {
+                bool anyclose = false;
+                for (int c0 = 0; c0 < C; c0 += ZGN) {
+                    const int c = c0 + gi;
+                    if (c >= C || !(IX(S.cfl, c) & 0x80) || IX(S.ccnt, c) >= k) continue;
+                    // doubles within 1e-9 give floats within 1e-9 + u(|x1|+|x2|)
+                    const float2 c32 = IX(S.c2, c);
+                    const float tx = 3.0f * kU32 * fabsf(c32.x) + 2e-9f, ty = 3.0f * kU32 * fabsf(c32.y) + 2e-9f;
+                    for (int c2 = gl; c2 < c; c2 += ZG) {
+                        if (!(IX(S.cfl, c2) & 0x80)) continue;
+                        const float2 o = IX(S.c2, c2);
+                        if (fabsf(o.x - c32.x) <= tx && fabsf(o.y - c32.y) <= ty) { anyclose = true; break; }
+                    }
+                }
+                if (__syncthreads_or(anyclose)) {
+                    if (tid == 0) {
+                        for (int c = 0; c < C; ++c) {
+                            if (!(IX(S.cfl, c) & 0x80)) continue;
+                            const double2 p = IX(S.cd, c);
+                            for (int c2 = 0; c2 < c; ++c2) {
+                                if (!(IX(S.cfl, c2) & 0x80)) continue;
+                                const double2 o = IX(S.cd, c2);
+                                if (fabs(__dsub_rn(o.x, p.x)) < EPS && fabs(__dsub_rn(o.y, p.y)) < EPS) { IX(S.cfl, c) &= 0x7f; break; }
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+
+            // (5) erase old vertices with count >= k (order kept), then append
+            //     the new vertices with count < k in candidate order
+            int w = 0;
+            for (int i0 = 0; i0 < nV0; i0 += ZT) {
+                const int i = i0 + tid;
+                bool keep = false;
+                float4 v = make_float4(0, 0, 0, 0);
+                double2 p = make_double2(0, 0);
+                if (i < nV0) {
+                    v = IX(S.v4, i);
+                    keep = vcnt_of(v.w) < ku;
+                    if (keep) p = IX(S.vd, i);
+                }
+                int tot;
+                const int r = block_rank<ZW>(keep, sh, tot);     // every read above precedes its barriers
+                if (keep) {
+                    const int o = w + r;
+                    v.w = vpack(vcnt_of(v.w), vfl_of(v.w) & ~VB_ON);
+                    IX(S.vd, o) = p;
+                    IX(S.v4, o) = v;
+                }
+                w += tot;
+            }
+            int nnew = 0;
+            for (int c0 = 0; c0 < C; c0 += ZT) {
+                const int c = c0 + tid;
+                const bool keep = c < C && (IX(S.cfl, c) & 0x80) && IX(S.ccnt, c) < k;
+                int tot;
+                const int r = block_rank<ZW>(keep, sh, tot);
+                const int o = w + nnew + r;
+                if (keep && o < VC) {
+                    const double2 p = IX(S.cd, c);
+                    const float2 c32 = IX(S.c2, c);
+                    IX(S.vd, o) = p;
+                    IX(S.v4, o) = make_float4(c32.x, c32.y, (float)d2_64(p.x, p.y, qx, qy),
+                                              vpack((uint32_t)IX(S.ccnt, c),
+                                                    (IX(S.cfl, c) & VB_BND) | edge_bits(p.x, p.y, sx0, sy0, sx1, sy1)));
+                }
+                nnew += tot;
+            }
+            zs.kept += nnew;
+            nV = w + nnew;
+            const bool vover = nV > VC;
+            if (vover) nV = VC;
+            __syncthreads();            // the vertex set is complete before (7) reads it
+
+            // (6) nearest bisector distance (computed by thread 32 while the
+            //     count pass ran; every barrier since makes it visible)
+            {
+                const double dl = sh.bd[2];
+                if (dl != nearb) {
+                    nearb = dl;
+                    K2 = sqrt_cut(2.0 * nearb, true);
+                }
+            }
+            nL += 1;
+            if (vover) flags |= QF_ZONE_V_OVERFLOW;
+            if (nV > zs.vmax) zs.vmax = nV;
+            // (7) furthest remaining vertex (inf.cpp:445-451): the FP64
+            //     maximum is among the vertices whose rounded float value is
+            //     the float maximum
+            {
+                float m32 = 0.0f;
+                for (int i = tid; i < nV; i += ZT) m32 = fmaxf(m32, IX(S.v4, i).z);
+                m32 = block_max_f<ZW>(m32, sh);
+                long long m = 0;
+                for (int i = tid; i < nV; i += ZT)
+                    if (IX(S.v4, i).z == m32) {
+                        const double2 p = IX(S.vd, i);
+                        m = max(m, __double_as_longlong(d2_64(p.x, p.y, qx, qy)));
+                    }
+                m = block_max_ll<ZW>(m, sh);
+                const double f = __dsqrt_rn(__longlong_as_double(m));
+                if (f != far_) {
+                    far_ = f;
+                    K1 = sqrt_cut(2.0 * far_, false);
+                    ring_gate(ring, rmaxf, (double)A.gf.cs, slack, far_, ring_open, ring_key);
+                }
+            }
+            PHASE(6);
+            if (flags) break;
+        }
+        __syncthreads();
+        qflags |= flags;
+        zs.nb = nL;
+        zs.cand = block_sum_i<ZW>(cand_local, sh);
+        zs.cand64 = block_sum_i<ZW>(cand64_local, sh);
+
+        // ---- epilogue 1: exact half-planes relative to q -------------------
+        float4* planes = A.planes + (size_t)s * A.pstride;
+        double cmax = 0.0;
+        for (int m = tid; m < nL; m += ZT) {
+            const int pos = IX(S.lpos, m);
+            const float2 f = A.fxy[GX(pos, A.nf, 101)];
+            const double dx = (double)f.x - qx, dy = (double)f.y - qy;
+            const double c = dx * dx + dy * dy;
+            const float4 p = make_float4((float)(-2.0 * dx), (float)(-2.0 * dy), (float)c, 0.0f);
+            planes[GX(m, A.pstride, 106)] = p;
+            IX(S.splanes, m) = p;
+            A.bis_pos[(size_t)s * A.pstride + GX(m, A.pstride, 107)] = pos;
+            cmax = fmax(cmax, c);
+        }
+        cmax = block_max_d<ZW>(cmax, sh);
+        const double Fp = sqrt(cmax) * (1.0 + 1e-6) + 1e-30;
+        const float k2f = (float)(8.0 * (double)kU32 * 2.0 * Fp * (1.0 + 1e-6));
+        const float kf2 = (float)(8.0 * (double)kU32 * Fp * Fp * (1.0 + 1e-6)) + 1e-30f;
+        const double k2f64 = 8.0 * kU64 * 2.0 * Fp * (1.0 + 1e-6);
+        const double kf264 = 8.0 * kU64 * Fp * Fp * (1.0 + 1e-6) + 1e-300;
+
+        // ---- epilogue 2: ring scan over user cells ------------------------
+        const Grid gu = A.gu;
+        const int ucx = cell_coord(qf.x, gu.x0, gu.inv, gu.gx);
+        const int ucy = cell_coord(qf.y, gu.y0, gu.inv, gu.gy);
+        const int RM = A.rmax;
+        const int W = 2 * RM + 1;
+        const int nwords = (W * W + 31) / 32;
+        for (int i = tid; i < nwords; i += ZT) IX(S.bitmap, i) = 0u;
+        __syncthreads();
+        const float delta = 8.0f * kU32 * (fabsf(gu.x0) + fabsf(gu.y0) + gu.cs * (float)max(gu.gx, gu.gy) + fabsf(qf.x) + fabsf(qf.y) + gu.cs) + 1e-30f;
+        const int rmaxu = max(max(ucx, gu.gx - 1 - ucx), max(ucy, gu.gy - 1 - ucy));
+        bool all_users = nL == 0 && A.nu > 0;
+        int rend = -1;
+        if (!all_users && A.nu > 0) {
+            for (int r = 0;; ++r) {
+                if (r > rmaxu) { rend = r - 1; break; }
+                if (r > RM) { all_users = true; break; }
+                const int ncell = r == 0 ? 1 : 8 * r;
+                bool anykeep = false;
+                for (int t0 = 0; t0 < ncell; t0 += ZT) {
+                    const int t = t0 + tid;
+                    int dx = 0, dy = 0;
+                    bool ok = t < ncell;
+                    if (ok && r > 0) {
+                        const int side = 2 * r + 1;
+                        if (t < side) { dx = -r + t; dy = -r; }
+                        else if (t < 2 * side) { dx = -r + (t - side); dy = r; }
+                        else if (t < 2 * side + (2 * r - 1)) { dx = -r; dy = -r + 1 + (t - 2 * side); }
+                        else { dx = r; dy = -r + 1 + (t - 2 * side - (2 * r - 1)); }
+                    }
+                    const int cxx = ucx + dx, cyy = ucy + dy;
+                    ok = ok && cxx >= 0 && cxx < gu.gx && cyy >= 0 && cyy < gu.gy;
+                    bool keep = false;
+                    if (ok) {
+                        const float X0 = (gu.x0 + (float)cxx * gu.cs) - qf.x - delta;
+                        const float X1 = (gu.x0 + (float)(cxx + 1) * gu.cs) - qf.x + delta;
+                        const float Y0 = (gu.y0 + (float)cyy * gu.cs) - qf.y - delta;
+                        const float Y1 = (gu.y0 + (float)(cyy + 1) * gu.cs) - qf.y + delta;
+                        int viol = 0;
+                        for (int m = 0; m < nL && viol < k; ++m) {
+                            const float4 p = IX(S.splanes, m);
+                            const float X = p.x > 0.0f ? X1 : X0;
+                            const float Y = p.y > 0.0f ? Y1 : Y0;
+                            const float mx = fmaf(p.x, X, fmaf(p.y, Y, p.z));
+                            const float bd = 8.0f * kU32 * fmaf(fabsf(p.x), fabsf(X), fmaf(fabsf(p.y), fabsf(Y), fabsf(p.z))) + 1e-30f;
+                            viol += (mx < -bd);
+                        }
+                        keep = viol < k;
+                    }
+                    if (keep) {
+                        const int bit = (dy + RM) * W + (dx + RM);
+                        atomicOr(&IX(S.bitmap, bit >> 5), 1u << (bit & 31));
+                    }
+                    anykeep |= keep;
+                }
+                anykeep = __syncthreads_or(anykeep);
+                if (!anykeep && r >= 1) { rend = r - 1; break; }
+                rend = r;
+            }
+            zs.rings = rend + 1;
+        }
+        __syncthreads();
+
+        // ---- segments: one user range per row ------------------------------
+        int2* seg = A.segs + (size_t)s * A.seg_cap;
+        int nseg = 0, ncand = 0;
+        if (all_users) {
+            if (tid == 0) {
+                seg[0] = make_int2(0, 0);
+                seg[1] = make_int2(0, A.nu);
+            }
+            nseg = 1;
+            ncand = A.nu;
+            qflags |= QF_ALL_USERS;
+        } else {
+            const int y0 = max(0, ucy - rend), y1 = min(gu.gy - 1, ucy + rend);
+            const int xl0 = max(0, ucx - rend), xl1 = min(gu.gx - 1, ucx + rend);
+            for (int r0 = y0; r0 <= y1; r0 += ZT) {
+                const int row = r0 + tid;
+                int st = 0, len = 0;
+                if (row <= y1) {
+                    const int dy = row - ucy;
+                    int xmin = INT_MAX, xmax = -1;
+                    for (int cxx = xl0; cxx <= xl1; ++cxx) {
+                        const int bit = (dy + RM) * W + (cxx - ucx + RM);
+                        if (IX(S.bitmap, bit >> 5) & (1u << (bit & 31))) {
+                            xmin = min(xmin, cxx);
+                            xmax = cxx;
+                        }
+                    }
+                    if (xmax >= 0) {
+                        st = A.ustart[GX(row * gu.gx + xmin, NCU + 1, 104)];
+                        len = A.ustart[GX(row * gu.gx + xmax + 1, NCU + 1, 104)] - st;
+                    }
+                }
+                const bool has = len > 0;
+                int pre, excl, tot_has, tot_len;
+                block_scan2<ZW>(has ? 1 : 0, has ? len : 0, sh, pre, excl, tot_has, tot_len);
+                if (has) seg[GX(nseg + pre, A.seg_cap, 108)] = make_int2(st, ncand + excl);
+                nseg += tot_has;
+                ncand += tot_len;
+            }
+            if (tid == 0) seg[GX(nseg, A.seg_cap, 109)] = make_int2(0, ncand);
+        }
+
+        PHASE(7);
+#undef PHASE
+        if (tid == 0) {
+            QDesc d;
+            d.qx = qf.x;
+            d.qy = qf.y;
+            d.qpos = qpos;
+            d.k = k;
+            d.nb = nL;
+            d.nseg = nseg;
+            d.k2f = k2f;
+            d.kf2 = kf2;
+            d.k2f64 = k2f64;
+            d.kf264 = kf264;
+            d.ncand = ncand;
+            d.flags = qflags;
+            d.rho = 0.0f;
+            d.pad = 0;
+            *qd = d;
+            A.zst[s] = zs;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(ZCTA_THREADS, 1) zone_kernel_cta(ZoneArgs a) { zone_cta_body<ZCTA_THREADS>(a); }
+__global__ void __launch_bounds__(ZCTA_THREADS / 2, 1) zone_kernel_cta_half(ZoneArgs a)
+{
+    zone_cta_body<ZCTA_THREADS / 2>(a);
+}
+
+}  // namespace rknn

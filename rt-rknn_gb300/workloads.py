@@ -98,6 +98,10 @@ def config3():
 
 
 def config4():
+    """One batch of the 16,384 mixed-k queries, both modes, then the
+    autotuner on that batch (FP32): the default and best device times, the
+    chosen grid densities, users per lane and warps per block, and both
+    modes again with the chosen settings."""
     ds = datagen.config(4)
     qs, ks = ds.queries.astype(np.int32), ds.ks.astype(np.int32)
     out = {"config": 4, "queries": len(qs)}
@@ -106,6 +110,10 @@ def config4():
             ms, st, _ = _batch(idx, qs, ks, mode, reps=2)
             out[mode] = {"device_ms": ms, "qps": len(qs) / (ms / 1e3), "results": st["results"],
                          "candidates": st["candidates"], "survivors": st["survivors"]}
+        out["tune"] = idx.tune(qs, ks, "fp32")
+        for mode in ("fp32", "fp64"):
+            ms, st, _ = _batch(idx, qs, ks, mode, reps=2)
+            out[mode + "_tuned"] = {"device_ms": ms, "qps": len(qs) / (ms / 1e3)}
     return out
 
 
@@ -131,12 +139,74 @@ def config5():
     return out
 
 
+def order_ab():
+    """Batch device time with the work queue ordered by k alone against
+    ordered by the candidate estimate within each k class (RKNN_ORDER=est at
+    index creation), on workloads 2 (k=10 and mixed k), 3 and 4, FP32 and
+    FP64; the result sets must not change."""
+    out = {"order_ab": {}}
+    rng = np.random.default_rng(8)
+    cases = []
+    ds2 = datagen.config(2)
+    cases.append(("config2_k10", ds2, ds2.queries.astype(np.int32), np.full(len(ds2.queries), 10, np.int32)))
+    cases.append(("config2_mixed", ds2, ds2.queries.astype(np.int32),
+                  np.floor(np.exp(rng.uniform(0, np.log(65), len(ds2.queries)))).clip(1, 64).astype(np.int32)))
+    ds3 = datagen.config(3)
+    cases.append(("config3", ds3, ds3.queries.astype(np.int32), ds3.ks.astype(np.int32)))
+    ds4 = datagen.config(4)
+    cases.append(("config4", ds4, ds4.queries.astype(np.int32), ds4.ks.astype(np.int32)))
+    for name, ds, qs, ks in cases:
+        row = {}
+        res = {}
+        for order in ("k", "est"):
+            os.environ["RKNN_ORDER"] = order
+            with rknn.Index.of(ds) as idx:
+                for mode in ("fp32", "fp64"):
+                    ms, _, r = _batch(idx, qs, ks, mode, reps=3)
+                    row[f"{mode}_{order}_ms"] = ms
+                    res[(order, mode)] = r
+        os.environ.pop("RKNN_ORDER", None)
+        row["same_results"] = all(all(np.array_equal(a, b) for a, b in zip(res[("k", m)], res[("est", m)]))
+                                  for m in ("fp32", "fp64"))
+        out["order_ab"][name] = row
+    return out
+
+
+def profile_single(k: int, n: int):
+    """n single FP64 queries through the influence zone on the config-2
+    workload (the plain form; the launch to capture with ncu is the last)."""
+    ds = datagen.config(2)
+    with rknn.Index.of(ds, filter="inf") as idx:
+        for q in ds.queries[:n]:
+            print(int(q), len(idx.query(int(q), k, "fp64")))
+
+
+def profile_index(c: int):
+    """Only the index build of workload c (the grid build kernels)."""
+    ds = datagen.config(c)
+    with rknn.Index.of(ds) as idx:
+        print(idx.info())
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--configs", default="1,2,3,4,5")
     ap.add_argument("--out", default=None)
+    ap.add_argument("--profile-single", nargs=2, type=int, metavar=("K", "N"),
+                    help="only N single FP64 influence-zone queries at k=K on workload 2")
+    ap.add_argument("--profile-index", type=int, metavar="C", help="only the index build of workload C")
+    ap.add_argument("--order-ab", action="store_true", help="only the work-order comparison")
     a = ap.parse_args(argv)
     build.build()
+    if a.order_ab:
+        print(json.dumps(order_ab()), flush=True)
+        return 0
+    if a.profile_single:
+        profile_single(*a.profile_single)
+        return 0
+    if a.profile_index:
+        profile_index(a.profile_index)
+        return 0
     fns = {1: config1, 2: config2, 3: config3, 4: config4, 5: config5}
     fh = open(a.out, "w") if a.out else None
     for c in (int(x) for x in a.configs.split(",")):

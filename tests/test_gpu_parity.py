@@ -262,10 +262,14 @@ def test_flat_batches_into_page_locked_ids(engine):
     idx.close()
 
 
-def test_zone_bisectors_match_port(engine):
+@pytest.mark.parametrize("cta", ["1", "0"])
+def test_zone_bisectors_match_port(engine, monkeypatch, cta):
     """Same grid, same rules: the zone kernel builds rknn-inf's bisector set
-    in the same order as the CPU restatement does."""
-    for nf, nu, k in ((1000, 10000, 5), (20000, 200000, 10), (20000, 200000, 3)):
+    in the same order as the CPU restatement does -- the one-block kernel
+    (small batches and single queries, cta=1) and the one-warp kernel
+    (cta=0) alike."""
+    monkeypatch.setenv("RKNN_ZONE_CTA", cta)
+    for nf, nu, k in ((1000, 10000, 5), (20000, 200000, 10), (20000, 200000, 3), (20000, 200000, 25)):
         ds = datagen.uniform(nf, nu, seed=31 + k, nq=40, k=k)
         idx = engine.Index.of(ds, filter="inf")
         info = idx.info()
@@ -273,12 +277,20 @@ def test_zone_bisectors_match_port(engine):
                                                info["fgrid_gx"], info["fgrid_gy"]))
         idx.query_batch(ds.queries, k, "fp32")
         same = 0
+        ports = []
         for slot, q in enumerate(ds.queries):
             gb, flags = idx.last_zone(slot)
             pb, _, _ = port.query(int(q), k, verify=False)
+            ports.append(pb)
             same += np.array_equal(gb, pb)
             assert flags & 7 == 0
-        assert same == len(ds.queries), (nf, k, same)
+        assert same == len(ds.queries), (nf, k, same, cta)
+        # one query per launch (the plain form)
+        for q, pb in list(zip(ds.queries, ports))[:8]:
+            idx.query(int(q), k, "fp64")
+            gb, flags = idx.last_zone(0)
+            assert np.array_equal(gb, pb) and flags & 7 == 0, (int(q), k, cta)
+        idx.close()
 
 
 def test_full_scale_checksum(engine):
