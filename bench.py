@@ -534,7 +534,7 @@ def run_ours(args):
         orc.add(si % len(pool), ids, off)
 
     # ---- end to end through the C ABI with host buffers ------------------
-    e2e_times, h2d, d2h = [], 0, 0
+    e2e_times, e2e_dev, h2d, d2h = [], [], 0, 0
     idx.query_batch_flat(qsets[0], ks, "fp32")                      # sizes the output buffers
     idx.query_batch_flat(qsets[1], ks, "fp32")                      # warm: ids written in place from now on
     for i in range(nsteps):
@@ -546,11 +546,24 @@ def run_ours(args):
         t1 = time.perf_counter()
         ids, offs = idx.query_batch_flat(q, ks, "fp32")
         e2e_times.append(time.perf_counter() - t1)
+        e2e_dev.append(idx.last_stats()["device_ms"])               # the engine's events around its launch
         h2d = q.nbytes + ks.nbytes
         d2h = 4 * (NQ + 1) + 4 * int(ids.shape[0])
         if orc:
             orc.add(si, ids, offs)
     e2e = NQ / statistics.mean(e2e_times) * ws
+    # the same calls back to back, without the flush and its synchronization
+    nf_times = []
+    for i in range(nsteps):
+        q = pool[(args.warmup + i) % len(pool)]
+        t1 = time.perf_counter()
+        idx.query_batch_flat(q, ks, "fp32")
+        nf_times.append(time.perf_counter() - t1)
+    e2e_diag = {"call_us_mean": 1e6 * statistics.mean(e2e_times), "call_us_median": 1e6 * statistics.median(e2e_times),
+                "call_us_max": 1e6 * max(e2e_times), "device_us_median": 1e3 * statistics.median(e2e_dev),
+                "no_flush_call_us_median": 1e6 * statistics.median(nf_times),
+                "note": "call = rknn_query_batch through the Python binding with host buffers; device = the "
+                        "engine's CUDA events around its launch inside the call"}
 
     # ---- plain FP64 single-query form (one query per launch, influence zone)
     single = pool[0][:200]
@@ -753,6 +766,7 @@ def run_ours(args):
                    "l2": "256 MB flush before each timed step", "parallelism": f"replicas x{ws}"},
         "wall_s": wall,
         "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e_diag": e2e_diag,
         "gpu_launches": 5 * nsteps,
         "mismatches_vs_oracle": orc.mismatches if orc and orc.ok else None,
         "checked_vs_oracle": (f"{orc.checked} query results (every timed device step, every end-to-end "

@@ -172,6 +172,29 @@ def order_ab():
     return out
 
 
+def profile_verify(upt: int, warps: int, nq: int = 16384):
+    """One batch of nq workload-2 queries at k=10 in FP32 (too many for the
+    fused verification: the separate verification kernel runs) with the
+    verification's users per lane and warps per block given, run twice (the
+    second launch is the one to capture), then its per-kernel device times
+    in profiling mode and its statistics."""
+    ds = datagen.config(2)
+    qs = np.random.default_rng(99).choice(ds.nf, size=nq, replace=False).astype(np.int32)
+    with rknn.Index.of(ds, users_per_thread=upt, verify_warps=warps) as idx:
+        idx.query_batch_flat(qs, 10, "fp32")
+        idx.query_batch_flat(qs, 10, "fp32")
+        idx.set_profiling(True)
+        ms = []
+        for _ in range(3):
+            idx.query_batch_flat(qs, 10, "fp32")
+            ms.append(idx.kernel_ms())
+        st = idx.last_stats()
+    kms = {n: float(np.median([m[n] for m in ms])) for n in ms[0]}
+    print(json.dumps({"upt": upt, "warps": warps, "queries": nq, "kernel_ms": kms,
+                      "plane_evals": st["plane_evals"], "candidates": st["candidates"],
+                      "bisectors": st["bisectors"], "survivors": st["survivors"]}), flush=True)
+
+
 def profile_single(k: int, n: int):
     """n single FP64 queries through the influence zone on the config-2
     workload (the plain form; the launch to capture with ncu is the last)."""
@@ -196,8 +219,13 @@ def main(argv=None) -> int:
                     help="only N single FP64 influence-zone queries at k=K on workload 2")
     ap.add_argument("--profile-index", type=int, metavar="C", help="only the index build of workload C")
     ap.add_argument("--order-ab", action="store_true", help="only the work-order comparison")
+    ap.add_argument("--profile-verify", nargs=2, type=int, metavar=("UPT", "WARPS"),
+                    help="only a 16384-query workload-2 batch with this verification shape")
     a = ap.parse_args(argv)
     build.build()
+    if a.profile_verify:
+        profile_verify(*a.profile_verify)
+        return 0
     if a.order_ab:
         print(json.dumps(order_ab()), flush=True)
         return 0
