@@ -69,7 +69,14 @@ typedef struct {
                                filter, smaller ones the influence zone (0: default 1) */
     int32_t users_per_thread;   /* verification: users per lane per work item, 2/4/8 (0: 4) */
     int32_t verify_warps;       /* verification: warps per block, 4/8/16 (0: 8) */
-    int32_t reserved[2];
+    int32_t zone_vertex_test;   /* influence zone's vertex test (inf.cpp:268-353): 0 (default)
+                                   the reference's, over vertices of count k-1 and the eight
+                                   extreme space-boundary vertices (it can drop a needed
+                                   facility: a superset filter); 1 every vertex of the zone's
+                                   boundary: count k-1 and every space-boundary vertex of
+                                   count < k (no needed facility dropped).  Results are exact
+                                   either way */
+    int32_t reserved[1];
 } rknn_index_opts;
 
 typedef enum {

@@ -179,6 +179,7 @@ struct rknn_index {
     int vupt = VERIFY_UPT;         // verification: users per lane per work item
     int vwarps = VERIFY_WARPS;     // verification: warps per block
     int skip_coincident = 1;
+    int zone_vertex_test = 0;   // see rknn_index_opts.zone_vertex_test
     int filter = RKNN_FILTER_AUTO;
     int slice_min_k = 1;
     int num_sms = 0;
@@ -707,6 +708,7 @@ rknn_status enqueue(rknn_index* ix, Ctx& c, const BatchPlan& b, bool events = fa
     const int* oin = c.io.q ? c.io.order : w.d_qko + 2 * nq;
     za.q_in = qin; za.k_in = kin;
     za.skip_coincident = ix->skip_coincident;
+    za.vertex_test = ix->zone_vertex_test;
     za.seg_cap = w.seg_cap;
     za.qd = w.d_qd; za.planes = w.d_planes; za.bis_pos = w.d_bispos; za.segs = w.d_segs; za.zst = w.d_zst;
     za.slice_r = w.d_slice_r;
@@ -1160,6 +1162,8 @@ rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf, 
     auto bail = [&](rknn_status s) { rknn_index_destroy(ix); return s; };
     ix->device = o.device;
     ix->skip_coincident = o.skip_coincident ? 1 : 0;
+    if (o.zone_vertex_test != 0 && o.zone_vertex_test != 1) return bail(fail(RKNN_ERR_ARG, "zone_vertex_test must be 0 or 1"));
+    ix->zone_vertex_test = o.zone_vertex_test;
     if (o.filter < RKNN_FILTER_AUTO || o.filter > RKNN_FILTER_SLICE) return bail(fail(RKNN_ERR_ARG, "bad filter"));
     ix->filter = o.filter;
     ix->slice_min_k = o.slice_min_k > 0 ? o.slice_min_k : 1;
@@ -1885,6 +1889,7 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     za.work_counter = L.counters + 0;
     za.caps = caps;
     za.skip_coincident = ix->skip_coincident;
+    za.vertex_test = ix->zone_vertex_test;
     za.rmax = caps.rm;
     za.seg_cap = seg_cap;
     za.pstride = caps.lc;

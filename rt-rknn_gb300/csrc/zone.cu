@@ -239,8 +239,10 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                             cnt = vcnt_of(w);
                             fl = vfl_of(w);
                         }
-                        const bool c = in && cnt == ku - 1;
-                        const bool b = in && (fl & VB_BND) && cnt < ku;
+                        // the zone-boundary test (vertex_test 1) also considers
+                        // every space-boundary vertex below count k
+                        const bool c = in && (cnt == ku - 1 || (A.vertex_test && (fl & VB_BND) && cnt < ku));
+                        const bool b = in && !A.vertex_test && (fl & VB_BND) && cnt < ku;
                         const unsigned mc = __ballot_sync(FULL, c), mb = __ballot_sync(FULL, b);
                         const unsigned below = (1u << lane) - 1;
                         if (c) IX(S.cons, nC + __popc(mc & below)) = (uint16_t)i;

@@ -119,6 +119,8 @@ struct ZoneArgs {
     int* work_counter;
     ZoneCaps caps;
     int skip_coincident;
+    int vertex_test = 0;     // 0: count k-1 and extreme boundary vertices (rknn-inf); 1: every
+                             // zone-boundary vertex (count k-1, space boundary with count < k)
     int rmax;                // == caps.rm
     int seg_cap;             // segments per query slot (>= 2*rmax+2)
     // outputs (per slot)

@@ -473,8 +473,10 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                             cnt = vcnt_of(w);
                             fl = vfl_of(w);
                         }
-                        const bool c = in && cnt == ku - 1;
-                        const bool b = in && (fl & VB_BND) && cnt < ku;
+                        // the zone-boundary test (vertex_test 1) also considers
+                        // every space-boundary vertex below count k
+                        const bool c = in && (cnt == ku - 1 || (A.vertex_test && (fl & VB_BND) && cnt < ku));
+                        const bool b = in && !A.vertex_test && (fl & VB_BND) && cnt < ku;
                         int rc, rb, tc, tb;
                         block_rank2<ZW>(c, b, sh, rc, rb, tc, tb);
                         if (c) IX(S.cons, nC + rc) = (uint16_t)i;

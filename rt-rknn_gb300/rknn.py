@@ -91,7 +91,8 @@ class RkNNError(RuntimeError):
 class Opts(C.Structure):
     _fields_ = [("device", C.c_int32), ("fac_per_cell", C.c_float), ("usr_per_cell", C.c_float),
                 ("skip_coincident", C.c_int32), ("filter", C.c_int32), ("slice_min_k", C.c_int32),
-                ("users_per_thread", C.c_int32), ("verify_warps", C.c_int32), ("reserved", C.c_int32 * 2)]
+                ("users_per_thread", C.c_int32), ("verify_warps", C.c_int32), ("zone_vertex_test", C.c_int32),
+                ("reserved", C.c_int32 * 1)]
 
 
 class TuneResult(C.Structure):
@@ -235,7 +236,7 @@ class Index:
     def __init__(self, fxy, uxy, fid=None, uid=None, device: int = 0,
                  fac_per_cell: float = 0.0, usr_per_cell: float = 0.0,
                  skip_coincident: bool = True, filter: str = "auto", slice_min_k: int = 0,
-                 users_per_thread: int = 0, verify_warps: int = 0):
+                 users_per_thread: int = 0, verify_warps: int = 0, zone_vertex_test: str = "reference"):
         L = load()
         self.fxy = np.ascontiguousarray(fxy, dtype=np.float32).reshape(-1, 2)
         self.uxy = np.ascontiguousarray(uxy, dtype=np.float32).reshape(-1, 2)
@@ -256,6 +257,7 @@ class Index:
         o.slice_min_k = int(slice_min_k)
         o.users_per_thread = int(users_per_thread)
         o.verify_warps = int(verify_warps)
+        o.zone_vertex_test = {"reference": 0, "boundary": 1}[zone_vertex_test]
         h = C.c_void_p()
         _check(L.rknn_index_create(_ptr(self.fxy), _ptr(self.fid), nf, _ptr(self.uxy),
                                    _ptr(self.uid), nu, C.byref(o), C.byref(h)))

@@ -195,6 +195,35 @@ def profile_verify(upt: int, warps: int, nq: int = 16384):
                       "bisectors": st["bisectors"], "survivors": st["survivors"]}), flush=True)
 
 
+def vertex_test_ab():
+    """The influence zone with rknn-inf's vertex test against the
+    zone-boundary test (rknn_index_opts.zone_vertex_test): bisectors,
+    candidate users and survivors per query, batch device time, and the
+    single-query latency, on workload 2 at k = 5, 10, 25; the result sets
+    must be the same."""
+    ds = datagen.config(2)
+    qs = ds.queries.astype(np.int32)
+    out = {"vertex_test_ab": {}}
+    for k in (5, 10, 25):
+        row, res = {}, {}
+        for vt in ("reference", "boundary"):
+            with rknn.Index.of(ds, filter="inf", zone_vertex_test=vt) as idx:
+                ms, st, r = _batch(idx, qs, k, "fp64", reps=2)
+                res[vt] = r
+                lat = []
+                for q in qs[:60]:
+                    t0 = time.perf_counter()
+                    idx.query(int(q), k, "fp64")
+                    lat.append(1e3 * (time.perf_counter() - t0))
+                n = len(qs)
+                row[vt] = {"bisectors_per_query": st["bisectors"] / n, "candidates_per_query": st["candidates"] / n,
+                           "survivors_per_query": st["survivors"] / n, "batch_fp64_ms": ms,
+                           "single_p50_ms": float(np.median(lat))}
+        row["same_results"] = all(np.array_equal(a, b) for a, b in zip(res["reference"], res["boundary"]))
+        out["vertex_test_ab"][k] = row
+    return out
+
+
 def profile_single(k: int, n: int):
     """n single FP64 queries through the influence zone on the config-2
     workload (the plain form; the launch to capture with ncu is the last)."""
@@ -219,12 +248,16 @@ def main(argv=None) -> int:
                     help="only N single FP64 influence-zone queries at k=K on workload 2")
     ap.add_argument("--profile-index", type=int, metavar="C", help="only the index build of workload C")
     ap.add_argument("--order-ab", action="store_true", help="only the work-order comparison")
+    ap.add_argument("--vertex-test-ab", action="store_true", help="only the zone vertex-test comparison")
     ap.add_argument("--profile-verify", nargs=2, type=int, metavar=("UPT", "WARPS"),
                     help="only a 16384-query workload-2 batch with this verification shape")
     a = ap.parse_args(argv)
     build.build()
     if a.profile_verify:
         profile_verify(*a.profile_verify)
+        return 0
+    if a.vertex_test_ab:
+        print(json.dumps(vertex_test_ab()), flush=True)
         return 0
     if a.order_ab:
         print(json.dumps(order_ab()), flush=True)

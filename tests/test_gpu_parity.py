@@ -382,3 +382,20 @@ def test_command_line_drop_in(engine, golden_dir, tmp_path):
     for q in qs:
         got = np.loadtxt(tmp_path / "log2" / f"fp32_k{k}_q{q}.txt", dtype=np.int64, ndmin=1)
         assert np.array_equal(got, o.query(q, k)), q
+
+
+def test_zone_boundary_vertex_test(engine):
+    """The zone-boundary vertex test (rknn_index_opts.zone_vertex_test = 1:
+    every zone-boundary vertex considered, instead of rknn-inf's count-(k-1)
+    and extreme boundary vertices) gives the oracle's results in both modes,
+    batched and one query per launch, both zone kernels."""
+    ds = datagen.uniform(20000, 200000, seed=51, nq=40, k=10)
+    o = O.Oracle.of(ds)
+    for k in (1, 5, 10, 25):
+        want = [o.query(int(q), k) for q in ds.queries]
+        with engine.Index.of(ds, filter="inf", zone_vertex_test="boundary") as idx:
+            for mode in MODES:
+                got = idx.query_batch(ds.queries, k, mode)
+                assert all(np.array_equal(g, w) for g, w in zip(got, want)), (k, mode)
+            for q, w in list(zip(ds.queries, want))[:5]:
+                assert np.array_equal(idx.query(int(q), k, "fp64"), w), (int(q), k)
