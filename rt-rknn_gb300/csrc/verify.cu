@@ -108,22 +108,23 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
         const int s = A.deflist ? A.deflist[VX(e, A.nq, 222)] : e;
         const QDesc d = A.qd[s];
         if (s != cur && A.mode == MODE_FP32) {
-            // stage_cap half-planes, seg_stage segments and the slice bounds,
-            // whatever the slot uses of them (the loads do not wait on the
-            // slot record), each lane's loads issued together
+            // the slot's half-planes (as many as are staged at most),
+            // seg_stage segments and the slice bounds, each lane's loads
+            // issued together
             __syncwarp();
             const float4* src = A.planes + (size_t)s * A.lc;
-            for (int m0 = lane; m0 < A.stage_cap; m0 += 32 * 8) {
+            const int nst = min(d.nb, A.stage_cap);
+            for (int m0 = lane; m0 < nst; m0 += 32 * 8) {
                 float4 p[8];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const int m = m0 + 32 * j;
-                    p[j] = m < A.stage_cap ? src[m] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    p[j] = m < nst ? src[m] : make_float4(0.f, 0.f, 0.f, 0.f);
                 }
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const int m = m0 + 32 * j;
-                    if (m < A.stage_cap) {
+                    if (m < nst) {
                         ((float4*)sp)[2 * m] = make_float4(p[j].x, p[j].x, p[j].y, p[j].y);
                         ((float4*)sp)[2 * m + 1] = make_float4(p[j].z, p[j].z, p[j].w, p[j].w);
                     }
