@@ -33,11 +33,15 @@ constexpr int ZMAXW = ZMAXT / 32;
 struct ZcShared {
     uint64_t tk[ZMAXT];   // a batch of new queue entries: keys
     uint32_t tc[ZMAXT];   //   and codes
-    int wc[2][ZMAXW];     // per-warp counts (ordered compactions, scans)
-    double rd[ZMAXW];     // per-warp partials of reductions
-    long long rl[ZMAXW];
-    float rf[ZMAXW];
-    int ri[2][ZMAXW];
+    // Per-warp partials of the block reductions, two copies used by
+    // alternate calls (the phase bit every thread flips at each call): a
+    // copy is written again only after a later call's barrier, which every
+    // thread passes after reading it, so one barrier per call suffices.
+    int wc[2][2][ZMAXW];  // per-warp counts (ordered compactions)
+    double rd[2][ZMAXW];
+    long long rl[2][ZMAXW];
+    float rf[2][ZMAXW];
+    int ri[2][2][ZMAXW];
     long long ek[ZMAXW][8];   // extreme boundary points: per-warp best keys
     int ei[ZMAXW][8];         //   and list positions
     double bd[4];         // values one thread computed for all
@@ -48,13 +52,16 @@ struct ZcShared {
 // order): the number of threads before this one with each predicate set,
 // and the totals.  Two barriers; the shared counts are free again on return.
 template <int ZW>
-__device__ __forceinline__ void block_rank2(bool p, bool q, ZcShared& sh, int& rp, int& rq, int& tp, int& tq)
+__device__ __forceinline__ void block_rank2(bool p, bool q, ZcShared& sh, unsigned& ph, int& rp, int& rq, int& tp,
+                                            int& tq)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int b = ph & 1;
+    ph ^= 1;
     const unsigned mp = __ballot_sync(FULL, p), mq = __ballot_sync(FULL, q);
     if (lane == 0) {
-        sh.wc[0][w] = __popc(mp);
-        sh.wc[1][w] = __popc(mq);
+        sh.wc[b][0][w] = __popc(mp);
+        sh.wc[b][1][w] = __popc(mq);
     }
     __syncthreads();
     int bp = 0, bq = 0;
@@ -62,30 +69,32 @@ __device__ __forceinline__ void block_rank2(bool p, bool q, ZcShared& sh, int& r
     tq = 0;
 #pragma unroll
     for (int j = 0; j < ZW; ++j) {
-        const int cp = sh.wc[0][j], cq = sh.wc[1][j];
+        const int cp = sh.wc[b][0][j], cq = sh.wc[b][1][j];
         if (j < w) { bp += cp; bq += cq; }
         tp += cp;
         tq += cq;
     }
-    __syncthreads();
     const unsigned below = (1u << lane) - 1;
     rp = bp + __popc(mp & below);
     rq = bq + __popc(mq & below);
 }
 
 template <int ZW>
-__device__ __forceinline__ int block_rank(bool p, ZcShared& sh, int& tot)
+__device__ __forceinline__ int block_rank(bool p, ZcShared& sh, unsigned& ph, int& tot)
 {
     int rp, rq, tq;
-    block_rank2<ZW>(p, false, sh, rp, rq, tot, tq);
+    block_rank2<ZW>(p, false, sh, ph, rp, rq, tot, tq);
     return rp;
 }
 
 // Exclusive ordered sums of two ints over the block, with totals.
 template <int ZW>
-__device__ __forceinline__ void block_scan2(int a, int b, ZcShared& sh, int& ea, int& eb, int& ta, int& tb)
+__device__ __forceinline__ void block_scan2(int a, int b, ZcShared& sh, unsigned& ph, int& ea, int& eb, int& ta,
+                                            int& tb)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int bf = ph & 1;
+    ph ^= 1;
     int xa = a, xb = b;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -93,8 +102,8 @@ __device__ __forceinline__ void block_scan2(int a, int b, ZcShared& sh, int& ea,
         if (lane >= o) { xa += ya; xb += yb; }
     }
     if (lane == 31) {
-        sh.ri[0][w] = xa;
-        sh.ri[1][w] = xb;
+        sh.ri[bf][0][w] = xa;
+        sh.ri[bf][1][w] = xb;
     }
     __syncthreads();
     int ba = 0, bb = 0;
@@ -102,67 +111,70 @@ __device__ __forceinline__ void block_scan2(int a, int b, ZcShared& sh, int& ea,
     tb = 0;
 #pragma unroll
     for (int j = 0; j < ZW; ++j) {
-        const int ca = sh.ri[0][j], cb = sh.ri[1][j];
+        const int ca = sh.ri[bf][0][j], cb = sh.ri[bf][1][j];
         if (j < w) { ba += ca; bb += cb; }
         ta += ca;
         tb += cb;
     }
-    __syncthreads();
     ea = ba + xa - a;
     eb = bb + xb - b;
 }
 
 template <int ZW>
-__device__ __forceinline__ double block_max_d(double v, ZcShared& sh)
+__device__ __forceinline__ double block_max_d(double v, ZcShared& sh, unsigned& ph)
 {
+    const int b = ph & 1;
+    ph ^= 1;
     v = warp_max(v);
-    if ((threadIdx.x & 31) == 0) sh.rd[threadIdx.x >> 5] = v;
+    if ((threadIdx.x & 31) == 0) sh.rd[b][threadIdx.x >> 5] = v;
     __syncthreads();
-    double r = sh.rd[0];
+    double r = sh.rd[b][0];
 #pragma unroll
-    for (int j = 1; j < ZW; ++j) r = fmax(r, sh.rd[j]);
-    __syncthreads();
+    for (int j = 1; j < ZW; ++j) r = fmax(r, sh.rd[b][j]);
     return r;
 }
 
 template <int ZW>
-__device__ __forceinline__ float block_max_f(float v, ZcShared& sh)
+__device__ __forceinline__ float block_max_f(float v, ZcShared& sh, unsigned& ph)
 {
+    const int b = ph & 1;
+    ph ^= 1;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(FULL, v, o));
-    if ((threadIdx.x & 31) == 0) sh.rf[threadIdx.x >> 5] = v;
+    if ((threadIdx.x & 31) == 0) sh.rf[b][threadIdx.x >> 5] = v;
     __syncthreads();
-    float r = sh.rf[0];
+    float r = sh.rf[b][0];
 #pragma unroll
-    for (int j = 1; j < ZW; ++j) r = fmaxf(r, sh.rf[j]);
-    __syncthreads();
+    for (int j = 1; j < ZW; ++j) r = fmaxf(r, sh.rf[b][j]);
     return r;
 }
 
 template <int ZW>
-__device__ __forceinline__ long long block_max_ll(long long v, ZcShared& sh)
+__device__ __forceinline__ long long block_max_ll(long long v, ZcShared& sh, unsigned& ph)
 {
+    const int b = ph & 1;
+    ph ^= 1;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = max(v, (long long)__shfl_xor_sync(FULL, v, o));
-    if ((threadIdx.x & 31) == 0) sh.rl[threadIdx.x >> 5] = v;
+    if ((threadIdx.x & 31) == 0) sh.rl[b][threadIdx.x >> 5] = v;
     __syncthreads();
-    long long r = sh.rl[0];
+    long long r = sh.rl[b][0];
 #pragma unroll
-    for (int j = 1; j < ZW; ++j) r = max(r, sh.rl[j]);
-    __syncthreads();
+    for (int j = 1; j < ZW; ++j) r = max(r, sh.rl[b][j]);
     return r;
 }
 
 template <int ZW>
-__device__ __forceinline__ int block_sum_i(int v, ZcShared& sh)
+__device__ __forceinline__ int block_sum_i(int v, ZcShared& sh, unsigned& ph)
 {
+    const int b = ph & 1;
+    ph ^= 1;
     v = warp_sum(v);
-    if ((threadIdx.x & 31) == 0) sh.ri[0][threadIdx.x >> 5] = v;
+    if ((threadIdx.x & 31) == 0) sh.ri[b][0][threadIdx.x >> 5] = v;
     __syncthreads();
     int r = 0;
 #pragma unroll
-    for (int j = 0; j < ZW; ++j) r += sh.ri[0][j];
-    __syncthreads();
+    for (int j = 0; j < ZW; ++j) r += sh.ri[b][0][j];
     return r;
 }
 
@@ -243,7 +255,7 @@ __device__ __forceinline__ void pq_merge(uint64_t* K, uint32_t* C, int& h, int& 
 // among equal keys.  Each thread keeps its best of the entries it reads, then
 // a block reduction by (key, position).  ext[j] = vertex index or -1.
 template <int ZT>
-__device__ __forceinline__ void extreme_points(const Slice& S, int nB, ZcShared& sh, int (&ext)[8])
+__device__ __forceinline__ void extreme_points(const Slice& S, int nV, uint32_t ku, ZcShared& sh, int (&ext)[8])
 {
     constexpr int ZW = ZT / 32;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -251,10 +263,13 @@ __device__ __forceinline__ void extreme_points(const Slice& S, int nB, ZcShared&
     int bp[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) { bk[j] = 0; bp[j] = INT_MAX; }
-    for (int t = tid; t < nB; t += ZT) {
-        const int vi = IX(S.blist, t);
-        const uint32_t fl = vfl_of(IX(S.v4, vi).w);
-        const double2 p = IX(S.vd, vi);
+    // the list of boundary vertices below count k, in vertex order: the
+    // vertex index serves as the list position
+    for (int t = tid; t < nV; t += ZT) {
+        const float vw = IX(S.v4, t).w;
+        const uint32_t fl = vfl_of(vw);
+        if (!(fl & VB_BND) || vcnt_of(vw) >= ku) continue;
+        const double2 p = IX(S.vd, t);
         const long long kx = order_key(p.x), ky = order_key(p.y);
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
@@ -265,33 +280,42 @@ __device__ __forceinline__ void extreme_points(const Slice& S, int nB, ZcShared&
             if (bp[j] == INT_MAX || ((j & 1) == 0 ? kk < bk[j] : kk > bk[j])) { bk[j] = kk; bp[j] = t; }
         }
     }
+    // Reduce by (key, position) with 32-bit warp minima: a key becomes an
+    // unsigned word pair ordered like it (the sign bit flipped; all bits
+    // flipped for a maximum, so that the best is always the least), and the
+    // least pair, then the least position among its holders, wins.
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const long long ok = __shfl_xor_sync(FULL, bk[j], o);
-            const int op = __shfl_xor_sync(FULL, bp[j], o);
-            const bool better = op != INT_MAX &&
-                                (bp[j] == INT_MAX || ((j & 1) == 0 ? ok < bk[j] : ok > bk[j]) || (ok == bk[j] && op < bp[j]));
-            if (better) { bk[j] = ok; bp[j] = op; }
+        const bool has = bp[j] != INT_MAX;
+        unsigned long long u = (unsigned long long)bk[j] ^ 0x8000000000000000ull;
+        if (j & 1) u = ~u;
+        const unsigned hi = has ? (unsigned)(u >> 32) : 0xffffffffu;
+        const unsigned lo = has ? (unsigned)u : 0xffffffffu;
+        const unsigned mhi = __reduce_min_sync(FULL, hi);
+        const bool c1 = hi == mhi;
+        const unsigned mlo = __reduce_min_sync(FULL, c1 ? lo : 0xffffffffu);
+        const bool c2 = c1 && lo == mlo;
+        const unsigned mpos = __reduce_min_sync(FULL, c2 ? (unsigned)bp[j] : 0xffffffffu);
+        if (lane == 0) {
+            sh.ek[w][j] = (long long)(((unsigned long long)mhi << 32) | mlo);
+            sh.ei[w][j] = mpos == 0xffffffffu ? INT_MAX : (int)mpos;
         }
-        if (lane == 0) { sh.ek[w][j] = bk[j]; sh.ei[w][j] = bp[j]; }
     }
     __syncthreads();
     if (tid < 8) {
         const int j = tid;
-        long long k0 = sh.ek[0][j];
+        unsigned long long k0 = (unsigned long long)sh.ek[0][j];
         int p0 = sh.ei[0][j];
 #pragma unroll
         for (int u = 1; u < ZW; ++u) {
-            const long long ok = sh.ek[u][j];
+            const unsigned long long ok = (unsigned long long)sh.ek[u][j];
             const int op = sh.ei[u][j];
-            if (op != INT_MAX && (p0 == INT_MAX || ((j & 1) == 0 ? ok < k0 : ok > k0) || (ok == k0 && op < p0))) {
+            if (op != INT_MAX && (p0 == INT_MAX || ok < k0 || (ok == k0 && op < p0))) {
                 k0 = ok;
                 p0 = op;
             }
         }
-        sh.bi[4 + j] = p0 == INT_MAX ? -1 : (int)IX(S.blist, p0);
+        sh.bi[4 + j] = p0 == INT_MAX ? -1 : p0;
     }
     __syncthreads();
 #pragma unroll
@@ -310,6 +334,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int gi = tid / ZG, gl = tid % ZG;
+    unsigned ph = 0;                     // the block reductions' phase bit (same in every thread)
 #ifdef RKNN_CHECKED
     if (tid == 0 && blockIdx.x == 0) g_fault = A.fault;
     __syncthreads();
@@ -369,7 +394,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             IX(S.v4, tid) = make_float4((float)x, (float)y, (float)d2c,
                                         vpack(0, VB_BND | edge_bits(x, y, sx0, sy0, sx1, sy1)));
         }
-        far_ = __dsqrt_rn(block_max_d<ZW>(d2c, sh));
+        far_ = __dsqrt_rn(block_max_d<ZW>(d2c, sh, ph));
         Cut K1 = sqrt_cut(2.0 * far_, false);
         Cut K2 = sqrt_cut(2.0 * DBL_MAX, true);
 
@@ -412,7 +437,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     }
                     const double key = ok ? rect_d2_64(qx, qy, A.fmbr[GX(cid, NCF, 103)]) : 0.0;
                     int m;
-                    const int r = block_rank<ZW>(ok, sh, m);
+                    const int r = block_rank<ZW>(ok, sh, ph, m);
                     if (ok) { sh.tk[r] = (uint64_t)__double_as_longlong(key); sh.tc[r] = (uint32_t)cid; }
                     bool over = false;
                     pq_merge<ZT>(S.pqk.p, S.pqc.p, hP, nP, m, PC, over, sh);
@@ -463,30 +488,24 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             else {
                 // ---- vertex test (inf.cpp:268-353, 466-551) -------------
                 if (nCons < 0) {
-                    int nC = 0, nB = 0;
-                    for (int i0 = 0; i0 < nV; i0 += ZT) {
-                        const int i = i0 + tid;
-                        uint32_t cnt = 0, fl = 0;
-                        const bool in = i < nV;
-                        if (in) {
-                            const float w = IX(S.v4, i).w;
-                            cnt = vcnt_of(w);
-                            fl = vfl_of(w);
-                        }
-                        // the zone-boundary test (vertex_test 1) also considers
-                        // every space-boundary vertex below count k
-                        const bool c = in && (cnt == ku - 1 || (A.vertex_test && (fl & VB_BND) && cnt < ku));
-                        const bool b = in && !A.vertex_test && (fl & VB_BND) && cnt < ku;
-                        int rc, rb, tc, tb;
-                        block_rank2<ZW>(c, b, sh, rc, rb, tc, tb);
-                        if (c) IX(S.cons, nC + rc) = (uint16_t)i;
-                        if (b) IX(S.blist, nB + rb) = (uint16_t)i;
-                        nC += tc;
-                        nB += tb;
-                    }
-                    __syncthreads();
+                    // Mark the vertices the test considers (VB_CONS): count
+                    // k-1, and the space-boundary vertices below count k that
+                    // lie within EPS of an extreme point (inf.cpp:283-346); or,
+                    // with the zone-boundary test, every space-boundary vertex
+                    // below count k.  The marks hold until the zone changes.
                     int ext[8];
-                    extreme_points<ZT>(S, nB, sh, ext);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) ext[j] = -1;
+                    if (!A.vertex_test) {
+                        // the reduction only when some space-boundary vertex
+                        // is below count k (a zone inside the space has none)
+                        bool hb = false;
+                        for (int i = tid; i < nV && !hb; i += ZT) {
+                            const float vw = IX(S.v4, i).w;
+                            hb = (vfl_of(vw) & VB_BND) && vcnt_of(vw) < ku;
+                        }
+                        if (__syncthreads_or(hb)) extreme_points<ZT>(S, nV, ku, sh, ext);
+                    }
                     float ex[8], ey[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
@@ -496,38 +515,30 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                             ex[j] = e.x; ey[j] = e.y;
                         }
                     }
-                    // boundary vertices (count < k, not already considered)
-                    // within EPS of an extreme point (inf.cpp:326-346)
-                    for (int t0 = 0; t0 < nB; t0 += ZT) {
-                        const int t = t0 + tid;
-                        bool c = false;
-                        int vi = 0;
-                        if (t < nB) {
-                            vi = IX(S.blist, t);
-                            const float4 v = IX(S.v4, vi);
-                            if (vcnt_of(v.w) != ku - 1) {
+                    for (int i = tid; i < nV; i += ZT) {
+                        const float4 v = IX(S.v4, i);
+                        const uint32_t cnt = vcnt_of(v.w), fl = vfl_of(v.w);
+                        const bool bnd = (fl & VB_BND) && cnt < ku;
+                        bool c = cnt == ku - 1 || (A.vertex_test && bnd);
+                        if (!c && bnd && !A.vertex_test) {
 #pragma unroll
-                                for (int j = 0; j < 8; ++j) {
-                                    if (c || ext[j] < 0 || fabsf(v.x - ex[j]) > tolE || fabsf(v.y - ey[j]) > tolE) continue;
-                                    const double2 a = IX(S.vd, vi), b = IX(S.vd, ext[j]);
-                                    if (fabs(__dsub_rn(a.x, b.x)) < EPS && fabs(__dsub_rn(a.y, b.y)) < EPS) c = true;
-                                }
+                            for (int j = 0; j < 8; ++j) {
+                                if (c || ext[j] < 0 || fabsf(v.x - ex[j]) > tolE || fabsf(v.y - ey[j]) > tolE) continue;
+                                const double2 a = IX(S.vd, i), b = IX(S.vd, ext[j]);
+                                if (fabs(__dsub_rn(a.x, b.x)) < EPS && fabs(__dsub_rn(a.y, b.y)) < EPS) c = true;
                             }
                         }
-                        int tot;
-                        const int r = block_rank<ZW>(c, sh, tot);
-                        if (c) IX(S.cons, nC + r) = (uint16_t)vi;
-                        nC += tot;
+                        const uint32_t nfl = c ? (fl | VB_CONS) : (fl & ~VB_CONS);
+                        if (nfl != fl) IX(S.v4, i).w = vpack(cnt, nfl);
                     }
-                    nCons = nC;
+                    nCons = 1;          // marks valid
                     __syncthreads();
                 }
-                const int nC = nCons;
                 bool hit = false;
                 const float px32 = (float)px, py32 = (float)py;
-                for (int t = tid; t < nC && !hit; t += ZT) {
-                    const int i = IX(S.cons, t);
+                for (int i = tid; i < nV && !hit; i += ZT) {
                     const float4 v = IX(S.v4, i);
+                    if (!(vfl_of(v.w) & VB_CONS)) continue;
                     int r;
                     if (is_point) r = closer32(px32 - v.x, py32 - v.y, E, v.z);
                     else r = closer32(rect_dx32(v.x, mbr.x, mbr.z), rect_dx32(v.y, mbr.y, mbr.w), E, v.z);
@@ -753,7 +764,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     const int i = i0 + tid;
                     const bool on = i < nV0 && (vfl_of(IX(S.v4, i).w) & VB_ON);
                     int tot;
-                    const int r = block_rank<ZW>(on, sh, tot);
+                    const int r = block_rank<ZW>(on, sh, ph, tot);
                     if (on) IX(S.cons, nOn + r) = (uint16_t)i;   // cons reused as scratch
                     nOn += tot;
                 }
@@ -871,7 +882,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     if (keep) p = IX(S.vd, i);
                 }
                 int tot;
-                const int r = block_rank<ZW>(keep, sh, tot);     // every read above precedes its barriers
+                const int r = block_rank<ZW>(keep, sh, ph, tot);     // every read above precedes its barriers
                 if (keep) {
                     const int o = w + r;
                     v.w = vpack(vcnt_of(v.w), vfl_of(v.w) & ~VB_ON);
@@ -885,7 +896,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 const int c = c0 + tid;
                 const bool keep = c < C && (IX(S.cfl, c) & 0x80) && IX(S.ccnt, c) < k;
                 int tot;
-                const int r = block_rank<ZW>(keep, sh, tot);
+                const int r = block_rank<ZW>(keep, sh, ph, tot);
                 const int o = w + nnew + r;
                 if (keep && o < VC) {
                     const double2 p = IX(S.cd, c);
@@ -921,14 +932,14 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             {
                 float m32 = 0.0f;
                 for (int i = tid; i < nV; i += ZT) m32 = fmaxf(m32, IX(S.v4, i).z);
-                m32 = block_max_f<ZW>(m32, sh);
+                m32 = block_max_f<ZW>(m32, sh, ph);
                 long long m = 0;
                 for (int i = tid; i < nV; i += ZT)
                     if (IX(S.v4, i).z == m32) {
                         const double2 p = IX(S.vd, i);
                         m = max(m, __double_as_longlong(d2_64(p.x, p.y, qx, qy)));
                     }
-                m = block_max_ll<ZW>(m, sh);
+                m = block_max_ll<ZW>(m, sh, ph);
                 const double f = __dsqrt_rn(__longlong_as_double(m));
                 if (f != far_) {
                     far_ = f;
@@ -942,8 +953,8 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
         __syncthreads();
         qflags |= flags;
         zs.nb = nL;
-        zs.cand = block_sum_i<ZW>(cand_local, sh);
-        zs.cand64 = block_sum_i<ZW>(cand64_local, sh);
+        zs.cand = block_sum_i<ZW>(cand_local, sh, ph);
+        zs.cand64 = block_sum_i<ZW>(cand64_local, sh, ph);
 
         // ---- epilogue 1: exact half-planes relative to q -------------------
         float4* planes = A.planes + (size_t)s * A.pstride;
@@ -959,7 +970,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             A.bis_pos[(size_t)s * A.pstride + GX(m, A.pstride, 107)] = pos;
             cmax = fmax(cmax, c);
         }
-        cmax = block_max_d<ZW>(cmax, sh);
+        cmax = block_max_d<ZW>(cmax, sh, ph);
         const double Fp = sqrt(cmax) * (1.0 + 1e-6) + 1e-30;
         const float k2f = (float)(8.0 * (double)kU32 * 2.0 * Fp * (1.0 + 1e-6));
         const float kf2 = (float)(8.0 * (double)kU32 * Fp * Fp * (1.0 + 1e-6)) + 1e-30f;
@@ -1063,7 +1074,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 }
                 const bool has = len > 0;
                 int pre, excl, tot_has, tot_len;
-                block_scan2<ZW>(has ? 1 : 0, has ? len : 0, sh, pre, excl, tot_has, tot_len);
+                block_scan2<ZW>(has ? 1 : 0, has ? len : 0, sh, ph, pre, excl, tot_has, tot_len);
                 if (has) seg[GX(nseg + pre, A.seg_cap, 108)] = make_int2(st, ncand + excl);
                 nseg += tot_has;
                 ncand += tot_len;

@@ -21,6 +21,9 @@ constexpr double EPS = 1e-9;           // inf.cpp:270,375,408; inf.h:324
 // and within EPS of the left / right / bottom / top edge (decided once in
 // FP64 when the vertex is created; inf.cpp:283-321 tests the same per lookup)
 constexpr uint32_t VB_BND = 1, VB_ON = 2, VB_EL = 4, VB_ER = 8, VB_EB = 16, VB_ET = 32;
+// the one-block kernel's mark of a vertex the vertex test considers (valid
+// while the zone is unchanged since it was set)
+constexpr uint32_t VB_CONS = 64;
 // flags of a line
 constexpr uint32_t LB_VERT = 1, LB_VALID = 2;
 
