@@ -394,7 +394,9 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             IX(S.v4, tid) = make_float4((float)x, (float)y, (float)d2c,
                                         vpack(0, VB_BND | edge_bits(x, y, sx0, sy0, sx1, sy1)));
         }
-        far_ = __dsqrt_rn(block_max_d<ZW>(d2c, sh, ph));
+        const double d2far = block_max_d<ZW>(d2c, sh, ph);
+        far_ = __dsqrt_rn(d2far);
+        long long far2 = __double_as_longlong(d2far);   // far_ squared, as bits
         Cut K1 = sqrt_cut(2.0 * far_, false);
         Cut K2 = sqrt_cut(2.0 * DBL_MAX, true);
 
@@ -792,6 +794,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             // (4) counts of the surviving candidates over earlier bisectors,
             //     a group per candidate: certain violations in float, the
             //     undecided ones in FP64
+            bool anyclose = false;
             for (int c0 = 0; c0 < C; c0 += ZGN) {
                 const int c = c0 + gi;
                 const bool live = c < C && (IX(S.cfl, c) & 0x80) != 0;
@@ -833,25 +836,20 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 }
                 cnt += group_sum<ZG>(extra);
                 if (c < C && gl == 0) IX(S.ccnt, c) = live ? cnt : k;
-            }
-            __syncthreads();
-            // (4b) a candidate closer than 1e-9 to an earlier one is not added
-            // (the reference keeps the first): float prefilter, then the exact
-            // sequential resolution when anything is close
-            {
-                bool anyclose = false;
-                for (int c0 = 0; c0 < C; c0 += ZGN) {
-                    const int c = c0 + gi;
-                    if (c >= C || !(IX(S.cfl, c) & 0x80) || IX(S.ccnt, c) >= k) continue;
-                    // doubles within 1e-9 give floats within 1e-9 + u(|x1|+|x2|)
-                    const float2 c32 = IX(S.c2, c);
+                // (4b), float prefilter: is a kept candidate within 1e-9 of
+                // an earlier one (the reference keeps the first)?  Doubles
+                // within 1e-9 give floats within 1e-9 + u(|x1|+|x2|).
+                if (live && cnt < k) {
                     const float tx = 3.0f * kU32 * fabsf(c32.x) + 2e-9f, ty = 3.0f * kU32 * fabsf(c32.y) + 2e-9f;
-                    for (int c2 = gl; c2 < c; c2 += ZG) {
+                    for (int c2 = gl; c2 < c && !anyclose; c2 += ZG) {
                         if (!(IX(S.cfl, c2) & 0x80)) continue;
                         const float2 o = IX(S.c2, c2);
-                        if (fabsf(o.x - c32.x) <= tx && fabsf(o.y - c32.y) <= ty) { anyclose = true; break; }
+                        if (fabsf(o.x - c32.x) <= tx && fabsf(o.y - c32.y) <= ty) anyclose = true;
                     }
                 }
+            }
+            // every count is written, and any close pair known, past this barrier
+            {
                 if (__syncthreads_or(anyclose)) {
                     if (tid == 0) {
                         for (int c = 0; c < C; ++c) {
@@ -870,8 +868,12 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
 
             // (5) erase old vertices with count >= k (order kept), then append
             //     the new vertices with count < k in candidate order
-            int w = 0;
-            for (int i0 = 0; i0 < nV0; i0 += ZT) {
+            // When every candidate fits one chunk, the ranks of the new
+            // vertices come from the first erase chunk's reduction.
+            const bool one = C <= ZT;
+            const bool nkeep = one && tid < C && (IX(S.cfl, tid) & 0x80) && IX(S.ccnt, tid) < k;
+            int w = 0, nr = 0, nnew = 0;
+            for (int i0 = 0; i0 < max(nV0, 1); i0 += ZT) {
                 const int i = i0 + tid;
                 bool keep = false;
                 float4 v = make_float4(0, 0, 0, 0);
@@ -881,8 +883,9 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     keep = vcnt_of(v.w) < ku;
                     if (keep) p = IX(S.vd, i);
                 }
-                int tot;
-                const int r = block_rank<ZW>(keep, sh, ph, tot);     // every read above precedes its barriers
+                int r, tot, rq, tq;
+                block_rank2<ZW>(keep, i0 == 0 && nkeep, sh, ph, r, rq, tot, tq);   // every read above precedes its barriers
+                if (i0 == 0) { nr = rq; nnew = tq; }
                 if (keep) {
                     const int o = w + r;
                     v.w = vpack(vcnt_of(v.w), vfl_of(v.w) & ~VB_ON);
@@ -891,14 +894,10 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 }
                 w += tot;
             }
-            int nnew = 0;
-            for (int c0 = 0; c0 < C; c0 += ZT) {
-                const int c = c0 + tid;
-                const bool keep = c < C && (IX(S.cfl, c) & 0x80) && IX(S.ccnt, c) < k;
-                int tot;
-                const int r = block_rank<ZW>(keep, sh, ph, tot);
-                const int o = w + nnew + r;
-                if (keep && o < VC) {
+            if (one) {
+                const int o = w + nr;
+                if (nkeep && o < VC) {
+                    const int c = tid;
                     const double2 p = IX(S.cd, c);
                     const float2 c32 = IX(S.c2, c);
                     IX(S.vd, o) = p;
@@ -906,7 +905,24 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                                               vpack((uint32_t)IX(S.ccnt, c),
                                                     (IX(S.cfl, c) & VB_BND) | edge_bits(p.x, p.y, sx0, sy0, sx1, sy1)));
                 }
-                nnew += tot;
+            } else {
+                nnew = 0;
+                for (int c0 = 0; c0 < C; c0 += ZT) {
+                    const int c = c0 + tid;
+                    const bool keep = c < C && (IX(S.cfl, c) & 0x80) && IX(S.ccnt, c) < k;
+                    int tot;
+                    const int r = block_rank<ZW>(keep, sh, ph, tot);
+                    const int o = w + nnew + r;
+                    if (keep && o < VC) {
+                        const double2 p = IX(S.cd, c);
+                        const float2 c32 = IX(S.c2, c);
+                        IX(S.vd, o) = p;
+                        IX(S.v4, o) = make_float4(c32.x, c32.y, (float)d2_64(p.x, p.y, qx, qy),
+                                                  vpack((uint32_t)IX(S.ccnt, c),
+                                                        (IX(S.cfl, c) & VB_BND) | edge_bits(p.x, p.y, sx0, sy0, sx1, sy1)));
+                    }
+                    nnew += tot;
+                }
             }
             zs.kept += nnew;
             nV = w + nnew;
@@ -940,11 +956,15 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                         m = max(m, __double_as_longlong(d2_64(p.x, p.y, qx, qy)));
                     }
                 m = block_max_ll<ZW>(m, sh, ph);
-                const double f = __dsqrt_rn(__longlong_as_double(m));
-                if (f != far_) {
-                    far_ = f;
-                    K1 = sqrt_cut(2.0 * far_, false);
-                    ring_gate(ring, rmaxf, (double)A.gf.cs, slack, far_, ring_open, ring_key);
+                // the same largest squared distance: the same distance
+                if (m != far2) {
+                    far2 = m;
+                    const double f = __dsqrt_rn(__longlong_as_double(m));
+                    if (f != far_) {
+                        far_ = f;
+                        K1 = sqrt_cut(2.0 * far_, false);
+                        ring_gate(ring, rmaxf, (double)A.gf.cs, slack, far_, ring_open, ring_key);
+                    }
                 }
             }
             PHASE(6);
