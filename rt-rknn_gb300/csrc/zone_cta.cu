@@ -79,6 +79,43 @@ __device__ __forceinline__ void block_rank2(bool p, bool q, ZcShared& sh, unsign
     rq = bq + __popc(mq & below);
 }
 
+// block_rank2 that also returns the block maximum xm of a non-negative
+// 64-bit key x (a warp maximum from two 32-bit reductions: the high words,
+// then the low words of the lanes holding the highest), on the same barrier.
+template <int ZW>
+__device__ __forceinline__ void block_rank2m(bool p, bool q, long long x, ZcShared& sh, unsigned& ph, int& rp,
+                                             int& rq, int& tp, int& tq, long long& xm)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int b = ph & 1;
+    ph ^= 1;
+    const unsigned mp = __ballot_sync(FULL, p), mq = __ballot_sync(FULL, q);
+    const unsigned hi = (unsigned)((unsigned long long)x >> 32), lo = (unsigned)x;
+    const unsigned mhi = __reduce_max_sync(FULL, hi);
+    const unsigned mlo = __reduce_max_sync(FULL, hi == mhi ? lo : 0u);
+    if (lane == 0) {
+        sh.wc[b][0][w] = __popc(mp);
+        sh.wc[b][1][w] = __popc(mq);
+        sh.rl[b][w] = (long long)(((unsigned long long)mhi << 32) | mlo);
+    }
+    __syncthreads();
+    int bp = 0, bq = 0;
+    tp = 0;
+    tq = 0;
+    xm = 0;
+#pragma unroll
+    for (int j = 0; j < ZW; ++j) {
+        const int cp = sh.wc[b][0][j], cq = sh.wc[b][1][j];
+        if (j < w) { bp += cp; bq += cq; }
+        tp += cp;
+        tq += cq;
+        xm = max(xm, sh.rl[b][j]);
+    }
+    const unsigned below = (1u << lane) - 1;
+    rp = bp + __popc(mp & below);
+    rq = bq + __popc(mq & below);
+}
+
 template <int ZW>
 __device__ __forceinline__ int block_rank(bool p, ZcShared& sh, unsigned& ph, int& tot)
 {
@@ -469,6 +506,18 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 px = pf.x; py = pf.y;
                 if (A.skip_coincident && pf.x == qf.x && pf.y == qf.y) continue;
                 zs.pts++;
+                // The facility's bisector, by one thread of the last warp (the
+                // one with the least vertex-test work) while the others run
+                // the tests; it is read only if the facility is accepted,
+                // after the vertex test's barrier or the accept's own.
+                if (tid == ZT - 32) {
+                    const Line64 l = make_bisector(qx, qy, px, py);
+                    sh.bd[0] = l.a;
+                    sh.bd[1] = l.b;
+                    sh.bi[1] = l.vert;
+                    sh.bi[2] = l.valid;
+                }
+                if (tid == 0) sh.bi[3] = 0;   // the count pass's on-line vertex counter
             } else {
                 mbr = A.fmbr[GX(id, NCF, 103)];
                 zs.cells++;
@@ -482,7 +531,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             else r1 = __dsqrt_rn(key) > 2.0 * far_;
             if (r1) break;
             // rule 2: keep when nearer than twice the nearest bisector
-            bool r2;
+            bool r2, tested = false;
             if (keybits >= K2.hi) r2 = false;
             else if (keybits <= K2.lo) r2 = true;
             else r2 = __dsqrt_rn(key) < 2.0 * nearb;
@@ -495,19 +544,13 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     // lie within EPS of an extreme point (inf.cpp:283-346); or,
                     // with the zone-boundary test, every space-boundary vertex
                     // below count k.  The marks hold until the zone changes.
+                    // The vertex update marks them itself except when
+                    // rknn-inf's extreme points are needed (some
+                    // space-boundary vertex below count k) and at the start.
                     int ext[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) ext[j] = -1;
-                    if (!A.vertex_test) {
-                        // the reduction only when some space-boundary vertex
-                        // is below count k (a zone inside the space has none)
-                        bool hb = false;
-                        for (int i = tid; i < nV && !hb; i += ZT) {
-                            const float vw = IX(S.v4, i).w;
-                            hb = (vfl_of(vw) & VB_BND) && vcnt_of(vw) < ku;
-                        }
-                        if (__syncthreads_or(hb)) extreme_points<ZT>(S, nV, ku, sh, ext);
-                    }
+                    if (!A.vertex_test) extreme_points<ZT>(S, nV, ku, sh, ext);
                     float ex[8], ey[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
@@ -534,7 +577,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                         if (nfl != fl) IX(S.v4, i).w = vpack(cnt, nfl);
                     }
                     nCons = 1;          // marks valid
-                    __syncthreads();
+                    // (the test below reads only the marks this thread wrote)
                 }
                 bool hit = false;
                 const float px32 = (float)px, py32 = (float)py;
@@ -561,6 +604,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     hit = r != 0;
                 }
                 prune = !__syncthreads_or(hit);
+                tested = true;
                 PHASE(2);
             }
             if (prune) continue;
@@ -585,17 +629,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
 
             // ================= accept facility `id`: add its bisector ======
             if (nL >= LC) { flags |= QF_ZONE_L_OVERFLOW; break; }
-            if (tid < 32) {
-                Line64 l = {0.0, 0.0, 0, 0};
-                if (lane == 0) {
-                    l = make_bisector(qx, qy, px, py);
-                    sh.bd[0] = l.a;
-                    sh.bd[1] = l.b;
-                    sh.bi[1] = l.vert;
-                    sh.bi[2] = l.valid;
-                }
-            }
-            __syncthreads();
+            if (!tested) __syncthreads();   // the bisector made at the pop is visible
             Line64 nb;
             nb.a = sh.bd[0];
             nb.b = sh.bd[1];
@@ -605,10 +639,11 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             const float nab = fabsf(na32);
             zs.nb++;
             // The nearest bisector distance (inf.cpp:430-434) and the new
-            // line's records, by thread 32 while the count pass runs (the
-            // FP64 square root and division leave the critical path): nothing
-            // reads them before step (6), and nothing before it reads line nL.
-            if (tid == 32) {
+            // line's records, by one thread of the last warp while the count
+            // pass runs (the FP64 square root and division leave the critical
+            // path): nothing reads them before step (6), and nothing before
+            // it reads line nL.
+            if (tid == ZT - 32) {
                 double dl = nearb;
                 bool need = true;
                 if (nearb < DBL_MAX) {
@@ -634,8 +669,11 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 IX(S.lpos, nL) = id;
             }
 
-            // (1) count pass over the existing vertices (inf.cpp:359-364)
+            // (1) count pass over the existing vertices (inf.cpp:359-364);
+            //     it lists the vertices near the new line for (3) and needs
+            //     no barrier before (2), which reads no vertex
             const int nV0 = nV;
+            float m32 = 0.0f;
             for (int i = tid; i < nV0; i += ZT) {
                 const float4 v = IX(S.v4, i);
                 float r32, err;
@@ -656,10 +694,21 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 }
                 const float tol = (1.0f + nab) * 1.2e-9f + err;
                 uint32_t fl = vfl_of(v.w) & ~VB_ON;
-                if (fabsf(r32) <= tol || !(fabsf(r32) < FLT_MAX)) fl |= VB_ON;
-                IX(S.v4, i).w = vpack(vcnt_of(v.w) + (valid ? 0u : 1u), fl);
+                const uint32_t nc = vcnt_of(v.w) + (valid ? 0u : 1u);
+                if (fabsf(r32) <= tol || !(fabsf(r32) < FLT_MAX)) {
+                    fl |= VB_ON;
+                    IX(S.cons, atomicAdd(&sh.bi[3], 1)) = (uint16_t)i;   // (3)'s list, in any order
+                }
+                IX(S.v4, i).w = vpack(nc, fl);
+                if (nc < ku) m32 = fmaxf(m32, v.z);
             }
-            __syncthreads();
+            // the float maximum of the squared distances of the vertices that
+            // stay, as per-warp partials read after the next barrier
+            const int bm32 = ph & 1;
+            ph ^= 1;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) m32 = fmaxf(m32, __shfl_xor_sync(FULL, m32, o));
+            if (lane == 0) sh.rf[bm32][tid >> 5] = m32;
 
             PHASE(3);
             // (2) candidate intersections: boundary edges (bottom, top, left,
@@ -755,23 +804,16 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     IX(S.cfl, c) = ok ? (uint8_t)(cf | 0x80) : (uint8_t)0;
                 }
             }
-            __syncthreads();
+            __syncthreads();            // (1) and (2) are complete
+            m32 = sh.rf[bm32][0];
+#pragma unroll
+            for (int j = 1; j < ZW; ++j) m32 = fmaxf(m32, sh.rf[bm32][j]);
 
             PHASE(4);
-            // (3) deduplicate (|dx| < 1e-9 and |dy| < 1e-9) against existing
-            //     vertices near the new line
+            // (3) deduplicate (|dx| < 1e-9 and |dy| < 1e-9) against the
+            //     existing vertices near the new line, listed by (1)
             {
-                int nOn = 0;
-                for (int i0 = 0; i0 < nV0; i0 += ZT) {
-                    const int i = i0 + tid;
-                    const bool on = i < nV0 && (vfl_of(IX(S.v4, i).w) & VB_ON);
-                    int tot;
-                    const int r = block_rank<ZW>(on, sh, ph, tot);
-                    if (on) IX(S.cons, nOn + r) = (uint16_t)i;   // cons reused as scratch
-                    nOn += tot;
-                }
-                __syncthreads();
-                nCons = -1;   // considered list must be rebuilt
+                const int nOn = sh.bi[3];
                 if (nOn > 0) {
                     for (int c = tid; c < C; c += ZT) {
                         if (!(IX(S.cfl, c) & 0x80)) continue;
@@ -786,8 +828,8 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                         }
                         if (dup) IX(S.cfl, c) &= 0x7f;
                     }
+                    __syncthreads();
                 }
-                __syncthreads();
             }
 
             PHASE(5);
@@ -867,12 +909,27 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             }
 
             // (5) erase old vertices with count >= k (order kept), then append
-            //     the new vertices with count < k in candidate order
-            // When every candidate fits one chunk, the ranks of the new
-            // vertices come from the first erase chunk's reduction.
+            //     the new vertices with count < k in candidate order.  The
+            //     same reductions give (7) the largest squared distance to q
+            //     of the vertices that stay (the FP64 value of the old ones
+            //     whose float value is the float maximum found by (1), and
+            //     of every new one), and each vertex written gets its
+            //     vertex-test mark.  When every candidate fits one chunk, the
+            //     ranks of the new vertices come from the first erase
+            //     chunk's reduction.
             const bool one = C <= ZT;
             const bool nkeep = one && tid < C && (IX(S.cfl, tid) & 0x80) && IX(S.ccnt, tid) < k;
+            long long mx = 0;               // this thread's candidates for (7), as bits
+            double2 np = make_double2(0, 0);
+            double nd2 = 0.0;
+            if (nkeep) {
+                np = IX(S.cd, tid);
+                nd2 = d2_64(np.x, np.y, qx, qy);
+                mx = __double_as_longlong(nd2);
+            }
+            bool hbl = false;               // a space-boundary vertex stays (below count k)
             int w = 0, nr = 0, nnew = 0;
+            long long mxb = 0;
             for (int i0 = 0; i0 < max(nV0, 1); i0 += ZT) {
                 const int i = i0 + tid;
                 bool keep = false;
@@ -881,14 +938,21 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 if (i < nV0) {
                     v = IX(S.v4, i);
                     keep = vcnt_of(v.w) < ku;
-                    if (keep) p = IX(S.vd, i);
+                    if (keep) {
+                        p = IX(S.vd, i);
+                        if (v.z == m32) mx = max(mx, __double_as_longlong(d2_64(p.x, p.y, qx, qy)));
+                    }
                 }
                 int r, tot, rq, tq;
-                block_rank2<ZW>(keep, i0 == 0 && nkeep, sh, ph, r, rq, tot, tq);   // every read above precedes its barriers
+                block_rank2m<ZW>(keep, i0 == 0 && nkeep, mx, sh, ph, r, rq, tot, tq, mxb);   // every read above precedes its barriers
                 if (i0 == 0) { nr = rq; nnew = tq; }
                 if (keep) {
                     const int o = w + r;
-                    v.w = vpack(vcnt_of(v.w), vfl_of(v.w) & ~VB_ON);
+                    const uint32_t cnt = vcnt_of(v.w), fl = vfl_of(v.w);
+                    const bool bnd = (fl & VB_BND) != 0;
+                    const bool cons = cnt == ku - 1 || (A.vertex_test && bnd);
+                    hbl |= bnd;
+                    v.w = vpack(cnt, (fl & ~(VB_ON | VB_CONS)) | (cons ? VB_CONS : 0u));
                     IX(S.vd, o) = p;
                     IX(S.v4, o) = v;
                 }
@@ -898,12 +962,15 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 const int o = w + nr;
                 if (nkeep && o < VC) {
                     const int c = tid;
-                    const double2 p = IX(S.cd, c);
                     const float2 c32 = IX(S.c2, c);
-                    IX(S.vd, o) = p;
-                    IX(S.v4, o) = make_float4(c32.x, c32.y, (float)d2_64(p.x, p.y, qx, qy),
-                                              vpack((uint32_t)IX(S.ccnt, c),
-                                                    (IX(S.cfl, c) & VB_BND) | edge_bits(p.x, p.y, sx0, sy0, sx1, sy1)));
+                    const uint32_t cnt = (uint32_t)IX(S.ccnt, c);
+                    const bool bnd = (IX(S.cfl, c) & VB_BND) != 0;
+                    const bool cons = cnt == ku - 1 || (A.vertex_test && bnd);
+                    hbl |= bnd;
+                    IX(S.vd, o) = np;
+                    IX(S.v4, o) = make_float4(c32.x, c32.y, (float)nd2,
+                                              vpack(cnt, (bnd ? VB_BND : 0u) | (cons ? VB_CONS : 0u) |
+                                                             edge_bits(np.x, np.y, sx0, sy0, sx1, sy1)));
                 }
             } else {
                 nnew = 0;
@@ -916,21 +983,32 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     if (keep && o < VC) {
                         const double2 p = IX(S.cd, c);
                         const float2 c32 = IX(S.c2, c);
+                        const double d2 = d2_64(p.x, p.y, qx, qy);
+                        const uint32_t cnt = (uint32_t)IX(S.ccnt, c);
+                        const bool bnd = (IX(S.cfl, c) & VB_BND) != 0;
+                        const bool cons = cnt == ku - 1 || (A.vertex_test && bnd);
+                        hbl |= bnd;
+                        mx = max(mx, __double_as_longlong(d2));
                         IX(S.vd, o) = p;
-                        IX(S.v4, o) = make_float4(c32.x, c32.y, (float)d2_64(p.x, p.y, qx, qy),
-                                                  vpack((uint32_t)IX(S.ccnt, c),
-                                                        (IX(S.cfl, c) & VB_BND) | edge_bits(p.x, p.y, sx0, sy0, sx1, sy1)));
+                        IX(S.v4, o) = make_float4(c32.x, c32.y, (float)d2,
+                                                  vpack(cnt, (bnd ? VB_BND : 0u) | (cons ? VB_CONS : 0u) |
+                                                                 edge_bits(p.x, p.y, sx0, sy0, sx1, sy1)));
                     }
                     nnew += tot;
                 }
+                mxb = block_max_ll<ZW>(mx, sh, ph);
             }
             zs.kept += nnew;
             nV = w + nnew;
             const bool vover = nV > VC;
             if (vover) nV = VC;
-            __syncthreads();            // the vertex set is complete before (7) reads it
+            // the vertex set is complete past this barrier; rknn-inf's
+            // extreme points must be found again when a space-boundary vertex
+            // stays, else the marks written here are the test's
+            if (__syncthreads_or(hbl) && !A.vertex_test) nCons = -1;
+            else nCons = 1;
 
-            // (6) nearest bisector distance (computed by thread 32 while the
+            // (6) nearest bisector distance (computed by one thread while the
             //     count pass ran; every barrier since makes it visible)
             {
                 const double dl = sh.bd[2];
@@ -942,20 +1020,9 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             nL += 1;
             if (vover) flags |= QF_ZONE_V_OVERFLOW;
             if (nV > zs.vmax) zs.vmax = nV;
-            // (7) furthest remaining vertex (inf.cpp:445-451): the FP64
-            //     maximum is among the vertices whose rounded float value is
-            //     the float maximum
+            // (7) furthest remaining vertex (inf.cpp:445-451), from (5)
             {
-                float m32 = 0.0f;
-                for (int i = tid; i < nV; i += ZT) m32 = fmaxf(m32, IX(S.v4, i).z);
-                m32 = block_max_f<ZW>(m32, sh, ph);
-                long long m = 0;
-                for (int i = tid; i < nV; i += ZT)
-                    if (IX(S.v4, i).z == m32) {
-                        const double2 p = IX(S.vd, i);
-                        m = max(m, __double_as_longlong(d2_64(p.x, p.y, qx, qy)));
-                    }
-                m = block_max_ll<ZW>(m, sh, ph);
+                const long long m = mxb;
                 // the same largest squared distance: the same distance
                 if (m != far2) {
                     far2 = m;
