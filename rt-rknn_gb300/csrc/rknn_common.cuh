@@ -39,6 +39,77 @@ __device__ __forceinline__ void prefetch_l2_span(const void* base, size_t base_b
         asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a0), "r"((unsigned)(a1 - a0)) : "memory");
 }
 
+// Correctly rounded FP64 square root and quotient (the results of
+// __dsqrt_rn and __ddiv_rn) as PTX statements.  The compiler may execute a
+// square-root or division intrinsic that a branch guards on both sides of the
+// branch (it has no side effects), paying for its long FP64 sequence on the
+// common path; it does not execute an asm statement speculatively.
+__device__ __forceinline__ double sqrt_rn64(double x)
+{
+    double r;
+    asm("sqrt.rn.f64 %0, %1;" : "=d"(r) : "d"(x));
+    return r;
+}
+__device__ __forceinline__ double div_rn64(double a, double b)
+{
+    double r;
+    asm("div.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+
+// Exact widening of a float, as a PTX statement for the same reason: a
+// conversion to or from double takes an FP64 pipe slot per lane, and the
+// compiler would hoist a plain one out of a rarely taken branch.
+__device__ __forceinline__ double f2d(float x)
+{
+    double r;
+    asm("cvt.f64.f32 %0, %1;" : "=d"(r) : "f"(x));
+    return r;
+}
+
+// Float rounding of a double by integer operations: a conversion
+// instruction between float and double takes an FP64 pipe slot, as long as
+// an FP64 add.  MODE 0 rounds to nearest (ties to even), -1 toward -inf, +1
+// toward +inf; results that are not normal floats (zero, subnormal,
+// overflow) come from the conversion instruction.
+template <int MODE>
+__device__ __forceinline__ float d2f_bits(double d)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    if (e <= 0 || e >= 255) {
+        float r;
+        if (MODE == 0) asm("cvt.rn.f32.f64 %0, %1;" : "=f"(r) : "d"(d));
+        else if (MODE < 0) asm("cvt.rm.f32.f64 %0, %1;" : "=f"(r) : "d"(d));
+        else asm("cvt.rp.f32.f64 %0, %1;" : "=f"(r) : "d"(d));
+        return r;
+    }
+    const unsigned sign = hi & 0x80000000u;
+    // the exponent and the top 23 of the 52 fraction bits; the 29 dropped
+    unsigned r = ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1fffffffu;
+    if (MODE == 0) {
+        if (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) r += 1u;   // a carry raises the exponent
+    } else if (MODE < 0) {
+        if (sign && rest) r += 1u;
+    } else {
+        if (!sign && rest) r += 1u;
+    }
+    return __uint_as_float(sign | r);
+}
+
+// Exact widening of a float by integer operations (zero, subnormals, inf and
+// nan take the conversion instruction).
+__device__ __forceinline__ double f2d_bits(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    if (e == 0u || e == 255u) return f2d(f);
+    const unsigned hi = (u & 0x80000000u) | ((e + 1023u - 127u) << 20) | ((u & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+
 // Programmatic dependent launch.  A kernel launched with programmatic stream
 // serialization may start while its predecessor in the stream still runs:
 // pdl_wait() blocks until that grid has completed and its memory operations

@@ -221,7 +221,7 @@ __device__ __forceinline__ int group_exact_count(float ux, float uy, const QDesc
     } else {
         const double dx = (double)ux - (double)qx, dy = (double)uy - (double)qy;
         Dq64 = fma(dx, dx, dy * dy);
-        r = (float)sqrt(Dq64) * (1.0f + 4e-6f) + slack;
+        r = (float)sqrt_rn64(Dq64) * (1.0f + 4e-6f) + slack;
     }
     if (G > 1) {
         if (gi == 0 && lane == 0) *sc = 0;

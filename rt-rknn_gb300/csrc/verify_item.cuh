@@ -47,7 +47,7 @@ __device__ __forceinline__ int exact_count(float ux, float uy, const QDesc& d, c
         double dx = (double)ux - (double)qx, dy = (double)uy - (double)qy;
         double D = fma(dx, dx, dy * dy);
         Dq = (T)D;
-        r = (float)sqrt(D) * (1.0f + 4e-6f) + slack;
+        r = (float)sqrt_rn64(D) * (1.0f + 4e-6f) + slack;
     }
     const Grid& g = A.gf;
     int cx0 = cell_coord(ux - r, g.x0, g.inv, g.gx), cx1 = cell_coord(ux + r, g.x0, g.inv, g.gx);

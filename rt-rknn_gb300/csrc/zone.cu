@@ -216,13 +216,13 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
             bool r1;
             if (keybits >= K1.hi) r1 = true;
             else if (keybits <= K1.lo) r1 = false;
-            else r1 = __dsqrt_rn(key) > 2.0 * far_;
+            else r1 = sqrt_rn64(key) > 2.0 * far_;
             if (r1) break;
             // rule 2: keep when nearer than twice the nearest bisector
             bool r2;
             if (keybits >= K2.hi) r2 = false;
             else if (keybits <= K2.lo) r2 = true;
-            else r2 = __dsqrt_rn(key) < 2.0 * nearb;
+            else r2 = sqrt_rn64(key) < 2.0 * nearb;
             if (r2) prune = false;
             else {
                 // ---- vertex test (inf.cpp:268-353, 466-551) -------------
@@ -728,7 +728,7 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
                     }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(FULL, m, o));
-                const double f = __dsqrt_rn(__longlong_as_double(m));
+                const double f = sqrt_rn64(__longlong_as_double(m));
                 if (f != far_) {
                     far_ = f;
                     K1 = sqrt_cut(2.0 * far_, false);

@@ -45,7 +45,9 @@ struct ZcShared {
     long long ek[ZMAXW][8];   // extreme boundary points: per-warp best keys
     int ei[ZMAXW][8];         //   and list positions
     double bd[4];         // values one thread computed for all
-    int bi[12];
+    uint64_t bk[2];
+    float bf[6];
+    int bi[16];
 };
 
 // Ordered ranks of two predicates over the block (thread order is item
@@ -386,6 +388,8 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
     const float fsx0 = __double2float_rd(sx0), fsy0 = __double2float_rd(sy0);
     const float fsx1 = __double2float_ru(sx1), fsy1 = __double2float_ru(sy1);
     const double slack = 1e-5 * ((double)A.gf.cs + fmax(fmax(fabs(sx0), fabs(sx1)), fmax(fabs(sy0), fabs(sy1))));
+    const float slack_ru = __double2float_ru(slack);
+    const long long kx0 = order_key(sx0), kx1 = order_key(sx1), ky0 = order_key(sy0), ky1 = order_key(sy1);
     const float tolE = (1e-9f + 2.0f * E) * (1.0f + 0x1p-20f);
 
     for (;;) {
@@ -418,7 +422,8 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
         const uint32_t ku = (uint32_t)k;
         // block-uniform state (identical in every thread)
         int nV = 4, nL = 0, nP = 0, hP = 0, nCons = -1, flags = 0;
-        double far_ = 0.0, nearb = DBL_MAX;
+        double nearb = DBL_MAX;
+        float nearf = INFINITY;              // nearb rounded up (thread ZT - 32 keeps it)
         int cand_local = 0, cand64_local = 0;   // per-thread statistics
 
         // ---- init: four space corners (inf.cpp:211-226) -------------------
@@ -431,10 +436,11 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             IX(S.v4, tid) = make_float4((float)x, (float)y, (float)d2c,
                                         vpack(0, VB_BND | edge_bits(x, y, sx0, sy0, sx1, sy1)));
         }
-        const double d2far = block_max_d<ZW>(d2c, sh, ph);
-        far_ = __dsqrt_rn(d2far);
-        long long far2 = __double_as_longlong(d2far);   // far_ squared, as bits
-        Cut K1 = sqrt_cut(2.0 * far_, false);
+        // the farthest vertex's squared distance (bits), and what rule 1
+        // and the ring gate derive from it without its square root
+        long long far2 = __double_as_longlong(block_max_d<ZW>(d2c, sh, ph));
+        Cut K1 = far_cut(far2);
+        float ring_T = ring_limit32(far2, slack_ru);
         Cut K2 = sqrt_cut(2.0 * DBL_MAX, true);
 
         long long tph = clock64();
@@ -445,7 +451,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
         int ring = 0;
         bool ring_open;
         uint64_t ring_key;
-        ring_gate(ring, rmaxf, (double)A.gf.cs, slack, far_, ring_open, ring_key);
+        ring_gate32(ring, rmaxf, A.gf.cs, slack_ru, ring_T, ring_open, ring_key);
 
         // ---- best-first search --------------------------------------------
         for (;;) {
@@ -483,7 +489,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     if (over) { flags |= QF_ZONE_PQ_OVERFLOW; break; }
                 }
                 ring++;
-                ring_gate(ring, rmaxf, (double)A.gf.cs, slack, far_, ring_open, ring_key);
+                ring_gate32(ring, rmaxf, A.gf.cs, slack_ru, ring_T, ring_open, ring_key);
                 if (flags) break;
             }
             PHASE(0);
@@ -498,26 +504,36 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
 
             const bool is_point = (code & KIND_POINT) != 0;
             const int id = (int)(code & ~KIND_POINT);
-            double px = 0, py = 0;
+            float2 pf = make_float2(0, 0);
             float4 mbr = make_float4(0, 0, 0, 0);
             if (is_point) {
                 if (id == qpos) continue;
-                const float2 pf = A.fxy[GX(id, A.nf, 101)];
-                px = pf.x; py = pf.y;
+                pf = A.fxy[GX(id, A.nf, 101)];
                 if (A.skip_coincident && pf.x == qf.x && pf.y == qf.y) continue;
                 zs.pts++;
-                // The facility's bisector, by one thread of the last warp (the
-                // one with the least vertex-test work) while the others run
-                // the tests; it is read only if the facility is accepted,
-                // after the vertex test's barrier or the accept's own.
+                // The facility's bisector, by one thread of the last warp
+                // while the other warps run the vertex test (the last warp
+                // takes no part in it); it is read only if the facility is
+                // accepted, after the vertex test's barrier or the accept's
+                // own.
                 if (tid == ZT - 32) {
-                    const Line64 l = make_bisector(qx, qy, px, py);
+                    const Line64 l = make_bisector(qx, qy, f2d_bits(pf.x), f2d_bits(pf.y));
                     sh.bd[0] = l.a;
                     sh.bd[1] = l.b;
                     sh.bi[1] = l.vert;
                     sh.bi[2] = l.valid;
+                    // its float forms, made once for all threads
+                    sh.bf[0] = d2f_bits<0>(l.a);
+                    sh.bf[1] = d2f_bits<0>(l.b);
+                    sh.bf[2] = d2f_bits<-1>(l.a);
+                    sh.bf[3] = d2f_bits<1>(l.a);
+                    sh.bf[4] = d2f_bits<-1>(l.b);
+                    sh.bf[5] = d2f_bits<1>(l.b);
                 }
-                if (tid == 0) sh.bi[3] = 0;   // the count pass's on-line vertex counter
+                if (tid == 0) {
+                    sh.bi[3] = 0;             // the count pass's on-line vertex counter
+                    sh.bi[12] = 0;            // and the FP64 intersection list's
+                }
             } else {
                 mbr = A.fmbr[GX(id, NCF, 103)];
                 zs.cells++;
@@ -528,13 +544,13 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             bool r1;
             if (keybits >= K1.hi) r1 = true;
             else if (keybits <= K1.lo) r1 = false;
-            else r1 = __dsqrt_rn(key) > 2.0 * far_;
+            else r1 = sqrt_rn64(key) > 2.0 * sqrt_rn64(__longlong_as_double(far2));
             if (r1) break;
             // rule 2: keep when nearer than twice the nearest bisector
             bool r2, tested = false;
             if (keybits >= K2.hi) r2 = false;
             else if (keybits <= K2.lo) r2 = true;
-            else r2 = __dsqrt_rn(key) < 2.0 * nearb;
+            else r2 = sqrt_rn64(key) < 2.0 * nearb;
             if (r2) prune = false;
             else {
                 // ---- vertex test (inf.cpp:268-353, 466-551) -------------
@@ -560,7 +576,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                             ex[j] = e.x; ey[j] = e.y;
                         }
                     }
-                    for (int i = tid; i < nV; i += ZT) {
+                    for (int i = tid; i < nV && tid < ZT - 32; i += ZT - 32) {
                         const float4 v = IX(S.v4, i);
                         const uint32_t cnt = vcnt_of(v.w), fl = vfl_of(v.w);
                         const bool bnd = (fl & VB_BND) && cnt < ku;
@@ -580,24 +596,24 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     // (the test below reads only the marks this thread wrote)
                 }
                 bool hit = false;
-                const float px32 = (float)px, py32 = (float)py;
-                for (int i = tid; i < nV && !hit; i += ZT) {
+                for (int i = tid; i < nV && !hit && tid < ZT - 32; i += ZT - 32) {
                     const float4 v = IX(S.v4, i);
                     if (!(vfl_of(v.w) & VB_CONS)) continue;
                     int r;
-                    if (is_point) r = closer32(px32 - v.x, py32 - v.y, E, v.z);
+                    if (is_point) r = closer32(pf.x - v.x, pf.y - v.y, E, v.z);
                     else r = closer32(rect_dx32(v.x, mbr.x, mbr.z), rect_dx32(v.y, mbr.y, mbr.w), E, v.z);
                     if (r < 0) {
                         const double2 p = IX(S.vd, i);
                         double dx64 = 0, dy64 = 0;
                         if (is_point) {
-                            dx64 = __dsub_rn(px, p.x);
-                            dy64 = __dsub_rn(py, p.y);
+                            dx64 = __dsub_rn(f2d(pf.x), p.x);
+                            dy64 = __dsub_rn(f2d(pf.y), p.y);
                         } else {
-                            if (p.x < (double)mbr.x) dx64 = __dsub_rn((double)mbr.x, p.x);
-                            else if (p.x > (double)mbr.z) dx64 = __dsub_rn(p.x, (double)mbr.z);
-                            if (p.y < (double)mbr.y) dy64 = __dsub_rn((double)mbr.y, p.y);
-                            else if (p.y > (double)mbr.w) dy64 = __dsub_rn(p.y, (double)mbr.w);
+                            const double x0 = f2d(mbr.x), y0 = f2d(mbr.y), x1 = f2d(mbr.z), y1 = f2d(mbr.w);
+                            if (p.x < x0) dx64 = __dsub_rn(x0, p.x);
+                            else if (p.x > x1) dx64 = __dsub_rn(p.x, x1);
+                            if (p.y < y0) dy64 = __dsub_rn(y0, p.y);
+                            else if (p.y > y1) dy64 = __dsub_rn(p.y, y1);
                         }
                         r = closer64(dx64, dy64, p.x, p.y, qx, qy);
                     }
@@ -616,7 +632,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     const int t = t0 + tid;
                     if (t < p1) {
                         const float2 pf = A.fxy[GX(t, A.nf, 101)];
-                        sh.tk[tid] = (uint64_t)__double_as_longlong(d2_64(qx, qy, (double)pf.x, (double)pf.y));
+                        sh.tk[tid] = (uint64_t)__double_as_longlong(d2_64(qx, qy, f2d_bits(pf.x), f2d_bits(pf.y)));
                         sh.tc[tid] = KIND_POINT | (uint32_t)t;
                     }
                     bool over = false;
@@ -635,40 +651,9 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             nb.b = sh.bd[1];
             nb.vert = sh.bi[1];
             nb.valid = sh.bi[2];
-            const float na32 = (float)nb.a, nb32 = (float)nb.b;
+            const float na32 = sh.bf[0], nb32 = sh.bf[1];
             const float nab = fabsf(na32);
             zs.nb++;
-            // The nearest bisector distance (inf.cpp:430-434) and the new
-            // line's records, by one thread of the last warp while the count
-            // pass runs (the FP64 square root and division leave the critical
-            // path): nothing reads them before step (6), and nothing before
-            // it reads line nL.
-            if (tid == ZT - 32) {
-                double dl = nearb;
-                bool need = true;
-                if (nearb < DBL_MAX) {
-                    float est, err;
-                    if (nb.vert) {
-                        est = fabsf(qf.x - nb32);
-                        err = 4.0f * kU32 * (fabsf(qf.x) + fabsf(nb32)) + 1e-30f;
-                    } else {
-                        const float den = sqrtf(fmaf(na32, na32, 1.0f));
-                        est = fabsf(fmaf(na32, qf.x, nb32 - qf.y)) / den;
-                        err = 8.0f * kU32 * ((fabsf(na32 * qf.x) + fabsf(qf.y) + fabsf(nb32)) / den + est) + 1e-30f;
-                    }
-                    if ((double)__fsub_rd(est, err) > nearb) need = false;   // NaN keeps need
-                }
-                if (need) {
-                    const double d = line_dist64(qx, qy, nb.a, nb.b, nb.vert);
-                    if (d < nearb) dl = d;
-                }
-                sh.bd[2] = dl;
-                const uint32_t lf = (nb.vert ? LB_VERT : 0) | (nb.valid ? LB_VALID : 0);
-                IX(S.ld, nL) = make_double2(nb.a, nb.b);
-                IX(S.l4, nL) = make_float4(na32, nb32, 3.01f * kU32 * fabsf(nb32) + 1e-37f, __uint_as_float(lf));
-                IX(S.lpos, nL) = id;
-            }
-
             // (1) count pass over the existing vertices (inf.cpp:359-364);
             //     it lists the vertices near the new line for (3) and needs
             //     no barrier before (2), which reads no vertex
@@ -711,20 +696,18 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             if (lane == 0) sh.rf[bm32][tid >> 5] = m32;
 
             PHASE(3);
-            // (2) candidate intersections: boundary edges (bottom, top, left,
-            //     right; inf.h:340-374) then every earlier bisector in order;
-            //     a group of ZG threads per candidate
+            // (2) candidate intersections, boundary edges then every earlier
+            //     bisector in order: a group of ZG threads per candidate
+            //     drops, in float, those certainly outside the space or
+            //     certainly beyond k earlier bisectors, and lists the others
             const int C = 4 + nL;
-            const float a1l = __double2float_rd(nb.a), a1h = __double2float_ru(nb.a);
-            const float b1l = __double2float_rd(nb.b), b1h = __double2float_ru(nb.b);
+            const float a1l = sh.bf[2], a1h = sh.bf[3];
+            const float b1l = sh.bf[4], b1h = sh.bf[5];
             // (every lane of a warp runs each pass, so that the group sums
             // see the whole warp; a group past C computes nothing)
             for (int c0 = 0; c0 < C; c0 += ZGN) {
                 const int c = c0 + gi;
                 const bool active = c < C;
-                double x = 0, y = 0;
-                bool ok = false;
-                uint8_t cf = 0;
                 bool need64 = true;           // bisector candidates: intersect in FP64
                 bool do_cert = false;         // the group counts certified violations
                 float xc = 0, yc = 0, KX = 0, KY = 0;
@@ -782,26 +765,16 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     for (int m = gl; m < nL; m += ZG) cert += inval32(IX(S.l4, m), xc, yc, KX, KY);
                 cert = group_sum<ZG>(cert);
                 if (do_cert && cert >= k) need64 = false;
-                if (active && gl == 0) {
-                    if (c < 4) {
-                        const double ea = 0, eb = (c == 0) ? sy0 : (c == 1) ? sy1 : (c == 2) ? sx0 : sx1;
-                        const int bev = c >= 2;
-                        if (intersect64(nb.a, nb.b, nb.vert, ea, eb, bev, x, y))
-                            ok = (c < 2) ? (x >= sx0 && x <= sx1) : (y >= sy0 && y <= sy1);
-                        cf = VB_BND;
-                        cand_local += ok;
+                // the candidates that need their FP64 intersection go to a
+                // list (in any order) for (2b)
+                if (active && gl == 0 && c >= 4) {
+                    cand_local++;
+                    if (need64) {
+                        cand64_local++;
+                        IX(S.ccnt, atomicAdd(&sh.bi[12], 1)) = c;   // ccnt is free until (4)
                     } else {
-                        if (need64) {
-                            cand64_local++;
-                            const double2 e = IX(S.ld, j);
-                            if (intersect64(nb.a, nb.b, nb.vert, e.x, e.y, ev, x, y))
-                                ok = x >= sx0 && x <= sx1 && y >= sy0 && y <= sy1;
-                        }
-                        cand_local++;
+                        IX(S.cfl, c) = 0;
                     }
-                    IX(S.cd, c) = make_double2(x, y);
-                    IX(S.c2, c) = make_float2((float)x, (float)y);
-                    IX(S.cfl, c) = ok ? (uint8_t)(cf | 0x80) : (uint8_t)0;
                 }
             }
             __syncthreads();            // (1) and (2) are complete
@@ -810,26 +783,101 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             for (int j = 1; j < ZW; ++j) m32 = fmaxf(m32, sh.rf[bm32][j]);
 
             PHASE(4);
-            // (3) deduplicate (|dx| < 1e-9 and |dy| < 1e-9) against the
-            //     existing vertices near the new line, listed by (1)
+            // (2b) the intersections in FP64, a thread each: the listed
+            //     bisectors' (packed from warp 0 on), with the exact side of
+            //     the generating bisector (0x40: on the invalid side), which
+            //     (4) counts, and the four boundary edges' (bottom, top,
+            //     left, right; inf.h:340-374) on lanes of the next-to-last
+            //     warp; then (3), deduplication (|dx| < 1e-9 and |dy| <
+            //     1e-9) against the existing vertices near the new line,
+            //     listed by (1).  An FP64 instruction takes its warp about 64
+            //     cycles however few lanes run it, and the warps of one SM
+            //     sub-partition share its FP64 pipe: compares and float
+            //     conversions are done on the bits instead.
             {
-                const int nOn = sh.bi[3];
-                if (nOn > 0) {
-                    for (int c = tid; c < C; c += ZT) {
-                        if (!(IX(S.cfl, c) & 0x80)) continue;
-                        const float2 c32 = IX(S.c2, c);
-                        bool dup = false;
-                        for (int t = 0; t < nOn && !dup; ++t) {
-                            const int i = IX(S.cons, t);
+                const int nX = sh.bi[12], nOn = sh.bi[3];
+                // the candidate's float coordinates, its deduplication and
+                // its records
+                auto finish = [&](int c, double x, double y, bool ok, uint8_t cf) {
+                    const float2 c32 = make_float2(d2f_bits<0>(x), d2f_bits<0>(y));
+                    if (ok) {
+                        for (int u = 0; u < nOn; ++u) {
+                            const int i = IX(S.cons, u);
                             const float4 v = IX(S.v4, i);
                             if (fabsf(v.x - c32.x) > tolE || fabsf(v.y - c32.y) > tolE) continue;
-                            const double2 p = IX(S.vd, i), q = IX(S.cd, c);
-                            if (fabs(__dsub_rn(p.x, q.x)) < EPS && fabs(__dsub_rn(p.y, q.y)) < EPS) dup = true;
+                            const double2 p = IX(S.vd, i);
+                            if (fabs(__dsub_rn(p.x, x)) < EPS && fabs(__dsub_rn(p.y, y)) < EPS) { ok = false; break; }
                         }
-                        if (dup) IX(S.cfl, c) &= 0x7f;
                     }
-                    __syncthreads();
+                    IX(S.cd, c) = make_double2(x, y);
+                    IX(S.c2, c) = c32;
+                    IX(S.cfl, c) = ok ? (uint8_t)(cf | 0x80) : (uint8_t)0;
+                };
+                const int c4 = tid - (ZT - 64);
+                if (c4 >= 0 && c4 < 4) {
+                    const double eb = (c4 == 0) ? sy0 : (c4 == 1) ? sy1 : (c4 == 2) ? sx0 : sx1;
+                    double x = 0, y = 0;
+                    bool ok = false;
+                    if (intersect64(nb.a, nb.b, nb.vert, 0.0, eb, c4 >= 2, x, y))
+                        ok = (c4 < 2) ? (order_key(x) >= kx0 && order_key(x) <= kx1)
+                                      : (order_key(y) >= ky0 && order_key(y) <= ky1);
+                    cand_local += ok;
+                    finish(c4, x, y, ok, VB_BND);
                 }
+                for (int t = tid; t < nX; t += ZT) {
+                    const int c = IX(S.ccnt, t);
+                    const int j = c - 4;
+                    const double2 e = IX(S.ld, j);
+                    const uint32_t lf = __float_as_uint(IX(S.l4, j).w);
+                    const int ev = (lf & LB_VERT) ? 1 : 0;
+                    double x = 0, y = 0;
+                    bool ok = false;
+                    uint8_t cf = 0;
+                    if (intersect64(nb.a, nb.b, nb.vert, e.x, e.y, ev, x, y)) {
+                        const long long xk = order_key(x), yk = order_key(y);
+                        ok = xk >= kx0 && xk <= kx1 && yk >= ky0 && yk <= ky1;
+                        if (ok && !valid64k(e.x, e.y, ev, (lf & LB_VALID) ? 1 : 0, x, y)) cf = 0x40;
+                    }
+                    finish(c, x, y, ok, cf);
+                }
+                // the nearest bisector distance (inf.cpp:430-434), rule 2's
+                // bounds for it and the new line's records, by one thread of
+                // the last warp (idle here): nothing reads them before (6),
+                // and nothing before it reads line nL
+                if (tid == ZT - 32) {
+                    double dl = nearb;
+                    bool need = true;
+                    if (nearb < DBL_MAX) {
+                        float est, err;
+                        if (nb.vert) {
+                            est = fabsf(qf.x - nb32);
+                            err = 4.0f * kU32 * (fabsf(qf.x) + fabsf(nb32)) + 1e-30f;
+                        } else {
+                            const float den = sqrtf(fmaf(na32, na32, 1.0f));
+                            est = fabsf(fmaf(na32, qf.x, nb32 - qf.y)) / den;
+                            err = 8.0f * kU32 * ((fabsf(na32 * qf.x) + fabsf(qf.y) + fabsf(nb32)) / den + est) + 1e-30f;
+                        }
+                        // certainly farther than nearb (<= nearf): skip; NaN keeps need
+                        if (__fsub_rd(est, err) > nearf) need = false;
+                    }
+                    if (need) {
+                        const double d = line_dist64(qx, qy, nb.a, nb.b, nb.vert);
+                        if (d < nearb) dl = d;
+                    }
+                    sh.bd[2] = dl;
+                    Cut k2 = K2;
+                    if (dl != nearb) {
+                        k2 = near_cut(dl);
+                        nearf = d2f_bits<1>(dl);
+                    }
+                    sh.bk[0] = k2.lo;
+                    sh.bk[1] = k2.hi;
+                    const uint32_t lf = (nb.vert ? LB_VERT : 0) | (nb.valid ? LB_VALID : 0);
+                    IX(S.ld, nL) = make_double2(nb.a, nb.b);
+                    IX(S.l4, nL) = make_float4(na32, nb32, 3.01f * kU32 * fabsf(nb32) + 1e-37f, __uint_as_float(lf));
+                    IX(S.lpos, nL) = id;
+                }
+                __syncthreads();
             }
 
             PHASE(5);
@@ -850,12 +898,9 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     c32 = IX(S.c2, c);
                     KX = kU32 * fabsf(c32.x) * (1.0f + kU32) + 3.01f * kU32 * fabsf(c32.x);
                     KY = kU32 * fabsf(c32.y) + 3.01f * kU32 * fabsf(c32.y) + 1e-37f;
-                    // the generating bisector passes through the candidate: FP64
-                    if (gen >= 0 && gl == 0) {
-                        const double2 g = IX(S.ld, gen);
-                        const uint32_t lf = __float_as_uint(IX(S.l4, gen).w);
-                        cnt += !valid64(g.x, g.y, lf & LB_VERT, (lf & LB_VALID) ? 1 : 0, p.x, p.y);
-                    }
+                    // the generating bisector passes through the candidate: its
+                    // exact side, from (2b)
+                    if (gen >= 0 && gl == 0) cnt += (IX(S.cfl, c) & 0x40) ? 1 : 0;
                     for (int m = gl; m < nL; m += ZG) {
                         const int sm = (m == gen) ? -1 : side32(IX(S.l4, m), c32.x, c32.y, KX, KY);
                         cnt += sm > 0;
@@ -968,9 +1013,9 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     const bool cons = cnt == ku - 1 || (A.vertex_test && bnd);
                     hbl |= bnd;
                     IX(S.vd, o) = np;
-                    IX(S.v4, o) = make_float4(c32.x, c32.y, (float)nd2,
-                                              vpack(cnt, (bnd ? VB_BND : 0u) | (cons ? VB_CONS : 0u) |
-                                                             edge_bits(np.x, np.y, sx0, sy0, sx1, sy1)));
+                    uint32_t fl = cons ? VB_CONS : 0u;
+                    if (bnd) fl |= VB_BND | edge_bits(np.x, np.y, sx0, sy0, sx1, sy1);   // read for boundary vertices only
+                    IX(S.v4, o) = make_float4(c32.x, c32.y, d2f_bits<0>(nd2), vpack(cnt, fl));
                 }
             } else {
                 nnew = 0;
@@ -990,9 +1035,9 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                         hbl |= bnd;
                         mx = max(mx, __double_as_longlong(d2));
                         IX(S.vd, o) = p;
-                        IX(S.v4, o) = make_float4(c32.x, c32.y, (float)d2,
-                                                  vpack(cnt, (bnd ? VB_BND : 0u) | (cons ? VB_CONS : 0u) |
-                                                                 edge_bits(p.x, p.y, sx0, sy0, sx1, sy1)));
+                        uint32_t fl = cons ? VB_CONS : 0u;
+                        if (bnd) fl |= VB_BND | edge_bits(p.x, p.y, sx0, sy0, sx1, sy1);
+                        IX(S.v4, o) = make_float4(c32.x, c32.y, d2f_bits<0>(d2), vpack(cnt, fl));
                     }
                     nnew += tot;
                 }
@@ -1008,31 +1053,21 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             if (__syncthreads_or(hbl) && !A.vertex_test) nCons = -1;
             else nCons = 1;
 
-            // (6) nearest bisector distance (computed by one thread while the
-            //     count pass ran; every barrier since makes it visible)
-            {
-                const double dl = sh.bd[2];
-                if (dl != nearb) {
-                    nearb = dl;
-                    K2 = sqrt_cut(2.0 * nearb, true);
-                }
-            }
+            // (6) nearest bisector distance and rule 2's bounds (computed by
+            //     one thread while the count pass ran; every barrier since
+            //     makes them visible)
+            nearb = sh.bd[2];
+            K2.lo = sh.bk[0];
+            K2.hi = sh.bk[1];
             nL += 1;
             if (vover) flags |= QF_ZONE_V_OVERFLOW;
             if (nV > zs.vmax) zs.vmax = nV;
             // (7) furthest remaining vertex (inf.cpp:445-451), from (5)
-            {
-                const long long m = mxb;
-                // the same largest squared distance: the same distance
-                if (m != far2) {
-                    far2 = m;
-                    const double f = __dsqrt_rn(__longlong_as_double(m));
-                    if (f != far_) {
-                        far_ = f;
-                        K1 = sqrt_cut(2.0 * far_, false);
-                        ring_gate(ring, rmaxf, (double)A.gf.cs, slack, far_, ring_open, ring_key);
-                    }
-                }
+            if (mxb != far2) {
+                far2 = mxb;
+                K1 = far_cut(far2);
+                ring_T = ring_limit32(far2, slack_ru);
+                ring_gate32(ring, rmaxf, A.gf.cs, slack_ru, ring_T, ring_open, ring_key);
             }
             PHASE(6);
             if (flags) break;

@@ -77,8 +77,8 @@ __device__ Line64 make_bisector(double qx, double qy, double px, double py)
     } else if (qy == py) {
         l.vert = 1; l.b = mx;
     } else {
-        double s = __ddiv_rn(__dsub_rn(py, qy), __dsub_rn(px, qx));
-        double ps = __ddiv_rn(-1.0, s);
+        double s = div_rn64(__dsub_rn(py, qy), __dsub_rn(px, qx));
+        double ps = div_rn64(-1.0, s);
         double yi = __dsub_rn(my, __dmul_rn(ps, mx));
         if (isinf(ps)) { l.vert = 1; l.b = yi; }
         else { l.a = ps; l.b = yi; }
@@ -97,6 +97,15 @@ __device__ __forceinline__ bool valid64(double a, double b, int vert, int valid,
     return valid ? (y >= t) : (y <= t);
 }
 
+// valid64 with the final comparison on order keys instead of the FP64 pipe
+// (for points that are not NaN: the same result).
+__device__ __forceinline__ bool valid64k(double a, double b, int vert, int valid, double x, double y)
+{
+    const long long u = order_key(vert ? x : y);
+    const long long t = order_key(vert ? b : __dadd_rn(__dmul_rn(a, x), b));
+    return valid ? (u >= t) : (u <= t);
+}
+
 // find_line_intersection (rknn-inf/inf.h:303-333) in FP64
 __device__ __forceinline__ bool intersect64(double a1, double b1, int v1,
                                             double a2, double b2, int v2,
@@ -106,7 +115,7 @@ __device__ __forceinline__ bool intersect64(double a1, double b1, int v1,
     if (v1) { x = b1; y = __dadd_rn(__dmul_rn(a2, b1), b2); return true; }
     if (v2) { x = b2; y = __dadd_rn(__dmul_rn(a1, b2), b1); return true; }
     if (fabs(__dsub_rn(a1, a2)) < EPS) return false;
-    x = __ddiv_rn(__dsub_rn(b2, b1), __dsub_rn(a1, a2));
+    x = div_rn64(__dsub_rn(b2, b1), __dsub_rn(a1, a2));
     y = __dadd_rn(__dmul_rn(a1, x), b1);
     return true;
 }
@@ -116,8 +125,8 @@ __device__ double line_dist64(double px, double py, double a, double b, int vert
 {
     if (vert) return fabs(__dsub_rn(px, b));
     double num = fabs(__dadd_rn(__dsub_rn(__dmul_rn(a, px), py), b));
-    double den = __dsqrt_rn(__dadd_rn(__dmul_rn(a, a), 1.0));
-    return __ddiv_rn(num, den);
+    double den = sqrt_rn64(__dadd_rn(__dmul_rn(a, a), 1.0));
+    return div_rn64(num, den);
 }
 
 // Per-warp state array.  With RKNN_CHECKED every index is checked against
@@ -244,7 +253,7 @@ __device__ __forceinline__ int closer32(float dxp, float dyp, float E, float V)
 // the offset from p (or the rectangle) to v.
 __device__ __forceinline__ bool closer64(double dx, double dy, double vx, double vy, double qx, double qy)
 {
-    return __dsqrt_rn(__dadd_rn(dsq(dx), dsq(dy))) < __dsqrt_rn(d2_64(vx, vy, qx, qy));
+    return sqrt_rn64(__dadd_rn(dsq(dx), dsq(dy))) < sqrt_rn64(d2_64(vx, vy, qx, qy));
 }
 
 // Edge flags of a vertex (within EPS of each side of the space, in FP64).
@@ -287,6 +296,59 @@ __device__ __forceinline__ Cut sqrt_cut(double T, bool rule2)
     c.lo = (uint64_t)__double_as_longlong(__dmul_rn(t2, 1.0 - 0x1p-48));
     c.hi = (uint64_t)__double_as_longlong(__dmul_rn(t2, 1.0 + 0x1p-48));
     return c;
+}
+
+// Rule 1's bounds from the farthest vertex's squared distance d2 (as bits),
+// without its square root: T = 2 sqrt_rn(d2), and T*T lies within about
+// 2^-51 of 4 d2, whose bits are d2's with the exponent raised by two.  Keys
+// 64 units in the last place or more above 4 d2 are at least 2^-47 above it,
+// so sqrt(key) exceeds T by more than 2^-49 and sqrt_rn(key) > T; keys 64 or
+// more below are below T likewise.  Outside [2^-1000, 2^1000] every key takes
+// the square root.
+__device__ __forceinline__ Cut far_cut(long long d2bits)
+{
+    Cut c;
+    const uint64_t b = (uint64_t)d2bits;
+    if (b < (uint64_t)(1023 - 1000) << 52 || b > (uint64_t)(1023 + 1000) << 52) { c.lo = 0; c.hi = NEVER; return c; }
+    const uint64_t b4 = b + (2ull << 52);
+    c.lo = b4 - 64;
+    c.hi = b4 + 64;
+    return c;
+}
+
+// Rule 2's bounds for the nearest bisector distance dl (T = 2 dl), with the
+// margin of far_cut: 4 dl^2 rounded, and 64 units in the last place either
+// side.  T = 0: rule 2 (sqrt_rn(key) < 0) never holds; outside [2^-500,
+// 2^500] every key takes the square root.
+__device__ __forceinline__ Cut near_cut(double dl)
+{
+    Cut c;
+    const uint64_t b = (uint64_t)__double_as_longlong(dl);
+    if (b == 0) { c.lo = 0; c.hi = 0; return c; }
+    if (b < (uint64_t)(1023 - 500) << 52 || b > (uint64_t)(1023 + 500) << 52) { c.lo = 0; c.hi = NEVER; return c; }
+    const double T = __dmul_rn(dl, 2.0);
+    const uint64_t t2 = (uint64_t)__double_as_longlong(__dmul_rn(T, T));
+    c.lo = t2 - 64;
+    c.hi = t2 + 64;
+    return c;
+}
+
+// FP32 form of ring_gate (below), conservative: Lr rounded down and the
+// threshold T >= 2 far (1 + 1e-9) + slack rounded up, so a ring opens no
+// later than the FP64 gate opens it (an earlier expansion only puts cells in
+// the queue sooner; the order of the entries taken is the same).
+__device__ __forceinline__ float ring_limit32(long long far2bits, float slack_ru)
+{
+    const float f = __fmul_ru(__fsqrt_ru(d2f_bits<1>(__longlong_as_double(far2bits))), 1.0f + 0x1p-22f);
+    return __fadd_ru(__fmul_ru(2.0f * (1.0f + 0x1p-22f), f), slack_ru);
+}
+__device__ __forceinline__ void ring_gate32(int ring, int rmaxf, float cs, float slack_ru, float T_ru, bool& open,
+                                            uint64_t& key)
+{
+    float Lr = ring == 0 ? 0.0f : __fsub_rd(__fmul_rd((float)(ring - 1), cs), slack_ru);
+    if (!(Lr > 0.0f)) Lr = 0.0f;
+    open = ring <= rmaxf && !(Lr > T_ru);
+    key = (uint64_t)__double_as_longlong((double)__fmul_rd(Lr, Lr));
 }
 
 // Whether facility ring `ring` (cells at Chebyshev distance `ring` from q's
