@@ -906,6 +906,8 @@ __device__ __forceinline__ void zone_body(const ZoneArgs& A)
 }
 #undef WSYNC
 
-__global__ void __launch_bounds__(ZONE_WARPS * 32) zone_kernel_smem(ZoneArgs a) { zone_body(a); }
+// at most 128 registers, so that 16 one-warp blocks fit an SM when the
+// shared state allows as many
+__global__ void __launch_bounds__(ZONE_WARPS * 32, 16) zone_kernel_smem(ZoneArgs a) { zone_body(a); }
 
 }  // namespace rknn

@@ -46,8 +46,13 @@ struct ZcShared {
     int ei[ZMAXW][8];         //   and list positions
     double bd[4];         // values one thread computed for all
     uint64_t bk[2];
-    float bf[6];
+    struct {              // the bisector of the facility taken
+        double a, b;
+        int vert, valid;
+        float f[6];       // a, b rounded to nearest; a down, up; b down, up
+    } sb;
     int bi[16];
+    unsigned long long fmax[2];   // (7)'s maximum, by accept parity
 };
 
 // Ordered ranks of two predicates over the block (thread order is item
@@ -75,43 +80,6 @@ __device__ __forceinline__ void block_rank2(bool p, bool q, ZcShared& sh, unsign
         if (j < w) { bp += cp; bq += cq; }
         tp += cp;
         tq += cq;
-    }
-    const unsigned below = (1u << lane) - 1;
-    rp = bp + __popc(mp & below);
-    rq = bq + __popc(mq & below);
-}
-
-// block_rank2 that also returns the block maximum xm of a non-negative
-// 64-bit key x (a warp maximum from two 32-bit reductions: the high words,
-// then the low words of the lanes holding the highest), on the same barrier.
-template <int ZW>
-__device__ __forceinline__ void block_rank2m(bool p, bool q, long long x, ZcShared& sh, unsigned& ph, int& rp,
-                                             int& rq, int& tp, int& tq, long long& xm)
-{
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int b = ph & 1;
-    ph ^= 1;
-    const unsigned mp = __ballot_sync(FULL, p), mq = __ballot_sync(FULL, q);
-    const unsigned hi = (unsigned)((unsigned long long)x >> 32), lo = (unsigned)x;
-    const unsigned mhi = __reduce_max_sync(FULL, hi);
-    const unsigned mlo = __reduce_max_sync(FULL, hi == mhi ? lo : 0u);
-    if (lane == 0) {
-        sh.wc[b][0][w] = __popc(mp);
-        sh.wc[b][1][w] = __popc(mq);
-        sh.rl[b][w] = (long long)(((unsigned long long)mhi << 32) | mlo);
-    }
-    __syncthreads();
-    int bp = 0, bq = 0;
-    tp = 0;
-    tq = 0;
-    xm = 0;
-#pragma unroll
-    for (int j = 0; j < ZW; ++j) {
-        const int cp = sh.wc[b][0][j], cq = sh.wc[b][1][j];
-        if (j < w) { bp += cp; bq += cq; }
-        tp += cp;
-        tq += cq;
-        xm = max(xm, sh.rl[b][j]);
     }
     const unsigned below = (1u << lane) - 1;
     rp = bp + __popc(mp & below);
@@ -185,21 +153,6 @@ __device__ __forceinline__ float block_max_f(float v, ZcShared& sh, unsigned& ph
     float r = sh.rf[b][0];
 #pragma unroll
     for (int j = 1; j < ZW; ++j) r = fmaxf(r, sh.rf[b][j]);
-    return r;
-}
-
-template <int ZW>
-__device__ __forceinline__ long long block_max_ll(long long v, ZcShared& sh, unsigned& ph)
-{
-    const int b = ph & 1;
-    ph ^= 1;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = max(v, (long long)__shfl_xor_sync(FULL, v, o));
-    if ((threadIdx.x & 31) == 0) sh.rl[b][threadIdx.x >> 5] = v;
-    __syncthreads();
-    long long r = sh.rl[b][0];
-#pragma unroll
-    for (int j = 1; j < ZW; ++j) r = max(r, sh.rl[b][j]);
     return r;
 }
 
@@ -361,6 +314,23 @@ __device__ __forceinline__ void extreme_points(const Slice& S, int nV, uint32_t 
     for (int j = 0; j < 8; ++j) ext[j] = sh.bi[4 + j];
 }
 
+// The bisector of q and the facility at (fx, fy), with its float forms, for
+// every thread of the block to read after a barrier.
+__device__ __forceinline__ void make_slot(ZcShared& sh, float fx, float fy, double qx, double qy)
+{
+    const Line64 l = make_bisector(qx, qy, f2d_bits(fx), f2d_bits(fy));
+    sh.sb.a = l.a;
+    sh.sb.b = l.b;
+    sh.sb.vert = l.vert;
+    sh.sb.valid = l.valid;
+    sh.sb.f[0] = d2f_bits<0>(l.a);
+    sh.sb.f[1] = d2f_bits<0>(l.b);
+    sh.sb.f[2] = d2f_bits<-1>(l.a);
+    sh.sb.f[3] = d2f_bits<1>(l.a);
+    sh.sb.f[4] = d2f_bits<-1>(l.b);
+    sh.sb.f[5] = d2f_bits<1>(l.b);
+}
+
 template <int ZT>
 __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
 {
@@ -516,23 +486,11 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 // takes no part in it); it is read only if the facility is
                 // accepted, after the vertex test's barrier or the accept's
                 // own.
-                if (tid == ZT - 32) {
-                    const Line64 l = make_bisector(qx, qy, f2d_bits(pf.x), f2d_bits(pf.y));
-                    sh.bd[0] = l.a;
-                    sh.bd[1] = l.b;
-                    sh.bi[1] = l.vert;
-                    sh.bi[2] = l.valid;
-                    // its float forms, made once for all threads
-                    sh.bf[0] = d2f_bits<0>(l.a);
-                    sh.bf[1] = d2f_bits<0>(l.b);
-                    sh.bf[2] = d2f_bits<-1>(l.a);
-                    sh.bf[3] = d2f_bits<1>(l.a);
-                    sh.bf[4] = d2f_bits<-1>(l.b);
-                    sh.bf[5] = d2f_bits<1>(l.b);
-                }
+                if (tid == ZT - 32) make_slot(sh, pf.x, pf.y, qx, qy);
                 if (tid == 0) {
                     sh.bi[3] = 0;             // the count pass's on-line vertex counter
                     sh.bi[12] = 0;            // and the FP64 intersection list's
+                    sh.fmax[nL & 1] = 0;      // and (7)'s maximum (read after the accept's last barrier)
                 }
             } else {
                 mbr = A.fmbr[GX(id, NCF, 103)];
@@ -586,7 +544,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                             for (int j = 0; j < 8; ++j) {
                                 if (c || ext[j] < 0 || fabsf(v.x - ex[j]) > tolE || fabsf(v.y - ey[j]) > tolE) continue;
                                 const double2 a = IX(S.vd, i), b = IX(S.vd, ext[j]);
-                                if (fabs(__dsub_rn(a.x, b.x)) < EPS && fabs(__dsub_rn(a.y, b.y)) < EPS) c = true;
+                                if (within_eps(a.x, b.x) && within_eps(a.y, b.y)) c = true;
                             }
                         }
                         const uint32_t nfl = c ? (fl | VB_CONS) : (fl & ~VB_CONS);
@@ -647,11 +605,11 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             if (nL >= LC) { flags |= QF_ZONE_L_OVERFLOW; break; }
             if (!tested) __syncthreads();   // the bisector made at the pop is visible
             Line64 nb;
-            nb.a = sh.bd[0];
-            nb.b = sh.bd[1];
-            nb.vert = sh.bi[1];
-            nb.valid = sh.bi[2];
-            const float na32 = sh.bf[0], nb32 = sh.bf[1];
+            nb.a = sh.sb.a;
+            nb.b = sh.sb.b;
+            nb.vert = sh.sb.vert;
+            nb.valid = sh.sb.valid;
+            const float na32 = sh.sb.f[0], nb32 = sh.sb.f[1];
             const float nab = fabsf(na32);
             zs.nb++;
             // (1) count pass over the existing vertices (inf.cpp:359-364);
@@ -701,8 +659,8 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             //     drops, in float, those certainly outside the space or
             //     certainly beyond k earlier bisectors, and lists the others
             const int C = 4 + nL;
-            const float a1l = sh.bf[2], a1h = sh.bf[3];
-            const float b1l = sh.bf[4], b1h = sh.bf[5];
+            const float a1l = sh.sb.f[2], a1h = sh.sb.f[3];
+            const float b1l = sh.sb.f[4], b1h = sh.sb.f[5];
             // (every lane of a warp runs each pass, so that the group sums
             // see the whole warp; a group past C computes nothing)
             for (int c0 = 0; c0 < C; c0 += ZGN) {
@@ -806,7 +764,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                             const float4 v = IX(S.v4, i);
                             if (fabsf(v.x - c32.x) > tolE || fabsf(v.y - c32.y) > tolE) continue;
                             const double2 p = IX(S.vd, i);
-                            if (fabs(__dsub_rn(p.x, x)) < EPS && fabs(__dsub_rn(p.y, y)) < EPS) { ok = false; break; }
+                            if (within_eps(p.x, x) && within_eps(p.y, y)) { ok = false; break; }
                         }
                     }
                     IX(S.cd, c) = make_double2(x, y);
@@ -945,7 +903,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                             for (int c2 = 0; c2 < c; ++c2) {
                                 if (!(IX(S.cfl, c2) & 0x80)) continue;
                                 const double2 o = IX(S.cd, c2);
-                                if (fabs(__dsub_rn(o.x, p.x)) < EPS && fabs(__dsub_rn(o.y, p.y)) < EPS) { IX(S.cfl, c) &= 0x7f; break; }
+                                if (within_eps(o.x, p.x) && within_eps(o.y, p.y)) { IX(S.cfl, c) &= 0x7f; break; }
                             }
                         }
                     }
@@ -965,16 +923,8 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             const bool one = C <= ZT;
             const bool nkeep = one && tid < C && (IX(S.cfl, tid) & 0x80) && IX(S.ccnt, tid) < k;
             long long mx = 0;               // this thread's candidates for (7), as bits
-            double2 np = make_double2(0, 0);
-            double nd2 = 0.0;
-            if (nkeep) {
-                np = IX(S.cd, tid);
-                nd2 = d2_64(np.x, np.y, qx, qy);
-                mx = __double_as_longlong(nd2);
-            }
             bool hbl = false;               // a space-boundary vertex stays (below count k)
             int w = 0, nr = 0, nnew = 0;
-            long long mxb = 0;
             for (int i0 = 0; i0 < max(nV0, 1); i0 += ZT) {
                 const int i = i0 + tid;
                 bool keep = false;
@@ -983,15 +933,13 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 if (i < nV0) {
                     v = IX(S.v4, i);
                     keep = vcnt_of(v.w) < ku;
-                    if (keep) {
-                        p = IX(S.vd, i);
-                        if (v.z == m32) mx = max(mx, __double_as_longlong(d2_64(p.x, p.y, qx, qy)));
-                    }
+                    if (keep) p = IX(S.vd, i);
                 }
                 int r, tot, rq, tq;
-                block_rank2m<ZW>(keep, i0 == 0 && nkeep, mx, sh, ph, r, rq, tot, tq, mxb);   // every read above precedes its barriers
+                block_rank2<ZW>(keep, i0 == 0 && nkeep, sh, ph, r, rq, tot, tq);   // every read above precedes its barriers
                 if (i0 == 0) { nr = rq; nnew = tq; }
                 if (keep) {
+                    if (v.z == m32) mx = max(mx, __double_as_longlong(d2_64(p.x, p.y, qx, qy)));
                     const int o = w + r;
                     const uint32_t cnt = vcnt_of(v.w), fl = vfl_of(v.w);
                     const bool bnd = (fl & VB_BND) != 0;
@@ -1005,17 +953,22 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             }
             if (one) {
                 const int o = w + nr;
-                if (nkeep && o < VC) {
-                    const int c = tid;
-                    const float2 c32 = IX(S.c2, c);
-                    const uint32_t cnt = (uint32_t)IX(S.ccnt, c);
-                    const bool bnd = (IX(S.cfl, c) & VB_BND) != 0;
-                    const bool cons = cnt == ku - 1 || (A.vertex_test && bnd);
-                    hbl |= bnd;
-                    IX(S.vd, o) = np;
-                    uint32_t fl = cons ? VB_CONS : 0u;
-                    if (bnd) fl |= VB_BND | edge_bits(np.x, np.y, sx0, sy0, sx1, sy1);   // read for boundary vertices only
-                    IX(S.v4, o) = make_float4(c32.x, c32.y, d2f_bits<0>(nd2), vpack(cnt, fl));
+                if (nkeep) {
+                    const double2 np = IX(S.cd, tid);
+                    const double nd2 = d2_64(np.x, np.y, qx, qy);
+                    mx = max(mx, __double_as_longlong(nd2));
+                    if (o < VC) {
+                        const int c = tid;
+                        const float2 c32 = IX(S.c2, c);
+                        const uint32_t cnt = (uint32_t)IX(S.ccnt, c);
+                        const bool bnd = (IX(S.cfl, c) & VB_BND) != 0;
+                        const bool cons = cnt == ku - 1 || (A.vertex_test && bnd);
+                        hbl |= bnd;
+                        IX(S.vd, o) = np;
+                        uint32_t fl = cons ? VB_CONS : 0u;
+                        if (bnd) fl |= VB_BND | edge_bits(np.x, np.y, sx0, sy0, sx1, sy1);   // read for boundary vertices only
+                        IX(S.v4, o) = make_float4(c32.x, c32.y, d2f_bits<0>(nd2), vpack(cnt, fl));
+                    }
                 }
             } else {
                 nnew = 0;
@@ -1041,8 +994,9 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     }
                     nnew += tot;
                 }
-                mxb = block_max_ll<ZW>(mx, sh, ph);
             }
+            // (7)'s maximum over the block, folded into the barrier below
+            if (mx != 0) atomicMax(&sh.fmax[nL & 1], (unsigned long long)mx);
             zs.kept += nnew;
             nV = w + nnew;
             const bool vover = nV > VC;
@@ -1052,6 +1006,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             // stays, else the marks written here are the test's
             if (__syncthreads_or(hbl) && !A.vertex_test) nCons = -1;
             else nCons = 1;
+            const long long mxb = (long long)sh.fmax[nL & 1];   // reset at the pop two accepts on
 
             // (6) nearest bisector distance and rule 2's bounds (computed by
             //     one thread while the count pass ran; every barrier since

@@ -52,6 +52,13 @@ __device__ __forceinline__ double rect_d2_64(double px, double py, float4 r)
     return __dadd_rn(dsq(dx), dsq(dy));
 }
 
+// |a - b| < EPS with the difference rounded in FP64 and the comparison on
+// its bits (the magnitude's bits order as its value; a NaN compares false).
+__device__ __forceinline__ bool within_eps(double a, double b)
+{
+    return (__double_as_longlong(__dsub_rn(a, b)) & 0x7fffffffffffffffll) < 0x3e112e0be826d695ll;   // bits of 1e-9
+}
+
 // Integer key with the numeric order of a finite double (-0 counts as +0).
 __device__ __forceinline__ long long order_key(double d)
 {
@@ -65,26 +72,40 @@ __device__ __forceinline__ float rect_dx32(float v, float lo, float hi)
     return v < lo ? lo - v : (v > hi ? v - hi : 0.0f);
 }
 
-// perpendicular_bisector (rknn-inf/inf.h:150-192), query first
+// Exact halving: the exponent lowered by one where the result is normal (the
+// product by 0.5 otherwise), which rounds as the reference's division by 2.
+__device__ __forceinline__ double half64(double d)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+    if (e > 1u && e < 0x7ffu) return __longlong_as_double((long long)(b - (1ull << 52)));
+    return __dmul_rn(d, 0.5);
+}
+
+// perpendicular_bisector (rknn-inf/inf.h:150-192), query first.  Equality
+// and order tests run on the bits (order_key; coordinates are never NaN):
+// each FP64 instruction costs its warp about 64 cycles on GB300, a compare
+// as much as a product.
 __device__ Line64 make_bisector(double qx, double qy, double px, double py)
 {
     Line64 l;
-    // halving is exact: the product by 0.5 rounds as the quotient by 2 does
-    double mx = __dmul_rn(__dadd_rn(qx, px), 0.5), my = __dmul_rn(__dadd_rn(qy, py), 0.5);
+    const double mx = half64(__dadd_rn(qx, px)), my = half64(__dadd_rn(qy, py));
     l.a = 0; l.b = 0; l.vert = 0;
-    if (qx == px) {
+    if (order_key(qx) == order_key(px)) {
         l.a = 0; l.b = my;
-    } else if (qy == py) {
+    } else if (order_key(qy) == order_key(py)) {
         l.vert = 1; l.b = mx;
     } else {
         double s = div_rn64(__dsub_rn(py, qy), __dsub_rn(px, qx));
         double ps = div_rn64(-1.0, s);
         double yi = __dsub_rn(my, __dmul_rn(ps, mx));
-        if (isinf(ps)) { l.vert = 1; l.b = yi; }
+        if ((__double_as_longlong(ps) & 0x7fffffffffffffffll) == 0x7ff0000000000000ll) { l.vert = 1; l.b = yi; }
         else { l.a = ps; l.b = yi; }
     }
-    if (l.vert) l.valid = (qx >= l.b) ? 1 : 0;
-    else l.valid = (qy >= __dadd_rn(__dmul_rn(l.a, qx), l.b)) ? 1 : 0;
+    // (a NaN b, from an infinite slope times a zero midpoint, compares false)
+    const bool nan_b = (__double_as_longlong(l.b) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+    if (l.vert) l.valid = (!nan_b && order_key(qx) >= order_key(l.b)) ? 1 : 0;
+    else l.valid = (order_key(qy) >= order_key(__dadd_rn(__dmul_rn(l.a, qx), l.b))) ? 1 : 0;
     return l;
 }
 
@@ -114,7 +135,7 @@ __device__ __forceinline__ bool intersect64(double a1, double b1, int v1,
     if (v1 && v2) return false;
     if (v1) { x = b1; y = __dadd_rn(__dmul_rn(a2, b1), b2); return true; }
     if (v2) { x = b2; y = __dadd_rn(__dmul_rn(a1, b2), b1); return true; }
-    if (fabs(__dsub_rn(a1, a2)) < EPS) return false;
+    if (within_eps(a1, a2)) return false;
     x = div_rn64(__dsub_rn(b2, b1), __dsub_rn(a1, a2));
     y = __dadd_rn(__dmul_rn(a1, x), b1);
     return true;
@@ -261,10 +282,10 @@ __device__ __forceinline__ uint8_t edge_bits(double x, double y, double sx0, dou
                                              double sx1, double sy1)
 {
     uint8_t f = 0;
-    if (fabs(__dsub_rn(x, sx0)) < EPS) f |= VB_EL;
-    if (fabs(__dsub_rn(x, sx1)) < EPS) f |= VB_ER;
-    if (fabs(__dsub_rn(y, sy0)) < EPS) f |= VB_EB;
-    if (fabs(__dsub_rn(y, sy1)) < EPS) f |= VB_ET;
+    if (within_eps(x, sx0)) f |= VB_EL;
+    if (within_eps(x, sx1)) f |= VB_ER;
+    if (within_eps(y, sy0)) f |= VB_EB;
+    if (within_eps(y, sy1)) f |= VB_ET;
     return f;
 }
 
