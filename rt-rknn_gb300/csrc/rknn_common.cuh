@@ -110,6 +110,16 @@ __device__ __forceinline__ double f2d_bits(float f)
     return __hiloint2double((int)hi, (int)(u << 29));
 }
 
+// Integer key with the numeric order of a double (-0 counts as +0; a NaN
+// orders above +inf or below -inf by its sign bit), for comparisons without
+// the FP64 pipe.
+__device__ __forceinline__ long long order_key(double d)
+{
+    long long b = __double_as_longlong(d);
+    if (b == (long long)0x8000000000000000ull) b = 0;
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
+}
+
 // Programmatic dependent launch.  A kernel launched with programmatic stream
 // serialization may start while its predecessor in the stream still runs:
 // pdl_wait() blocks until that grid has completed and its memory operations

@@ -59,14 +59,6 @@ __device__ __forceinline__ bool within_eps(double a, double b)
     return (__double_as_longlong(__dsub_rn(a, b)) & 0x7fffffffffffffffll) < 0x3e112e0be826d695ll;   // bits of 1e-9
 }
 
-// Integer key with the numeric order of a finite double (-0 counts as +0).
-__device__ __forceinline__ long long order_key(double d)
-{
-    long long b = __double_as_longlong(d);
-    if (b == (long long)0x8000000000000000ull) b = 0;
-    return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
-}
-
 __device__ __forceinline__ float rect_dx32(float v, float lo, float hi)
 {
     return v < lo ? lo - v : (v > hi ? v - hi : 0.0f);
