@@ -246,10 +246,13 @@ __device__ __forceinline__ void pq_merge(uint64_t* K, uint32_t* C, int& h, int& 
 // its edge -- the smallest key (largest for a maximum), the earliest entry
 // among equal keys.  Each thread keeps its best of the entries it reads, then
 // a block reduction by (key, position).  ext[j] = vertex index or -1.
+// Run by all warps but the last (which makes the facility's bisector
+// meanwhile), synchronised by named barrier 1 over those warps only.
 template <int ZT>
 __device__ __forceinline__ void extreme_points(const Slice& S, int nV, uint32_t ku, ZcShared& sh, int (&ext)[8])
 {
-    constexpr int ZW = ZT / 32;
+    constexpr int ZW = ZT / 32 - 1;       // the warps taking part
+    constexpr int NT = ZW * 32;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     long long bk[8];
     int bp[8];
@@ -257,7 +260,7 @@ __device__ __forceinline__ void extreme_points(const Slice& S, int nV, uint32_t 
     for (int j = 0; j < 8; ++j) { bk[j] = 0; bp[j] = INT_MAX; }
     // the list of boundary vertices below count k, in vertex order: the
     // vertex index serves as the list position
-    for (int t = tid; t < nV; t += ZT) {
+    for (int t = tid; t < nV; t += NT) {
         const float vw = IX(S.v4, t).w;
         const uint32_t fl = vfl_of(vw);
         if (!(fl & VB_BND) || vcnt_of(vw) >= ku) continue;
@@ -293,7 +296,7 @@ __device__ __forceinline__ void extreme_points(const Slice& S, int nV, uint32_t 
             sh.ei[w][j] = mpos == 0xffffffffu ? INT_MAX : (int)mpos;
         }
     }
-    __syncthreads();
+    asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory");
     if (tid < 8) {
         const int j = tid;
         unsigned long long k0 = (unsigned long long)sh.ek[0][j];
@@ -309,7 +312,7 @@ __device__ __forceinline__ void extreme_points(const Slice& S, int nV, uint32_t 
         }
         sh.bi[4 + j] = p0 == INT_MAX ? -1 : p0;
     }
-    __syncthreads();
+    asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory");
 #pragma unroll
     for (int j = 0; j < 8; ++j) ext[j] = sh.bi[4 + j];
 }
@@ -524,7 +527,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     int ext[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) ext[j] = -1;
-                    if (!A.vertex_test) extreme_points<ZT>(S, nV, ku, sh, ext);
+                    if (!A.vertex_test && tid < ZT - 32) extreme_points<ZT>(S, nV, ku, sh, ext);
                     float ex[8], ey[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
