@@ -233,6 +233,39 @@ def profile_single(k: int, n: int):
             print(int(q), len(idx.query(int(q), k, "fp64")))
 
 
+def explain(c: int):
+    """Where one FP32 batch of workload c (2, 3 or 4; its own queries and k)
+    spends its time: per-kernel device ms (profiling mode, events between
+    the kernels), the filter's phase cycles per query (warp 0 of each
+    query: ring walk, of it the facility offers; the slice bound; the
+    half-planes and user segments; the fused verification), and the work
+    per query."""
+    ds = datagen.config(c)
+    qs = ds.queries.astype(np.int32)
+    ks = ds.ks.astype(np.int32) if c == 4 else np.full(len(qs), 10, np.int32)
+    nq = len(qs)
+    with rknn.Index.of(ds) as idx:
+        for _ in range(2):
+            idx.query_batch_flat(qs, ks, "fp32")
+        ms, st, _ = _batch(idx, qs, ks, "fp32", reps=3)
+        idx.set_profiling(True)
+        km = []
+        for _ in range(3):
+            idx.query_batch(qs, ks, "fp32")
+            km.append(idx.kernel_ms())
+        idx.set_profiling(False)
+    cyc = np.array(st["zone_cycles"], float) / nq
+    out = {"config": c, "queries": nq, "device_ms": ms, "qps": nq / (ms / 1e3),
+           "kernel_ms": {k: float(np.median([m[k] for m in km])) for k in km[0]},
+           "filter_cycles_per_query": {"ring_walk": cyc[0], "of_it_offers": cyc[1], "slice_bound": cyc[2],
+                                       "half_planes_and_segments": cyc[7], "fused_verification": cyc[6]},
+           "per_query": {k: st[k] / nq for k in ("bisectors", "candidates", "plane_evals", "survivors",
+                                                   "fac_checks", "rechecks", "results")},
+           "fused_queries": st.get("fused_slots")}
+    print(json.dumps(out), flush=True)
+    return out
+
+
 def profile_index(c: int):
     """Only the index build of workload c (the grid build kernels)."""
     ds = datagen.config(c)
@@ -247,6 +280,7 @@ def main(argv=None) -> int:
     ap.add_argument("--profile-single", nargs=2, type=int, metavar=("K", "N"),
                     help="only N single FP64 influence-zone queries at k=K on workload 2")
     ap.add_argument("--profile-index", type=int, metavar="C", help="only the index build of workload C")
+    ap.add_argument("--explain", type=int, metavar="C", help="only the time split of one batch of workload C")
     ap.add_argument("--order-ab", action="store_true", help="only the work-order comparison")
     ap.add_argument("--vertex-test-ab", action="store_true", help="only the zone vertex-test comparison")
     ap.add_argument("--profile-verify", nargs=2, type=int, metavar=("UPT", "WARPS"),
@@ -261,6 +295,9 @@ def main(argv=None) -> int:
         return 0
     if a.order_ab:
         print(json.dumps(order_ab()), flush=True)
+        return 0
+    if a.explain:
+        explain(a.explain)
         return 0
     if a.profile_single:
         profile_single(*a.profile_single)
