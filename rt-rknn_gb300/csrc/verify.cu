@@ -451,49 +451,66 @@ scan_counts_kernel(const int* res_count, const int* reg_len, const long long* re
 namespace {
 __device__ __forceinline__ unsigned okey(int v) { return (unsigned)v ^ 0x80000000u; }
 
-// stable LSD radix pass of one block over global memory (256 threads)
-__device__ void block_radix_pass(const unsigned* in, unsigned* out, int n, int shift,
-                                 unsigned* hist, unsigned (*wc)[256])
+// LSD radix sort of one slot's ids by its warp: 8-bit digits over the bits
+// in which the keys differ (key - min), stable passes of 32 keys at a time
+// in order, ping-ponging between the slot's pool region (scratch by now)
+// and its output range; bins: the warp's 256 shared counters.  Work linear
+// in n (about three passes for ids below 2^24), where a bitonic network
+// pads to a power of two and takes log^2 steps.
+__device__ void warp_radix_slot(unsigned* src, unsigned* dst, int n, int lane, unsigned* bins)
 {
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    hist[tid] = 0;
-    __syncthreads();
-    for (int i = tid; i < n; i += 256) atomicAdd(&hist[(in[i] >> shift) & 255], 1u);
-    __syncthreads();
-    // exclusive scan of the 256 bins (thread tid owns bin tid)
-    unsigned v = hist[tid], x = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        unsigned y = __shfl_up_sync(FULL, x, o);
-        if (lane >= o) x += y;
+    unsigned mn = 0xffffffffu, mx = 0u;
+    for (int i = lane; i < n; i += 32) {
+        const unsigned k = okey((int)src[i]);
+        src[i] = k;
+        mn = min(mn, k);
+        mx = max(mx, k);
     }
-    __shared__ unsigned wsum[8];
-    if (lane == 31) wsum[w] = x;
-    __syncthreads();
-    unsigned add = 0;
-    for (int j = 0; j < w; ++j) add += wsum[j];
-    __syncthreads();
-    hist[tid] = x - v + add;     // running base of digit tid
-    __syncthreads();
-    for (int t0 = 0; t0 < n; t0 += 256) {
-        int i = t0 + tid;
-        bool ok = i < n;
-        unsigned key = ok ? in[i] : 0u;
-        unsigned dg = ok ? (key >> shift) & 255 : 256u;
-        unsigned mm = __match_any_sync(FULL, dg);
-        int rank = __popc(mm & ((1u << lane) - 1));
-        for (int j = 0; j < 8; ++j) wc[w][lane * 8 + j] = 0;
+    mn = __reduce_min_sync(FULL, mn);
+    mx = __reduce_max_sync(FULL, mx);
+    const unsigned span = mx - mn;
+    const int passes = span ? (32 - __clz((int)span) + 7) / 8 : 0;
+    unsigned* a = src;
+    unsigned* b = dst;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = 8 * p;
+        for (int j = lane; j < 256; j += 32) bins[j] = 0u;
         __syncwarp();
-        if (ok && rank == 0) wc[w][dg] = __popc(mm);
-        __syncthreads();
-        {   // per digit: prefix over warps
-            unsigned acc = hist[tid];
-            for (int j = 0; j < 8; ++j) { unsigned c = wc[j][tid]; wc[j][tid] = acc; acc += c; }
-            hist[tid] = acc;
+        for (int i = lane; i < n; i += 32) atomicAdd(&bins[((a[i] - mn) >> shift) & 255u], 1u);
+        __syncwarp();
+        // exclusive scan of the bins: lane l owns bins 8l .. 8l + 7
+        unsigned v[8], sum = 0u;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) { v[j] = bins[8 * lane + j]; sum += v[j]; }
+        unsigned incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
         }
-        __syncthreads();
-        if (ok) out[wc[w][dg] + rank] = key;
-        __syncthreads();
+        unsigned run = incl - sum;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) { bins[8 * lane + j] = run; run += v[j]; }
+        __syncwarp();
+        for (int i0 = 0; i0 < n; i0 += 32) {
+            const int i = i0 + lane;
+            const bool ok = i < n;
+            const unsigned key = ok ? a[i] : 0u;
+            const unsigned d = ok ? ((key - mn) >> shift) & 255u : 256u + (unsigned)lane;   // idle lanes: own groups
+            const unsigned mm = __match_any_sync(FULL, d);
+            const unsigned base = ok ? bins[d] : 0u;
+            __syncwarp();
+            if (ok) {
+                b[base + __popc(mm & ((1u << lane) - 1))] = key;
+                if ((mm >> lane) == 1u) bins[d] = base + __popc(mm);   // the group's last lane moves the bin on
+            }
+            __syncwarp();
+        }
+        unsigned* t = a;
+        a = b;
+        b = t;
     }
+    for (int i = lane; i < n; i += 32) dst[i] = a[i] ^ 0x80000000u;   // a is src or dst, element for element
 }
 }  // namespace
 
@@ -552,9 +569,7 @@ __device__ __forceinline__ void warp_sort_slot(const unsigned* src, unsigned* ds
 
 // One warp per slot sorts the slot's stored ids into its output range: up to
 // 32 ids by rank counting in registers, up to FIN_WCAP by a bitonic network
-// in registers.  Larger sets are sorted by the whole block afterwards: in
-// shared memory up to FIN_BCAP ids, by four stable radix passes through the
-// pool region above that.
+// in registers, larger sets by a radix sort through the slot's pool region.
 __global__ void __launch_bounds__(32 * FIN_WARPS, 1)
 finalize_kernel(int* res_pool, const long long* cand_off, const int* reg_len, const int* res_count,
                 int* out_off, int* out, int nq, long long out_cap, int* zero, long long zero_n, FinScan S)
@@ -565,14 +580,11 @@ finalize_kernel(int* res_pool, const long long* cand_off, const int* reg_len, co
          i += (long long)gridDim.x * blockDim.x)
         zero[i] = 0;
     pdl_wait();
-    __shared__ unsigned skeys[FIN_BCAP];
-    __shared__ int big[FIN_WARPS];
-    __shared__ int nbig;
+    __shared__ unsigned bins[FIN_WARPS][256];
     __shared__ int s_part[FIN_WARPS];
     __shared__ int s_off[FIN_WARPS];      // this block's slots' output offsets
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int first = blockIdx.x * FIN_WARPS;
-    if (tid == 0) nbig = 0;
     if (S.on) {
         // stored ids of the slots before this block's (four loads in flight
         // per thread)
@@ -621,7 +633,7 @@ finalize_kernel(int* res_pool, const long long* cand_off, const int* reg_len, co
     if (s < nq) {
         const int n = min(res_count[s], reg_len[s]);
         const int os = S.on ? s_off[w] : out_off[s];
-        const unsigned* src = (const unsigned*)(res_pool + cand_off[s]);
+        unsigned* src = (unsigned*)(res_pool + cand_off[s]);
         unsigned* dst = (unsigned*)(out + os);
         if ((long long)os + n > out_cap) {
             // past the output's capacity: left out (the batch fails on the host)
@@ -642,51 +654,9 @@ finalize_kernel(int* res_pool, const long long* cand_off, const int* reg_len, co
             warp_sort_slot<8>(src, dst, n, lane);
         } else if (n <= FIN_WCAP) {
             warp_sort_slot<16>(src, dst, n, lane);
-        } else if (lane == 0) {
-            big[atomicAdd(&nbig, 1)] = s;
-        }
-    }
-    __syncthreads();
-    const int nb = nbig;
-    __shared__ unsigned hist[256];
-    __shared__ unsigned wc[8][256];
-    for (int bi = 0; bi < nb; ++bi) {
-        const int t = big[bi];
-        const int n = min(res_count[t], reg_len[t]);
-        unsigned* src = (unsigned*)(res_pool + cand_off[t]);
-        unsigned* dst = (unsigned*)(out + (S.on ? s_off[t - first] : out_off[t]));
-        if (n <= FIN_BCAP) {
-            int P = 1;
-            while (P < n) P <<= 1;
-            for (int i = tid; i < P; i += blockDim.x) skeys[i] = i < n ? okey((int)src[i]) : 0xffffffffu;
-            __syncthreads();
-            for (int kk = 2; kk <= P; kk <<= 1) {
-                for (int j = kk >> 1; j > 0; j >>= 1) {
-                    for (int i = tid; i < P; i += blockDim.x) {
-                        const int ixj = i ^ j;
-                        if (ixj > i) {
-                            const unsigned x = skeys[i], y = skeys[ixj];
-                            if ((x > y) == ((i & kk) == 0)) { skeys[i] = y; skeys[ixj] = x; }
-                        }
-                    }
-                    __syncthreads();
-                }
-            }
-            for (int i = tid; i < n; i += blockDim.x) dst[i] = skeys[i] ^ 0x80000000u;
         } else {
-            for (int i = tid; i < n; i += blockDim.x) src[i] = okey((int)src[i]);
-            __syncthreads();
-            block_radix_pass(src, dst, n, 0, hist, wc);
-            __syncthreads();
-            block_radix_pass(dst, src, n, 8, hist, wc);
-            __syncthreads();
-            block_radix_pass(src, dst, n, 16, hist, wc);
-            __syncthreads();
-            block_radix_pass(dst, src, n, 24, hist, wc);
-            __syncthreads();
-            for (int i = tid; i < n; i += blockDim.x) dst[i] = src[i] ^ 0x80000000u;
+            warp_radix_slot(src, dst, n, lane, bins[w]);
         }
-        __syncthreads();
     }
 }
 

@@ -10,7 +10,6 @@ constexpr int VERIFY_WARPS = 8;                     // default warps per block
 constexpr int VERIFY_SAMPLES = 4096;                // work-item offsets cached per block
 constexpr int FIN_WARPS = 8;                        // finalize: slots per block (one warp each)
 constexpr int FIN_WCAP = 512;                       // ids one warp sorts in registers
-constexpr int FIN_BCAP = FIN_WARPS * FIN_WCAP;      // ids the block sorts in shared memory
 
 enum { MODE_FP64 = 0, MODE_FP32 = 1 };
 
