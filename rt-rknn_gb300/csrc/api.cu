@@ -368,7 +368,8 @@ ZoneLaunch zone_launch(rknn_index* ix, const ZoneCaps& c, int nq, bool slice = f
             return L;
         }
     }
-    if (!slice && ix->zone_cta && c.pc <= ZCTA_PQ_MAX) {
+    // (the one-block kernel tags vertex indices with bit 15 in a 16-bit list)
+    if (!slice && ix->zone_cta && c.pc <= ZCTA_PQ_MAX && c.vc < 32768) {
         // the influence zone with a block per query when every query of the
         // class gets one at once: the same search, its steps spread over the
         // block (lower latency per query)

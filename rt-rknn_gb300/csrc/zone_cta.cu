@@ -317,6 +317,58 @@ __device__ __forceinline__ void extreme_points(const Slice& S, int nV, uint32_t 
     for (int j = 0; j < 8; ++j) ext[j] = sh.bi[4 + j];
 }
 
+// A float estimate of the bisector make_bisector gives, in its branches,
+// with bounds on its error against the FP64 coefficients: |a - a32| <= da,
+// |b - b32| <= db (vertical: x = b).  The FP64 line divides twice, each
+// with one rounding of 2^-53, on differences and midpoints rounded once; the
+// estimate divides once, -dx/dy, with about three float roundings of 2^-24
+// (relative error below 2^-22.4), and b = my - a mx adds the error of a
+// times |mx| and the roundings of my and of the product: da = 2^-20 |a32| and
+// db = 2^-19 (|my| + |a mx|) hold with room.  valid is the side of q
+// (q >= a qx + b, or qx >= b when vertical), decided only when the estimate
+// leaves no doubt; ok = false when it does not (or the slope overflows),
+// and every float test against the estimate then stands aside.
+struct Line32 {
+    float a, b, da, db;
+    int vert, valid;
+    bool ok;
+};
+__device__ __forceinline__ Line32 approx_bisector(float qx, float qy, float px, float py)
+{
+    Line32 l;
+    l.a = 0.0f; l.b = 0.0f; l.da = 0.0f; l.db = 0.0f; l.vert = 0; l.valid = 0; l.ok = true;
+    if (qx == px) {                       // y = (qy + py) / 2
+        l.b = 0.5f * (qy + py);
+        l.db = 0x1p-22f * fabsf(l.b) + 1e-37f;
+    } else if (qy == py) {                // x = (qx + px) / 2
+        l.vert = 1;
+        l.b = 0.5f * (qx + px);
+        l.db = 0x1p-22f * fabsf(l.b) + 1e-37f;
+    } else {
+        const float dx = px - qx, dy = py - qy;
+        l.a = __fdiv_rn(-dx, dy);
+        const float mx = 0.5f * (qx + px), my = 0.5f * (qy + py);
+        const float am = l.a * mx;
+        l.b = my - am;
+        l.da = 0x1p-20f * fabsf(l.a) + 1e-37f;
+        l.db = 0x1p-19f * (fabsf(my) + fabsf(am)) + 1e-37f;
+        if (!(fabsf(l.a) < 0x1p100f) || !(fabsf(am) < 0x1p100f)) l.ok = false;
+    }
+    float r, e;
+    if (l.vert) {
+        r = qx - l.b;
+        e = l.db + 0x1p-22f * (fabsf(qx) + fabsf(l.b)) + 1e-37f;
+    } else {
+        const float t = fmaf(l.a, qx, l.b);
+        r = qy - t;
+        e = l.da * fabsf(qx) + l.db + 0x1p-22f * (fabsf(qy) + fabsf(l.a * qx) + fabsf(l.b)) + 1e-37f;
+    }
+    if (r > e) l.valid = 1;
+    else if (r < -e) l.valid = 0;
+    else l.ok = false;
+    return l;
+}
+
 // The bisector of q and the facility at (fx, fy), with its float forms, for
 // every thread of the block to read after a barrier.
 __device__ __forceinline__ void make_slot(ZcShared& sh, float fx, float fy, double qx, double qy)
@@ -411,6 +463,13 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
         }
         // the farthest vertex's squared distance (bits), and what rule 1
         // and the ring gate derive from it without its square root
+        if (tid == 0) {
+            // the first addition's list counters and (7)'s maximum (later
+            // ones are cleared by the addition before them)
+            sh.bi[3] = 0;
+            sh.bi[12] = 0;
+            sh.fmax[0] = 0;
+        }
         long long far2 = __double_as_longlong(block_max_d<ZW>(d2c, sh, ph));
         Cut K1 = far_cut(far2);
         float ring_T = ring_limit32(far2, slack_ru);
@@ -484,17 +543,6 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 pf = A.fxy[GX(id, A.nf, 101)];
                 if (A.skip_coincident && pf.x == qf.x && pf.y == qf.y) continue;
                 zs.pts++;
-                // The facility's bisector, by one thread of the last warp
-                // while the other warps run the vertex test (the last warp
-                // takes no part in it); it is read only if the facility is
-                // accepted, after the vertex test's barrier or the accept's
-                // own.
-                if (tid == ZT - 32) make_slot(sh, pf.x, pf.y, qx, qy);
-                if (tid == 0) {
-                    sh.bi[3] = 0;             // the count pass's on-line vertex counter
-                    sh.bi[12] = 0;            // and the FP64 intersection list's
-                    sh.fmax[nL & 1] = 0;      // and (7)'s maximum (read after the accept's last barrier)
-                }
             } else {
                 mbr = A.fmbr[GX(id, NCF, 103)];
                 zs.cells++;
@@ -508,7 +556,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             else r1 = sqrt_rn64(key) > 2.0 * sqrt_rn64(__longlong_as_double(far2));
             if (r1) break;
             // rule 2: keep when nearer than twice the nearest bisector
-            bool r2, tested = false;
+            bool r2;
             if (keybits >= K2.hi) r2 = false;
             else if (keybits <= K2.lo) r2 = true;
             else r2 = sqrt_rn64(key) < 2.0 * nearb;
@@ -581,7 +629,6 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     hit = r != 0;
                 }
                 prune = !__syncthreads_or(hit);
-                tested = true;
                 PHASE(2);
             }
             if (prune) continue;
@@ -606,47 +653,52 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
 
             // ================= accept facility `id`: add its bisector ======
             if (nL >= LC) { flags |= QF_ZONE_L_OVERFLOW; break; }
-            if (!tested) __syncthreads();   // the bisector made at the pop is visible
-            Line64 nb;
-            nb.a = sh.sb.a;
-            nb.b = sh.sb.b;
-            nb.vert = sh.sb.vert;
-            nb.valid = sh.sb.valid;
-            const float na32 = sh.sb.f[0], nb32 = sh.sb.f[1];
+            // The exact FP64 bisector (two dependent divisions, about 1.5 k
+            // cycles) is made by one lane of the last warp, which takes no
+            // part in (1) and (2): those run on a float estimate with error
+            // bounds and leave what it cannot settle to (2b), after the
+            // barrier that makes the exact line visible.
+            if (tid == ZT - 32) make_slot(sh, pf.x, pf.y, qx, qy);
+            const Line32 la = approx_bisector(qf.x, qf.y, pf.x, pf.y);
+            const bool lok = la.ok;
+            const float na32 = la.a, nb32 = la.b;
             const float nab = fabsf(na32);
+            const bool vw = tid < ZT - 32;       // this thread's warp works in (1) and (2)
             zs.nb++;
             // (1) count pass over the existing vertices (inf.cpp:359-364);
             //     it lists the vertices near the new line for (3) and needs
             //     no barrier before (2), which reads no vertex
             const int nV0 = nV;
             float m32 = 0.0f;
-            for (int i = tid; i < nV0; i += ZT) {
+            // (the vertex test's marks used the same thread for each vertex)
+            for (int i = tid; i < nV0 && vw; i += ZT - 32) {
                 const float4 v = IX(S.v4, i);
                 float r32, err;
-                if (nb.vert) {
+                if (la.vert) {
                     r32 = v.x - nb32;
-                    err = 3.0f * kU32 * (fabsf(v.x) + fabsf(nb32)) + 1e-37f;
+                    err = 3.0f * kU32 * (fabsf(v.x) + fabsf(nb32)) + la.db + 1e-37f;
                 } else {
                     const float t = nab * fabsf(v.x);
                     r32 = v.y - fmaf(na32, v.x, nb32);
-                    err = 5.0f * kU32 * (fabsf(v.y) + t + fabsf(nb32)) + 1e-37f;
+                    err = 5.0f * kU32 * (fabsf(v.y) + t + fabsf(nb32)) + la.da * fabsf(v.x) * (1.0f + 0x1p-20f) +
+                          la.db + 1e-37f;
                 }
-                bool valid;
-                if (r32 > err) valid = nb.valid == 1;
-                else if (r32 < -err) valid = nb.valid == 0;
-                else {
-                    const double2 p = IX(S.vd, i);
-                    valid = valid64(nb.a, nb.b, nb.vert, nb.valid, p.x, p.y);
+                // 1: the valid side, 0: the invalid one, -1: left to (2b)
+                int dec = -1;
+                if (lok) {
+                    if (r32 > err) dec = la.valid == 1;
+                    else if (r32 < -err) dec = la.valid == 0;
                 }
                 const float tol = (1.0f + nab) * 1.2e-9f + err;
                 uint32_t fl = vfl_of(v.w) & ~VB_ON;
-                const uint32_t nc = vcnt_of(v.w) + (valid ? 0u : 1u);
-                if (fabsf(r32) <= tol || !(fabsf(r32) < FLT_MAX)) {
+                const uint32_t nc = vcnt_of(v.w) + (dec == 0 ? 1u : 0u);
+                if (dec < 0 || fabsf(r32) <= tol || !(fabsf(r32) < FLT_MAX)) {
                     fl |= VB_ON;
-                    IX(S.cons, atomicAdd(&sh.bi[3], 1)) = (uint16_t)i;   // (3)'s list, in any order
+                    // (3)'s list, in any order; bit 15: the count is (2b)'s
+                    IX(S.cons, atomicAdd(&sh.bi[3], 1)) = (uint16_t)(i | (dec < 0 ? 0x8000 : 0));
                 }
                 IX(S.v4, i).w = vpack(nc, fl);
-                if (nc < ku) m32 = fmaxf(m32, v.z);
+                if (dec >= 0 && nc < ku) m32 = fmaxf(m32, v.z);
             }
             // the float maximum of the squared distances of the vertices that
             // stay, as per-warp partials read after the next barrier
@@ -662,11 +714,13 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             //     drops, in float, those certainly outside the space or
             //     certainly beyond k earlier bisectors, and lists the others
             const int C = 4 + nL;
-            const float a1l = sh.sb.f[2], a1h = sh.sb.f[3];
-            const float b1l = sh.sb.f[4], b1h = sh.sb.f[5];
+            // intervals holding the FP64 coefficients (unbounded without an estimate)
+            const float a1l = lok ? __fsub_rd(la.a, la.da) : -INFINITY, a1h = lok ? __fadd_ru(la.a, la.da) : INFINITY;
+            const float b1l = lok ? __fsub_rd(la.b, la.db) : -INFINITY, b1h = lok ? __fadd_ru(la.b, la.db) : INFINITY;
+            constexpr int ZGW = (ZT - 32) / ZG;  // candidates per pass (groups of the working warps)
             // (every lane of a warp runs each pass, so that the group sums
             // see the whole warp; a group past C computes nothing)
-            for (int c0 = 0; c0 < C; c0 += ZGN) {
+            for (int c0 = 0; c0 < C && vw; c0 += ZGW) {
                 const int c = c0 + gi;
                 const bool active = c < C;
                 bool need64 = true;           // bisector candidates: intersect in FP64
@@ -677,7 +731,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 if (active && c >= 4) {
                     const float4 e4 = IX(S.l4, j);
                     ev = (__float_as_uint(e4.w) & LB_VERT) ? 1 : 0;
-                    if (!nb.vert && !ev) {
+                    if (!la.vert && !ev) {
                         // float interval of the intersection (directed rounding)
                         const float a2l = lo32(e4.x), a2h = hi32(e4.x);
                         const float b2l = lo32(e4.y), b2h = hi32(e4.y);
@@ -738,10 +792,15 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     }
                 }
             }
-            __syncthreads();            // (1) and (2) are complete
+            __syncthreads();            // (1) and (2) are complete, the exact bisector visible
             m32 = sh.rf[bm32][0];
 #pragma unroll
             for (int j = 1; j < ZW; ++j) m32 = fmaxf(m32, sh.rf[bm32][j]);
+            Line64 nb;
+            nb.a = sh.sb.a;
+            nb.b = sh.sb.b;
+            nb.vert = sh.sb.vert;
+            nb.valid = sh.sb.valid;
 
             PHASE(4);
             // (2b) the intersections in FP64, a thread each: the listed
@@ -763,7 +822,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     const float2 c32 = make_float2(d2f_bits<0>(x), d2f_bits<0>(y));
                     if (ok) {
                         for (int u = 0; u < nOn; ++u) {
-                            const int i = IX(S.cons, u);
+                            const int i = IX(S.cons, u) & 0x7fff;
                             const float4 v = IX(S.v4, i);
                             if (fabsf(v.x - c32.x) > tolE || fabsf(v.y - c32.y) > tolE) continue;
                             const double2 p = IX(S.vd, i);
@@ -774,6 +833,22 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     IX(S.c2, c) = c32;
                     IX(S.cfl, c) = ok ? (uint8_t)(cf | 0x80) : (uint8_t)0;
                 };
+                // the vertices (1) left undecided: their side of the new line in
+                // FP64, and, if they stay, their exact squared distance for (7)
+                // (they are outside the float maximum)
+                for (int u = tid; u < nOn; u += ZT) {
+                    const int e = IX(S.cons, u);
+                    if (!(e & 0x8000)) continue;
+                    const int i = e & 0x7fff;
+                    const double2 p = IX(S.vd, i);
+                    const uint32_t vw4 = __float_as_uint(IX(S.v4, i).w);
+                    uint32_t nc = vcnt_of(__uint_as_float(vw4));
+                    if (!valid64(nb.a, nb.b, nb.vert, nb.valid, p.x, p.y)) {
+                        ++nc;
+                        IX(S.v4, i).w = vpack(nc, vfl_of(__uint_as_float(vw4)));
+                    }
+                    if (nc < ku) atomicMax(&sh.fmax[nL & 1], (unsigned long long)__double_as_longlong(d2_64(p.x, p.y, qx, qy)));
+                }
                 const int c4 = tid - (ZT - 64);
                 if (c4 >= 0 && c4 < 4) {
                     const double eb = (c4 == 0) ? sy0 : (c4 == 1) ? sy1 : (c4 == 2) ? sx0 : sx1;
@@ -806,17 +881,19 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 // the last warp (idle here): nothing reads them before (6),
                 // and nothing before it reads line nL
                 if (tid == ZT - 32) {
+                    // the exact coefficients rounded to float
+                    const float ea32 = sh.sb.f[0], eb32 = sh.sb.f[1];
                     double dl = nearb;
                     bool need = true;
                     if (nearb < DBL_MAX) {
                         float est, err;
                         if (nb.vert) {
-                            est = fabsf(qf.x - nb32);
-                            err = 4.0f * kU32 * (fabsf(qf.x) + fabsf(nb32)) + 1e-30f;
+                            est = fabsf(qf.x - eb32);
+                            err = 4.0f * kU32 * (fabsf(qf.x) + fabsf(eb32)) + 1e-30f;
                         } else {
-                            const float den = sqrtf(fmaf(na32, na32, 1.0f));
-                            est = fabsf(fmaf(na32, qf.x, nb32 - qf.y)) / den;
-                            err = 8.0f * kU32 * ((fabsf(na32 * qf.x) + fabsf(qf.y) + fabsf(nb32)) / den + est) + 1e-30f;
+                            const float den = sqrtf(fmaf(ea32, ea32, 1.0f));
+                            est = fabsf(fmaf(ea32, qf.x, eb32 - qf.y)) / den;
+                            err = 8.0f * kU32 * ((fabsf(ea32 * qf.x) + fabsf(qf.y) + fabsf(eb32)) / den + est) + 1e-30f;
                         }
                         // certainly farther than nearb (<= nearf): skip; NaN keeps need
                         if (__fsub_rd(est, err) > nearf) need = false;
@@ -835,7 +912,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     sh.bk[1] = k2.hi;
                     const uint32_t lf = (nb.vert ? LB_VERT : 0) | (nb.valid ? LB_VALID : 0);
                     IX(S.ld, nL) = make_double2(nb.a, nb.b);
-                    IX(S.l4, nL) = make_float4(na32, nb32, 3.01f * kU32 * fabsf(nb32) + 1e-37f, __uint_as_float(lf));
+                    IX(S.l4, nL) = make_float4(ea32, eb32, 3.01f * kU32 * fabsf(eb32) + 1e-37f, __uint_as_float(lf));
                     IX(S.lpos, nL) = id;
                 }
                 __syncthreads();
@@ -1000,6 +1077,13 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             }
             // (7)'s maximum over the block, folded into the barrier below
             if (mx != 0) atomicMax(&sh.fmax[nL & 1], (unsigned long long)mx);
+            if (tid == 0) {
+                // the next addition's list counters and maximum (every read of
+                // them in this one lies before the barrier below)
+                sh.bi[3] = 0;
+                sh.bi[12] = 0;
+                sh.fmax[(nL + 1) & 1] = 0;
+            }
             zs.kept += nnew;
             nV = w + nnew;
             const bool vover = nV > VC;
@@ -1009,7 +1093,7 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             // stays, else the marks written here are the test's
             if (__syncthreads_or(hbl) && !A.vertex_test) nCons = -1;
             else nCons = 1;
-            const long long mxb = (long long)sh.fmax[nL & 1];   // reset at the pop two accepts on
+            const long long mxb = (long long)sh.fmax[nL & 1];   // cleared again by the next addition
 
             // (6) nearest bisector distance and rule 2's bounds (computed by
             //     one thread while the count pass ran; every barrier since
