@@ -315,9 +315,11 @@ using ZoneFn = void (*)(ZoneArgs);
 ZoneFn slice_fn(int kmax, bool two = false)
 {
     if (two)
-        return kmax <= 4 ? slice_kernel2_r4 : kmax <= 8 ? slice_kernel2_r8 : kmax <= 12 ? slice_kernel2_r12
+        return kmax <= 4 ? slice_kernel2_r4 : kmax <= 8 ? slice_kernel2_r8 : kmax <= 10 ? slice_kernel2_r10
+             : kmax <= 12 ? slice_kernel2_r12
              : kmax <= 16 ? slice_kernel2_r16 : kmax <= 24 ? slice_kernel2_r24 : slice_kernel2_r32;
-    return kmax <= 4 ? slice_kernel_r4 : kmax <= 8 ? slice_kernel_r8 : kmax <= 12 ? slice_kernel_r12
+    return kmax <= 4 ? slice_kernel_r4 : kmax <= 8 ? slice_kernel_r8 : kmax <= 10 ? slice_kernel_r10
+         : kmax <= 12 ? slice_kernel_r12
          : kmax <= 16 ? slice_kernel_r16 : kmax <= 24 ? slice_kernel_r24 : kmax <= 32 ? slice_kernel_r32
          : slice_kernel;
 }
@@ -329,9 +331,9 @@ bool is_filter_kernel(const void* f)
     for (const void* g : {(const void*)zone_kernel_smem, (const void*)zone_kernel_cta, (const void*)zone_kernel_cta_half,
                           (const void*)slice_kernel,
                           (const void*)slice_kernel_r4,
-                          (const void*)slice_kernel_r8, (const void*)slice_kernel_r12, (const void*)slice_kernel_r16,
+                          (const void*)slice_kernel_r8, (const void*)slice_kernel_r10, (const void*)slice_kernel_r12, (const void*)slice_kernel_r16,
                           (const void*)slice_kernel_r24, (const void*)slice_kernel_r32, (const void*)slice_kernel2_r4,
-                          (const void*)slice_kernel2_r8, (const void*)slice_kernel2_r12, (const void*)slice_kernel2_r16,
+                          (const void*)slice_kernel2_r8, (const void*)slice_kernel2_r10, (const void*)slice_kernel2_r12, (const void*)slice_kernel2_r16,
                           (const void*)slice_kernel2_r24, (const void*)slice_kernel2_r32})
         if (f == g) return true;
     return false;
@@ -1217,9 +1219,9 @@ rknn_status rknn_index_create(const float* fxy, const int32_t* fid, int64_t nf, 
         ix->recount_grid = std::max(1, per) * ix->num_sms;
     }
     CKB(allow_dynamic_smem((const void*)slice_kernel, optin));
-    for (const void* f : {(const void*)slice_kernel_r4, (const void*)slice_kernel_r8, (const void*)slice_kernel_r12,
+    for (const void* f : {(const void*)slice_kernel_r4, (const void*)slice_kernel_r8, (const void*)slice_kernel_r10, (const void*)slice_kernel_r12,
                           (const void*)slice_kernel_r16, (const void*)slice_kernel_r24, (const void*)slice_kernel_r32,
-                          (const void*)slice_kernel2_r4, (const void*)slice_kernel2_r8, (const void*)slice_kernel2_r12,
+                          (const void*)slice_kernel2_r4, (const void*)slice_kernel2_r8, (const void*)slice_kernel2_r10, (const void*)slice_kernel2_r12,
                           (const void*)slice_kernel2_r16, (const void*)slice_kernel2_r24, (const void*)slice_kernel2_r32})
         CKB(allow_dynamic_smem(f, optin));
     CKB(allow_dynamic_smem((const void*)verify_kernel, optin));

@@ -919,12 +919,14 @@ __device__ __forceinline__ void slice_body(const ZoneArgs& A)
 __global__ void __launch_bounds__(32, 1) slice_kernel(ZoneArgs A) { slice_body<0, 1>(A); }
 __global__ void __launch_bounds__(32, 1) slice_kernel_r4(ZoneArgs A) { slice_body<4, 1>(A); }
 __global__ void __launch_bounds__(32, 1) slice_kernel_r8(ZoneArgs A) { slice_body<8, 1>(A); }
+__global__ void __launch_bounds__(32, 1) slice_kernel_r10(ZoneArgs A) { slice_body<10, 1>(A); }
 __global__ void __launch_bounds__(32, 1) slice_kernel_r12(ZoneArgs A) { slice_body<12, 1>(A); }
 __global__ void __launch_bounds__(32, 1) slice_kernel_r16(ZoneArgs A) { slice_body<16, 1>(A); }
 __global__ void __launch_bounds__(32, 1) slice_kernel_r24(ZoneArgs A) { slice_body<24, 1>(A); }
 __global__ void __launch_bounds__(32, 1) slice_kernel_r32(ZoneArgs A) { slice_body<32, 1>(A); }
 __global__ void __launch_bounds__(64, 7) slice_kernel2_r4(ZoneArgs A) { slice_body<4, 2>(A); }
 __global__ void __launch_bounds__(64, 7) slice_kernel2_r8(ZoneArgs A) { slice_body<8, 2>(A); }
+__global__ void __launch_bounds__(64, 7) slice_kernel2_r10(ZoneArgs A) { slice_body<10, 2>(A); }
 __global__ void __launch_bounds__(64, 7) slice_kernel2_r12(ZoneArgs A) { slice_body<12, 2>(A); }
 __global__ void __launch_bounds__(64, 7) slice_kernel2_r16(ZoneArgs A) { slice_body<16, 2>(A); }
 __global__ void __launch_bounds__(64, 7) slice_kernel2_r24(ZoneArgs A) { slice_body<24, 2>(A); }

@@ -192,6 +192,7 @@ __global__ void zone_kernel_cta_half(ZoneArgs a);
 __global__ void slice_kernel(ZoneArgs a);
 __global__ void slice_kernel_r4(ZoneArgs a);
 __global__ void slice_kernel_r8(ZoneArgs a);
+__global__ void slice_kernel_r10(ZoneArgs a);
 __global__ void slice_kernel_r12(ZoneArgs a);
 __global__ void slice_kernel_r16(ZoneArgs a);
 __global__ void slice_kernel_r24(ZoneArgs a);
@@ -199,6 +200,7 @@ __global__ void slice_kernel_r32(ZoneArgs a);
 // the same with two warps per query (blocks of 64 threads)
 __global__ void slice_kernel2_r4(ZoneArgs a);
 __global__ void slice_kernel2_r8(ZoneArgs a);
+__global__ void slice_kernel2_r10(ZoneArgs a);
 __global__ void slice_kernel2_r12(ZoneArgs a);
 __global__ void slice_kernel2_r16(ZoneArgs a);
 __global__ void slice_kernel2_r24(ZoneArgs a);
