@@ -609,9 +609,9 @@ BatchPlan plan_batch(rknn_index* ix, int nq, int mode, bool use_order, const int
         b.cls.push_back(ZClass{0, nq, std::max(1, kmax), false, {}, {}});
     }
     b.key = {nq, mode, use_order ? 1 : 0};
-    // half-planes the verification can stage per warp (128 KB per block;
-    // 32 bytes each in both modes: FP32 stages them pre-duplicated for the
-    // packed FMA)
+    // half-planes the verification can stage per warp (128 KB per block at
+    // 32 bytes each: FP64, and the fused filter's pre-duplicated FP32 pairs
+    // for the packed FMA; the verification kernel's FP32 staging is compact)
     const int bpp = 32;
     const int stage_max = std::max(1, (128 << 10) / (ix->vwarps * bpp));
     for (auto& c : b.cls) {
@@ -650,7 +650,9 @@ BatchPlan plan_batch(rknn_index* ix, int nq, int mode, bool use_order, const int
     if (!b.fuse)
         for (auto& c : b.cls) c.zl = zone_launch(ix, c.caps, c.n, c.slice, c.kmax);
     b.key.push_back(b.fuse ? 1 : 0);
-    b.vsmem = (size_t)b.vwarps * ((size_t)b.stage_cap * bpp + (size_t)b.seg_stage * sizeof(int2) + 32 * sizeof(float));
+    // (the verification kernel stages FP32 half-planes in 16 bytes)
+    const size_t vbpp = mode == MODE_FP32 ? 16 : (size_t)bpp;
+    b.vsmem = (size_t)b.vwarps * ((size_t)b.stage_cap * vbpp + (size_t)b.seg_stage * sizeof(int2) + 32 * sizeof(float));
     const int vper = occupancy(ix, (const void*)verify_fn(b.vupt), b.vwarps * 32, b.vsmem);
     b.vgrid = vper * ix->num_sms;
     b.key.push_back(b.vupt);

@@ -44,9 +44,10 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
     // a fused batch with no slot left over: nothing to do here
     if (A.deflist && __ldcg(A.ndef) == 0) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    // per warp: stage_cap half-planes (32 bytes each), seg_stage segments,
+    // per warp: stage_cap half-planes (16 bytes each in FP32, compact: the
+    // packed pairs are made in registers; 32 in FP64), seg_stage segments,
     // the slot's 32 slice bounds
-    const size_t plane_bytes = (size_t)A.stage_cap * 32;
+    const size_t plane_bytes = (size_t)A.stage_cap * (A.mode == MODE_FP32 ? 16 : 32);
     char* sp = smem + w * (plane_bytes + (size_t)A.seg_stage * sizeof(int2) + 32 * sizeof(float));
     int2* ssg = (int2*)(sp + plane_bytes);
     float* sr = (float*)(ssg + A.seg_stage);
@@ -124,10 +125,7 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const int m = m0 + 32 * j;
-                    if (m < nst) {
-                        ((float4*)sp)[2 * m] = make_float4(p[j].x, p[j].x, p[j].y, p[j].y);
-                        ((float4*)sp)[2 * m + 1] = make_float4(p[j].z, p[j].z, p[j].w, p[j].w);
-                    }
+                    if (m < nst) ((float4*)sp)[m] = p[j];
                 }
             }
             // the slot's segments (nseg ranges and the terminal entry), when
@@ -175,7 +173,7 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
         }
         const int v0 = (g - c_off) * (32 * UPT);
         const int2* sg = seg_staged ? ssg : A.segs + (size_t)s * A.seg_cap;
-        verify_item<UPT>(A, d, s, v0, sp, sg, sr, min(d.nb, A.stage_cap), -1, -1, vc);
+        verify_item<UPT, true>(A, d, s, v0, sp, sg, sr, min(d.nb, A.stage_cap), -1, -1, vc);
     }
     vc.flush(A.vstats);
 }

@@ -74,7 +74,7 @@ __device__ __forceinline__ int exact_count(float ux, float uy, const QDesc& d, c
 // Stage 1 over the first nb staged half-planes: cnt = certified
 // violations (the loop leaves once every lane's users reached k), und =
 // half-planes the bound could not decide.
-template <typename T, int UPT>
+template <typename T, int UPT, bool COMPACT>
 __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char* sp, const int* pos,
                                              const float2* u, const bool* valid, int* cnt, int* und,
                                              unsigned& evals, float rho2)
@@ -111,7 +111,9 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
     int m = 0;
     if constexpr (sizeof(T) == 4) {
         // FP32: users in pairs through the packed FMA (each half rounds as
-        // fmaf); half-plane m is staged as (a, a, b, b), (c, c, w, w).  With
+        // fmaf); half-plane m is staged as (a, a, b, b), (c, c, w, w), or,
+        // COMPACT, as (a, b, c, w), the pairs made in registers (half the
+        // shared memory: twice the warps per SM where the staging bounds it).  With
         // r = fl(mv + bu): mv < -bu exactly when r is negative (a nonzero
         // exact sum of two floats never rounds to zero, and bu > 0 rules out
         // -0), and |mv| <= bu implies 0 <= r <= 2bu (rounding is monotone):
@@ -147,9 +149,20 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
         // two half-planes a trip (the second one's loads overlap the first
         // one's arithmetic); the early exit is tested after every eighth
         bool stopped = false;
+        auto load = [&](int i, float4& ab, float4& cw) {
+            if constexpr (COMPACT) {
+                const float4 p = sp4[i];
+                ab = make_float4(p.x, p.x, p.y, p.y);
+                cw = make_float4(p.z, p.z, p.w, p.w);
+            } else {
+                ab = sp4[2 * i];
+                cw = sp4[2 * i + 1];
+            }
+        };
         for (; m + 2 <= nb; m += 2) {
-            const float4 ab0 = sp4[2 * m], cw0 = sp4[2 * m + 1];
-            const float4 ab1 = sp4[2 * m + 2], cw1 = sp4[2 * m + 3];
+            float4 ab0, cw0, ab1, cw1;
+            load(m, ab0, cw0);
+            load(m + 1, ab1, cw1);
             plane(ab0, cw0);
             plane(ab1, cw1);
             if ((m & 7) == 6) {
@@ -160,7 +173,9 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
             }
         }
         if (!stopped && m < nb) {
-            plane(sp4[2 * m], sp4[2 * m + 1]);
+            float4 ab, cw;
+            load(m, ab, cw);
+            plane(ab, cw);
             ++m;
         }
 #pragma unroll
@@ -287,7 +302,7 @@ struct VCount {
 // FP64: four doubles), sg: its segments (shared or global memory), sr: its
 // 32 slice bounds.  r0_in/region_in: the slot's result region, or -1 to read
 // it from cand_off/reg_len.
-template <int UPT>
+template <int UPT, bool COMPACT = false>
 __device__ __forceinline__ void verify_item(const VerifyArgs& A, const QDesc& d, int s, int v0, const char* sp,
                                             const int2* sg, const float* sr, int nbs, long long r0_in,
                                             long long region_in, VCount& vc)
@@ -352,8 +367,8 @@ __device__ __forceinline__ void verify_item(const VerifyArgs& A, const QDesc& d,
     // certified count is the exact count.  (All half-planes must be
     // staged for this.)
     const float rho2 = (nbs == d.nb) ? d.rho * d.rho * (1.0f - 1e-5f) : 0.0f;
-    if (A.mode == MODE_FP32) filter_users<float, UPT>(d, nbs, sp, pos, u, valid, cnt, und, vc.evals, rho2);
-    else filter_users<double, UPT>(d, nbs, sp, pos, u, valid, cnt, und, vc.evals, rho2);
+    if (A.mode == MODE_FP32) filter_users<float, UPT, COMPACT>(d, nbs, sp, pos, u, valid, cnt, und, vc.evals, rho2);
+    else filter_users<double, UPT, false>(d, nbs, sp, pos, u, valid, cnt, und, vc.evals, rho2);
     bool direct[UPT];
 #pragma unroll
     for (int t = 0; t < UPT; ++t) direct[t] = valid[t] && cnt[t] < d.k && und[t] == 0;
