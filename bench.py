@@ -82,7 +82,7 @@ FUSED_INSTR_PER_QUERY = 21.4463e6 / 1000
 # queries of this workload, from one ncu capture (smsp__inst_executed.sum of
 # the launch over its queries or its half-plane evaluations)
 SAT_NQ = 16384
-INSTR = {"slice_kernel_per_query": 160.077e6 / 16384, "verify_kernel_per_eval": 101.042e6 / 176245793}
+INSTR = {"slice_kernel_per_query": 160.077e6 / 16384, "verify_kernel_per_eval": 95.899e6 / 176245793}
 
 
 def peaks():
