@@ -557,7 +557,10 @@ ZoneCaps slice_caps(int kmax, int lc_cap = 512)
 {
     ZoneCaps c;
     c.vc = std::max(1, kmax);
-    c.lc = (int)std::max<long long>(1, std::min<long long>(10LL * c.vc + 60, lc_cap));
+    // half-planes: the first 24 k + 60 facilities streamed (more half-planes
+    // reach farther: fewer users left to the exact recount; at k=10 on the
+    // uniform workload 0.03 a query instead of 0.53 with 10 k + 60)
+    c.lc = (int)std::max<long long>(1, std::min<long long>(24LL * c.vc + 60, lc_cap));
     c.pc = 0;
     c.rm = 64;
     return c;
