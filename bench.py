@@ -75,14 +75,14 @@ WORKLOAD = "uniform 100k facilities / 1M users, k=10, 1000 queries per step"
 # DRAM bytes (read + write) per launch of the slice filter with the fused
 # verification on this workload's 1000-query batch, from one ncu capture of
 # that launch (the capture's commit is recorded with its summary)
-TRAFFIC = {"fused_slice_kernel": 4881920}
+TRAFFIC = {"fused_slice_kernel": 4883968}
 # warp instructions per query of that kernel (two warps a query), same capture
-FUSED_INSTR_PER_QUERY = 21.4463e6 / 1000
+FUSED_INSTR_PER_QUERY = 21.4742e6 / 1000
 # warp instructions per unit of work of the two kernels in a batch of SAT_NQ
 # queries of this workload, from one ncu capture (smsp__inst_executed.sum of
 # the launch over its queries or its half-plane evaluations)
 SAT_NQ = 16384
-INSTR = {"slice_kernel_per_query": 160.077e6 / 16384, "verify_kernel_per_eval": 95.899e6 / 176245793}
+INSTR = {"slice_kernel_per_query": 160.539e6 / 16384, "verify_kernel_per_eval": 95.848e6 / 176643960}
 
 
 def peaks():
