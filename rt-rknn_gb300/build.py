@@ -53,7 +53,7 @@ def sources():
     out = []
     for d in (CSRC, HOST, os.path.join(REPO, "include")):
         for f in os.listdir(d):
-            if f.endswith((".cu", ".cuh", ".h", ".cpp", ".hpp")):
+            if f.endswith((".cu", ".cuh", ".h", ".c", ".cpp", ".hpp")):
                 out.append(os.path.join(d, f))
     return out
 
@@ -96,9 +96,29 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"CLI build failed:\n{r.stderr}")
     os.replace(CLI + ".tmp", CLI)
+    _build_pycall()
     with open(stamp, "w") as fh:
         fh.write(dig)
     return LIB
+
+
+def _build_pycall():
+    """The CPython fast path for rknn_query_batch (host/pycall.c), where the
+    interpreter's headers are installed; rknn.py falls back to ctypes."""
+    import sysconfig
+    inc = sysconfig.get_paths().get("include") or ""
+    suffix = sysconfig.get_config_var("EXT_SUFFIX") or ".so"
+    dst = os.path.join(HERE, "_rknn_call" + suffix)
+    if not os.path.exists(os.path.join(inc, "Python.h")):
+        if os.path.exists(dst):
+            os.remove(dst)
+        return
+    r = subprocess.run(["gcc", "-O2", "-shared", "-fPIC", f"-I{inc}", f"-I{os.path.join(REPO, 'include')}",
+                        os.path.join(HOST, "pycall.c"), "-o", dst + ".tmp", f"-L{HERE}", "-lrknn_gb300",
+                        "-Wl,-rpath,$ORIGIN"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"pycall build failed:\n{r.stderr}")
+    os.replace(dst + ".tmp", dst)
 
 
 if __name__ == "__main__":

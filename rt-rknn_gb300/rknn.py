@@ -191,6 +191,28 @@ def load(path: str = LIB_PATH):
     return L
 
 
+_fast = None
+
+
+def _fast_call():
+    """The CPython entry point for rknn_query_batch (host/pycall.c, built
+    beside the library where the interpreter's headers are installed), or
+    False: ctypes then makes the same call."""
+    global _fast
+    if _fast is None:
+        load()                  # the module links against the loaded library
+        import importlib.util
+        import sysconfig
+        path = os.path.join(os.path.dirname(LIB_PATH), "_rknn_call" + (sysconfig.get_config_var("EXT_SUFFIX") or ".so"))
+        _fast = False
+        if os.path.exists(path):
+            spec = importlib.util.spec_from_file_location("_rknn_call", path)
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            _fast = mod
+    return _fast
+
+
 def _check(rc: int):
     if rc != 0:
         raise RkNNError(rc, load().rknn_last_error().decode())
@@ -356,9 +378,13 @@ class Index:
         sorted ids at ids[offsets[i]:offsets[i+1]] (no per-query copies; the
         output buffers are reused between calls)."""
         L = load()
-        qs = np.ascontiguousarray(qs, dtype=np.int32)
+        fast = _fast_call()
+        if type(qs) is not np.ndarray or qs.dtype != np.int32 or not qs.flags.c_contiguous:
+            qs = np.ascontiguousarray(qs, dtype=np.int32)
         nq = qs.shape[0]
-        if np.ndim(ks) == 0:
+        if type(ks) is np.ndarray and ks.dtype == np.int32 and ks.shape == qs.shape and ks.flags.c_contiguous:
+            pass
+        elif np.ndim(ks) == 0:
             # a scalar k: one cached array of it per batch size
             kc = getattr(self, "_flat_k", None)
             if kc is None or kc[0] != (nq, int(ks)):
@@ -379,8 +405,11 @@ class Index:
             fb = self._flat_out = (b, b.ctypes.data, b.shape[0])
         while True:
             out, out_p, cap = fb
-            rc = L.rknn_query_batch(self.h, qs.ctypes.data, ks.ctypes.data, nq, _MODES[mode], out_p, cap, off_p,
-                                    None)
+            if fast:
+                rc = fast.query_batch(self.h.value, qs, ks, _MODES[mode], out_p, cap, off_p)
+            else:
+                rc = L.rknn_query_batch(self.h, qs.ctypes.data, ks.ctypes.data, nq, _MODES[mode], out_p, cap,
+                                        off_p, None)
             if rc == 5 and off[nq] > cap:
                 b = pinned_ids(int(off[nq] * 5 // 4))
                 fb = self._flat_out = (b, b.ctypes.data, b.shape[0])

@@ -51,6 +51,20 @@ def test_library_exports_every_declared_symbol(engine):
     assert b"sm_103a" in lib.rknn_version()
 
 
+def test_fast_batch_entry_checks_its_buffers(engine):
+    """The CPython entry point for rknn_query_batch (built where the
+    interpreter's headers are installed) takes contiguous int32 buffers of
+    equal length and hands anything else back as an argument error."""
+    fast = engine._fast_call()
+    if not fast:
+        pytest.skip("no CPython headers here: the ctypes route is used")
+    q = np.zeros(4, np.int32)
+    assert fast.query_batch(0, q, np.ones(4, np.int32), 0, 0, 0, 0) == 1      # null index
+    assert fast.query_batch(0, q, np.ones(3, np.int32), 0, 0, 0, 0) == 1      # lengths differ
+    with pytest.raises((BufferError, ValueError)):       # not contiguous
+        fast.query_batch(0, np.zeros(8, np.int32)[::2], np.ones(4, np.int32), 0, 0, 0, 0)
+
+
 def test_cli_rejects_bad_arguments(engine, tmp_path):
     cli = os.path.join(REPO, "rt-rknn_gb300", "rknn-gb300")
     r = subprocess.run([cli, "-h"], capture_output=True, text=True)
