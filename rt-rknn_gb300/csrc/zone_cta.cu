@@ -670,8 +670,13 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             //     no barrier before (2), which reads no vertex
             const int nV0 = nV;
             float m32 = 0.0f;
-            // (the vertex test's marks used the same thread for each vertex)
-            for (int i = tid; i < nV0 && vw; i += ZT - 32) {
+            // The other warps take vertices [0, n0) in turn; the last warp,
+            // once the bisector is made (about two passes' time), takes the
+            // last n7 of a large set.
+            const int npass = (nV0 + ZT - 1) / ZT;
+            const int n7 = min(nV0, 32 * max(0, npass - 2));
+            const int n0 = nV0 - n7;
+            for (int i = vw ? tid : n0 + lane; i < (vw ? n0 : nV0); i += vw ? ZT - 32 : 32) {
                 const float4 v = IX(S.v4, i);
                 float r32, err;
                 if (la.vert) {
