@@ -17,7 +17,15 @@
 //     (ordered compactions keep the reference's vertex order);
 //   * a candidate intersection's certified pre-discard and its count over the
 //     earlier bisectors are split over a group of ZG threads, each taking
-//     every ZG-th bisector, and summed within the group.
+//     every ZG-th bisector, and summed within the group;
+//   * an FP64 instruction holds its warp about 64 cycles on GB300 however
+//     few lanes run it (a division about 670), so FP64 values the whole
+//     block needs are made once, by one lane: the new bisector by the last
+//     warp while the others run the vertex count and candidate passes on a
+//     float estimate of it with proven error bounds, the nearest distance
+//     and rule 2's bounds by one lane during the FP64 intersections; rule 1
+//     and the ring gate use bounds from the farthest squared distance's bits;
+//     conversions and comparisons of doubles run on their bits.
 // It serves batches in which every query can have a block of its own (the
 // plain single-query form first of all); larger batches run the one-warp
 // kernel, which keeps more queries in flight per SM.
@@ -57,7 +65,8 @@ struct ZcShared {
 
 // Ordered ranks of two predicates over the block (thread order is item
 // order): the number of threads before this one with each predicate set,
-// and the totals.  Two barriers; the shared counts are free again on return.
+// and the totals.  One barrier (the per-warp counts alternate between two
+// copies, see ZcShared).
 template <int ZW>
 __device__ __forceinline__ void block_rank2(bool p, bool q, ZcShared& sh, unsigned& ph, int& rp, int& rq, int& tp,
                                             int& tq)
