@@ -262,12 +262,12 @@ def test_flat_batches_into_page_locked_ids(engine):
     idx.close()
 
 
-@pytest.mark.parametrize("cta", ["1", "0"])
+@pytest.mark.parametrize("cta", ["256", "128", "0"])
 def test_zone_bisectors_match_port(engine, monkeypatch, cta):
     """Same grid, same rules: the zone kernel builds rknn-inf's bisector set
     in the same order as the CPU restatement does -- the one-block kernel
-    (small batches and single queries, cta=1) and the one-warp kernel
-    (cta=0) alike."""
+    (small batches and single queries) at 256 and at 128 threads, and the
+    one-warp kernel (cta=0) alike."""
     monkeypatch.setenv("RKNN_ZONE_CTA", cta)
     for nf, nu, k in ((1000, 10000, 5), (20000, 200000, 10), (20000, 200000, 3), (20000, 200000, 25)):
         ds = datagen.uniform(nf, nu, seed=31 + k, nq=40, k=k)
