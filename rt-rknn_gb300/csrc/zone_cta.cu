@@ -933,57 +933,78 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
             }
 
             PHASE(5);
-            // (4) counts of the surviving candidates over earlier bisectors,
-            //     a group per candidate: certain violations in float, the
-            //     undecided ones in FP64
+            // (4) counts of the live candidates over earlier bisectors, a
+            //     group per candidate: certain violations in float, the
+            //     undecided ones in FP64.  Most slots died in (2) or (2b), so
+            //     the live ones are listed first (in slot order, ZT slots at
+            //     a time) and the groups take the list.
             bool anyclose = false;
-            for (int c0 = 0; c0 < C; c0 += ZGN) {
-                const int c = c0 + gi;
-                const bool live = c < C && (IX(S.cfl, c) & 0x80) != 0;
-                int cnt = 0, undec = 0;
-                double2 p = make_double2(0, 0);
-                float2 c32 = make_float2(0, 0);
-                float KX = 0, KY = 0;
-                const int gen = c - 4;
-                if (live) {
-                    p = IX(S.cd, c);
-                    c32 = IX(S.c2, c);
-                    KX = kU32 * fabsf(c32.x) * (1.0f + kU32) + 3.01f * kU32 * fabsf(c32.x);
-                    KY = kU32 * fabsf(c32.y) + 3.01f * kU32 * fabsf(c32.y) + 1e-37f;
-                    // the generating bisector passes through the candidate: its
-                    // exact side, from (2b)
-                    if (gen >= 0 && gl == 0) cnt += (IX(S.cfl, c) & 0x40) ? 1 : 0;
-                    for (int m = gl; m < nL; m += ZG) {
-                        const int sm = (m == gen) ? -1 : side32(IX(S.l4, m), c32.x, c32.y, KX, KY);
-                        cnt += sm > 0;
-                        undec += sm == 0;
+            for (int s0 = 0; s0 < C; s0 += ZT) {
+                const int cs = s0 + tid;
+                const bool lv = cs < C && (IX(S.cfl, cs) & 0x80) != 0;
+                int nlv;
+                const int r = block_rank<ZW>(lv, sh, ph, nlv);   // every read of the last list precedes it
+                if (lv) sh.tc[r] = (uint32_t)cs;
+                __syncthreads();
+                for (int u0 = 0; u0 < nlv; u0 += ZGN) {
+                    const int u = u0 + gi;
+                    const bool live = u < nlv;
+                    const int c = live ? (int)sh.tc[u] : 0;
+                    int cnt = 0, undec = 0;
+                    double2 p = make_double2(0, 0);
+                    float2 c32 = make_float2(0, 0);
+                    float KX = 0, KY = 0;
+                    const int gen = c - 4;
+                    if (live) {
+                        p = IX(S.cd, c);
+                        c32 = IX(S.c2, c);
+                        KX = kU32 * fabsf(c32.x) * (1.0f + kU32) + 3.01f * kU32 * fabsf(c32.x);
+                        KY = kU32 * fabsf(c32.y) + 3.01f * kU32 * fabsf(c32.y) + 1e-37f;
+                        // the generating bisector passes through the candidate: its
+                        // exact side, from (2b)
+                        if (gen >= 0 && gl == 0) cnt += (IX(S.cfl, c) & 0x40) ? 1 : 0;
+#pragma unroll 4
+                        for (int m = gl; m < nL; m += ZG) {
+                            const int sm = (m == gen) ? -1 : side32(IX(S.l4, m), c32.x, c32.y, KX, KY);
+                            cnt += sm > 0;
+                            undec += sm == 0;
+                        }
                     }
-                }
-                cnt = group_sum<ZG>(cnt);
-                undec = group_sum<ZG>(undec);
-                // the bisectors the float test left undecided, in FP64
-                int extra = 0;
-                if (live && cnt < k && undec > 0) {
-                    for (int m = gl; m < nL; m += ZG) {
-                        if (m == gen) continue;
-                        const float4 q = IX(S.l4, m);
-                        if (side32(q, c32.x, c32.y, KX, KY) != 0) continue;
-                        const double2 g = IX(S.ld, m);
-                        const uint32_t lf = __float_as_uint(q.w);
-                        extra += !valid64(g.x, g.y, lf & LB_VERT, (lf & LB_VALID) ? 1 : 0, p.x, p.y);
+                    cnt = group_sum<ZG>(cnt);
+                    undec = group_sum<ZG>(undec);
+                    // the bisectors the float test left undecided, in FP64
+                    // (rare: skipped by warps without any)
+                    const bool need = live && cnt < k && undec > 0;
+                    if (__any_sync(FULL, need)) {
+                        int extra = 0;
+                        if (need) {
+                            for (int m = gl; m < nL; m += ZG) {
+                                if (m == gen) continue;
+                                const float4 q = IX(S.l4, m);
+                                if (side32(q, c32.x, c32.y, KX, KY) != 0) continue;
+                                const double2 g = IX(S.ld, m);
+                                const uint32_t lf = __float_as_uint(q.w);
+                                extra += !valid64(g.x, g.y, lf & LB_VERT, (lf & LB_VALID) ? 1 : 0, p.x, p.y);
+                            }
+                        }
+                        cnt += group_sum<ZG>(extra);
                     }
-                }
-                cnt += group_sum<ZG>(extra);
-                if (c < C && gl == 0) IX(S.ccnt, c) = live ? cnt : k;
-                // (4b), float prefilter: is a kept candidate within 1e-9 of
-                // an earlier one (the reference keeps the first)?  Doubles
-                // within 1e-9 give floats within 1e-9 + u(|x1|+|x2|).
-                if (live && cnt < k) {
-                    const float tx = 3.0f * kU32 * fabsf(c32.x) + 2e-9f, ty = 3.0f * kU32 * fabsf(c32.y) + 2e-9f;
-                    for (int c2 = gl; c2 < c && !anyclose; c2 += ZG) {
-                        if (!(IX(S.cfl, c2) & 0x80)) continue;
-                        const float2 o = IX(S.c2, c2);
-                        if (fabsf(o.x - c32.x) <= tx && fabsf(o.y - c32.y) <= ty) anyclose = true;
+                    // (only live slots' counts are read)
+                    if (live && gl == 0) IX(S.ccnt, c) = cnt;
+                    // (4b), float prefilter: is a kept candidate within 1e-9 of
+                    // an earlier live one (the reference keeps the first)?
+                    // Doubles within 1e-9 give floats within 1e-9 + u(|x1|+|x2|).
+                    if (live && cnt < k) {
+                        const float tx = 3.0f * kU32 * fabsf(c32.x) + 2e-9f, ty = 3.0f * kU32 * fabsf(c32.y) + 2e-9f;
+                        for (int u2 = gl; u2 < u && !anyclose; u2 += ZG) {
+                            const float2 o = IX(S.c2, (int)sh.tc[u2]);
+                            if (fabsf(o.x - c32.x) <= tx && fabsf(o.y - c32.y) <= ty) anyclose = true;
+                        }
+                        for (int c2 = gl; c2 < s0 && !anyclose; c2 += ZG) {   // earlier chunks' slots
+                            if (!(IX(S.cfl, c2) & 0x80)) continue;
+                            const float2 o = IX(S.c2, c2);
+                            if (fabsf(o.x - c32.x) <= tx && fabsf(o.y - c32.y) <= ty) anyclose = true;
+                        }
                     }
                 }
             }
