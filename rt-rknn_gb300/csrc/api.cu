@@ -1904,11 +1904,19 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     za.slice_r = nullptr;
     za.qd = L.qd; za.planes = L.planes; za.bis_pos = L.bispos; za.segs = L.segs; za.zst = L.zst;
     za.fault = L.counters + 4;
-    const size_t zsmem = zone_layout(caps).bytes * ZONE_WARPS;
-    zone_kernel_smem<<<1, 32 * ZONE_WARPS, zsmem, st>>>(za);
+    // the kernels rknn_query picks for one query: the zone over a block
+    // (when its capacities allow it, as in zone_launch) and the verification
+    // in items of 64 users, which spread a lone query's FP64 evaluations
+    // over more warps
+    const size_t zl = zone_layout(caps).bytes;
+    const bool cta = ix->zone_cta && caps.pc <= ZCTA_PQ_MAX && caps.vc < 32768;
+    if (cta && ix->zone_cta == ZCTA_THREADS) zone_kernel_cta<<<1, ZCTA_THREADS, zl, st>>>(za);
+    else if (cta) zone_kernel_cta_half<<<1, ZCTA_THREADS / 2, zl, st>>>(za);
+    else zone_kernel_smem<<<1, 32 * ZONE_WARPS, zl * ZONE_WARPS, st>>>(za);
     CK(cudaGetLastError());
+    constexpr int NA_UPT = 2;
     plan_kernel<<<1, 1024, 0, st>>>(L.qd, 1, L.cand_off, L.reg_len, L.region_top, L.chunk_off, L.pool_cap,
-                                    (int)std::min<long long>(L.pool_cap, INT32_MAX), VERIFY_CHUNK);
+                                    (int)std::min<long long>(L.pool_cap, INT32_MAX), 32 * NA_UPT);
     CK(cudaGetLastError());
 
     VerifyArgs va;
@@ -1927,7 +1935,7 @@ extern "C" rknn_status rknn_query_noalloc(rknn_index* ix, int32_t q, int32_t k, 
     // exact count
     va.stage_cap = std::max(1, std::min(caps.lc, (128 << 10) / (VERIFY_WARPS * 32)));
     const size_t vsmem = (size_t)VERIFY_WARPS * ((size_t)va.stage_cap * 32 + 32 * sizeof(float));
-    verify_kernel<<<2 * ix->num_sms, VERIFY_WARPS * 32, vsmem, st>>>(va);
+    verify_fn(NA_UPT)<<<2 * ix->num_sms, VERIFY_WARPS * 32, vsmem, st>>>(va);
     CK(cudaGetLastError());
     scan_counts_kernel<<<1, 1024, 0, st>>>(L.res_count, L.reg_len, L.region_top, 1, L.out_off, L.counters, nullptr);
     CK(cudaGetLastError());

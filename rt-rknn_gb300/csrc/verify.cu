@@ -33,7 +33,7 @@ namespace rknn {
 
 using namespace vitem;
 
-template <int UPT>
+template <int UPT, bool BITS = false>
 __device__ __forceinline__ void verify_body(const VerifyArgs& A)
 {
     extern __shared__ __align__(16) char smem[];
@@ -173,7 +173,7 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
         }
         const int v0 = (g - c_off) * (32 * UPT);
         const int2* sg = seg_staged ? ssg : A.segs + (size_t)s * A.seg_cap;
-        verify_item<UPT, true>(A, d, s, v0, sp, sg, sr, min(d.nb, A.stage_cap), -1, -1, vc);
+        verify_item<UPT, true, BITS>(A, d, s, v0, sp, sg, sr, min(d.nb, A.stage_cap), -1, -1, vc);
     }
     vc.flush(A.vstats);
 }
@@ -181,7 +181,7 @@ __device__ __forceinline__ void verify_body(const VerifyArgs& A)
 // The verification kernel with 2, 4 or 8 users per lane per work item
 // (32 * UPT users per item); blocks of up to 16 warps.
 __global__ void __maxnreg__(80) verify_kernel(VerifyArgs a) { verify_body<4>(a); }
-__global__ void __maxnreg__(80) verify_kernel_u2(VerifyArgs a) { verify_body<2>(a); }
+__global__ void __maxnreg__(80) verify_kernel_u2(VerifyArgs a) { verify_body<2, true>(a); }
 __global__ void __launch_bounds__(512) verify_kernel_u8(VerifyArgs a) { verify_body<8>(a); }
 
 // One warp per listed survivor.  Lane r computes the facility range of

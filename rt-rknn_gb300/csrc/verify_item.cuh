@@ -74,7 +74,7 @@ __device__ __forceinline__ int exact_count(float ux, float uy, const QDesc& d, c
 // Stage 1 over the first nb staged half-planes: cnt = certified
 // violations (the loop leaves once every lane's users reached k), und =
 // half-planes the bound could not decide.
-template <typename T, int UPT, bool COMPACT>
+template <typename T, int UPT, bool COMPACT, bool BITS = false>
 __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char* sp, const int* pos,
                                              const float2* u, const bool* valid, int* cnt, int* und,
                                              unsigned& evals, float rho2)
@@ -184,6 +184,14 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
         evals += (unsigned)(m * nvalid);
         return;
     }
+    // FP64 with BITS: the compares of each evaluation on the bits (integer
+    // pipes).  A warp's FP64 instruction holds its sub-partition's FP64 pipe
+    // for about 64 cycles on GB300, so a lone query's evaluations, two FMAs
+    // and three compares each, are bound by that pipe; in large batches the
+    // extra registers cost more than the compares (the kernels with four
+    // and eight users a lane spill).  mv is finite (finite half-planes and
+    // users) and bu >= kf264 > 0, so mv < -bu is order_key(mv) < ~bits(bu),
+    // and -bu <= mv <= bu is |mv| <= bu on the magnitude bits.
     for (; m < nb; ++m) {
         T a, b, c;
         float wm;
@@ -199,8 +207,14 @@ __device__ __forceinline__ void filter_users(const QDesc& d, int nb, const char*
 #pragma unroll
         for (int t = 0; t < UPT; ++t) {
             T mv = fma(a, x[t], fma(b, y[t], c));
-            cnt[t] += (mv < -bu[t]);
-            und[t] += (mv <= bu[t]) & (mv >= -bu[t]);
+            if constexpr (BITS && sizeof(T) == 8) {
+                const long long bb = __double_as_longlong((double)bu[t]);
+                cnt[t] += order_key((double)mv) < ~bb;
+                und[t] += (__double_as_longlong((double)mv) & 0x7fffffffffffffffll) <= bb;
+            } else {
+                cnt[t] += (mv < -bu[t]);
+                und[t] += (mv <= bu[t]) & (mv >= -bu[t]);
+            }
         }
         if ((m & 7) == 7) {
             bool done = true;
@@ -302,7 +316,7 @@ struct VCount {
 // FP64: four doubles), sg: its segments (shared or global memory), sr: its
 // 32 slice bounds.  r0_in/region_in: the slot's result region, or -1 to read
 // it from cand_off/reg_len.
-template <int UPT, bool COMPACT = false>
+template <int UPT, bool COMPACT = false, bool BITS = false>
 __device__ __forceinline__ void verify_item(const VerifyArgs& A, const QDesc& d, int s, int v0, const char* sp,
                                             const int2* sg, const float* sr, int nbs, long long r0_in,
                                             long long region_in, VCount& vc)
@@ -368,7 +382,7 @@ __device__ __forceinline__ void verify_item(const VerifyArgs& A, const QDesc& d,
     // staged for this.)
     const float rho2 = (nbs == d.nb) ? d.rho * d.rho * (1.0f - 1e-5f) : 0.0f;
     if (A.mode == MODE_FP32) filter_users<float, UPT, COMPACT>(d, nbs, sp, pos, u, valid, cnt, und, vc.evals, rho2);
-    else filter_users<double, UPT, false>(d, nbs, sp, pos, u, valid, cnt, und, vc.evals, rho2);
+    else filter_users<double, UPT, false, BITS>(d, nbs, sp, pos, u, valid, cnt, und, vc.evals, rho2);
     bool direct[UPT];
 #pragma unroll
     for (int t = 0; t < UPT; ++t) direct[t] = valid[t] && cnt[t] < d.k && und[t] == 0;
