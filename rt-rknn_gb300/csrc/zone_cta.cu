@@ -57,7 +57,7 @@ struct ZcShared {
     struct {              // the bisector of the facility taken
         double a, b;
         int vert, valid;
-        float f[6];       // a, b rounded to nearest; a down, up; b down, up
+        float f[2];       // a, b rounded to nearest
     } sb;
     int bi[16];
     unsigned long long fmax[2];   // (7)'s maximum, by accept parity
@@ -389,10 +389,6 @@ __device__ __forceinline__ void make_slot(ZcShared& sh, float fx, float fy, doub
     sh.sb.valid = l.valid;
     sh.sb.f[0] = d2f_bits<0>(l.a);
     sh.sb.f[1] = d2f_bits<0>(l.b);
-    sh.sb.f[2] = d2f_bits<-1>(l.a);
-    sh.sb.f[3] = d2f_bits<1>(l.a);
-    sh.sb.f[4] = d2f_bits<-1>(l.b);
-    sh.sb.f[5] = d2f_bits<1>(l.b);
 }
 
 template <int ZT>
