@@ -168,3 +168,38 @@ def test_cli_parser_number_forms(engine, tmp_path):
     assert fid.tolist() == [int(r[0]) for r in rows_f] and uid.tolist() == [int(r[0]) for r in rows_u]
     assert np.array_equal(fxy, np.array([[num(r[1]), num(r[2])] for r in rows_f], np.float32))
     assert np.array_equal(uxy, np.array([[num(r[1]), num(r[2])] for r in rows_u], np.float32))
+
+
+def _order_key(d):
+    """order_key of rt-rknn_gb300/csrc/rknn_common.cuh restated: an int64
+    key with the numeric order of finite doubles (-0 counts as +0)."""
+    b = d.view(np.int64).copy()
+    b[b == np.int64(-0x8000000000000000)] = 0
+    return np.where(b >= 0, b, b ^ np.int64(0x7FFFFFFFFFFFFFFF))
+
+
+def test_fp64_verification_bit_compares():
+    """The small-batch FP64 verification decides mv < -bu and -bu <= mv <= bu
+    on the bits (csrc/verify_item.cuh, filter_users with BITS): for finite mv
+    and bu > 0, order_key(mv) < ~bits(bu) and |mv| <= bu on the magnitude
+    bits.  Checked against the double compares on random values, signed
+    zeros, subnormals, equal magnitudes and neighbours of bu."""
+    rng = np.random.default_rng(7)
+    n = 400_000
+    bu = np.abs(rng.standard_normal(n)) * 10.0 ** rng.integers(-310, 300, n)
+    bu = np.where(bu > 0, bu, 5e-324)
+    mv = rng.standard_normal(n) * 10.0 ** rng.integers(-310, 300, n)
+    pick = rng.integers(0, 8, n)
+    mv = np.where(pick == 0, bu, mv)
+    mv = np.where(pick == 1, -bu, mv)
+    mv = np.where(pick == 2, np.nextafter(-bu, 0), mv)
+    mv = np.where(pick == 3, np.nextafter(-bu, -np.inf), mv)
+    mv = np.where(pick == 4, np.nextafter(bu, np.inf), mv)
+    mv = np.where(pick == 5, np.where(rng.integers(0, 2, n) == 1, 0.0, -0.0), mv)
+    mv = np.where(pick == 6, rng.choice([5e-324, -5e-324, 2.2e-308, -2.2e-308], n), mv)
+    assert np.all(np.isfinite(mv)) and np.all(bu > 0)
+    bb = bu.view(np.int64)
+    lt = _order_key(mv) < ~bb
+    inband = (mv.view(np.int64) & np.int64(0x7FFFFFFFFFFFFFFF)) <= bb
+    assert np.array_equal(lt, mv < -bu)
+    assert np.array_equal(inband, (mv <= bu) & (mv >= -bu))
