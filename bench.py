@@ -475,7 +475,11 @@ def run_ours(args):
     ds = dataset()
     # the chosen form: batched, FP32-filtered predicates, default candidate
     # filter (angular slices); the plain form: rknn-inf's influence zone
-    idx = rknn.Index.of(ds, device=local)
+    cells = {}
+    if args.cells:
+        f, u = (float(x) for x in args.cells.split(","))
+        cells = {"fac_per_cell": f, "usr_per_cell": u}
+    idx = rknn.Index.of(ds, device=local, **cells)
     idx_inf = rknn.Index.of(ds, device=local, filter="inf")
     stream = torch.cuda.Stream(device=local)
     idx.set_stream(stream.cuda_stream)
@@ -815,6 +819,8 @@ def main():
                     help="reference arm: skip the reference's other binaries")
     ap.add_argument("--no-serving5", action="store_true", help="skip the 1M/10M serving workload")
     ap.add_argument("--no-saturation", action="store_true", help="skip the 16384-query saturation batch")
+    ap.add_argument("--cells", default="", metavar="F,U",
+                    help="facilities and users per grid cell of the batch index (default: the index's defaults)")
     ap.add_argument("--queries", type=int, default=NQ,
                     help="queries per step (default 1000, the headline workload; larger batches for profiling)")
     args = ap.parse_args()
