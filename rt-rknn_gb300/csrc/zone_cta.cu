@@ -1191,8 +1191,11 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                 if (r > RM) { all_users = true; break; }
                 const int ncell = r == 0 ? 1 : 8 * r;
                 bool anykeep = false;
-                for (int t0 = 0; t0 < ncell; t0 += ZT) {
-                    const int t = t0 + tid;
+                // a group of ZG threads per cell, the half-planes split over
+                // it (a ring has few cells; one thread each would walk every
+                // half-plane in turn)
+                for (int t0 = 0; t0 < ncell; t0 += ZGN) {
+                    const int t = t0 + gi;
                     int dx = 0, dy = 0;
                     bool ok = t < ncell;
                     if (ok && r > 0) {
@@ -1204,14 +1207,13 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                     }
                     const int cxx = ucx + dx, cyy = ucy + dy;
                     ok = ok && cxx >= 0 && cxx < gu.gx && cyy >= 0 && cyy < gu.gy;
-                    bool keep = false;
+                    int viol = 0;
                     if (ok) {
                         const float X0 = (gu.x0 + (float)cxx * gu.cs) - qf.x - delta;
                         const float X1 = (gu.x0 + (float)(cxx + 1) * gu.cs) - qf.x + delta;
                         const float Y0 = (gu.y0 + (float)cyy * gu.cs) - qf.y - delta;
                         const float Y1 = (gu.y0 + (float)(cyy + 1) * gu.cs) - qf.y + delta;
-                        int viol = 0;
-                        for (int m = 0; m < nL && viol < k; ++m) {
+                        for (int m = gl; m < nL && viol < k; m += ZG) {
                             const float4 p = IX(S.splanes, m);
                             const float X = p.x > 0.0f ? X1 : X0;
                             const float Y = p.y > 0.0f ? Y1 : Y0;
@@ -1219,9 +1221,11 @@ __device__ __forceinline__ void zone_cta_body(const ZoneArgs& A)
                             const float bd = 8.0f * kU32 * fmaf(fabsf(p.x), fabsf(X), fmaf(fabsf(p.y), fabsf(Y), fabsf(p.z))) + 1e-30f;
                             viol += (mx < -bd);
                         }
-                        keep = viol < k;
                     }
-                    if (keep) {
+                    // (every lane of a warp takes part in the group sums)
+                    viol = group_sum<ZG>(viol);
+                    const bool keep = ok && viol < k;
+                    if (keep && gl == 0) {
                         const int bit = (dy + RM) * W + (dx + RM);
                         atomicOr(&IX(S.bitmap, bit >> 5), 1u << (bit & 31));
                     }
