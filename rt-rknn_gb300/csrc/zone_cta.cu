@@ -151,21 +151,6 @@ __device__ __forceinline__ double block_max_d(double v, ZcShared& sh, unsigned& 
 }
 
 template <int ZW>
-__device__ __forceinline__ float block_max_f(float v, ZcShared& sh, unsigned& ph)
-{
-    const int b = ph & 1;
-    ph ^= 1;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(FULL, v, o));
-    if ((threadIdx.x & 31) == 0) sh.rf[b][threadIdx.x >> 5] = v;
-    __syncthreads();
-    float r = sh.rf[b][0];
-#pragma unroll
-    for (int j = 1; j < ZW; ++j) r = fmaxf(r, sh.rf[b][j]);
-    return r;
-}
-
-template <int ZW>
 __device__ __forceinline__ int block_sum_i(int v, ZcShared& sh, unsigned& ph)
 {
     const int b = ph & 1;
